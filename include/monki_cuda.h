@@ -1,0 +1,92 @@
+/* C ABI of libmonki_cuda.so: MONKI photon transport on one GB300 (sm_103a).
+ *
+ * Each entry point replaces one entry point of the reference's Metal host bridge
+ * (kernels/metal/bridge.m, bound from python/monki/execution/metal.py:125-155); the
+ * reference has no CUDA path. Plain pointers and sizes only. Every call that can fail
+ * returns nonzero (or NULL) and writes a message into err[0..errlen).
+ *
+ * Transport tables: the float64 stream of kernels/cpu/worker.f90:1102-1120 (version 1)
+ * or version 2, which adds one view azimuth per view after the view zeniths.
+ *
+ * Controls (eight uint32 words, as kernels/metal/README.md:52-55): photon count, first
+ * flattened photon of the round group, first statistical round, seed, step limit per
+ * history and per detector ray, profiling flag, photons per round, rounds in the group.
+ *
+ * Output of a run: rounds x tally_count float64 values; each round holds, in Fortran
+ * order, stokes(nmat,nx,ny,angles) with the mu0/mu factor applied, then (when the
+ * tables request path diagnostics) paths(nx,ny,nz,angles) and weights(nx,ny,angles) -
+ * the RawTallies layout of python/monki/execution/tallies.py:21-32.
+ *
+ * Failure flags in error messages: 1 nonfinite contribution, 2 detector step limit,
+ * 4 sampling limit, 8 invalid Stokes vector, 16 history step limit
+ * (kernels/metal/README.md:57-59). A failed run rejects the whole round group.
+ */
+#ifndef MONKI_CUDA_H
+#define MONKI_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Replaces monki_metal_abi_version (kernels/metal/bridge.m:26). Returns 1. */
+int monki_cuda_abi_version(void);
+
+/* Replaces monki_metal_create (kernels/metal/bridge.m:30-84). Validates and packs the
+ * table stream, uploads it, allocates tally banks for round_capacity rounds. config is
+ * "key=value" items separated by ',' or ';': precision=fp32|fp64, shards=1..64,
+ * block=32..256, blocks_per_sm=0..64, uniform_prefix=0|1. Returns NULL on failure. */
+void *monki_cuda_create(uint32_t device, const double *tables, size_t table_count,
+                        uint32_t round_capacity, const char *config, char *err, size_t errlen);
+
+/* Replaces monki_metal_run (kernels/metal/bridge.m:88-133). Runs one round group and
+ * copies its FP64 tallies to out (rounds x tally_count). Nonzero on failure. */
+int monki_cuda_run(void *session, const uint32_t controls[8], double *out, char *err,
+                   size_t errlen);
+
+/* Replaces monki_metal_gpu_seconds (kernels/metal/bridge.m:135): summed transport time
+ * of runs whose profiling flag was set. */
+double monki_cuda_gpu_seconds(void *session);
+
+/* Device time of the last run in milliseconds from CUDA events on the session stream:
+ * out[0] the transport kernel, out[1] transport plus the FP64 flush. No reference
+ * counterpart. */
+int monki_cuda_last_timing(void *session, float out[2]);
+
+/* Session totals: scatters, free-path cell visits, detector cell visits, tally updates,
+ * photons. No reference counterpart (the scatter count is mc.f90's nscat). */
+int monki_cuda_counters(void *session, uint64_t out[5]);
+
+/* Number of float64 values per round in a run's output; no reference counterpart. */
+size_t monki_cuda_tally_count(void *session);
+
+/* Replaces monki_metal_device_name (kernels/metal/bridge.m:140). */
+const char *monki_cuda_device_name(void *session);
+
+/* Replaces monki_metal_close (kernels/metal/bridge.m:145-150). Safe on NULL. */
+void monki_cuda_close(void *session);
+
+/* Host-only check of the table packer (no GPU needed): validates the stream and returns
+ * the first layer of the horizontally uniform top and the optical depth above each
+ * layer, at fp32 or fp64 transport precision. The counterpart of the uniform-top prefix
+ * of python/monki/execution/metal_tables.py:93-107. */
+int monki_cuda_inspect(const double *tables, size_t table_count, int fp64, int32_t *uniform_top,
+                       double *tau_above, size_t tau_capacity, char *err, size_t errlen);
+
+/* Device probes of the production helpers, the counterpart of the reference's probe
+ * kernels (tests/integration/test_metal.py:23-103). */
+int monki_cuda_probe_philox(uint32_t device, const uint32_t *counters, const uint32_t *keys,
+                            uint32_t n, uint32_t *out, char *err, size_t errlen);
+int monki_cuda_probe_uniforms(uint32_t device, uint32_t photon, uint32_t round, uint32_t seed,
+                              uint32_t n, float *out, char *err, size_t errlen);
+int monki_cuda_probe_scatter_stokes(uint32_t device, int fp64, double depol,
+                                    const double *geometry, const double *stokes, uint32_t n,
+                                    double *out, char *err, size_t errlen);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MONKI_CUDA_H */

@@ -1,0 +1,70 @@
+// Device-resident scene for MONKI photon transport on sm_103a.
+//
+// The host packer (session.cu) turns the prepared float64 table stream (transport.bin
+// v1 of kernels/cpu/worker.f90:1102-1120, or v2 with one azimuth per view) into one
+// contiguous device allocation. The kernel receives a SceneView<T> by value; every
+// pointer in it points into that allocation.
+//
+// HBM/L2 layout (T = float for the product build, double for the FP64 check build):
+//   cells[4 * cell]          {beta, cumulative fraction of species 1..3} per cell,
+//                            cell = i + nx * (j + ny * k), 0-based, k = nz - 1 vacuum
+//   zunit[nz], zsum[nz + 1]  layer thickness and its running sum from the surface
+//   ssalb_gas[nz], albedo[nx * ny]
+//   tau_above[nz]            optical depth of the horizontally uniform layers above k
+//   lut_f[4 * n]             {F11, F22, F33, F12} per scattering angle, per species
+//   lut_cos[n], lut_cdf[n]   ascending cosine grid and the bound-function CDF
+//   guide[kGuide + 1]        CDF guide table: largest i with cdf[i] <= g / kGuide
+#pragma once
+#include <stdint.h>
+
+namespace monki {
+
+constexpr int kMaxViews = 16;
+constexpr int kMaxSpecies = 3;
+constexpr int kMaxLayers = 64;   // including the vacuum layer
+constexpr int kGuide = 4096;
+
+// Failure flags shared with the Python host (kernels/metal/README.md:57-59).
+enum Failure : uint32_t {
+    kNonfinite = 1u,
+    kDetectorCap = 2u,
+    kSamplingCap = 4u,
+    kInvalidStokes = 8u,
+    kHistoryCap = 16u,
+};
+
+template <typename T>
+struct SceneView {
+    int nx, ny, nz, nmat, angles, ntypes, paths, uniform_top;
+    int lut_n[kMaxSpecies];
+    T xunit, yunit, depol;
+    T a0, b0, c0, phi0;  // solar propagation direction cosines and azimuth (rad)
+    T va[kMaxViews], vb[kMaxViews], vc[kMaxViews], vphi[kMaxViews];
+    T ssalb_aer[kMaxSpecies];
+    const T* cells;
+    const T* zunit;
+    const T* zsum;
+    const T* ssalb_gas;
+    const T* albedo;
+    const T* tau_above;
+    const T* lut_f[kMaxSpecies];
+    const T* lut_cos[kMaxSpecies];
+    const T* lut_cdf[kMaxSpecies];
+    const int* guide[kMaxSpecies];
+};
+
+// Per-launch controls, the eight words of the Metal ABI v2 (kernels/metal/README.md:52-55).
+struct Controls {
+    uint32_t count, first, first_round, seed, max_steps, profile, per_round, rounds;
+};
+
+// Device tally layout of one round and one shard (TA = float or double):
+//   stokes[m + nmat * (i + nx * (j + ny * ia))]
+//   paths [k + nz * (i + nx * (j + ny * ia))]      k contiguous for vector reductions
+//   weights[i + nx * (j + ny * ia)]
+struct TallyLayout {
+    uint32_t stokes, paths, weights, count;  // element counts; count = sum
+    uint32_t shards;
+};
+
+}  // namespace monki

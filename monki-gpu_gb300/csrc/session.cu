@@ -1,0 +1,525 @@
+// C-ABI session for MONKI photon transport on one GB300 (sm_103a).
+//
+// The boundary mirrors the Metal bridge ABI v2 of the reference (kernels/metal/bridge.m:
+// create :30-84, run :88-133, gpu_seconds :135, device_name :140, close :145) with the
+// CUDA names declared in include/monki_cuda.h. A session owns: the packed scene, the FP32
+// (or FP64) tally banks of one round group, the FP64 per-round output, a failure word and
+// the work counters, all allocated once at create time. A run launches the transport
+// kernel and the FP64 flush on the session stream, copies the finished rounds to the
+// caller's buffer and reports any failure flag as an error; it never falls back to the CPU.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "transport.cuh"
+
+namespace monki {
+namespace {
+
+constexpr double kDegToRad = 0.017453292519943295;
+
+struct Config {
+    bool fp64 = false;
+    uint32_t shards = 8;
+    int block = 256;
+    int blocks_per_sm = 0;     // 0 = occupancy-derived
+    bool uniform_prefix = true;
+};
+
+Config parse_config(const char* text) {
+    Config c;
+    if (!text) return c;
+    std::string s(text);
+    size_t pos = 0;
+    while (pos < s.size()) {
+        size_t end = s.find_first_of(",;", pos);
+        if (end == std::string::npos) end = s.size();
+        std::string item = s.substr(pos, end - pos);
+        pos = end + 1;
+        if (item.empty()) continue;
+        size_t eq = item.find('=');
+        if (eq == std::string::npos) throw std::runtime_error("Malformed config item: " + item);
+        std::string key = item.substr(0, eq), value = item.substr(eq + 1);
+        auto as_int = [&](long lo, long hi) {
+            char* e = nullptr;
+            long v = std::strtol(value.c_str(), &e, 10);
+            if (!e || *e || v < lo || v > hi) throw std::runtime_error("Invalid config value: " + item);
+            return v;
+        };
+        if (key == "precision") {
+            if (value == "fp32") c.fp64 = false;
+            else if (value == "fp64") c.fp64 = true;
+            else throw std::runtime_error("precision must be fp32 or fp64");
+        } else if (key == "shards") c.shards = uint32_t(as_int(1, 64));
+        else if (key == "block") c.block = int(as_int(32, 256));
+        else if (key == "blocks_per_sm") c.blocks_per_sm = int(as_int(0, 64));
+        else if (key == "uniform_prefix") c.uniform_prefix = as_int(0, 1) != 0;
+        else throw std::runtime_error("Unknown config key: " + key);
+    }
+    if (c.block % 32) throw std::runtime_error("block must be a multiple of 32");
+    return c;
+}
+
+// Parsed transport table stream (transport.bin v1, kernels/cpu/worker.f90:1102-1120;
+// version 2 adds one view azimuth per view after the view zeniths).
+struct Prepared {
+    int nx, ny, nz, nmat, angles, ntypes;
+    bool paths;
+    double xunit, yunit, depol, vartheta0, phi0;
+    std::vector<double> zunit, vartheta, vphi, albedo, beta, fractions, ssalb_gas;
+    struct Lut { int n; double ssalb; std::vector<double> cos, cdf, f11, f22, f33, f12; };
+    std::vector<Lut> luts;
+};
+
+Prepared parse(const double* raw, size_t count) {
+    Prepared p{};
+    size_t off = 0;
+    auto take = [&](size_t n) {
+        if (off + n > count) throw std::runtime_error("Truncated transport export");
+        const double* q = raw + off;
+        off += n;
+        return q;
+    };
+    auto integer = [](double v) {
+        if (!std::isfinite(v) || v != std::floor(v) || std::fabs(v) > 1e9)
+            throw std::runtime_error("Unsupported transport export version or dimensions");
+        return int(v);
+    };
+    if (!raw || count < 18) throw std::runtime_error("Invalid/nonfinite prepared transport export");
+    for (size_t q = 0; q < count; ++q)
+        if (!std::isfinite(raw[q])) throw std::runtime_error("Invalid/nonfinite prepared transport export");
+    const double* h = take(12);
+    int version = integer(h[0]);
+    if (version != 1 && version != 2) throw std::runtime_error("Unsupported transport export version");
+    p.nx = integer(h[1]); p.ny = integer(h[2]); p.nz = integer(h[3]);
+    p.nmat = integer(h[4]); p.angles = integer(h[5]); p.ntypes = integer(h[6]);
+    int ks = integer(h[7]), kd = integer(h[8]), kr = integer(h[9]);
+    p.paths = integer(h[10]) != 0;
+    bool backward = integer(h[11]) != 0;
+    if (p.nx < 1 || p.ny < 1 || p.nz < 2 || p.nz > kMaxLayers || p.angles < 1 || p.angles > kMaxViews)
+        throw std::runtime_error("Scene exceeds the supported grid limits");
+    if (uint64_t(p.nx) * p.ny * p.nz > (1ull << 28)) throw std::runtime_error("Scene exceeds the supported grid limits");
+    if ((p.nmat != 1 && p.nmat != 3) || p.ntypes < 0 || p.ntypes > kMaxSpecies || backward ||
+        ks != p.nz || kd != p.nz || kr != p.nz)
+        throw std::runtime_error("CUDA supports forward I/IQU, up to 3 particle species, TOA source/detector/grid");
+    const double* g = take(6);
+    p.xunit = g[0]; p.yunit = g[1]; p.depol = g[2]; p.vartheta0 = g[3]; p.phi0 = g[4];
+    const double phi = g[5];
+    const size_t cols = size_t(p.nx) * p.ny, cells = cols * p.nz;
+    const double* q = take(p.nz); p.zunit.assign(q, q + p.nz);
+    q = take(p.angles); p.vartheta.assign(q, q + p.angles);
+    if (version == 2) { q = take(p.angles); p.vphi.assign(q, q + p.angles); }
+    else p.vphi.assign(p.angles, phi);
+    const double* surface = take(cols);
+    q = take(cols); p.albedo.assign(q, q + cols);
+    const double* elevation = take(cols);
+    q = take(cells); p.beta.assign(q, q + cells);
+    q = take(cells * (p.ntypes + 1)); p.fractions.assign(q, q + cells * (p.ntypes + 1));
+    q = take(p.nz); p.ssalb_gas.assign(q, q + p.nz);
+    for (int sp = 0; sp < p.ntypes; ++sp) {
+        const double* hd = take(2);
+        Prepared::Lut l;
+        l.n = integer(hd[0]); l.ssalb = hd[1];
+        if (l.n < 2 || l.n > 100000) throw std::runtime_error("Invalid scattering LUT size");
+        const double* t = take(size_t(l.n) * 6);
+        l.cos.assign(t, t + l.n); l.cdf.assign(t + l.n, t + 2 * l.n);
+        l.f11.assign(t + 2 * l.n, t + 3 * l.n); l.f22.assign(t + 3 * l.n, t + 4 * l.n);
+        l.f33.assign(t + 4 * l.n, t + 5 * l.n); l.f12.assign(t + 5 * l.n, t + 6 * l.n);
+        p.luts.push_back(std::move(l));
+    }
+    if (off != count) throw std::runtime_error("Trailing data in transport export");
+    for (size_t c = 0; c < cols; ++c)
+        if (surface[c] != -1 || elevation[c] != 1)
+            throw std::runtime_error("CUDA supports only flat Lambertian surfaces");
+    for (double z : p.zunit) if (!(z > 0)) throw std::runtime_error("Invalid layer dimensions, extinction, or scattering angle grid");
+    for (double b : p.beta) if (b < 0) throw std::runtime_error("Invalid layer dimensions, extinction, or scattering angle grid");
+    for (double v : p.vartheta) if (!(v >= 0 && v < 90)) throw std::runtime_error("Viewing zenith angles must be in [0, 90)");
+    for (double a : p.albedo) if (!(a >= 0 && a <= 1)) throw std::runtime_error("Surface albedo must be in [0, 1]");
+    for (const auto& l : p.luts) {
+        for (int i = 1; i < l.n; ++i)
+            if (!(l.cos[i] > l.cos[i - 1]) || l.cdf[i] < l.cdf[i - 1])
+                throw std::runtime_error("Invalid layer dimensions, extinction, or scattering angle grid");
+        if (std::fabs(l.cdf[0]) > 1e-12 || std::fabs(l.cdf[l.n - 1] - 1) > 1e-9)
+            throw std::runtime_error("Invalid scattering CDF");
+        // The bracket search guesses the index from a uniform 0..180 degree grid.
+        for (int i = 0; i < l.n; ++i) {
+            double angle = 180.0 - 180.0 * i / (l.n - 1);
+            if (std::fabs(std::acos(std::max(-1.0, std::min(1.0, l.cos[i]))) / kDegToRad - angle) > 1e-6 * 180.0 + 1e-9)
+                throw std::runtime_error("Scattering LUT must use a uniform angle grid from 180 to 0 degrees");
+        }
+    }
+    return p;
+}
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Host image of the device scene: element offsets into one allocation of T, plus the
+// guide tables (int) appended after the T region.
+template <typename T>
+struct Packed {
+    std::vector<T> values;
+    std::vector<int> guides;
+    size_t cells, zunit, zsum, ssalb_gas, albedo, tau_above;
+    size_t lut_f[kMaxSpecies], lut_cos[kMaxSpecies], lut_cdf[kMaxSpecies], guide[kMaxSpecies];
+    int uniform_top;
+};
+
+template <typename T>
+Packed<T> pack(const Prepared& p, bool uniform_prefix) {
+    Packed<T> k{};
+    auto& v = k.values;
+    const size_t cols = size_t(p.nx) * p.ny, ncell = cols * p.nz;
+    auto reserve = [&](size_t n) { size_t at = v.size(); v.resize(align_up(at + n, 4), T(0)); return at; };
+    k.cells = reserve(4 * ncell);
+    for (size_t c = 0; c < ncell; ++c) {
+        v[k.cells + 4 * c] = T(p.beta[c]);
+        double work = 0.0;  // cumulative fraction in the order of mc.f90:1028-1036
+        for (int s = 0; s < p.ntypes; ++s) {
+            work = s == 0 ? p.fractions[c * (p.ntypes + 1)] : work + p.fractions[c * (p.ntypes + 1) + s];
+            v[k.cells + 4 * c + 1 + s] = T(work);
+        }
+        for (int s = p.ntypes; s < 3; ++s) v[k.cells + 4 * c + 1 + s] = T(2);  // never selected
+    }
+    k.zunit = reserve(p.nz);
+    for (int z = 0; z < p.nz; ++z) v[k.zunit + z] = T(p.zunit[z]);
+    k.zsum = reserve(p.nz + 1);
+    {
+        double acc = 0.0;
+        v[k.zsum] = T(0);
+        for (int z = 0; z < p.nz; ++z) { acc += p.zunit[z]; v[k.zsum + z + 1] = T(acc); }
+    }
+    k.ssalb_gas = reserve(p.nz);
+    for (int z = 0; z < p.nz; ++z) v[k.ssalb_gas + z] = T(p.ssalb_gas[z]);
+    k.albedo = reserve(cols);
+    for (size_t c = 0; c < cols; ++c) v[k.albedo + c] = T(p.albedo[c]);
+    // Highest horizontally varying physical layer, compared at transport precision.
+    int varying = -1;
+    for (int z = 0; z < p.nz - 1; ++z) {
+        T b0 = T(p.beta[size_t(z) * cols]);
+        for (size_t c = 1; c < cols; ++c)
+            if (T(p.beta[size_t(z) * cols + c]) != b0) { varying = z; break; }
+    }
+    k.uniform_top = uniform_prefix ? varying + 1 : p.nz;
+    k.tau_above = reserve(p.nz);
+    {
+        // tau_above[k] = sum over physical layers above k of thickness * extinction,
+        // accumulated from the top at transport precision.
+        T acc = T(0);
+        v[k.tau_above + p.nz - 1] = T(0);
+        if (p.nz >= 2) v[k.tau_above + p.nz - 2] = T(0);
+        for (int z = p.nz - 3; z >= 0; --z) {
+            acc += T(p.zunit[z + 1]) * T(p.beta[size_t(z + 1) * cols]);
+            v[k.tau_above + z] = acc;
+        }
+    }
+    for (int s = 0; s < p.ntypes; ++s) {
+        const auto& l = p.luts[s];
+        k.lut_f[s] = reserve(4 * size_t(l.n));
+        for (int i = 0; i < l.n; ++i) {
+            v[k.lut_f[s] + 4 * i] = T(l.f11[i]); v[k.lut_f[s] + 4 * i + 1] = T(l.f22[i]);
+            v[k.lut_f[s] + 4 * i + 2] = T(l.f33[i]); v[k.lut_f[s] + 4 * i + 3] = T(l.f12[i]);
+        }
+        k.lut_cos[s] = reserve(l.n);
+        for (int i = 0; i < l.n; ++i) v[k.lut_cos[s] + i] = T(l.cos[i]);
+        k.lut_cdf[s] = reserve(l.n);
+        for (int i = 0; i < l.n; ++i) v[k.lut_cdf[s] + i] = T(l.cdf[i]);
+        // Guide: largest i <= n - 2 with cdf[i] <= g / kGuide (at transport precision).
+        k.guide[s] = k.guides.size();
+        int i = 0;
+        for (int gidx = 0; gidx <= kGuide; ++gidx) {
+            T level = T(gidx) / T(kGuide);
+            while (i < l.n - 2 && T(l.cdf[i + 1]) <= level) ++i;
+            k.guides.push_back(i);
+        }
+    }
+    return k;
+}
+
+struct Session {
+    int device = 0;
+    Config cfg;
+    Prepared prep;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t t0 = nullptr, t1 = nullptr, t2 = nullptr;
+    void* scene = nullptr;        // T values then int guides
+    void* banks = nullptr;        // round_capacity x shards x tally count, TA
+    double* out = nullptr;        // round_capacity x tally count
+    double* mu0mu = nullptr;
+    uint32_t* failure = nullptr;
+    unsigned long long* counters = nullptr;
+    uint32_t round_capacity = 1;
+    TallyLayout layout{};
+    SceneView<float> view32{};
+    SceneView<double> view64{};
+    int grid = 0;
+    double gpu_seconds = 0.0;
+    // scatters, free-path cell visits, detector cell visits, tally updates, photons
+    uint64_t totals[5] = {0, 0, 0, 0, 0};
+    float last_kernel_ms = 0.f;   // transport kernel
+    float last_run_ms = 0.f;      // transport kernel + FP64 flush
+    std::string name;
+};
+
+void check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+SceneView<T> make_view(const Prepared& p, const Packed<T>& k, void* base) {
+    SceneView<T> s{};
+    const T* tv = static_cast<const T*>(base);
+    const int* gv = reinterpret_cast<const int*>(static_cast<const char*>(base) + k.values.size() * sizeof(T));
+    s.nx = p.nx; s.ny = p.ny; s.nz = p.nz; s.nmat = p.nmat; s.angles = p.angles; s.ntypes = p.ntypes;
+    s.paths = p.paths; s.uniform_top = k.uniform_top;
+    s.xunit = T(p.xunit); s.yunit = T(p.yunit); s.depol = T(p.depol);
+    const double th0 = kDegToRad * p.vartheta0, ph0 = kDegToRad * p.phi0;
+    s.a0 = T(std::sin(th0) * std::cos(ph0)); s.b0 = T(std::sin(th0) * std::sin(ph0)); s.c0 = T(std::cos(th0));
+    s.phi0 = T(ph0);
+    for (int ia = 0; ia < p.angles; ++ia) {
+        double th = kDegToRad * p.vartheta[ia], ph = kDegToRad * p.vphi[ia];
+        s.va[ia] = T(std::cos(ph) * std::sin(th)); s.vb[ia] = T(std::sin(ph) * std::sin(th));
+        s.vc[ia] = T(std::cos(th)); s.vphi[ia] = T(ph);
+    }
+    s.cells = tv + k.cells; s.zunit = tv + k.zunit; s.zsum = tv + k.zsum; s.ssalb_gas = tv + k.ssalb_gas;
+    s.albedo = tv + k.albedo; s.tau_above = tv + k.tau_above;
+    for (int sp = 0; sp < p.ntypes; ++sp) {
+        s.lut_n[sp] = p.luts[sp].n; s.ssalb_aer[sp] = T(p.luts[sp].ssalb);
+        s.lut_f[sp] = tv + k.lut_f[sp]; s.lut_cos[sp] = tv + k.lut_cos[sp]; s.lut_cdf[sp] = tv + k.lut_cdf[sp];
+        s.guide[sp] = gv + k.guide[sp];
+    }
+    return s;
+}
+
+template <typename T>
+void upload(Session& s) {
+    Packed<T> k = pack<T>(s.prep, s.cfg.uniform_prefix);
+    size_t bytes = k.values.size() * sizeof(T) + k.guides.size() * sizeof(int);
+    check(cudaMalloc(&s.scene, std::max<size_t>(bytes, 16)), "cudaMalloc(scene)");
+    check(cudaMemcpy(s.scene, k.values.data(), k.values.size() * sizeof(T), cudaMemcpyHostToDevice), "upload(scene)");
+    if (!k.guides.empty())
+        check(cudaMemcpy(static_cast<char*>(s.scene) + k.values.size() * sizeof(T), k.guides.data(),
+                         k.guides.size() * sizeof(int), cudaMemcpyHostToDevice), "upload(guides)");
+    SceneView<T> v = make_view<T>(s.prep, k, s.scene);
+    if constexpr (sizeof(T) == 4) s.view32 = v; else s.view64 = v;
+}
+
+template <typename T, int NMAT, bool PATHS>
+const void* kernel_symbol() { return reinterpret_cast<const void*>(&transport_kernel<T, T, NMAT, PATHS>); }
+
+template <typename T>
+void launch_transport(Session& s, const Controls& c, int grid) {
+    const SceneView<T>& v = [&]() -> const SceneView<T>& {
+        if constexpr (sizeof(T) == 4) return s.view32; else return s.view64;
+    }();
+    T* banks = static_cast<T*>(s.banks);
+    const int nm = s.prep.nmat;
+    const bool paths = s.prep.paths;
+    if (nm == 1 && !paths) transport_kernel<T, T, 1, false><<<grid, s.cfg.block, 0, s.stream>>>(v, c, banks, s.layout, s.failure, s.counters);
+    else if (nm == 1) transport_kernel<T, T, 1, true><<<grid, s.cfg.block, 0, s.stream>>>(v, c, banks, s.layout, s.failure, s.counters);
+    else if (!paths) transport_kernel<T, T, 3, false><<<grid, s.cfg.block, 0, s.stream>>>(v, c, banks, s.layout, s.failure, s.counters);
+    else transport_kernel<T, T, 3, true><<<grid, s.cfg.block, 0, s.stream>>>(v, c, banks, s.layout, s.failure, s.counters);
+}
+
+template <typename T>
+int occupancy(const Session& s) {
+    const void* fn;
+    if (s.prep.nmat == 1) fn = s.prep.paths ? kernel_symbol<T, 1, true>() : kernel_symbol<T, 1, false>();
+    else fn = s.prep.paths ? kernel_symbol<T, 3, true>() : kernel_symbol<T, 3, false>();
+    int blocks = 0;
+    check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, s.cfg.block, 0), "occupancy");
+    return std::max(blocks, 1);
+}
+
+void destroy(Session* s) {
+    if (!s) return;
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    cudaFree(s->scene); cudaFree(s->banks); cudaFree(s->out); cudaFree(s->mu0mu);
+    cudaFree(s->failure); cudaFree(s->counters);
+    if (s->t0) cudaEventDestroy(s->t0);
+    if (s->t1) cudaEventDestroy(s->t1);
+    if (s->t2) cudaEventDestroy(s->t2);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+void write_error(char* err, size_t n, const std::string& msg) {
+    if (err && n) std::snprintf(err, n, "%s", msg.c_str());
+}
+
+}  // namespace
+}  // namespace monki
+
+using namespace monki;
+
+extern "C" {
+
+int monki_cuda_abi_version(void) { return 1; }
+
+void* monki_cuda_create(uint32_t device, const double* tables, size_t table_count, uint32_t round_capacity,
+                        const char* config, char* err, size_t errlen) {
+    Session* s = nullptr;
+    try {
+        Config cfg = parse_config(config);
+        Prepared prep = parse(tables, table_count);
+        if (round_capacity < 1 || round_capacity > 4096) throw std::runtime_error("round_capacity must be in [1, 4096]");
+        int n = 0;
+        cudaError_t e = cudaGetDeviceCount(&n);
+        if (e != cudaSuccess || n == 0) throw std::runtime_error("No CUDA device is available");
+        if (device >= uint32_t(n)) throw std::runtime_error("Requested CUDA device is unavailable");
+        s = new Session();
+        s->device = int(device);
+        s->cfg = cfg;
+        s->prep = std::move(prep);
+        s->round_capacity = round_capacity;
+        check(cudaSetDevice(s->device), "cudaSetDevice");
+        cudaDeviceProp prop{};
+        check(cudaGetDeviceProperties(&prop, s->device), "cudaGetDeviceProperties");
+        if (prop.major < 10) throw std::runtime_error("This build targets sm_103a (GB300)");
+        s->name = prop.name;
+        check(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        check(cudaEventCreate(&s->t0), "cudaEventCreate");
+        check(cudaEventCreate(&s->t1), "cudaEventCreate");
+        check(cudaEventCreate(&s->t2), "cudaEventCreate");
+        const Prepared& p = s->prep;
+        TallyLayout& L = s->layout;
+        L.stokes = uint32_t(p.nmat * p.nx * p.ny * p.angles);
+        L.paths = p.paths ? uint32_t(p.nx * p.ny * p.nz * p.angles) : 0u;
+        L.weights = p.paths ? uint32_t(p.nx * p.ny * p.angles) : 0u;
+        L.count = L.stokes + L.paths + L.weights;
+        L.shards = cfg.shards;
+        const size_t elem = cfg.fp64 ? sizeof(double) : sizeof(float);
+        const size_t bank_bytes = size_t(round_capacity) * L.shards * L.count * elem;
+        check(cudaMalloc(&s->banks, bank_bytes), "cudaMalloc(banks)");
+        check(cudaMemset(s->banks, 0, bank_bytes), "cudaMemset(banks)");
+        check(cudaMalloc(&s->out, size_t(round_capacity) * L.count * sizeof(double)), "cudaMalloc(out)");
+        std::vector<double> mu(size_t(p.angles));
+        for (int ia = 0; ia < p.angles; ++ia)
+            mu[size_t(ia)] = std::fabs(std::cos(kDegToRad * p.vartheta0)) / std::fabs(std::cos(kDegToRad * p.vartheta[ia]));
+        check(cudaMalloc(&s->mu0mu, mu.size() * sizeof(double)), "cudaMalloc(mu0mu)");
+        check(cudaMemcpy(s->mu0mu, mu.data(), mu.size() * sizeof(double), cudaMemcpyHostToDevice), "upload(mu0mu)");
+        check(cudaMalloc(&s->failure, sizeof(uint32_t)), "cudaMalloc(failure)");
+        check(cudaMalloc(&s->counters, 4 * sizeof(unsigned long long)), "cudaMalloc(counters)");
+        if (cfg.fp64) upload<double>(*s); else upload<float>(*s);
+        int per_sm = cfg.blocks_per_sm ? cfg.blocks_per_sm : (cfg.fp64 ? occupancy<double>(*s) : occupancy<float>(*s));
+        s->grid = prop.multiProcessorCount * per_sm;
+        check(cudaDeviceSynchronize(), "create");
+        return s;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        destroy(s);
+        return nullptr;
+    }
+}
+
+int monki_cuda_run(void* handle, const uint32_t controls[8], double* out, char* err, size_t errlen) {
+    Session* s = static_cast<Session*>(handle);
+    if (!s || !controls || !out) { write_error(err, errlen, "Invalid CUDA session or buffers"); return 1; }
+    try {
+        Controls c{controls[0], controls[1], controls[2], controls[3], controls[4], controls[5], controls[6], controls[7]};
+        if (!c.per_round || !c.rounds || c.rounds > s->round_capacity || !c.max_steps ||
+            uint64_t(c.first) + c.count > uint64_t(c.per_round) * c.rounds)
+            throw std::runtime_error("Invalid CUDA round group");
+        check(cudaSetDevice(s->device), "cudaSetDevice");
+        check(cudaMemsetAsync(s->failure, 0, sizeof(uint32_t), s->stream), "memset(failure)");
+        check(cudaMemsetAsync(s->counters, 0, 4 * sizeof(unsigned long long), s->stream), "memset(counters)");
+        const int needed = int(std::min<uint64_t>((uint64_t(c.count) + s->cfg.block - 1) / s->cfg.block, uint64_t(s->grid)));
+        check(cudaEventRecord(s->t0, s->stream), "event");
+        if (c.count) {
+            if (s->cfg.fp64) launch_transport<double>(*s, c, std::max(needed, 1));
+            else launch_transport<float>(*s, c, std::max(needed, 1));
+            check(cudaGetLastError(), "transport launch");
+        }
+        check(cudaEventRecord(s->t1, s->stream), "event");
+        const uint64_t total = uint64_t(s->layout.count) * c.rounds;
+        const int fgrid = int(std::min<uint64_t>((total + 255) / 256, 4096));
+        if (s->cfg.fp64)
+            flush_kernel<double><<<fgrid, 256, 0, s->stream>>>(static_cast<double*>(s->banks), s->layout, s->prep.nmat,
+                s->prep.nx, s->prep.ny, s->prep.nz, s->prep.angles, s->mu0mu, c.rounds, s->out);
+        else
+            flush_kernel<float><<<fgrid, 256, 0, s->stream>>>(static_cast<float*>(s->banks), s->layout, s->prep.nmat,
+                s->prep.nx, s->prep.ny, s->prep.nz, s->prep.angles, s->mu0mu, c.rounds, s->out);
+        check(cudaGetLastError(), "flush launch");
+        check(cudaEventRecord(s->t2, s->stream), "event");
+        uint32_t flag = 0;
+        unsigned long long cnt[4] = {0, 0, 0, 0};
+        check(cudaMemcpyAsync(&flag, s->failure, sizeof(flag), cudaMemcpyDeviceToHost, s->stream), "copy(failure)");
+        check(cudaMemcpyAsync(cnt, s->counters, sizeof(cnt), cudaMemcpyDeviceToHost, s->stream), "copy(counters)");
+        check(cudaMemcpyAsync(out, s->out, total * sizeof(double), cudaMemcpyDeviceToHost, s->stream), "copy(tallies)");
+        check(cudaStreamSynchronize(s->stream), "transport");
+        float ms = 0.f, run_ms = 0.f;
+        check(cudaEventElapsedTime(&ms, s->t0, s->t1), "elapsed");
+        check(cudaEventElapsedTime(&run_ms, s->t0, s->t2), "elapsed");
+        s->last_kernel_ms = ms;
+        s->last_run_ms = run_ms;
+        if (controls[5]) s->gpu_seconds += run_ms * 1e-3;
+        for (int q = 0; q < 4; ++q) s->totals[q] += cnt[q];
+        s->totals[4] += c.count;
+        if (flag) {
+            char msg[128];
+            std::snprintf(msg, sizeof msg, "CUDA transport failed (flag %u); round rejected", flag);
+            throw std::runtime_error(msg);
+        }
+        return 0;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        return 1;
+    }
+}
+
+double monki_cuda_gpu_seconds(void* handle) {
+    return handle ? static_cast<Session*>(handle)->gpu_seconds : 0.0;
+}
+
+int monki_cuda_last_timing(void* handle, float out[2]) {
+    if (!handle || !out) return 1;
+    Session* s = static_cast<Session*>(handle);
+    out[0] = s->last_kernel_ms;
+    out[1] = s->last_run_ms;
+    return 0;
+}
+
+int monki_cuda_counters(void* handle, uint64_t out[5]) {
+    if (!handle || !out) return 1;
+    Session* s = static_cast<Session*>(handle);
+    for (int q = 0; q < 5; ++q) out[q] = s->totals[q];
+    return 0;
+}
+
+size_t monki_cuda_tally_count(void* handle) {
+    return handle ? static_cast<Session*>(handle)->layout.count : 0;
+}
+
+const char* monki_cuda_device_name(void* handle) {
+    return handle ? static_cast<Session*>(handle)->name.c_str() : "";
+}
+
+void monki_cuda_close(void* handle) { destroy(static_cast<Session*>(handle)); }
+
+int monki_cuda_inspect(const double* tables, size_t table_count, int fp64, int32_t* uniform_top,
+                       double* tau_above, size_t tau_capacity, char* err, size_t errlen) {
+    try {
+        Prepared p = parse(tables, table_count);
+        if (tau_capacity < size_t(p.nz)) throw std::runtime_error("tau_above needs nz values");
+        if (fp64) {
+            Packed<double> k = pack<double>(p, true);
+            *uniform_top = k.uniform_top;
+            for (int z = 0; z < p.nz; ++z) tau_above[z] = k.values[k.tau_above + z];
+        } else {
+            Packed<float> k = pack<float>(p, true);
+            *uniform_top = k.uniform_top;
+            for (int z = 0; z < p.nz; ++z) tau_above[z] = double(k.values[k.tau_above + z]);
+        }
+        return 0;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        return 1;
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,323 @@
+"""GB300 transport backend: every photon history runs in the sm_103a kernels.
+
+``CUDA`` mirrors the reference's ``Metal`` backend (python/monki/execution/metal.py:23-349):
+settings validated eagerly, ``prepare`` uploads resident tables once, equal-size rounds
+are grouped into one launch with independent random streams and tallies, requests are
+validated before any device work, and any native failure closes the session. The device
+flushes FP32 tally banks into FP64 per-round sums, so the host only copies results out.
+There is no CPU path: a missing library, a missing GPU or a failed launch raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import hashlib
+import platform
+
+import numpy as np
+
+from ..scenes import TransportScene
+from . import native as _native
+from .backend import Backend
+from .tallies import BatchControls, RawTallies
+
+_PRECISIONS = ("fp32", "fp64")
+
+
+class CUDA(Backend):
+    """Resident GB300 transport session; one caller per instance.
+
+    ``precision="fp32"`` is the production transport. ``"fp64"`` runs the same kernels in
+    double precision: it is the on-device check build against which the FP32 bias of
+    each result is stated.
+    """
+
+    def __init__(
+        self,
+        device: int = 0,
+        *,
+        save_path: bool | None = None,
+        profile: bool = False,
+        seed: int = 23274,
+        photons_per_dispatch: int = 1 << 26,
+        tally_shards: int = 8,
+        max_steps: int = 100_000,
+        precision: str = "fp32",
+        block: int = 256,
+        library=None,
+    ):
+        for name, value, minimum, maximum in (
+            ("device", device, 0, 2**32 - 1),
+            ("seed", seed, 0, 2**32 - 1),
+            ("tally_shards", tally_shards, 1, 64),
+            ("photons_per_dispatch", photons_per_dispatch, 1, 2**31 - 1),
+            ("max_steps", max_steps, 1, 10_000_000),
+            ("block", block, 32, 256),
+        ):
+            if type(value) is not int or not minimum <= value <= maximum:
+                raise ValueError(f"{name} must be an integer in [{minimum}, {maximum}]")
+
+        if save_path is not None and type(save_path) is not bool:
+            raise ValueError("save_path must be a bool or None")
+
+        if type(profile) is not bool:
+            raise ValueError("profile must be a bool")
+
+        if precision not in _PRECISIONS:
+            raise ValueError("precision must be 'fp32' or 'fp64'")
+
+        if block % 32:
+            raise ValueError("block must be a multiple of 32")
+
+        self.device = device
+        self.save_path = save_path
+        self.profile = profile
+        self.seed = seed
+        self.photons_per_dispatch = photons_per_dispatch
+        self.tally_shards = tally_shards
+        self.max_steps = max_steps
+        self.precision = precision
+        self.block = block
+        self.library = library or _native.LIBRARY
+        self.metadata = None
+        self.provenance: dict = {}
+        self._native = None
+        self._handle = None
+        self._shape = (0, 0, 0, 0, 0)
+        self._paths = False
+        self._configuration = None
+        self._round = 0
+        self._tally_count = 0
+        self._round_capacity = 1
+
+    # ------------------------------------------------------------------ lifecycle
+    def prepare(self, scene: object) -> None:
+        """Validate the prepared tables, upload them once and size the round banks."""
+
+        self.close()
+
+        if not isinstance(scene, TransportScene):
+            if type(scene).__name__ == "ReferenceCase":
+                raise NotImplementedError(
+                    "CUDA.prepare needs prepared tables (monki.scenes.TransportScene); "
+                    "fixture preparation from INPUT files is not implemented"
+                )
+
+            raise TypeError("CUDA.prepare expects a TransportScene")
+
+        if scene.backward:
+            raise NotImplementedError("CUDA backward transport is not implemented")
+
+        tables = np.array(scene.tables, dtype=np.float64, copy=True)
+
+        if tables.ndim != 1 or tables.size < 18 or not np.all(np.isfinite(tables)):
+            raise ValueError("Invalid/nonfinite prepared transport export")
+
+        if self.save_path is not None:
+            tables[10] = float(self.save_path)
+
+        nx, ny, nz, nmat, angles = (int(v) for v in tables[1:6])
+        paths = bool(tables[10])
+        tally_count = nmat * nx * ny * angles + (nx * ny * (nz + 1) * angles if paths else 0)
+        per_round = scene.photons_per_column * nx * ny
+        bytes_per_round = tally_count * self.tally_shards * (4 if self.precision == "fp32" else 8)
+        capacity = max(
+            1,
+            min(
+                64,
+                self.photons_per_dispatch // max(per_round, 1),
+                (1 << 30) // max(bytes_per_round, 1),
+            ),
+        )
+        native = _native.load(self.library)
+        error = ctypes.create_string_buffer(8192)
+        config = f"precision={self.precision},shards={self.tally_shards},block={self.block}".encode()
+        handle = native.monki_cuda_create(
+            self.device,
+            tables.ctypes.data_as(_native.F64P),
+            tables.size,
+            capacity,
+            config,
+            error,
+            len(error),
+        )
+
+        if not handle:
+            raise RuntimeError(error.value.decode() or "CUDA session creation failed")
+
+        self._native = native
+        self._handle = handle
+        self._shape = (nmat, nx, ny, nz, angles)
+        self._paths = paths
+        self._tally_count = int(native.monki_cuda_tally_count(handle))
+        self._round_capacity = capacity
+        self._round = 0
+        self._configuration = self._settings()
+        self.metadata = scene.metadata
+
+        if self._tally_count != tally_count:
+            self.close()
+            raise RuntimeError("CUDA tally layout disagrees with the prepared tables")
+
+        self.provenance = {
+            "backend": "CUDA",
+            "device": native.monki_cuda_device_name(handle).decode(),
+            "scene": scene.name,
+            "rng": "Philox4x32-10; seed/round/photon/draw-block",
+            "seed": self.seed,
+            "transport_precision": "float32" if self.precision == "fp32" else "float64",
+            "tally_precision": "float32 banks, float64 per-round flush"
+            if self.precision == "fp32"
+            else "float64",
+            "round_precision": "float64",
+            "photons_per_dispatch": self.photons_per_dispatch,
+            "tally_shards": self.tally_shards,
+            "round_capacity": capacity,
+            "max_steps": self.max_steps,
+            "block": self.block,
+            "library_sha256": hashlib.sha256(open(self.library, "rb").read()).hexdigest(),
+            "tables_sha256": hashlib.sha256(tables.tobytes()).hexdigest(),
+            "machine": platform.machine(),
+            "python_version": platform.python_version(),
+            "gpu_dispatches": 0,
+            "scatters": 0,
+            "photons": 0,
+        }
+
+    def run_batch(self, controls: object) -> RawTallies:
+        """Execute exactly one complete statistical round."""
+
+        return self._run_group([controls])[0]
+
+    def run_batches(self, controls: list) -> list:
+        """Group consecutive equal-size rounds into shared launches, preserving order."""
+
+        self._validate_requests(controls)
+        results = []
+        first = 0
+        _, nx, ny, _, _ = self._shape
+
+        while first < len(controls):
+            photons = controls[first].photons_per_column * nx * ny
+            capacity = max(1, min(self._round_capacity, self.photons_per_dispatch // photons))
+            last = first + 1
+
+            while last < min(len(controls), first + capacity):
+                if controls[last].photons_per_column != controls[first].photons_per_column:
+                    break
+
+                last += 1
+
+            results.extend(self._run_group(controls[first:last]))
+            first = last
+
+        return results
+
+    def close(self) -> None:
+        """Release device memory; returned arrays stay valid."""
+
+        if self._handle is not None and self._native is not None:
+            self._native.monki_cuda_close(self._handle)
+
+        self._handle = None
+        self._native = None
+        self.metadata = None
+        self._configuration = None
+
+    # ------------------------------------------------------------------ internals
+    def _settings(self) -> tuple:
+        return (
+            self.device,
+            self.save_path,
+            self.seed,
+            self.photons_per_dispatch,
+            self.max_steps,
+            self.profile,
+            self.tally_shards,
+            self.precision,
+            self.block,
+        )
+
+    def _validate_requests(self, controls: list) -> None:
+        if self._handle is None or self._native is None:
+            raise RuntimeError("CUDA must be prepared before running a batch")
+
+        if self._settings() != self._configuration:
+            raise ValueError("CUDA settings changed; reprepare before running another batch")
+
+        _, nx, ny, _, _ = self._shape
+
+        for offset, request in enumerate(controls, start=1):
+            if not isinstance(request, BatchControls):
+                raise TypeError("run_batch expects BatchControls")
+
+            if request.round_index != self._round + offset:
+                raise ValueError("round_index must be sequential, starting at one")
+
+            if request.photons_per_column * nx * ny >= 2**32:
+                raise ValueError("CUDA photon identity exceeds its 32-bit round range")
+
+    def _run_group(self, controls: list) -> list[RawTallies]:
+        self._validate_requests(controls)
+        assert self._native is not None
+        nmat, nx, ny, nz, angles = self._shape
+        per_round = controls[0].photons_per_column * nx * ny
+        photon_count = per_round * len(controls)
+        total = np.zeros((len(controls), self._tally_count), dtype=np.float64)
+        scratch = np.empty_like(total)
+        error = ctypes.create_string_buffer(8192)
+
+        try:
+            for first in range(0, photon_count, self.photons_per_dispatch):
+                count = min(self.photons_per_dispatch, photon_count - first)
+                command = (ctypes.c_uint32 * 8)(
+                    count,
+                    first,
+                    controls[0].round_index,
+                    self.seed,
+                    self.max_steps,
+                    int(self.profile),
+                    per_round,
+                    len(controls),
+                )
+                status = self._native.monki_cuda_run(
+                    self._handle, command, scratch.ctypes.data_as(_native.F64P), error, len(error)
+                )
+
+                if status or not np.all(np.isfinite(scratch)):
+                    raise RuntimeError(error.value.decode() or "Nonfinite CUDA tallies")
+
+                total += scratch
+                self.provenance["gpu_dispatches"] += 1
+
+            counters = (ctypes.c_uint64 * 5)()
+            self._native.monki_cuda_counters(self._handle, counters)
+            self.provenance["scatters"] = int(counters[0])
+            self.provenance["photons"] = int(counters[4])
+
+            if self.profile:
+                self.provenance["gpu_seconds"] = self._native.monki_cuda_gpu_seconds(self._handle)
+
+            results = []
+            stokes_count = nmat * nx * ny * angles
+
+            for request, values in zip(controls, total, strict=True):
+                stokes = values[:stokes_count].reshape((nmat, nx, ny, angles), order="F").copy()
+                paths = weights = None
+
+                if self._paths:
+                    path_count = nx * ny * nz * angles
+                    paths = (
+                        values[stokes_count : stokes_count + path_count]
+                        .reshape((nx, ny, nz, angles), order="F")
+                        .copy()
+                    )
+                    weights = values[stokes_count + path_count :].reshape((nx, ny, angles), order="F").copy()
+
+                results.append(RawTallies(request, stokes, paths, weights))
+
+            self._round = controls[-1].round_index
+            return results
+        except BaseException:
+            self.close()
+            raise

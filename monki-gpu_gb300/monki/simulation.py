@@ -1,0 +1,175 @@
+"""Round statistics and the saved product, shared by every backend.
+
+Follows the reference driver (python/monki/simulation.py:17-189): fixed or
+convergence-scheduled rounds, FP64 sums of each round's normalized Stokes tallies and
+their squares, the standard error of the mean with the 999 sentinel through round 30,
+the U sign flip of backward transport, layer AMF = paths / weights / thickness without
+the vacuum layer, an exclusive-create NetCDF product and a ``.run.json`` receipt.
+"""
+
+from __future__ import annotations
+
+import hashlib
+import json
+from dataclasses import asdict
+from pathlib import Path
+
+import numpy as np
+
+from .convergence import AMFConvergence, AMFStopping, RadianceConvergence, RadianceStopping
+from .execution.backend import Backend
+from .execution.tallies import BatchControls, RawTallies
+from .output import SimulationResult
+
+
+def file_hash(path: Path) -> str:
+    return hashlib.sha256(Path(path).read_bytes()).hexdigest()
+
+
+def simulate(case, backend: Backend, output, *, convergence: AMFConvergence | None = None) -> SimulationResult:
+    """Run equally sized rounds, save the product and its receipt, return the result.
+
+    With a convergence policy, ``case.rounds`` is the hard round cap; the receipt tells
+    convergence apart from exhausting the cap.
+    """
+
+    if convergence is not None and case.rounds < convergence.minimum_rounds:
+        raise ValueError("round cap must be at least minimum_rounds")
+
+    output = Path(output).resolve()
+    receipt = output.with_suffix(".run.json")
+
+    if output.exists() or receipt.exists():
+        raise FileExistsError(f"Refusing to overwrite an existing result: {output}")
+
+    with backend:
+        backend.prepare(case)
+        metadata = backend.metadata
+
+        if metadata is None:
+            raise RuntimeError("Backend did not supply prepared scene metadata")
+
+        stopping = None
+
+        if isinstance(convergence, RadianceConvergence):
+            stopping = RadianceStopping(convergence, case.photons_per_column)
+            batches = stopping.batches(backend, case)
+        elif convergence is not None:
+            if "AMF_layer" not in metadata.values:
+                raise ValueError("AMF stopping requires layer path diagnostics")
+
+            stopping = AMFStopping(convergence, np.diff(metadata.values["alt"]) / 1000)
+            batches = stopping.batches(backend, case)
+        else:
+            requests = [BatchControls(i, case.photons_per_column) for i in range(1, case.rounds + 1)]
+            batches = backend.run_batches(requests)
+
+            if len(batches) != case.rounds:
+                raise ValueError("Backend returned the wrong number of statistical rounds")
+
+        total = rounds_sum = rounds_squared = paths = weights = None
+        history = []
+
+        for index, batch in enumerate(batches, start=1):
+            if not isinstance(batch, RawTallies):
+                raise TypeError("Backend must return RawTallies")
+
+            if batch.controls != BatchControls(index, case.photons_per_column):
+                raise ValueError("Backend returned tallies for a different round")
+
+            if total is None:
+                total = np.zeros_like(batch.stokes)
+                rounds_sum = np.zeros_like(batch.stokes)
+                rounds_squared = np.zeros_like(batch.stokes)
+
+                if batch.weighted_paths is not None:
+                    paths = np.zeros_like(batch.weighted_paths)
+                    weights = np.zeros_like(batch.weights)
+
+            total += batch.stokes
+            normalized = batch.stokes / case.photons_per_column
+            rounds_sum += normalized
+            rounds_squared += normalized**2
+            _, nx, ny, angles = total.shape
+            # Successive spatial sums then divisions, all Stokes components kept.
+            history.append(rounds_sum.sum(axis=1).sum(axis=1).sum(axis=1) / nx / ny / angles / index)
+
+            if paths is not None:
+                if batch.weighted_paths is None or batch.weights is None:
+                    raise ValueError("Backend dropped path diagnostics during a session")
+
+                paths += batch.weighted_paths
+                weights += batch.weights
+
+        completed = len(history)
+        radiance = total / completed / case.photons_per_column
+        uncertainty = np.full_like(radiance, 999.0)
+
+        # 999 marks an unavailable uncertainty through round 30.
+        if completed > 30:
+            variance_sum = rounds_squared - (1.0 / completed) * rounds_sum**2
+            tolerance = 64 * np.finfo(float).eps * np.maximum(rounds_squared, 1e-300)
+
+            if np.any(variance_sum < -tolerance):
+                raise ArithmeticError("Negative round variance exceeds floating-point roundoff")
+
+            uncertainty = np.sqrt(np.maximum(variance_sum, 0) / (completed - 1)) / np.sqrt(completed)
+
+        radiance_history = np.asarray(history)
+
+        if case.backward and radiance.shape[0] >= 3:
+            radiance[2] *= -1
+            radiance_history[:, 2] *= -1
+
+        intensity = radiance[0]
+        polarization = np.sqrt(np.sum(radiance[1:] ** 2, axis=0))
+        dop = np.divide(polarization, intensity, out=np.zeros_like(intensity), where=intensity > 1e-16)
+        values = {name: value.copy() for name, value in metadata.values.items()}
+        values["radiance"] = radiance.transpose(3, 2, 1, 0)[..., None]
+        values["std_radiance"] = uncertainty.transpose(3, 2, 1, 0)[..., None]
+        values["DOP"] = dop.transpose(2, 1, 0)[..., None]
+        values["radiance_convergence"] = radiance_history[..., None]
+        values["n_rounds"] = np.full_like(values["n_rounds"], completed)
+        values["n_photons_per_column"] = np.full_like(values["n_photons_per_column"], case.photons_per_column)
+
+        if paths is not None:
+            if np.any(weights <= 0):
+                raise ValueError("Layer AMF is undefined for a pixel with no detected weight")
+
+            # Lengths are km; altitudes are m. The vacuum layer is dropped.
+            thickness = np.diff(values["alt"]) / 1000.0
+            amf = paths[:, :, :-1, :] / weights[:, :, None, :] / thickness[None, None, :, None]
+            values["AMF_layer"] = amf.transpose(3, 2, 1, 0)[..., None]
+
+        dimensions = dict(metadata.dimensions)
+        attributes = dict(metadata.attributes)
+
+        if isinstance(stopping, AMFStopping) and not isinstance(stopping, RadianceStopping):
+            _, amf_error = stopping.moments.estimate(stopping.thickness)
+            values["std_AMF_layer"] = amf_error.transpose(3, 2, 1, 0)[..., None]
+            dimensions["std_AMF_layer"] = dimensions["AMF_layer"]
+            attributes["std_AMF_layer"] = {"long_name": "Layer AMF standard error", "units": "-"}
+
+        result = SimulationResult(output, values, dimensions, attributes)
+        result.save()
+        provenance = {
+            **backend.provenance,
+            "status": "complete",
+            "completed_rounds": completed,
+            "total_photons": completed * case.photons_per_column * nx * ny,
+            "output_sha256": file_hash(output),
+        }
+
+        if stopping is not None:
+            provenance["status"] = "converged" if stopping.converged else "max_rounds_reached"
+            provenance["radiance_convergence" if isinstance(stopping, RadianceStopping) else "amf_convergence"] = {
+                "policy": asdict(stopping.policy),
+                "converged": stopping.converged,
+                "checks": stopping.history,
+                "uncertainty": "pointwise relative standard error",
+            }
+
+        with receipt.open("x") as stream:
+            stream.write(json.dumps(provenance, indent=2) + "\n")
+
+        return result

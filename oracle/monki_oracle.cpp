@@ -1,0 +1,840 @@
+// MONKI photon-transport oracle: a CPU FP64 restatement of the reference Fortran.
+//
+// TEST INFRASTRUCTURE ONLY. This file is the checker for the CUDA transport path and the
+// timed CPU baseline; nothing in the product links, loads or calls it. Only tests/,
+// __graft_entry__.smoke() and bench.py's cpu_baseline / --impl reference legs may use it.
+//
+// Parity pins: the Philox4x32-10 stream is checked against the published Random123
+// known-answer vector (tests/integration/test_metal.py:43-59 of the reference); the
+// transport itself has no golden output readable in this container (the archived
+// goldens are NetCDF-4/HDF5 and the Fortran needs gfortran, which is absent), so its
+// agreement with the Fortran is statistical, through the restated algorithm below.
+//
+// Restated routines (paths relative to the reference project):
+//   fortran/monki/upstream/PROGRAM/mc.f90:314-1436        monte_carlo photon loop
+//   fortran/monki/upstream/PROGRAM/mc.f90:1531-1580       ADVANCE_internal
+//   .../modules/mc_routines_general_mod.f90:31-65          GROUND_LAMB2
+//   .../modules/mc_routines_general_mod.f90:74-136         ray_scat_matrix
+//   .../modules/mc_routines_general_mod.f90:147-246        ray_scat_elements / ray_scat_element
+//   .../modules/mc_routines_general_mod.f90:257-480        mie_scat_matrix / mie_scat_elements
+//   .../modules/mc_routines_general_mod.f90:492-670        rayl_scatter_pol
+//   .../modules/mc_routines_general_mod.f90:682-932        mie_scatter_pol_bound
+//   .../modules/mc_routines_general_mod.f90:942-1242       stokes_rot_mat / matmul_stokes_rot
+//   .../modules/mc_routines_cartesian_mod.f90:37-393       calc_radiances_pol
+//   .../modules/mc_routines_cartesian_mod.f90:849-1282     calc_radiances_and_paths_pol, ADVANCE
+//   .../modules/interpol_sp.f:105-151                      linpol_dp_single
+//   kernels/cpu/worker.f90:1102-1120                       transport.bin v1 layout
+//   kernels/cpu/worker.f90:1126-1204                       one batch = one statistical round
+//
+// Deliberate differences from the Fortran, none of which changes a statistic:
+//   * Random numbers come from Philox4x32-10 keyed by (seed), counter (photon, round,
+//     draw block, 0), mapped to the float32 grid (w>>9 + 0.5)*2^-23 — the stream layout
+//     of kernels/metal/transport.metal:64-92 — instead of gfortran RANDOM_NUMBER.
+//   * Intermediates the Fortran keeps in REAL (float32) — the species cumulative sum
+//     (mc.f90:1028-1036) and GROUND_LAMB2's ACOS(SQRT(P)) — are carried in FP64.
+//   * Version 2 of the table stream adds one azimuth per view (the v1 stream has one).
+//   * Failure caps (history steps, detector steps, 4096 rejection attempts) report a
+//     flag (1 nonfinite, 2 detector cap, 4 sampling cap, 8 invalid Stokes, 16 history
+//     cap; kernels/metal/README.md:57-59) where the Fortran loops or prints.
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <stdexcept>
+#include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+constexpr double kEps = 1.0e-16;
+constexpr double kPi = 3.141592653589793;
+constexpr double kDegToRad = 0.017453292519943295;
+constexpr double kStokesCriterium = 1.0e-2;  // mc.f90 stokes_criterium_error
+constexpr int kMaxAttempts = 4096;
+
+// ---------------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al. 2011, "Parallel random numbers: as easy as 1, 2, 3").
+// ---------------------------------------------------------------------------------
+void philox(uint32_t ctr[4], const uint32_t key_in[2]) {
+    uint32_t k0 = key_in[0], k1 = key_in[1];
+    for (int round = 0; round < 10; ++round) {
+        uint64_t p0 = uint64_t(0xD2511F53u) * ctr[0];
+        uint64_t p1 = uint64_t(0xCD9E8D57u) * ctr[2];
+        uint32_t n0 = uint32_t(p1 >> 32) ^ ctr[1] ^ k0;
+        uint32_t n1 = uint32_t(p1);
+        uint32_t n2 = uint32_t(p0 >> 32) ^ ctr[3] ^ k1;
+        uint32_t n3 = uint32_t(p0);
+        ctr[0] = n0; ctr[1] = n1; ctr[2] = n2; ctr[3] = n3;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+struct Stream {
+    uint32_t photon, round, seed, block = 0, lane = 4;
+    uint32_t words[4] = {0, 0, 0, 0};
+    // One uniform on the open float32 grid; returned widened to double exactly.
+    double uniform() {
+        if (lane == 4) {
+            uint32_t ctr[4] = {photon, round, block++, 0};
+            uint32_t key[2] = {seed, 0};
+            philox(ctr, key);
+            std::memcpy(words, ctr, sizeof(words));
+            lane = 0;
+        }
+        float u = (float(words[lane++] >> 9) + 0.5f) * 0x1p-23f;
+        return double(u);
+    }
+};
+
+// ---------------------------------------------------------------------------------
+// Prepared tables (transport.bin v1, worker.f90:1102-1120; v2 adds per-view azimuths).
+// ---------------------------------------------------------------------------------
+struct Species {
+    int n = 0;
+    double ssalb = 0;
+    std::vector<double> cosines, cdf, f11, f22, f33, f12;
+};
+
+struct Tables {
+    int version = 0, nx = 0, ny = 0, nz = 0, nmat = 0, angles = 0, ntypes = 0;
+    int k_source = 0, k_detector = 0, k_register = 0;
+    bool paths = false, backward = false;
+    double xunit = 0, yunit = 0, depol = 0, vartheta0 = 0, phi0 = 0, phi = 0;
+    std::vector<double> zunit, vartheta, view_phi, surface, albedo, elevation;
+    std::vector<double> beta, fractions, ssalb_gas;
+    std::vector<Species> species;
+
+    double beta_at(int i, int j, int k) const {  // 1-based Fortran indices
+        return beta[size_t(i - 1) + size_t(nx) * (size_t(j - 1) + size_t(ny) * size_t(k - 1))];
+    }
+    double fraction_at(int s, int i, int j, int k) const {
+        size_t cell = size_t(i - 1) + size_t(nx) * (size_t(j - 1) + size_t(ny) * size_t(k - 1));
+        return fractions[size_t(s - 1) + size_t(ntypes + 1) * cell];
+    }
+    double zu(int k) const { return zunit[size_t(k - 1)]; }
+};
+
+Tables parse_tables(const double* raw, size_t count) {
+    Tables t;
+    size_t offset = 0;
+    auto take = [&](size_t n) -> const double* {
+        if (offset + n > count) throw std::runtime_error("Truncated transport export");
+        const double* p = raw + offset;
+        offset += n;
+        return p;
+    };
+    auto as_int = [](double v, const char* what) {
+        if (!std::isfinite(v) || v != std::floor(v)) throw std::runtime_error(std::string("Non-integer ") + what);
+        return int(v);
+    };
+    if (count < 18) throw std::runtime_error("Invalid/nonfinite prepared transport export");
+    for (size_t i = 0; i < count; ++i)
+        if (!std::isfinite(raw[i])) throw std::runtime_error("Invalid/nonfinite prepared transport export");
+    const double* h = take(12);
+    t.version = as_int(h[0], "version");
+    if (t.version != 1 && t.version != 2) throw std::runtime_error("Unsupported transport export version");
+    t.nx = as_int(h[1], "nx"); t.ny = as_int(h[2], "ny"); t.nz = as_int(h[3], "nz");
+    t.nmat = as_int(h[4], "nmat"); t.angles = as_int(h[5], "angles"); t.ntypes = as_int(h[6], "species");
+    t.k_source = as_int(h[7], "k_source"); t.k_detector = as_int(h[8], "k_detector");
+    t.k_register = as_int(h[9], "k_register");
+    t.paths = as_int(h[10], "save_path") != 0; t.backward = as_int(h[11], "backward") != 0;
+    if (t.nx < 1 || t.ny < 1 || t.nz < 2 || t.angles < 1 || t.ntypes < 0)
+        throw std::runtime_error("Invalid transport export dimensions");
+    if (t.nmat != 1 && t.nmat != 3) throw std::runtime_error("Only nmat 1 or 3 is supported");
+    if (t.backward) throw std::runtime_error("Backward transport is not supported");
+    if (t.k_source != t.nz || t.k_detector != t.nz || t.k_register != t.nz)
+        throw std::runtime_error("Only TOA source, detector and output grid are supported");
+    const double* g = take(6);
+    t.xunit = g[0]; t.yunit = g[1]; t.depol = g[2]; t.vartheta0 = g[3]; t.phi0 = g[4]; t.phi = g[5];
+    const size_t cells = size_t(t.nx) * t.ny * t.nz, columns = size_t(t.nx) * t.ny;
+    const double* p = take(t.nz); t.zunit.assign(p, p + t.nz);
+    p = take(t.angles); t.vartheta.assign(p, p + t.angles);
+    if (t.version == 2) { p = take(t.angles); t.view_phi.assign(p, p + t.angles); }
+    else t.view_phi.assign(t.angles, t.phi);
+    p = take(columns); t.surface.assign(p, p + columns);
+    p = take(columns); t.albedo.assign(p, p + columns);
+    p = take(columns); t.elevation.assign(p, p + columns);
+    p = take(cells); t.beta.assign(p, p + cells);
+    p = take(cells * (t.ntypes + 1)); t.fractions.assign(p, p + cells * (t.ntypes + 1));
+    p = take(t.nz); t.ssalb_gas.assign(p, p + t.nz);
+    for (int s = 0; s < t.ntypes; ++s) {
+        Species sp;
+        const double* q = take(2);
+        sp.n = as_int(q[0], "LUT size"); sp.ssalb = q[1];
+        if (sp.n < 2 || sp.n > 100000) throw std::runtime_error("Invalid scattering LUT size");
+        const double* c = take(size_t(sp.n) * 6);
+        sp.cosines.assign(c, c + sp.n); sp.cdf.assign(c + sp.n, c + 2 * sp.n);
+        sp.f11.assign(c + 2 * sp.n, c + 3 * sp.n); sp.f22.assign(c + 3 * sp.n, c + 4 * sp.n);
+        sp.f33.assign(c + 4 * sp.n, c + 5 * sp.n); sp.f12.assign(c + 5 * sp.n, c + 6 * sp.n);
+        t.species.push_back(std::move(sp));
+    }
+    if (offset != count) throw std::runtime_error("Trailing data in transport export");
+    for (double s : t.surface) if (s != -1) throw std::runtime_error("Only Lambertian surfaces are supported");
+    for (double e : t.elevation) if (e != 1) throw std::runtime_error("Only flat surfaces are supported");
+    for (double z : t.zunit) if (!(z > 0)) throw std::runtime_error("Invalid layer thickness");
+    for (double b : t.beta) if (b < 0) throw std::runtime_error("Negative extinction");
+    for (double v : t.vartheta) if (!(v >= 0 && v < 90)) throw std::runtime_error("Viewing zenith must be in [0, 90)");
+    for (const auto& sp : t.species) {
+        for (int i = 1; i < sp.n; ++i)
+            if (!(sp.cosines[i] > sp.cosines[i - 1])) throw std::runtime_error("Scattering cosines must increase");
+        for (int i = 1; i < sp.n; ++i)
+            if (sp.cdf[i] < sp.cdf[i - 1]) throw std::runtime_error("Invalid scattering CDF");
+        if (std::fabs(sp.cdf[0]) > 1e-12 || std::fabs(sp.cdf[sp.n - 1] - 1) > 1e-9)
+            throw std::runtime_error("Invalid scattering CDF");
+    }
+    return t;
+}
+
+// ---------------------------------------------------------------------------------
+// Scattering helpers (mc_routines_general_mod.f90). Matrices are nmat x nmat with
+// nmat <= 3, stored row-major m[r][c] with 0-based indices.
+// ---------------------------------------------------------------------------------
+struct Mat3 { double m[3][3]; };
+
+// interpol_sp.f:105-151 linpol_dp_single for a two-point bracket.
+double linpol2(const double x[2], const double y[2], double xp) {
+    if (xp < x[0]) return (y[1] - y[0]) / (x[1] - x[0]) * (xp - x[0]) + y[0];
+    if (xp > x[1]) return (y[1] - y[0]) / (x[1] - x[0]) * (xp - x[1]) + y[1];
+    if (xp == x[1]) return y[1];
+    if (xp == x[0]) return y[0];
+    return (y[1] - y[0]) / (x[1] - x[0]) * (xp - x[0]) + y[0];
+}
+
+// mc_routines_general_mod.f90:74-136
+Mat3 ray_scat_matrix(int nmat, double cs, double depol) {
+    Mat3 f{};
+    double sin_sca = (1.0 - cs * cs < kEps) ? 0.0 : std::sqrt(1.0 - cs * cs);
+    double delta = (1.0 - depol) / (1.0 + depol / 2.0);
+    f.m[0][0] = 3.0 / 4.0 * (1.0 + cs * cs);
+    if (nmat > 1) {
+        f.m[0][1] = -3.0 / 4.0 * sin_sca * sin_sca;
+        f.m[1][0] = f.m[0][1];
+        f.m[1][1] = 3.0 / 4.0 * (1.0 + cs * cs);
+        f.m[2][2] = 3.0 / 2.0 * cs;
+    }
+    for (auto& r : f.m) for (double& v : r) v *= delta;
+    f.m[0][0] += 1.0 - delta;
+    for (auto& r : f.m) for (double& v : r) v /= 4.0;
+    return f;
+}
+
+// mc_routines_general_mod.f90:147-197 (F11, F12)
+void ray_scat_elements(double cs, double depol, double& f11, double& f12) {
+    double sin_sca = (1.0 - cs * cs < kEps) ? 0.0 : std::sqrt(1.0 - cs * cs);
+    double delta = (1.0 - depol) / (1.0 + depol / 2.0);
+    f11 = delta * (3.0 / 4.0 * (1.0 + cs * cs)) + (1.0 - delta);
+    f12 = delta * (-3.0 / 4.0 * sin_sca * sin_sca);
+    f11 /= 4.0; f12 /= 4.0;
+}
+
+// mc_routines_general_mod.f90:208-246 (F11 only)
+double ray_scat_element(double cs, double depol) {
+    double delta = (1.0 - depol) / (1.0 + depol / 2.0);
+    return (delta * (3.0 / 4.0 * (1.0 + cs * cs)) + (1.0 - delta)) / 4.0;
+}
+
+// Bracket search of mie_scat_matrix (mc_routines_general_mod.f90:296-340): an index
+// guess from the uniform 0..180 degree angle grid, then a one-step correction.
+int mie_bracket(const Species& sp, double cs, bool& single) {
+    int n = sp.n;
+    int imin = std::max(1, int((180.0 - std::acos(cs) / kDegToRad) / 180.0 * (n - 1)) + 1);
+    int imax = std::min(imin + 1, n);
+    single = (imax == imin);
+    if (single) return imax;
+    if (cs < sp.cosines[imin - 1]) imin -= 1;
+    else if (cs > sp.cosines[imax - 1]) imin += 1;
+    // The Fortran stops if the corrected bracket still misses; the guess relies on a
+    // uniform angle grid, which the table builders here always produce.
+    if (imin < 1 || imin + 1 > n || cs < sp.cosines[imin - 1] || cs > sp.cosines[imin])
+        throw std::runtime_error("mie_scat_matrix: scattering cosine outside its bracket");
+    return imin;
+}
+
+// mc_routines_general_mod.f90:257-388
+Mat3 mie_scat_matrix(int nmat, double cs, const Species& sp) {
+    Mat3 f{};
+    bool single = false;
+    int lo = mie_bracket(sp, cs, single);
+    double f11, f22 = 0, f33 = 0, f12 = 0;
+    if (single) {
+        f11 = sp.f11[lo - 1]; f22 = sp.f22[lo - 1]; f33 = sp.f33[lo - 1]; f12 = sp.f12[lo - 1];
+    } else {
+        const double x[2] = {sp.cosines[lo - 1], sp.cosines[lo]};
+        const double y11[2] = {sp.f11[lo - 1], sp.f11[lo]}, y22[2] = {sp.f22[lo - 1], sp.f22[lo]};
+        const double y33[2] = {sp.f33[lo - 1], sp.f33[lo]}, y12[2] = {sp.f12[lo - 1], sp.f12[lo]};
+        f11 = linpol2(x, y11, cs);
+        f22 = linpol2(x, y22, cs); f33 = linpol2(x, y33, cs); f12 = linpol2(x, y12, cs);
+    }
+    f.m[0][0] = f11;
+    if (nmat > 1) { f.m[1][1] = f22; f.m[2][2] = f33; f.m[0][1] = f12; f.m[1][0] = f12; }
+    for (auto& r : f.m) for (double& v : r) v /= 4.0;
+    return f;
+}
+
+// mc_routines_general_mod.f90:400-480 (F11, F12)
+void mie_scat_elements(double cs, const Species& sp, double& f11, double& f12) {
+    bool single = false;
+    int lo = mie_bracket(sp, cs, single);
+    if (single) { f11 = sp.f11[lo - 1]; f12 = sp.f12[lo - 1]; }
+    else {
+        const double x[2] = {sp.cosines[lo - 1], sp.cosines[lo]};
+        const double y11[2] = {sp.f11[lo - 1], sp.f11[lo]}, y12[2] = {sp.f12[lo - 1], sp.f12[lo]};
+        f11 = linpol2(x, y11, cs); f12 = linpol2(x, y12, cs);
+    }
+    f11 /= 4.0; f12 /= 4.0;
+}
+
+double fortran_sign(double a, double b) { return std::signbit(b) ? -std::fabs(a) : std::fabs(a); }
+
+// mc_routines_general_mod.f90:942-1174. Returns L1, L2 for nmat == 3 as the
+// (C, S) pairs: L(2,2) = L(3,3) = C, L(3,2) = S, L(2,3) = -S.
+struct Rotation { double c1 = 1, s1 = 0, c2 = 1, s2 = 0; };
+
+Rotation stokes_rot_mat(double cs, double uo, double u1, double phio, double phi1, int nmat) {
+    Rotation r;
+    if (nmat < 3) return r;
+    double dphi = std::fabs(phio - phi1);
+    double rem = std::fmod(dphi, kPi);
+    if (rem < kEps || std::fabs(rem - kPi) < kEps) return r;
+    if (std::fabs(uo) > 1.0 - kEps && std::fabs(u1) > 1.0 - kEps) return r;
+    double fac = 1.0 - uo * uo;
+    double sino = fac < kEps ? 0.0 : std::sqrt(fac);
+    fac = 1.0 - u1 * u1;
+    double sin1 = fac < kEps ? 0.0 : std::sqrt(fac);
+    double wo[3] = {sino * std::cos(phio), sino * std::sin(phio), uo};
+    double w1[3] = {sin1 * std::cos(phi1), sin1 * std::sin(phi1), u1};
+    double cosi1, cosi2, q;
+    if (std::fabs(uo) > 1.0 - kEps || std::fabs(u1) > 1.0 - kEps) {
+        double wophi[2] = {std::cos(phio), std::sin(phio)};
+        double w1phi[2] = {std::cos(phi1), std::sin(phi1)};
+        if (std::fabs(u1) > 1.0 - kEps) {
+            cosi1 = fortran_sign(1.0, u1);
+            cosi2 = -cosi1 * (w1phi[0] * wophi[0] + w1phi[1] * wophi[1]);
+            q = wo[1] * w1phi[0] - wo[0] * w1phi[1];
+        } else {
+            cosi2 = fortran_sign(1.0, uo);
+            cosi1 = -cosi2 * (w1phi[0] * wophi[0] + w1phi[1] * wophi[1]);
+            q = wophi[1] * w1[0] - wophi[0] * w1[1];
+        }
+    } else {
+        cosi1 = (u1 - uo * cs) / std::sqrt(std::max(kEps, (1.0 - uo * uo) * (1.0 - cs * cs)));
+        cosi2 = (uo - u1 * cs) / std::sqrt(std::max(kEps, (1.0 - u1 * u1) * (1.0 - cs * cs)));
+        q = wo[1] * w1[0] - wo[0] * w1[1];
+    }
+    fac = 1.0 - cosi1 * cosi1;
+    double sini1 = fac < kEps ? 0.0 : std::sqrt(fac) * fortran_sign(1.0, q);
+    fac = 1.0 - cosi2 * cosi2;
+    double sini2 = fac < kEps ? 0.0 : std::sqrt(fac) * fortran_sign(1.0, q);
+    // L(2,2) = cos^2 - sin^2 ; L(2,3) = -2 sin cos ; L(3,2) = -L(2,3)
+    r.c1 = cosi1 * cosi1 - sini1 * sini1;
+    r.s1 = 2.0 * sini1 * cosi1;
+    r.c2 = cosi2 * cosi2 - sini2 * sini2;
+    r.s2 = 2.0 * sini2 * cosi2;
+    return r;
+}
+
+// mc_routines_general_mod.f90:1184-1242
+Mat3 matmul_stokes_rot(int nmat, const Mat3& a, const Rotation& r) {
+    Mat3 p{};
+    p.m[0][0] = a.m[0][0];
+    if (nmat > 1) {
+        double C1 = r.c1, S1 = r.s1, C2 = r.c2, S2 = r.s2;
+        p.m[0][1] = a.m[0][1] * C1;
+        p.m[0][2] = -a.m[0][1] * S1;
+        p.m[1][0] = C2 * a.m[1][0];
+        p.m[1][1] = C1 * C2 * a.m[1][1] - S1 * S2 * a.m[2][2];
+        p.m[1][2] = -C2 * S1 * a.m[1][1] - C1 * S2 * a.m[2][2];
+        p.m[2][0] = S2 * a.m[1][0];
+        p.m[2][1] = C1 * S2 * a.m[1][1] + C2 * S1 * a.m[2][2];
+        p.m[2][2] = C1 * C2 * a.m[2][2] - S1 * S2 * a.m[1][1];
+    }
+    return p;
+}
+
+void apply(int nmat, const Mat3& p, const double s[3], double out[3]) {
+    for (int r = 0; r < nmat; ++r) {
+        double acc = 0;
+        for (int c = 0; c < nmat; ++c) acc += p.m[r][c] * s[c];
+        out[r] = acc;
+    }
+}
+
+// Spherical trigonometry shared by rayl_scatter_pol and mie_scatter_pol_bound
+// (mc_routines_general_mod.f90:633-667 and :905-931).
+void outgoing_direction(double cos_in, double cos_sca, double sigma1, double& cos_out, double& dphi) {
+    double sin_in = std::sqrt(std::max(kEps, 1.0 - cos_in * cos_in));
+    double sin_sca = std::sqrt(std::max(kEps, 1.0 - cos_sca * cos_sca));
+    cos_out = cos_in * cos_sca + sin_in * sin_sca * std::cos(sigma1);
+    double sin_out = std::sqrt(std::max(kEps, 1.0 - cos_out * cos_out));
+    double frac = (cos_sca - cos_in * cos_out) / (sin_in * sin_out);
+    if (frac >= 1.0 - kEps) dphi = 0.0;
+    else if (frac <= -1.0 + kEps) dphi = kPi;
+    else dphi = std::acos(frac) * fortran_sign(1.0, sigma1);
+    dphi = -dphi;
+}
+
+// rayl_scatter_pol (forward sign = -1), with a 4096-attempt cap.
+bool rayl_scatter_pol(int nmat, double depol, const double s[3], double cos_in, Stream& rng,
+                      double& cos_out, double& dphi, double& cos_sca) {
+    double pdf_max = ray_scat_element(1.0, depol);
+    for (int attempt = 0; attempt < kMaxAttempts; ++attempt) {
+        double ran1 = rng.uniform();
+        double rc = 2.0 * ran1 - 1.0;
+        double ran2 = rng.uniform();
+        double sigma = 2.0 * kPi * ran2 - kPi;
+        double f11, f12;
+        ray_scat_elements(rc, depol, f11, f12);
+        if (nmat == 1) f12 = 0.0;
+        double pdf = nmat == 1 ? f11 : f11 + f12 * (s[1] * std::cos(2.0 * sigma) - s[2] * std::sin(2.0 * sigma));
+        double ran3 = rng.uniform();
+        if (ran3 * pdf_max > pdf) continue;
+        cos_sca = rc;
+        outgoing_direction(cos_in, cos_sca, sigma, cos_out, dphi);
+        return true;
+    }
+    return false;
+}
+
+// mie_scatter_pol_bound (forward sign = -1), with a 4096-attempt cap.
+bool mie_scatter_pol_bound(int nmat, const Species& sp, const double s[3], double cos_in, Stream& rng,
+                           double& cos_out, double& dphi, double& cos_sca) {
+    for (int attempt = 0; attempt < kMaxAttempts; ++attempt) {
+        double ran_cdf = rng.uniform();
+        // Binary search of mie_scatter_pol_bound (:733-756) on 1-based indices.
+        int low = 1, high = sp.n, middle = 0;
+        bool found = false;
+        while (low <= high && !found) {
+            middle = (low + high) / 2;
+            if (middle + 1 > sp.n) break;
+            double v0 = sp.cdf[middle - 1], v1 = sp.cdf[middle];
+            if (ran_cdf >= v0 && ran_cdf <= v1) found = true;
+            else if (ran_cdf < v0) high = middle;
+            else low = middle;
+        }
+        if (!found) throw std::runtime_error("ran_CDF not found in CDF_bound");
+        const double cdf2[2] = {sp.cdf[middle - 1], sp.cdf[middle]};
+        const double ang2[2] = {sp.cosines[middle - 1], sp.cosines[middle]};
+        double rc = linpol2(cdf2, ang2, ran_cdf);
+        double ran2 = rng.uniform();
+        double sigma = 2.0 * kPi * ran2 - kPi;
+        double f11, f12;
+        mie_scat_elements(rc, sp, f11, f12);
+        if (nmat == 1) f12 = 0.0;
+        double pdf = nmat == 1 ? f11 : f11 + f12 * (s[1] * std::cos(2.0 * sigma) - s[2] * std::sin(2.0 * sigma));
+        double ran3 = rng.uniform();
+        double bound = f11 + std::fabs(f12);
+        if (ran3 * bound > pdf) continue;
+        cos_sca = rc;
+        outgoing_direction(cos_in, cos_sca, sigma, cos_out, dphi);
+        return true;
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------------------------
+// Per-round tallies in the RawTallies order: stokes(nmat,nx,ny,angles),
+// paths(nx,ny,nz,angles), weights(nx,ny,angles), all Fortran order, FP64.
+// ---------------------------------------------------------------------------------
+struct Counters {
+    uint64_t scatters = 0, photons = 0, free_path_visits = 0, detector_visits = 0, tally_updates = 0;
+    void add(const Counters& o) {
+        scatters += o.scatters; photons += o.photons; free_path_visits += o.free_path_visits;
+        detector_visits += o.detector_visits; tally_updates += o.tally_updates;
+    }
+};
+
+struct Transport {
+    const Tables& t;
+    uint32_t max_steps;
+    double a0, b0, c0, phi0_rad, vartheta0_rad;
+    std::vector<double> va, vb, vc, view_phi_rad, zsum;  // zsum[k] = SUM(zunit(1:k))
+    size_t stokes_count, path_count, weight_count, tally_count;
+
+    Transport(const Tables& tables, uint32_t steps) : t(tables), max_steps(steps) {
+        vartheta0_rad = kDegToRad * t.vartheta0;
+        phi0_rad = kDegToRad * t.phi0;
+        a0 = std::sin(vartheta0_rad) * std::cos(phi0_rad);
+        b0 = std::sin(vartheta0_rad) * std::sin(phi0_rad);
+        c0 = std::cos(vartheta0_rad);
+        for (int ia = 0; ia < t.angles; ++ia) {
+            double th = kDegToRad * t.vartheta[ia], ph = kDegToRad * t.view_phi[ia];
+            va.push_back(std::cos(ph) * std::sin(th));
+            vb.push_back(std::sin(ph) * std::sin(th));
+            vc.push_back(std::cos(th));
+            view_phi_rad.push_back(ph);
+        }
+        zsum.assign(t.nz + 1, 0.0);
+        for (int k = 1; k <= t.nz; ++k) zsum[k] = zsum[k - 1] + t.zu(k);
+        stokes_count = size_t(t.nmat) * t.nx * t.ny * t.angles;
+        path_count = t.paths ? size_t(t.nx) * t.ny * t.nz * t.angles : 0;
+        weight_count = t.paths ? size_t(t.nx) * t.ny * t.angles : 0;
+        tally_count = stokes_count + path_count + weight_count;
+    }
+
+    size_t stokes_index(int m, int i, int j, int ia) const {
+        return size_t(m) + size_t(t.nmat) * (size_t(i - 1) + size_t(t.nx) * (size_t(j - 1) + size_t(t.ny) * size_t(ia)));
+    }
+    size_t path_index(int i, int j, int k, int ia) const {
+        return stokes_count + size_t(i - 1) + size_t(t.nx) * (size_t(j - 1) + size_t(t.ny) * (size_t(k - 1) + size_t(t.nz) * size_t(ia)));
+    }
+    size_t weight_index(int i, int j, int ia) const {
+        return stokes_count + path_count + size_t(i - 1) + size_t(t.nx) * (size_t(j - 1) + size_t(t.ny) * size_t(ia));
+    }
+
+    // ADVANCE / ADVANCE_internal (identical bodies; mc.f90:1531-1580).
+    void advance(int& i, int& j, int& k, double& x, double& y, double& z, int is, int js, int ks,
+                 double aa, double ba, double ca, double ai, double bi, double ci, double& dist) const {
+        double dx = x * ai, dy = y * bi, dz = z * ci;
+        dist = std::min(dx, std::min(dy, dz));
+        if (dx == dist) {
+            i = (i + is + t.nx - 1) % t.nx + 1;
+            x = t.xunit;
+            y = std::max(0.0, y - ba * dist);
+            z = std::max(0.0, z - ca * dist);
+        } else if (dy == dist) {
+            j = (j + js + t.ny - 1) % t.ny + 1;
+            x = std::max(0.0, x - aa * dist);
+            y = t.yunit;
+            z = std::max(0.0, z - ca * dist);
+        } else {
+            k = k + ks;
+            x = std::max(0.0, x - aa * dist);
+            y = std::max(0.0, y - ba * dist);
+            if (k >= 1 && k <= t.nz) z = t.zu(k);
+        }
+    }
+
+    // calc_radiances_pol / calc_radiances_and_paths_pol (mc_routines_cartesian_mod.f90).
+    // Returns false when a detector ray exceeds the step cap.
+    bool peel_off(double a_bak, double b_bak, double c_bak, int i_bak, int j_bak, int k_bak,
+                  double x_bak, double y_bak, double z_bak, const std::vector<double>& s_prob,
+                  const std::vector<double>& path_layers, double* tally,
+                  std::vector<double>& path_angle, Counters& cnt) const {
+        const int nmat = t.nmat, nz = t.nz;
+        for (int ia = 0; ia < t.angles; ++ia) {
+            double p1 = s_prob[size_t(ia) * nmat];
+            if (!(p1 > kEps)) continue;
+            double a = va[ia], b = vb[ia], c = vc[ia];
+            int i = i_bak, j = j_bak, k = k_bak;
+            double x = x_bak, y = y_bak, z = z_bak;
+            if (a * a_bak < 0.0) x = std::max(0.0, t.xunit - x);
+            if (b * b_bak < 0.0) y = std::max(0.0, t.yunit - y);
+            if (c * c_bak < 0.0) z = std::max(0.0, t.zu(k) - z);
+            double tau = 0.0;
+            if (t.paths) std::fill(path_angle.begin(), path_angle.end(), 0.0);
+            int is = int(fortran_sign(1.0, a)), js = int(fortran_sign(1.0, b)), ks = int(fortran_sign(1.0, c));
+            double aa = std::fabs(a), ba = std::fabs(b), ca = std::fabs(c);
+            double ai = 1.0 / std::max(aa, kEps), bi = 1.0 / std::max(ba, kEps), ci = 1.0 / std::max(ca, kEps);
+            double x_old = x, y_old = y, z_old = z;
+            uint32_t steps = 0;
+            while (k >= 1 && k < nz) {
+                if (++steps > max_steps) return false;
+                double bv = t.beta_at(i, j, k);
+                int k_old = k;
+                double dist;
+                advance(i, j, k, x, y, z, is, js, ks, aa, ba, ca, ai, bi, ci, dist);
+                tau += dist * bv;
+                if (t.paths) path_angle[size_t(k_old - 1)] += dist;
+                ++cnt.detector_visits;
+            }
+            // Register grid mapping (k_register == k_detector == nz: direction = +1).
+            double height = zsum[size_t(k_bak - 1)];
+            height += ks > 0 ? t.zu(k_bak) - z_old : z_old;
+            height = zsum[size_t(nz - 1)] - height;
+            double delta_x = aa * height / ca, delta_y = ba * height / ca;
+            int di = int(((t.xunit - x_old) + delta_x) / t.xunit);
+            int dj = int(((t.yunit - y_old) + delta_y) / t.yunit);
+            auto modulo = [](long long v, long long m) { long long r = v % m; return r < 0 ? r + m : r; };
+            int inew = int(modulo((long long)i_bak + is * (long long)di + t.nx - 1, t.nx)) + 1;
+            int jnew = int(modulo((long long)j_bak + js * (long long)dj + t.ny - 1, t.ny)) + 1;
+            double att = std::exp(-tau);
+            for (int m = 0; m < nmat; ++m) tally[stokes_index(m, inew, jnew, ia)] += s_prob[size_t(ia) * nmat + m] * att;
+            cnt.tally_updates += nmat;
+            if (t.paths) {
+                double c1 = p1 * att;
+                for (int kk = 1; kk <= nz; ++kk)
+                    tally[path_index(inew, jnew, kk, ia)] += c1 * (path_layers[size_t(kk - 1)] + path_angle[size_t(kk - 1)]);
+                tally[weight_index(inew, jnew, ia)] += c1;
+                cnt.tally_updates += nz + 1;
+            }
+        }
+        return true;
+    }
+
+    // One photon history (mc.f90:351-1436). Returns a failure flag (0 on success).
+    uint32_t photon(uint32_t photon_id, uint32_t round, uint32_t seed, double* tally,
+                    Counters& cnt, std::vector<double>& path_layers, std::vector<double>& path_angle,
+                    std::vector<double>& s_prob) const {
+        const int nx = t.nx, ny = t.ny, nz = t.nz, nmat = t.nmat;
+        Stream rng{photon_id, round, seed};
+        ++cnt.photons;
+        int column = int(photon_id % uint32_t(nx * ny));
+        int i = column % nx + 1;
+        int j = std::min(column / nx + 1, ny);
+        int k = t.k_source;
+        double x = t.xunit * rng.uniform();
+        double y = t.yunit * rng.uniform();
+        double z = t.zu(k);
+        double s[3] = {1.0, 0.0, 0.0};
+        double weight = 1.0;
+        if (t.paths) std::fill(path_layers.begin(), path_layers.end(), 0.0);
+        double a = a0, b = b0, c = c0, phi_in = phi0_rad;
+        double remains = 0;
+        bool new_path = true;  // label 1000 (draw a new optical path) vs 1010
+        uint32_t steps = 0;
+        for (;;) {
+            if (new_path) remains = -std::log(std::max(rng.uniform(), kEps));
+            new_path = false;
+            // label 1010
+            int is = int(fortran_sign(1.0, a)), js = int(fortran_sign(1.0, b)), ks = int(fortran_sign(1.0, c));
+            double aa = std::fabs(a), ba = std::fabs(b), ca = std::fabs(c);
+            double ai = 1.0 / std::max(aa, kEps), bi = 1.0 / std::max(ba, kEps), ci = 1.0 / std::max(ca, kEps);
+            bool surface = false, event = false;
+            // label 1020 loop
+            for (;;) {
+                if (++steps > max_steps) return 16;
+                ++cnt.free_path_visits;
+                double bv = (k < nz && k > 0) ? t.beta_at(i, j, k) : 0.0;
+                if (bv > kEps) {
+                    double de = remains / bv;
+                    if (de < x * ai && de < y * bi && de < z * ci) {
+                        x = std::max(0.0, x - aa * de);
+                        y = std::max(0.0, y - ba * de);
+                        z = std::max(0.0, z - ca * de);
+                        if (t.paths) path_layers[size_t(k - 1)] += de;
+                        event = true;
+                        break;
+                    }
+                }
+                int k_old = k;
+                double dist;
+                advance(i, j, k, x, y, z, is, js, ks, aa, ba, ca, ai, bi, ci, dist);
+                if (t.paths) path_layers[size_t(k_old - 1)] += dist;
+                remains -= dist * bv;
+                if (k <= nz && k >= 1) continue;
+                if (k > nz) return 0;  // escaped through TOA
+                surface = true;
+                break;
+            }
+            if (surface) {
+                double a_int = a, b_int = b, c_int = c;
+                k = std::max(k, 1);
+                z = 0.0;
+                weight *= t.albedo[size_t(i - 1) + size_t(nx) * size_t(j - 1)];
+                if (weight < kEps) return 0;
+                ++cnt.scatters;
+                for (int ia = 0; ia < t.angles; ++ia) {
+                    for (int m = 0; m < nmat; ++m) s_prob[size_t(ia) * nmat + m] = 0.0;
+                    if (vc[ia] > 0) s_prob[size_t(ia) * nmat] = s[0] * vc[ia] * weight;
+                    if (!std::isfinite(s_prob[size_t(ia) * nmat])) return 1;
+                }
+                if (!peel_off(a_int, b_int, c_int, i, j, k, x, y, z, s_prob, path_layers, tally, path_angle, cnt))
+                    return 2;
+                // GROUND_LAMB2: theta = acos(sqrt(P)), phi = 2 pi U.
+                double P = rng.uniform(), U = rng.uniform();
+                double theta = std::acos(std::sqrt(P));
+                double phi_out = 2.0 * kPi * U;
+                a = std::sin(theta) * std::cos(phi_out);
+                b = std::sin(theta) * std::sin(phi_out);
+                c = std::fabs(std::cos(theta));
+                s[1] = 0.0; s[2] = 0.0;  // As * S keeps only I
+                if (s[0] > kEps) { double s0 = s[0]; for (int m = 0; m < nmat; ++m) s[m] /= s0; }
+                if (a * a_int < 0.0) x = std::max(0.0, t.xunit - x);
+                if (b * b_int < 0.0) y = std::max(0.0, t.yunit - y);
+                if (c * c_int < 0.0) z = std::max(0.0, t.zu(k) - z);
+                phi_in = phi_out;
+                continue;  // GOTO 1010 (keeps remains)
+            }
+            (void)event;
+            // label 3000: species selection (gas is index ntypes + 1).
+            double rtemp = rng.uniform();
+            int sp = 1;
+            double work = t.fraction_at(1, i, j, k);
+            while (work <= rtemp && sp < t.ntypes + 1) {
+                ++sp;
+                work += t.fraction_at(sp, i, j, k);
+            }
+            bool gas = sp == t.ntypes + 1;
+            weight *= gas ? t.ssalb_gas[size_t(k - 1)] : t.species[size_t(sp - 1)].ssalb;
+            if (weight < kEps) return 0;
+            ++cnt.scatters;
+            for (int ia = 0; ia < t.angles; ++ia) {
+                double cs = c * vc[ia] + std::sqrt(std::max(kEps, 1.0 - c * c)) *
+                                             std::sqrt(std::max(kEps, 1.0 - vc[ia] * vc[ia])) *
+                                             std::cos(phi_in - view_phi_rad[ia]);
+                Rotation rot = stokes_rot_mat(cs, c, vc[ia], phi_in, view_phi_rad[ia], nmat);
+                Mat3 f = gas ? ray_scat_matrix(nmat, cs, t.depol) : mie_scat_matrix(nmat, cs, t.species[size_t(sp - 1)]);
+                Mat3 p = matmul_stokes_rot(nmat, f, rot);
+                double back[3];
+                apply(nmat, p, s, back);
+                for (int m = 0; m < nmat; ++m) s_prob[size_t(ia) * nmat + m] = back[m] * weight;
+                if (s_prob[size_t(ia) * nmat] < 1.0e-100)
+                    for (int m = 0; m < nmat; ++m) s_prob[size_t(ia) * nmat + m] = 0.0;
+                for (int m = 0; m < nmat; ++m)
+                    if (!std::isfinite(s_prob[size_t(ia) * nmat + m])) return 1;
+            }
+            if (!peel_off(a, b, c, i, j, k, x, y, z, s_prob, path_layers, tally, path_angle, cnt)) return 2;
+            double cos_in = c, cos_out, dphi, cos_sca;
+            bool ok = gas ? rayl_scatter_pol(nmat, t.depol, s, cos_in, rng, cos_out, dphi, cos_sca)
+                          : mie_scatter_pol_bound(nmat, t.species[size_t(sp - 1)], s, cos_in, rng, cos_out, dphi, cos_sca);
+            if (!ok) return 4;
+            double phi_out = phi_in + dphi;
+            Rotation rot = stokes_rot_mat(cos_sca, cos_in, cos_out, phi_in, phi_out, nmat);
+            Mat3 f = gas ? ray_scat_matrix(nmat, cos_sca, t.depol) : mie_scat_matrix(nmat, cos_sca, t.species[size_t(sp - 1)]);
+            Mat3 p = matmul_stokes_rot(nmat, f, rot);
+            double ns[3];
+            apply(nmat, p, s, ns);
+            double s0 = ns[0];
+            for (int m = 0; m < nmat; ++m) s[m] = ns[m] / s0;
+            if (s[0] < 1.0e-100) for (int m = 0; m < nmat; ++m) s[m] = 0.0;
+            for (int m = 0; m < nmat; ++m) if (!std::isfinite(s[m])) return 8;
+            if (nmat == 3 && std::sqrt(s[1] * s[1] + s[2] * s[2]) > s[0] + kStokesCriterium) return 8;
+            double a_bak = a, b_bak = b, c_bak = c;
+            a = std::cos(phi_out) * std::sqrt(std::max(0.0, 1.0 - cos_out * cos_out));
+            b = std::sin(phi_out) * std::sqrt(std::max(0.0, 1.0 - cos_out * cos_out));
+            c = cos_out;
+            if (a * a_bak < 0.0) x = std::max(0.0, t.xunit - x);
+            if (b * b_bak < 0.0) y = std::max(0.0, t.yunit - y);
+            if (c * c_bak < 0.0) z = std::max(0.0, t.zu(k) - z);
+            phi_in = phi_out;
+            new_path = true;  // GOTO 1000
+        }
+    }
+};
+
+void write_error(char* err, size_t n, const std::string& msg) {
+    if (err && n) std::snprintf(err, n, "%s", msg.c_str());
+}
+
+}  // namespace
+
+extern "C" {
+
+int monki_oracle_abi_version(void) { return 1; }
+
+// Philox4x32-10 of one counter/key pair (known-answer tests).
+void monki_oracle_philox(const uint32_t counter[4], const uint32_t key[2], uint32_t out[4]) {
+    uint32_t ctr[4] = {counter[0], counter[1], counter[2], counter[3]};
+    philox(ctr, key);
+    std::memcpy(out, ctr, sizeof(ctr));
+}
+
+// One uniform draw sequence of a photon stream: n values of Stream::uniform().
+void monki_oracle_uniforms(uint32_t photon, uint32_t round, uint32_t seed, uint32_t n, double* out) {
+    Stream s{photon, round, seed};
+    for (uint32_t i = 0; i < n; ++i) out[i] = s.uniform();
+}
+
+// The polarization probe: ray_scat_matrix, stokes_rot_mat and matmul_stokes_rot applied
+// to S (tests/native/metal_probe.f90 of the reference).
+void monki_oracle_scatter_stokes(double depol, double uo, double u1, double phio, double phi1,
+                                 const double stokes[3], double out[3]) {
+    double cs = uo * u1 + std::sqrt(1 - uo * uo) * std::sqrt(1 - u1 * u1) * std::cos(phio - phi1);
+    Mat3 f = ray_scat_matrix(3, cs, depol);
+    Rotation r = stokes_rot_mat(cs, uo, u1, phio, phi1, 3);
+    Mat3 p = matmul_stokes_rot(3, f, r);
+    apply(3, p, stokes, out);
+}
+
+// Validate a transport table stream; 0 on success, else the message in err.
+int monki_oracle_validate(const double* tables, size_t count, char* err, size_t errlen) {
+    try {
+        parse_tables(tables, count);
+        return 0;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        return 1;
+    }
+}
+
+// Run photons [first, first + count) of the flattened round group, exactly like one
+// monki_cuda_run call. controls: count, first photon, first round, seed, max_steps,
+// profile (ignored), photons per round, active rounds. out: active rounds x tally
+// count FP64, each round in RawTallies order with the mu0/mu factor applied to Stokes.
+// counters (5 x u64): scatters, photons, free-path cell visits, detector cell visits,
+// tally updates. Returns the failure flag (0 on success); a nonzero flag rejects the run.
+int monki_oracle_run(const double* tables, size_t table_count, const uint32_t controls[8], int threads,
+                     double* out, uint64_t* counters, char* err, size_t errlen) {
+    try {
+        Tables t = parse_tables(tables, table_count);
+        const uint32_t count = controls[0], first = controls[1], first_round = controls[2];
+        const uint32_t seed = controls[3], max_steps = controls[4], per_round = controls[6];
+        const uint32_t rounds = controls[7];
+        if (!per_round || !rounds || uint64_t(first) + count > uint64_t(per_round) * rounds) {
+            write_error(err, errlen, "Invalid round group");
+            return 1;
+        }
+        Transport tr(t, max_steps);
+        const size_t tc = tr.tally_count;
+        std::fill(out, out + tc * rounds, 0.0);
+        int nthreads = threads > 0 ? threads : 1;
+        std::vector<std::vector<double>> partial(size_t(nthreads), std::vector<double>(tc * rounds, 0.0));
+        std::vector<Counters> cnts(static_cast<size_t>(nthreads));
+        std::vector<uint32_t> flags(static_cast<size_t>(nthreads), 0u);
+        std::vector<std::string> errors(static_cast<size_t>(nthreads));
+#pragma omp parallel num_threads(nthreads)
+        {
+            int tid = 0;
+#ifdef _OPENMP
+            tid = omp_get_thread_num();
+#endif
+            std::vector<double> path_layers(size_t(t.nz), 0.0), path_angle(size_t(t.nz), 0.0);
+            std::vector<double> s_prob(size_t(t.angles) * t.nmat, 0.0);
+#pragma omp for schedule(dynamic, 256)
+            for (long long n = 0; n < (long long)count; ++n) {
+                if (flags[size_t(tid)]) continue;
+                uint32_t identity = first + uint32_t(n);
+                uint32_t round_offset = identity / per_round;
+                uint32_t photon_id = identity % per_round;
+                double* tally = partial[size_t(tid)].data() + size_t(round_offset) * tc;
+                try {
+                    uint32_t flag = tr.photon(photon_id, first_round + round_offset, seed, tally,
+                                              cnts[size_t(tid)], path_layers, path_angle, s_prob);
+                    if (flag) flags[size_t(tid)] |= flag;
+                } catch (const std::exception& e) {
+                    errors[size_t(tid)] = e.what();
+                    flags[size_t(tid)] |= 0x100;
+                }
+            }
+        }
+        uint32_t flag = 0;
+        Counters total;
+        for (int q = 0; q < nthreads; ++q) {
+            flag |= flags[size_t(q)];
+            total.add(cnts[size_t(q)]);
+            const std::vector<double>& p = partial[size_t(q)];
+            for (size_t v = 0; v < tc * rounds; ++v) out[v] += p[v];
+        }
+        // mu0/mu geometry factor on Stokes only (mc.f90:1456-1474).
+        for (uint32_t r = 0; r < rounds; ++r)
+            for (int ia = 0; ia < t.angles; ++ia) {
+                double f = std::fabs(std::cos(tr.vartheta0_rad)) / std::fabs(std::cos(kDegToRad * t.vartheta[ia]));
+                for (int j = 1; j <= t.ny; ++j)
+                    for (int i = 1; i <= t.nx; ++i)
+                        for (int m = 0; m < t.nmat; ++m) out[size_t(r) * tc + tr.stokes_index(m, i, j, ia)] *= f;
+            }
+        if (counters) {
+            counters[0] = total.scatters; counters[1] = total.photons; counters[2] = total.free_path_visits;
+            counters[3] = total.detector_visits; counters[4] = total.tally_updates;
+        }
+        if (flag) {
+            std::string msg;
+            for (const auto& e : errors) if (!e.empty()) { msg = e; break; }
+            if (msg.empty()) msg = "Oracle transport failed (flag " + std::to_string(flag) + "); round rejected";
+            write_error(err, errlen, msg);
+            return int(flag);
+        }
+        return 0;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        return 0x100;
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,355 @@
+"""Generate the golden fixtures of tests/golden from the reference project.
+
+Run in a container where the reference is mounted (default /root/reference, or the
+MONKI_REFERENCE environment variable); the fixtures it writes are committed, so the
+tests never need the reference at run time.
+
+What each fixture pins, and where it comes from:
+  philox_kat.json        Random123 Philox4x32-10 known-answer vector, read from the
+                         reference's device test (tests/integration/test_metal.py:43-59).
+  polarization_probe.json
+                         The probe geometries of tests/native/metal_probe.f90:10-16 with
+                         expected L2 F L1 S from an independent numpy restatement of
+                         ray_scat_matrix / stokes_rot_mat / matmul_stokes_rot
+                         (mc_routines_general_mod.f90:74-136, 942-1242); the Fortran
+                         itself cannot be compiled here (no gfortran).
+  amf_moments.npz        The reference's own AMFMoments (python/monki/convergence.py)
+                         on seeded synthetic rounds: inputs, AMF and its standard error.
+  uniform_top.json       The reference's own pack_tables (python/monki/execution/
+                         metal_tables.py) on version-1 streams built here: the first
+                         uniform layer and the optical depth above each layer.
+  driver_statistics.npz  The reference's own simulate() (python/monki/simulation.py)
+                         driven by a fixed synthetic backend: radiance, standard error,
+                         DOP, convergence history, layer AMF and its standard error.
+"""
+
+from __future__ import annotations
+
+import json
+import os
+import re
+import sys
+import tempfile
+import types
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REFERENCE = Path(os.environ.get("MONKI_REFERENCE", "/root/reference"))
+REPO = HERE.parents[1]
+
+
+def reference_package():
+    """Import the reference's pure-Python package with a stand-in for netCDF4."""
+
+    class Variable:
+        def __init__(self, store, name):
+            self.store, self.name = store, name
+
+        def setncatts(self, attributes):
+            self.store.setdefault("_attributes", {})[self.name] = dict(attributes)
+
+        def __setitem__(self, key, value):
+            self.store[self.name] = np.array(value, copy=True)
+
+    class Dataset:
+        written: dict = {}
+
+        def __init__(self, path, mode="r", clobber=True):
+            self.path = Path(path)
+            self.store = {}
+            Dataset.written[str(self.path)] = self.store
+            self.path.write_bytes(b"golden-placeholder")
+
+        def __enter__(self):
+            return self
+
+        def __exit__(self, *args):
+            return False
+
+        def createDimension(self, name, size):
+            self.store.setdefault("_dimensions", {})[name] = size
+
+        def createVariable(self, name, dtype, dimensions):
+            return Variable(self.store, name)
+
+    stub = types.ModuleType("netCDF4")
+    stub.Dataset = Dataset
+    sys.modules["netCDF4"] = stub
+    sys.path.insert(0, str(REFERENCE / "python"))
+    import monki  # the reference package
+    import monki.convergence
+    import monki.execution.metal_tables
+    import monki.simulation
+
+    return monki, Dataset
+
+
+def philox_kat():
+    text = (REFERENCE / "tests/integration/test_metal.py").read_text()
+    words = re.search(r"assert_array_equal\(actual, \[([^\]]+)\]\)", text).group(1)
+    return {
+        "counter": [0, 0, 0, 0],
+        "key": [0, 0],
+        "expected": [int(w.strip(), 16) for w in words.split(",")],
+        "source": "Random123 kat_vectors via tests/integration/test_metal.py:43-59",
+    }
+
+
+def _probe_geometry():
+    text = (REFERENCE / "tests/native/metal_probe.f90").read_text()
+
+    def vector(name):
+        match = re.search(name + r"\s*=\s*\[([^\]]+)\]", text)
+        return [float(v.split("_")[0]) for v in match.group(1).split(",")]
+
+    return vector("incoming"), vector("outgoing"), vector("phi_in"), vector("phi_out"), vector("stokes")
+
+
+def _numpy_probe(depol, uo, u1, phio, phi1, stokes):
+    """L2 F L1 S for Rayleigh scattering, written from the Fortran formulas."""
+
+    eps = 1e-16
+    cs = uo * u1 + np.sqrt(1 - uo * uo) * np.sqrt(1 - u1 * u1) * np.cos(phio - phi1)
+    sin2 = 0.0 if 1 - cs * cs < eps else 1 - cs * cs
+    delta = (1 - depol) / (1 + depol / 2)
+    F = np.zeros((3, 3))
+    F[0, 0] = 0.75 * (1 + cs * cs)
+    F[0, 1] = F[1, 0] = -0.75 * sin2
+    F[1, 1] = 0.75 * (1 + cs * cs)
+    F[2, 2] = 1.5 * cs
+    F *= delta
+    F[0, 0] += 1 - delta
+    F /= 4
+    L = []
+
+    # Meridian rotation angles (general, vertical-incident and vertical-scattered cases).
+    dphi = abs(phio - phi1)
+    rem = dphi % np.pi
+
+    if rem < eps or abs(rem - np.pi) < eps or (abs(uo) > 1 - eps and abs(u1) > 1 - eps):
+        c1 = c2 = 1.0
+        s1 = s2 = 0.0
+    else:
+        sino = 0.0 if 1 - uo * uo < eps else np.sqrt(1 - uo * uo)
+        sin1 = 0.0 if 1 - u1 * u1 < eps else np.sqrt(1 - u1 * u1)
+        wo = np.array([sino * np.cos(phio), sino * np.sin(phio)])
+        w1 = np.array([sin1 * np.cos(phi1), sin1 * np.sin(phi1)])
+        wophi = np.array([np.cos(phio), np.sin(phio)])
+        w1phi = np.array([np.cos(phi1), np.sin(phi1)])
+
+        if abs(u1) > 1 - eps:
+            cosi1 = np.copysign(1.0, u1)
+            cosi2 = -cosi1 * (w1phi @ wophi)
+            q = wo[1] * w1phi[0] - wo[0] * w1phi[1]
+        elif abs(uo) > 1 - eps:
+            cosi2 = np.copysign(1.0, uo)
+            cosi1 = -cosi2 * (w1phi @ wophi)
+            q = wophi[1] * w1[0] - wophi[0] * w1[1]
+        else:
+            cosi1 = (u1 - uo * cs) / np.sqrt(max(eps, (1 - uo * uo) * (1 - cs * cs)))
+            cosi2 = (uo - u1 * cs) / np.sqrt(max(eps, (1 - u1 * u1) * (1 - cs * cs)))
+            q = wo[1] * w1[0] - wo[0] * w1[1]
+
+        sini1 = 0.0 if 1 - cosi1**2 < eps else np.sqrt(1 - cosi1**2) * np.copysign(1.0, q)
+        sini2 = 0.0 if 1 - cosi2**2 < eps else np.sqrt(1 - cosi2**2) * np.copysign(1.0, q)
+        c1, s1 = cosi1**2 - sini1**2, 2 * sini1 * cosi1
+        c2, s2 = cosi2**2 - sini2**2, 2 * sini2 * cosi2
+
+    for c, s in ((c1, s1), (c2, s2)):
+        L.append(np.array([[1, 0, 0], [0, c, -s], [0, s, c]]))
+
+    P = L[1] @ F @ L[0]
+    return P @ np.asarray(stokes)
+
+
+def polarization_probe():
+    uo, u1, phio, phi1, stokes = _probe_geometry()
+    expected = [
+        _numpy_probe(0.03, uo[i], u1[i], phio[i], phi1[i], stokes).tolist() for i in range(3)
+    ]
+    return {
+        "depol": 0.03,
+        "incoming": uo,
+        "outgoing": u1,
+        "phi_in": phio,
+        "phi_out": phi1,
+        "stokes": stokes,
+        "expected": expected,
+        "rtol": 1e-5,
+        "atol": 1e-7,
+        "source": "geometries of tests/native/metal_probe.f90; values from a numpy restatement",
+    }
+
+
+def amf_moments(ref):
+    from monki.convergence import AMFMoments
+    from monki.execution.tallies import BatchControls, RawTallies
+
+    rng = np.random.default_rng(123)
+    weights = rng.uniform(1, 4, (100, 2, 3, 2))
+    paths = weights[:, :, :, None, :] * rng.uniform(1, 5, (100, 2, 3, 5, 2))
+    moments = AMFMoments()
+
+    for index in range(100):
+        moments.add(RawTallies(BatchControls(index + 1, 100), np.zeros((3, 2, 3, 2)), paths[index], weights[index]))
+
+    thickness = np.array([0.5, 2.0, 5.0, 1.0])
+    amf, error = moments.estimate(thickness)
+    return {"paths": paths, "weights": weights, "thickness": thickness, "amf": amf, "error": error}
+
+
+def _v1_stream(varying: bool):
+    """A version-1 stream (one species) for pack_tables, built without the product code."""
+
+    nx, ny = 6, 4
+    levels = np.concatenate([np.arange(0, 10, 0.5), np.arange(10, 30, 2.0), np.arange(30, 60.01, 7.5)])
+    layers = len(levels) - 1
+    nz = layers + 1
+    zunit = np.append(np.diff(levels), 1e-9)
+    tau_gas = 0.7 * (np.exp(-levels[:-1] / 8) - np.exp(-levels[1:] / 8)) / (1 - np.exp(-60 / 8))
+    tau_aer = np.zeros((nx, ny, layers))
+    tau_aer[:, :, :4] = 0.05
+
+    if varying:
+        tau_aer[2:4, 1:3, 2:6] += 3.0  # a box occupying layers 2..5
+
+    ext = np.zeros((2, nx, ny, nz))
+    ext[0, :, :, :layers] = tau_aer / zunit[:layers]
+    ext[1, :, :, :layers] = (tau_gas / zunit[:layers])[None, None, :]
+    beta = ext.sum(0)
+    frac = np.divide(ext, beta[None], out=np.zeros_like(ext), where=beta[None] > 1e-16)
+    n = 181
+    cosines = np.cos(np.deg2rad(np.linspace(180, 0, n)))
+    f11 = 0.51 / (1.49 - 1.4 * cosines) ** 1.5
+    cdf = np.concatenate([[0], np.cumsum(np.diff(cosines) * (f11[1:] + f11[:-1]) / 2)])
+    cdf /= cdf[-1]
+    parts = [
+        [1, nx, ny, nz, 3, 3, 1, nz, nz, nz, 1, 0],
+        [1.0, 1.0, 0.0279, 150.0, 0.0, 40.0],
+        zunit,
+        [0.0, 30.0, 60.0],
+        -np.ones(nx * ny),
+        np.full(nx * ny, 0.05),
+        np.ones(nx * ny),
+        beta.ravel(order="F"),
+        frac.ravel(order="F"),
+        np.ones(nz),
+        [n, 0.92],
+        cosines,
+        cdf,
+        f11,
+        f11,
+        f11,
+        np.zeros(n),
+    ]
+    return np.concatenate([np.asarray(p, dtype=float) for p in parts])
+
+
+def uniform_top(ref):
+    from monki.execution.metal_tables import pack_tables
+
+    cases = {}
+
+    for name, varying in (("uniform", False), ("box", True)):
+        raw = _v1_stream(varying)
+        packed, (nmat, nx, ny, nz, angles) = pack_tables(raw)
+        cases[name] = {
+            "tables": raw.tolist(),
+            "uniform_top": int(packed[15]),
+            "tau_above": packed[-nz:].astype(float).tolist(),
+            "height_above": packed[-2 * nz : -nz].astype(float).tolist(),
+        }
+
+    return cases
+
+
+def driver_statistics(ref, Dataset):
+    from monki import AMFConvergence, simulate
+    from monki.execution.backend import Backend
+    from monki.execution.tallies import RawTallies
+    from monki.output import SimulationResult
+
+    nmat, nx, ny, nz, angles, ppc = 3, 3, 2, 5, 2, 40
+    rng = np.random.default_rng(7)
+    rounds = 64
+    stokes = rng.uniform(0.5, 2.0, (rounds, nmat, nx, ny, angles))
+    stokes[:, 1:] -= 1.25
+    weights = rng.uniform(1.0, 3.0, (rounds, nx, ny, angles))
+    paths = weights[:, :, :, None, :] * rng.uniform(0.5, 4.0, (rounds, nx, ny, nz, angles))
+    alt = np.array([0.0, 500.0, 1500.0, 4000.0, 10000.0])
+    metadata = SimulationResult(
+        Path("scene.nc"),
+        {
+            "alt": alt,
+            "n_rounds": np.array([0], dtype=np.int32),
+            "n_photons_per_column": np.array([0], dtype=np.int32),
+            "AMF_layer": np.zeros((angles, nz - 1, ny, nx, 1)),
+        },
+        {
+            "alt": ("nlev",),
+            "n_rounds": ("single",),
+            "n_photons_per_column": ("single",),
+            "AMF_layer": ("nvza", "nz", "ny", "nx", "nwavs"),
+            "radiance": ("nvza", "ny", "nx", "nmat", "nwavs"),
+            "std_radiance": ("nvza", "ny", "nx", "nmat", "nwavs"),
+            "DOP": ("nvza", "ny", "nx", "nwavs"),
+            "radiance_convergence": ("nrounds", "nmat", "nwavs"),
+        },
+        {},
+    )
+
+    class Fixed(Backend):
+        def __init__(self):
+            self.metadata = None
+            self.provenance = {"backend": "fixed"}
+
+        def prepare(self, scene):
+            self.metadata = metadata
+
+        def run_batch(self, controls):
+            r = controls.round_index - 1
+            return RawTallies(controls, stokes[r].copy(), paths[r].copy(), weights[r].copy())
+
+        def close(self):
+            pass
+
+    Case = type("Case", (), {"photons_per_column": ppc, "rounds": rounds, "backward": False})
+
+    results = {}
+
+    with tempfile.TemporaryDirectory() as tmp:
+        for label, convergence in (("fixed", None), ("amf", AMFConvergence(minimum_rounds=32, check_every=16))):
+            out = Path(tmp) / f"{label}.nc"
+            simulate(Case(), Fixed(), out, convergence=convergence)
+            store = Dataset.written[str(out.resolve())]
+
+            for name in ("radiance", "std_radiance", "DOP", "radiance_convergence", "AMF_layer", "std_AMF_layer"):
+                if name in store:
+                    results[f"{label}_{name}"] = store[name]
+
+    results.update(
+        {
+            "stokes": stokes,
+            "paths": paths,
+            "weights": weights,
+            "alt": alt,
+            "photons_per_column": np.array(ppc),
+        }
+    )
+    return results
+
+
+def main():
+    ref, Dataset = reference_package()
+    (HERE / "philox_kat.json").write_text(json.dumps(philox_kat(), indent=1) + "\n")
+    (HERE / "polarization_probe.json").write_text(json.dumps(polarization_probe(), indent=1) + "\n")
+    np.savez_compressed(HERE / "amf_moments.npz", **amf_moments(ref))
+    (HERE / "uniform_top.json").write_text(json.dumps(uniform_top(ref)) + "\n")
+    np.savez_compressed(HERE / "driver_statistics.npz", **driver_statistics(ref, Dataset))
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()
