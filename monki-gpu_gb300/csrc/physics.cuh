@@ -177,6 +177,10 @@ __device__ __forceinline__ Rot<T> rotation(T cs, T uo, T u1, T phio, T phi1) {
         cosi2 = (uo - u1 * cs) / sqrt(d2 > eps ? d2 : eps);
         q = (sino * spo) * (sin1 * cp1) - (sino * cpo) * (sin1 * sp1);
     }
+    // Near-degenerate geometry can push the rounded cosines past +-1; without the clamp
+    // C = cos^2 would exceed 1 and the rotation would amplify Q and U (in FP32 often).
+    cosi1 = fmin(T(1), fmax(T(-1), cosi1));
+    cosi2 = fmin(T(1), fmax(T(-1), cosi2));
     fac = T(1) - cosi1 * cosi1;
     T sini1 = fac < Tol<T>::eps ? T(0) : sqrt(fac) * fsign(T(1), q);
     fac = T(1) - cosi2 * cosi2;
@@ -237,9 +241,9 @@ __device__ __forceinline__ T sample_cdf(const SceneView<T>& s, int sp, T u) {
 
 // Polarized rejection sampling (forward sign -1). Rayleigh: uniform cosine with the
 // F11(0 deg) bound; particles: bound F11 + |F12| drawn from its CDF. Capped at 4096.
-template <typename T>
+template <typename T, typename Stream>
 __device__ __forceinline__ bool sample_direction(const SceneView<T>& s, int sp, int nmat, const T* st,
-                                                 T cos_in, PhotonStream& rng, T& cos_out, T& dphi,
+                                                 T cos_in, Stream& rng, T& cos_out, T& dphi,
                                                  T& cos_sca) {
     const T pi = pi_v<T>();
     const T bound_gas = rayleigh<T>(T(1), s.depol, 1).f11;

@@ -16,7 +16,7 @@
 #include <string>
 #include <vector>
 
-#include "transport.cuh"
+#include "wavefront.cuh"
 
 namespace monki {
 namespace {
@@ -25,10 +25,13 @@ constexpr double kDegToRad = 0.017453292519943295;
 
 struct Config {
     bool fp64 = false;
+    bool wavefront = true;       // engine=wavefront (default) or engine=megakernel
     uint32_t shards = 8;
     int block = 256;
-    int blocks_per_sm = 0;     // 0 = occupancy-derived
+    int blocks_per_sm = 0;       // 0 = occupancy-derived
     bool uniform_prefix = true;
+    uint32_t pool = 1u << 20;    // wavefront photon slots
+    uint32_t check_every = 8;    // wavefront iterations between host checks
 };
 
 Config parse_config(const char* text) {
@@ -59,6 +62,12 @@ Config parse_config(const char* text) {
         else if (key == "block") c.block = int(as_int(32, 256));
         else if (key == "blocks_per_sm") c.blocks_per_sm = int(as_int(0, 64));
         else if (key == "uniform_prefix") c.uniform_prefix = as_int(0, 1) != 0;
+        else if (key == "engine") {
+            if (value == "wavefront") c.wavefront = true;
+            else if (value == "megakernel") c.wavefront = false;
+            else throw std::runtime_error("engine must be wavefront or megakernel");
+        } else if (key == "pool") c.pool = uint32_t(as_int(1024, 1l << 26));
+        else if (key == "check_every") c.check_every = uint32_t(as_int(1, 1024));
         else throw std::runtime_error("Unknown config key: " + key);
     }
     if (c.block % 32) throw std::runtime_error("block must be a multiple of 32");
@@ -253,7 +262,14 @@ struct Session {
     uint32_t* failure = nullptr;
     unsigned long long* counters = nullptr;
     uint32_t round_capacity = 1;
-    TallyLayout layout{};
+    TallyLayout layout{};       // output layout (and the megakernel's device layout)
+    WaveTally wave{};           // wavefront device layout
+    void* pool_memory = nullptr;
+    Pool<float> pool32{};
+    Pool<double> pool64{};
+    double* flush_info = nullptr;
+    uint32_t* host_counts = nullptr;  // pinned
+    uint64_t iterations = 0;
     SceneView<float> view32{};
     SceneView<double> view64{};
     int grid = 0;
@@ -308,6 +324,32 @@ void upload(Session& s) {
     if constexpr (sizeof(T) == 4) s.view32 = v; else s.view64 = v;
 }
 
+template <typename T>
+Pool<T> allocate_pool(Session& s) {
+    const uint32_t n = s.cfg.pool;
+    const size_t nz = size_t(s.prep.nz);
+    const size_t u32 = size_t(n) * sizeof(uint32_t), tv = size_t(n) * sizeof(T);
+    const size_t bytes = 5 * u32 + align_up(n, 16) + 12 * tv + size_t(n) * nz * sizeof(T) + 3 * u32 + 256;
+    check(cudaMalloc(&s.pool_memory, bytes + 64 * 16), "cudaMalloc(pool)");
+    char* p = static_cast<char*>(s.pool_memory);
+    auto take = [&](size_t b) { char* q = p; p += align_up(b, 256); return q; };
+    Pool<T> P{};
+    P.capacity = n;
+    P.pid = reinterpret_cast<uint32_t*>(take(u32));
+    P.draw = reinterpret_cast<uint32_t*>(take(u32));
+    P.steps = reinterpret_cast<uint32_t*>(take(u32));
+    P.cell = reinterpret_cast<uint32_t*>(take(u32));
+    P.layers = reinterpret_cast<uint32_t*>(take(u32));
+    P.kind = reinterpret_cast<uint8_t*>(take(n));
+    T** fields[] = {&P.x, &P.y, &P.z, &P.a, &P.b, &P.c, &P.phi, &P.q, &P.u, &P.weight, &P.remains, &P.init_part};
+    for (T** f : fields) *f = reinterpret_cast<T*>(take(tv));
+    P.wander = reinterpret_cast<T*>(take(size_t(n) * nz * sizeof(T)));
+    for (int q = 0; q < 3; ++q) P.queue[q] = reinterpret_cast<uint32_t*>(take(u32));
+    P.counts = reinterpret_cast<uint32_t*>(take(16 * sizeof(uint32_t)));
+    if (size_t(p - static_cast<char*>(s.pool_memory)) > bytes + 64 * 16) throw std::runtime_error("pool layout overflow");
+    return P;
+}
+
 template <typename T, int NMAT, bool PATHS>
 const void* kernel_symbol() { return reinterpret_cast<const void*>(&transport_kernel<T, T, NMAT, PATHS>); }
 
@@ -323,6 +365,49 @@ void launch_transport(Session& s, const Controls& c, int grid) {
     else if (nm == 1) transport_kernel<T, T, 1, true><<<grid, s.cfg.block, 0, s.stream>>>(v, c, banks, s.layout, s.failure, s.counters);
     else if (!paths) transport_kernel<T, T, 3, false><<<grid, s.cfg.block, 0, s.stream>>>(v, c, banks, s.layout, s.failure, s.counters);
     else transport_kernel<T, T, 3, true><<<grid, s.cfg.block, 0, s.stream>>>(v, c, banks, s.layout, s.failure, s.counters);
+}
+
+template <typename T, int NMAT, bool PATHS>
+void wave_iteration(Session& s, const SceneView<T>& v, Pool<T>& P, const Controls& c, int grid) {
+    T* banks = static_cast<T*>(s.banks);
+    check(cudaMemsetAsync(P.counts, 0, 3 * sizeof(uint32_t), s.stream), "memset(queues)");
+    wf_transit<T, PATHS><<<grid, s.cfg.block, 0, s.stream>>>(v, c, P, s.failure, s.counters);
+    wf_peel<T, T, NMAT, PATHS><<<grid, s.cfg.block, 0, s.stream>>>(v, c, P, banks, s.wave, s.failure, s.counters);
+    wf_scatter<T, NMAT><<<grid, s.cfg.block, 0, s.stream>>>(v, c, P, s.failure);
+}
+
+template <typename T>
+void run_wavefront(Session& s, const Controls& c) {
+    const SceneView<T>& v = [&]() -> const SceneView<T>& {
+        if constexpr (sizeof(T) == 4) return s.view32; else return s.view64;
+    }();
+    Pool<T> P = [&]() -> Pool<T>& {
+        if constexpr (sizeof(T) == 4) return s.pool32; else return s.pool64;
+    }();
+    // Small groups scan only as many slots as they have photons.
+    P.capacity = uint32_t(std::min<uint64_t>(P.capacity, (uint64_t(c.count) + 255) / 256 * 256));
+    check(cudaMemsetAsync(P.counts, 0, 16 * sizeof(uint32_t), s.stream), "memset(counts)");
+    check(cudaMemsetAsync(P.pid, 0xFF, size_t(P.capacity) * sizeof(uint32_t), s.stream), "memset(pool)");
+    const int grid = s.grid;
+    const int nm = s.prep.nmat;
+    const bool paths = s.prep.paths;
+    const uint64_t limit = uint64_t(c.max_steps) + 16;  // events per photon are bounded by its steps
+    uint64_t it = 0;
+    for (;;) {
+        for (uint32_t b = 0; b < s.cfg.check_every; ++b, ++it) {
+            if (nm == 1 && !paths) wave_iteration<T, 1, false>(s, v, P, c, grid);
+            else if (nm == 1) wave_iteration<T, 1, true>(s, v, P, c, grid);
+            else if (!paths) wave_iteration<T, 3, false>(s, v, P, c, grid);
+            else wave_iteration<T, 3, true>(s, v, P, c, grid);
+        }
+        check(cudaGetLastError(), "wavefront launch");
+        check(cudaMemcpyAsync(s.host_counts, P.counts, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s.stream), "copy(counts)");
+        check(cudaStreamSynchronize(s.stream), "wavefront");
+        const uint32_t* h = s.host_counts;
+        if (h[3] >= c.count && h[0] == 0 && h[1] == 0 && h[2] == 0) break;
+        if (it > limit * 4 + 1024 && it > 1000000) throw std::runtime_error("wavefront did not drain");
+    }
+    s.iterations += it;
 }
 
 template <typename T>
@@ -341,6 +426,8 @@ void destroy(Session* s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     cudaFree(s->scene); cudaFree(s->banks); cudaFree(s->out); cudaFree(s->mu0mu);
     cudaFree(s->failure); cudaFree(s->counters);
+    cudaFree(s->pool_memory); cudaFree(s->flush_info);
+    if (s->host_counts) cudaFreeHost(s->host_counts);
     if (s->t0) cudaEventDestroy(s->t0);
     if (s->t1) cudaEventDestroy(s->t1);
     if (s->t2) cudaEventDestroy(s->t2);
@@ -393,8 +480,18 @@ void* monki_cuda_create(uint32_t device, const double* tables, size_t table_coun
         L.weights = p.paths ? uint32_t(p.nx * p.ny * p.angles) : 0u;
         L.count = L.stokes + L.paths + L.weights;
         L.shards = cfg.shards;
+        const uint32_t pixels = uint32_t(p.nx * p.ny * p.angles);
+        WaveTally& W = s->wave;
+        W.stokes = L.stokes;
+        W.layer = p.paths ? pixels * uint32_t(p.nz) : 0u;
+        W.first = p.paths ? pixels * uint32_t(p.nz + 1) : 0u;
+        W.view = p.paths ? pixels * uint32_t(p.nz) : 0u;
+        W.weights = p.paths ? pixels : 0u;
+        W.count = W.stokes + W.layer + W.first + W.view + W.weights;
+        W.shards = cfg.shards;
         const size_t elem = cfg.fp64 ? sizeof(double) : sizeof(float);
-        const size_t bank_bytes = size_t(round_capacity) * L.shards * L.count * elem;
+        const size_t per_round = cfg.wavefront ? W.count : L.count;
+        const size_t bank_bytes = size_t(round_capacity) * L.shards * per_round * elem;
         check(cudaMalloc(&s->banks, bank_bytes), "cudaMalloc(banks)");
         check(cudaMemset(s->banks, 0, bank_bytes), "cudaMemset(banks)");
         check(cudaMalloc(&s->out, size_t(round_capacity) * L.count * sizeof(double)), "cudaMalloc(out)");
@@ -406,7 +503,34 @@ void* monki_cuda_create(uint32_t device, const double* tables, size_t table_coun
         check(cudaMalloc(&s->failure, sizeof(uint32_t)), "cudaMalloc(failure)");
         check(cudaMalloc(&s->counters, 4 * sizeof(unsigned long long)), "cudaMalloc(counters)");
         if (cfg.fp64) upload<double>(*s); else upload<float>(*s);
-        int per_sm = cfg.blocks_per_sm ? cfg.blocks_per_sm : (cfg.fp64 ? occupancy<double>(*s) : occupancy<float>(*s));
+        if (cfg.wavefront) {
+            if (cfg.fp64) s->pool64 = allocate_pool<double>(*s); else s->pool32 = allocate_pool<float>(*s);
+            std::vector<double> info(size_t(p.nz) + 1 + 2 * size_t(p.angles));
+            for (int z = 0; z < p.nz; ++z) info[size_t(z)] = p.zunit[size_t(z)];
+            // The same direction cosines the kernels use, rounded to transport precision.
+            const double c0 = std::cos(kDegToRad * p.vartheta0);
+            info[size_t(p.nz)] = 1.0 / std::fabs(cfg.fp64 ? c0 : double(float(c0)));
+            for (int ia = 0; ia < p.angles; ++ia) {
+                const double vc = std::cos(kDegToRad * p.vartheta[size_t(ia)]);
+                info[size_t(p.nz) + 1 + ia] = 1.0 / std::fabs(cfg.fp64 ? vc : double(float(vc)));
+                info[size_t(p.nz) + 1 + p.angles + ia] = mu[size_t(ia)];
+            }
+            check(cudaMalloc(&s->flush_info, info.size() * sizeof(double)), "cudaMalloc(flush info)");
+            check(cudaMemcpy(s->flush_info, info.data(), info.size() * sizeof(double), cudaMemcpyHostToDevice), "upload(flush info)");
+            check(cudaMallocHost(&s->host_counts, 16 * sizeof(uint32_t)), "cudaMallocHost(counts)");
+        }
+        int per_sm = cfg.blocks_per_sm;
+        if (!per_sm) {
+            if (cfg.wavefront) {
+                int blocks = 0;
+                const void* fn = cfg.fp64 ? reinterpret_cast<const void*>(&wf_peel<double, double, 3, true>)
+                                          : reinterpret_cast<const void*>(&wf_peel<float, float, 3, true>);
+                check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, cfg.block, 0), "occupancy");
+                per_sm = std::max(blocks, 1);
+            } else {
+                per_sm = cfg.fp64 ? occupancy<double>(*s) : occupancy<float>(*s);
+            }
+        }
         s->grid = prop.multiProcessorCount * per_sm;
         check(cudaDeviceSynchronize(), "create");
         return s;
@@ -431,20 +555,38 @@ int monki_cuda_run(void* handle, const uint32_t controls[8], double* out, char* 
         const int needed = int(std::min<uint64_t>((uint64_t(c.count) + s->cfg.block - 1) / s->cfg.block, uint64_t(s->grid)));
         check(cudaEventRecord(s->t0, s->stream), "event");
         if (c.count) {
-            if (s->cfg.fp64) launch_transport<double>(*s, c, std::max(needed, 1));
-            else launch_transport<float>(*s, c, std::max(needed, 1));
+            if (s->cfg.wavefront) {
+                if (s->cfg.fp64) run_wavefront<double>(*s, c); else run_wavefront<float>(*s, c);
+            } else {
+                if (s->cfg.fp64) launch_transport<double>(*s, c, std::max(needed, 1));
+                else launch_transport<float>(*s, c, std::max(needed, 1));
+            }
             check(cudaGetLastError(), "transport launch");
         }
         check(cudaEventRecord(s->t1, s->stream), "event");
         const uint64_t total = uint64_t(s->layout.count) * c.rounds;
         const int fgrid = int(std::min<uint64_t>((total + 255) / 256, 4096));
-        if (s->cfg.fp64)
-            flush_kernel<double><<<fgrid, 256, 0, s->stream>>>(static_cast<double*>(s->banks), s->layout, s->prep.nmat,
-                s->prep.nx, s->prep.ny, s->prep.nz, s->prep.angles, s->mu0mu, c.rounds, s->out);
-        else
-            flush_kernel<float><<<fgrid, 256, 0, s->stream>>>(static_cast<float*>(s->banks), s->layout, s->prep.nmat,
-                s->prep.nx, s->prep.ny, s->prep.nz, s->prep.angles, s->mu0mu, c.rounds, s->out);
-        check(cudaGetLastError(), "flush launch");
+        const Prepared& p = s->prep;
+        if (s->cfg.wavefront) {
+            if (s->cfg.fp64)
+                wf_flush<double><<<fgrid, 256, 0, s->stream>>>(static_cast<const double*>(s->banks), s->wave, p.nmat,
+                    p.nx, p.ny, p.nz, p.angles, s->flush_info, c.rounds, s->layout.count, p.paths, s->out);
+            else
+                wf_flush<float><<<fgrid, 256, 0, s->stream>>>(static_cast<const float*>(s->banks), s->wave, p.nmat,
+                    p.nx, p.ny, p.nz, p.angles, s->flush_info, c.rounds, s->layout.count, p.paths, s->out);
+            check(cudaGetLastError(), "flush launch");
+            const size_t elem = s->cfg.fp64 ? sizeof(double) : sizeof(float);
+            check(cudaMemsetAsync(s->banks, 0, size_t(c.rounds) * s->wave.shards * s->wave.count * elem, s->stream),
+                  "memset(banks)");
+        } else {
+            if (s->cfg.fp64)
+                flush_kernel<double><<<fgrid, 256, 0, s->stream>>>(static_cast<double*>(s->banks), s->layout, p.nmat,
+                    p.nx, p.ny, p.nz, p.angles, s->mu0mu, c.rounds, s->out);
+            else
+                flush_kernel<float><<<fgrid, 256, 0, s->stream>>>(static_cast<float*>(s->banks), s->layout, p.nmat,
+                    p.nx, p.ny, p.nz, p.angles, s->mu0mu, c.rounds, s->out);
+            check(cudaGetLastError(), "flush launch");
+        }
         check(cudaEventRecord(s->t2, s->stream), "event");
         uint32_t flag = 0;
         unsigned long long cnt[4] = {0, 0, 0, 0};

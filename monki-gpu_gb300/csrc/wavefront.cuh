@@ -1,0 +1,554 @@
+// Wavefront transport for MONKI on sm_103a: photon state lives in a device pool and each
+// stage of a history runs as its own kernel over event queues, so a warp always executes
+// one kind of work.
+//
+//   transit  walks every pooled photon along its free path (ADVANCE, mc.f90:1531-1580)
+//            to its next interaction, draws the species and applies the single-scattering
+//            albedo (mc.f90:1028-1074) or the surface albedo (mc.f90:681-728), and appends
+//            the photon to the surface / gas / particle queue. Slots whose photon escaped or
+//            died claim the next photon of the round group, so the pool stays full.
+//   peel     one thread per (event, view): phase matrix and rotations, optical depth to the
+//            top along the view (calc_radiances_and_paths_pol,
+//            mc_routines_cartesian_mod.f90:849-1222) and the tallies.
+//   scatter  Lambertian reflection (GROUND_LAMB2) or polarized rejection sampling of the
+//            new direction with the Stokes update (mc.f90:1266-1431).
+//
+// Each photon's random stream is addressed by a draw index, so the draw sequence of a
+// history is the same as in one thread (and as in the CPU oracle) however the stages split.
+//
+// Layer-path (AMF) tallies are decomposed exactly: a history's path per layer is the
+// straight initial descent (whole layers above the first event at 1/|mu0|, a partial piece
+// in the first-event layer), then the wandering after it, and each detector ray adds whole
+// layers above the event at 1/mu plus a partial piece. The straight parts are tallied as
+// one weight per (pixel, first layer) and are expanded by a prefix sum in the FP64 flush;
+// only the wandering range is tallied layer by layer.
+#pragma once
+#include "transport.cuh"
+
+namespace monki {
+
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+
+enum Queue : int { kQueueSurface = 0, kQueueGas = 1, kQueueParticle = 2 };
+
+// Device tally layout of one round and one shard for the wavefront engine.
+struct WaveTally {
+    uint32_t stokes;   // nmat * pixels,        [m + nmat * pixel]
+    uint32_t layer;    // pixels * nz,          wandering + partial pieces, [pixel * nz + k]
+    uint32_t first;    // pixels * (nz + 1),    weight by first-event slot k1 + 1
+    uint32_t view;     // pixels * nz,          weight by event layer (detector-ray prefix)
+    uint32_t weights;  // pixels
+    uint32_t count;    // sum of the above
+    uint32_t shards;
+};
+
+template <typename T>
+struct Pool {
+    uint32_t capacity;
+    uint32_t* pid;     // flattened photon identity in the round group, kNone when empty
+    uint32_t* draw;    // index of the next random draw of the photon's stream
+    uint32_t* steps;   // cell visits so far (history step limit)
+    uint32_t* cell;    // i | j << 16
+    uint32_t* layers;  // k + 1 | (k1 + 2) << 8 | wmin << 16 | wmax << 24
+    uint8_t* kind;     // species of the pending event: 0 gas, 1 + s particle s, 255 surface
+    T *x, *y, *z, *a, *b, *c, *phi, *q, *u, *weight, *remains, *init_part;
+    T* wander;         // capacity * nz path lengths after the first event
+    uint32_t* queue[3];
+    uint32_t* counts;  // [0..2] queue sizes, [3] next photon to claim
+};
+
+__device__ __forceinline__ uint32_t pack_layers(int k, int k1, int wmin, int wmax) {
+    return uint32_t(k + 1) | (uint32_t(k1 + 2) << 8) | (uint32_t(wmin) << 16) | (uint32_t(wmax) << 24);
+}
+__device__ __forceinline__ void unpack_layers(uint32_t v, int& k, int& k1, int& wmin, int& wmax) {
+    k = int(v & 0xFF) - 1;
+    k1 = int((v >> 8) & 0xFF) - 2;
+    wmin = int((v >> 16) & 0xFF);
+    wmax = int(v >> 24);
+}
+
+// A photon's Philox stream addressed by draw index: draw d is word d % 4 of block d / 4.
+struct DrawStream {
+    uint32_t photon, round, seed, draw, loaded;
+    uint4 words;
+    __device__ __forceinline__ void init(uint32_t p, uint32_t r, uint32_t s, uint32_t d) {
+        photon = p; round = r; seed = s; draw = d; loaded = kNone;
+    }
+    __device__ __forceinline__ float next() {
+        const uint32_t blk = draw >> 2;
+        if (blk != loaded) {
+            words = philox4x32_10(make_uint4(photon, round, blk, 0u), make_uint2(seed, 0u));
+            loaded = blk;
+        }
+        const uint32_t lane = draw & 3u;
+        const uint32_t w = lane == 0 ? words.x : lane == 1 ? words.y : lane == 2 ? words.z : words.w;
+        ++draw;
+        return (float(w >> 9) + 0.5f) * 0x1p-23f;
+    }
+};
+
+// Reserve `n` consecutive entries of a counter for the lanes that call this together.
+__device__ __forceinline__ uint32_t warp_reserve(uint32_t* counter) {
+    const uint32_t active = __activemask();
+    const int leader = __ffs(active) - 1;
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t base = 0;
+    if (int(lane) == leader) base = atomicAdd(counter, uint32_t(__popc(active)));
+    base = __shfl_sync(active, base, leader);
+    return base + uint32_t(__popc(active & ((1u << lane) - 1u)));
+}
+
+// Add v to the wander entry of layer kk, keeping [wmin, wmax] the only valid range:
+// entries newly covered by the range are zeroed first, so a new photon needs no clearing.
+template <typename T>
+__device__ __forceinline__ void wander_add(T* w, int kk, T v, int& wmin, int& wmax) {
+    if (wmin > wmax) {
+        w[kk] = v;
+        wmin = wmax = kk;
+    } else if (kk > wmax) {
+        for (int q = wmax + 1; q < kk; ++q) w[q] = T(0);
+        w[kk] = v;
+        wmax = kk;
+    } else if (kk < wmin) {
+        for (int q = kk + 1; q < wmin; ++q) w[q] = T(0);
+        w[kk] = v;
+        wmin = kk;
+    } else {
+        w[kk] += v;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void photon_origin(const SceneView<T>& s, const Controls& ctl, uint32_t pid,
+                                              uint32_t& photon, uint32_t& round) {
+    photon = pid % ctl.per_round;
+    round = ctl.first_round + pid / ctl.per_round;
+}
+
+// ----------------------------------------------------------------------------------
+// transit: free path to the next interaction for every pooled photon.
+// ----------------------------------------------------------------------------------
+template <typename T, bool PATHS>
+__global__ void __launch_bounds__(256)
+wf_transit(SceneView<T> s, Controls ctl, Pool<T> P, uint32_t* __restrict__ failure,
+           unsigned long long* __restrict__ counters) {
+    const T eps = Tol<T>::eps;
+    const int top = s.nz - 1;
+    const uint32_t ncol = uint32_t(s.nx * s.ny);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    uint64_t scatters = 0, visits = 0;
+
+    for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < P.capacity; slot += stride) {
+        uint32_t pid = P.pid[slot];
+        DrawStream rng;
+        int i = 0, j = 0, k = 0, k1 = -2, wmin = 255, wmax = 0;
+        T x = 0, y = 0, z = 0, a = 0, b = 0, c = 0, weight = 0, remains = 0, init_part = 0;
+        uint32_t steps = 0;
+        bool fresh = false;
+
+        if (pid != kNone) {
+            uint32_t photon, round;
+            photon_origin(s, ctl, pid, photon, round);
+            rng.init(photon, round, ctl.seed, P.draw[slot]);
+            const uint32_t cell = P.cell[slot];
+            i = int(cell & 0xFFFF); j = int(cell >> 16);
+            unpack_layers(P.layers[slot], k, k1, wmin, wmax);
+            x = P.x[slot]; y = P.y[slot]; z = P.z[slot];
+            a = P.a[slot]; b = P.b[slot]; c = P.c[slot];
+            weight = P.weight[slot]; remains = P.remains[slot];
+            steps = P.steps[slot];
+            if (PATHS) init_part = P.init_part[slot];
+        }
+
+        for (;;) {
+            if (pid == kNone) {
+                // Read first so a drained group stops reserving (the counter never wraps).
+                if (*reinterpret_cast<volatile uint32_t*>(P.counts + 3) >= ctl.count) break;
+                const uint32_t n = warp_reserve(P.counts + 3);
+                if (n >= ctl.count) break;
+                pid = ctl.first + n;
+                uint32_t photon, round;
+                photon_origin(s, ctl, pid, photon, round);
+                rng.init(photon, round, ctl.seed, 0u);
+                const uint32_t column = photon % ncol;
+                i = int(column % uint32_t(s.nx));
+                j = int(column / uint32_t(s.nx));
+                if (j > s.ny - 1) j = s.ny - 1;
+                k = top;
+                x = s.xunit * T(rng.next());
+                y = s.yunit * T(rng.next());
+                z = __ldg(s.zunit + k);
+                a = s.a0; b = s.b0; c = s.c0;
+                weight = T(1);
+                steps = 0;
+                k1 = -2; wmin = 255; wmax = 0; init_part = T(0);
+                remains = -log(fmax(T(rng.next()), eps));
+                fresh = true;
+            }
+            const int is = signbit(a) ? -1 : 1, js = signbit(b) ? -1 : 1, ks = signbit(c) ? -1 : 1;
+            const T aa = fabs(a), ba = fabs(b), ca = fabs(c);
+            const T ai = T(1) / fmax(aa, eps), bi = T(1) / fmax(ba, eps), ci = T(1) / fmax(ca, eps);
+            // Path length of the current layer, added to the wander array on layer change.
+            T* wander = PATHS ? P.wander + size_t(slot) * s.nz : nullptr;
+            int acc_k = -1;
+            T acc = T(0);
+            int outcome = -1;  // 0 atmosphere, 1 surface, 2 escaped, 3 step limit
+            for (;;) {
+                if (++steps > ctl.max_steps) { outcome = 3; break; }
+                ++visits;
+                const T bv = (k < top && k >= 0) ? beta_at(s, i, j, k) : T(0);
+                if (bv > eps) {
+                    const T de = remains / bv;
+                    if (de < x * ai && de < y * bi && de < z * ci) {
+                        x = fmax(T(0), x - aa * de);
+                        y = fmax(T(0), y - ba * de);
+                        z = fmax(T(0), z - ca * de);
+                        if (PATHS && k1 > -2) {
+                            if (acc_k != k) {
+                                if (acc_k >= 0) wander_add(wander, acc_k, acc, wmin, wmax);
+                                acc_k = k; acc = T(0);
+                            }
+                            acc += de;
+                        }
+                        outcome = 0;
+                        break;
+                    }
+                }
+                const int k_old = k;
+                const T dist = advance(s, i, j, k, x, y, z, is, js, ks, aa, ba, ca, ai, bi, ci);
+                if (PATHS && k1 > -2) {
+                    if (acc_k != k_old) {
+                        if (acc_k >= 0) wander_add(wander, acc_k, acc, wmin, wmax);
+                        acc_k = k_old; acc = T(0);
+                    }
+                    acc += dist;
+                }
+                remains -= dist * bv;
+                if (k >= 0 && k <= top) continue;
+                outcome = k > top ? 2 : 1;
+                break;
+            }
+            if (PATHS && acc_k >= 0) wander_add(wander, acc_k, acc, wmin, wmax);
+            if (outcome == 3) { atomicOr(failure, kHistoryCap); pid = kNone; continue; }
+            if (outcome == 2) { pid = kNone; continue; }
+            int kind;
+            if (outcome == 1) {
+                if (PATHS && k1 == -2) { k1 = -1; init_part = T(0); }
+                k = 0;
+                z = T(0);
+                weight *= __ldg(s.albedo + i + s.nx * j);
+                if (weight < eps) { pid = kNone; continue; }
+                kind = 255;
+            } else {
+                if (PATHS && k1 == -2) {
+                    k1 = k;
+                    init_part = (__ldg(s.zunit + k) - z) * ci;
+                }
+                const T rtemp = T(rng.next());
+                int sp = -1;
+                const T* cellp = s.cells + 4 * (i + s.nx * (j + s.ny * k));
+                for (int q = 0; q < s.ntypes; ++q)
+                    if (__ldg(cellp + 1 + q) > rtemp) { sp = q; break; }
+                weight *= sp < 0 ? __ldg(s.ssalb_gas + k) : s.ssalb_aer[sp];
+                if (weight < eps) { pid = kNone; continue; }
+                kind = sp + 1;
+            }
+            ++scatters;
+            const int queue = kind == 255 ? kQueueSurface : (kind == 0 ? kQueueGas : kQueueParticle);
+            const uint32_t at = warp_reserve(P.counts + queue);
+            P.queue[queue][at] = slot;
+            P.kind[slot] = uint8_t(kind);
+            break;
+        }
+
+        if (pid == kNone) {
+            P.pid[slot] = kNone;
+            continue;
+        }
+        if (fresh) P.pid[slot] = pid;
+        P.draw[slot] = rng.draw;
+        P.steps[slot] = steps;
+        P.cell[slot] = uint32_t(i) | (uint32_t(j) << 16);
+        P.layers[slot] = pack_layers(k, k1, wmin, wmax);
+        P.x[slot] = x; P.y[slot] = y; P.z[slot] = z;
+        P.weight[slot] = weight;
+        P.remains[slot] = remains;
+        if (fresh) {
+            P.a[slot] = a; P.b[slot] = b; P.c[slot] = c;
+            P.phi[slot] = s.phi0; P.q[slot] = T(0); P.u[slot] = T(0);
+        }
+        if (PATHS) P.init_part[slot] = init_part;
+    }
+
+    unsigned long long v0 = scatters, v1 = visits;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        v0 += __shfl_down_sync(0xffffffffu, v0, off);
+        v1 += __shfl_down_sync(0xffffffffu, v1, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(counters + 0, v0);
+        atomicAdd(counters + 1, v1);
+    }
+}
+
+// ----------------------------------------------------------------------------------
+// peel: one (event, view) pair per thread.
+// ----------------------------------------------------------------------------------
+template <typename T, typename TA, int NMAT, bool PATHS>
+__global__ void __launch_bounds__(256)
+wf_peel(SceneView<T> s, Controls ctl, Pool<T> P, TA* __restrict__ banks, WaveTally L,
+        uint32_t* __restrict__ failure, unsigned long long* __restrict__ counters) {
+    const T eps = Tol<T>::eps;
+    const int top = s.nz - 1;
+    const uint32_t ns = P.counts[0], ng = P.counts[1], np = P.counts[2];
+    const uint32_t views = uint32_t(s.angles);
+    const uint64_t total = uint64_t(ns + ng + np) * views;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint64_t visits = 0, updates = 0;
+
+    for (uint64_t t = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; t < total;
+         t += uint64_t(gridDim.x) * blockDim.x) {
+        const uint32_t e = uint32_t(t / views);
+        const int ia = int(t % views);
+        uint32_t slot;
+        bool surface = false;
+        if (e < ns) { slot = P.queue[kQueueSurface][e]; surface = true; }
+        else if (e < ns + ng) slot = P.queue[kQueueGas][e - ns];
+        else slot = P.queue[kQueueParticle][e - ns - ng];
+
+        const uint32_t pid = P.pid[slot];
+        const uint32_t cell = P.cell[slot];
+        const int i = int(cell & 0xFFFF), j = int(cell >> 16);
+        int k, k1, wmin, wmax;
+        unpack_layers(P.layers[slot], k, k1, wmin, wmax);
+        const T x = P.x[slot], y = P.y[slot], z = P.z[slot];
+        const T a = P.a[slot], b = P.b[slot], c = P.c[slot];
+        const T weight = P.weight[slot];
+        T prob[3] = {T(0), T(0), T(0)};
+        const T vc = s.vc[ia];
+        if (surface) {
+            prob[0] = vc > T(0) ? vc * weight : T(0);
+        } else {
+            const int sp = int(P.kind[slot]) - 1;
+            const T phi = P.phi[slot];
+            const T st[3] = {T(1), P.q[slot], P.u[slot]};
+            const T cs = c * vc + sqrt(fmax(eps, T(1) - c * c)) * sqrt(fmax(eps, T(1) - vc * vc)) *
+                                     cos(phi - s.vphi[ia]);
+            const Rot<T> r = NMAT > 1 ? rotation<T>(cs, c, vc, phi, s.vphi[ia]) : Rot<T>{T(1), T(0), T(1), T(0)};
+            const Phase<T> f = phase<T>(s, sp, cs, NMAT);
+            T back[3];
+            scatter_stokes<T>(f, r, NMAT, st, back);
+            for (int m = 0; m < NMAT; ++m) prob[m] = back[m] * weight;
+            if (prob[0] < Tol<T>::negligible) for (int m = 0; m < NMAT; ++m) prob[m] = T(0);
+        }
+        bool finite = true;
+        for (int m = 0; m < NMAT; ++m) finite = finite && isfinite(prob[m]);
+        if (!finite) { atomicOr(failure, kNonfinite); continue; }
+        if (!(prob[0] > eps)) continue;
+
+        // Detector ray (as detector() in transport.cuh) with the decomposed path tallies.
+        const T va = s.va[ia], vb = s.vb[ia];
+        T rx = x, ry = y, rz = z;
+        if (va * a < T(0)) rx = fmax(T(0), s.xunit - rx);
+        if (vb * b < T(0)) ry = fmax(T(0), s.yunit - ry);
+        if (vc * c < T(0)) rz = fmax(T(0), __ldg(s.zunit + k) - rz);
+        const int is = signbit(va) ? -1 : 1, js = signbit(vb) ? -1 : 1, ks = signbit(vc) ? -1 : 1;
+        const T aa = fabs(va), ba = fabs(vb), ca = fabs(vc);
+        const T ai = T(1) / fmax(aa, eps), bi = T(1) / fmax(ba, eps), ci = T(1) / fmax(ca, eps);
+        const T x_old = rx, y_old = ry, z_old = rz;
+        T tau = T(0);
+        int ri = i, rj = j, rk = k;
+        uint32_t rsteps = 0;
+        bool capped = false;
+        while (rk >= 0 && rk < top) {
+            if (rk >= s.uniform_top) {
+                tau += (rz * beta_at(s, ri, rj, rk) + __ldg(s.tau_above + rk)) * ci;
+                ++visits;
+                break;
+            }
+            if (++rsteps > ctl.max_steps) { capped = true; break; }
+            const T bv = beta_at(s, ri, rj, rk);
+            const T dist = advance(s, ri, rj, rk, rx, ry, rz, is, js, ks, aa, ba, ca, ai, bi, ci);
+            tau += dist * bv;
+            ++visits;
+        }
+        if (capped) { atomicOr(failure, kDetectorCap); continue; }
+        T height = __ldg(s.zsum + k) + (ks > 0 ? __ldg(s.zunit + k) - z_old : z_old);
+        height = __ldg(s.zsum + top) - height;
+        const T dxp = aa * height / ca, dyp = ba * height / ca;
+        const int di = int(((s.xunit - x_old) + dxp) / s.xunit);
+        const int dj = int(((s.yunit - y_old) + dyp) / s.yunit);
+        int pi_ = (i + is * (di % s.nx)) % s.nx; pi_ = pi_ < 0 ? pi_ + s.nx : pi_;
+        int pj_ = (j + js * (dj % s.ny)) % s.ny; pj_ = pj_ < 0 ? pj_ + s.ny : pj_;
+        const uint32_t pixel = uint32_t(pi_ + s.nx * (pj_ + s.ny * ia));
+        const T att = exp(-tau);
+        const uint32_t round_offset = pid / ctl.per_round;
+        TA* bank = banks + (size_t(round_offset) * L.shards + (warp % L.shards)) * L.count;
+#pragma unroll
+        for (int m = 0; m < NMAT; ++m) tally_add(bank + NMAT * pixel + m, TA(prob[m] * att));
+        updates += NMAT;
+        if (PATHS) {
+            const T w = prob[0] * att;
+            TA* layer = bank + L.stokes + size_t(pixel) * s.nz;
+            TA* first = bank + L.stokes + L.layer + size_t(pixel) * (s.nz + 1);
+            TA* view = bank + L.stokes + L.layer + L.first + size_t(pixel) * s.nz;
+            const T* wander = P.wander + size_t(slot) * s.nz;
+            for (int kk = wmin; kk <= wmax; ++kk) {
+                const T v = w * wander[kk];
+                if (v != T(0)) { tally_add(layer + kk, TA(v)); ++updates; }
+            }
+            tally_add(first + (k1 + 1), TA(w));
+            if (k1 >= 0) tally_add(layer + k1, TA(w * P.init_part[slot]));
+            tally_add(view + k, TA(w));
+            tally_add(layer + k, TA(w * z_old * ci));
+            tally_add(bank + L.stokes + L.layer + L.first + L.view + pixel, TA(w));
+            updates += 5;
+        }
+    }
+    unsigned long long v2 = visits, v3 = updates;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        v2 += __shfl_down_sync(0xffffffffu, v2, off);
+        v3 += __shfl_down_sync(0xffffffffu, v3, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(counters + 2, v2);
+        atomicAdd(counters + 3, v3);
+    }
+}
+
+// ----------------------------------------------------------------------------------
+// scatter: new direction (and Stokes vector) for every queued event.
+// ----------------------------------------------------------------------------------
+template <typename T, int NMAT>
+__global__ void __launch_bounds__(256)
+wf_scatter(SceneView<T> s, Controls ctl, Pool<T> P, uint32_t* __restrict__ failure) {
+    const T eps = Tol<T>::eps;
+    const T pi = pi_v<T>();
+    const uint32_t ns = P.counts[0], ng = P.counts[1], np = P.counts[2];
+    const uint32_t total = ns + ng + np;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        uint32_t slot;
+        bool surface = false;
+        if (e < ns) { slot = P.queue[kQueueSurface][e]; surface = true; }
+        else if (e < ns + ng) slot = P.queue[kQueueGas][e - ns];
+        else slot = P.queue[kQueueParticle][e - ns - ng];
+        const uint32_t pid = P.pid[slot];
+        uint32_t photon, round;
+        photon_origin(s, ctl, pid, photon, round);
+        DrawStream rng;
+        rng.init(photon, round, ctl.seed, P.draw[slot]);
+        const T a0 = P.a[slot], b0 = P.b[slot], c0 = P.c[slot];
+        T a, b, c, phi_out, q = T(0), u = T(0);
+        bool fresh_path = false;
+        if (surface) {
+            const T Pd = T(rng.next()), U = T(rng.next());
+            const T mu = sqrt(Pd);
+            phi_out = T(2) * pi * U;
+            const T sine = sqrt(fmax(T(0), T(1) - mu * mu));
+            T sp, cp;
+            sincos(phi_out, &sp, &cp);
+            a = sine * cp; b = sine * sp; c = fabs(mu);
+        } else {
+            const int sp = int(P.kind[slot]) - 1;
+            const T phi = P.phi[slot];
+            T st[3] = {T(1), P.q[slot], P.u[slot]};
+            T cos_out, dphi, cos_sca;
+            if (!sample_direction<T>(s, sp, NMAT, st, c0, rng, cos_out, dphi, cos_sca)) {
+                atomicOr(failure, kSamplingCap);
+                P.pid[slot] = kNone;
+                continue;
+            }
+            phi_out = phi + dphi;
+            const Rot<T> r = NMAT > 1 ? rotation<T>(cos_sca, c0, cos_out, phi, phi_out) : Rot<T>{T(1), T(0), T(1), T(0)};
+            const Phase<T> f = phase<T>(s, sp, cos_sca, NMAT);
+            T ns_[3];
+            scatter_stokes<T>(f, r, NMAT, st, ns_);
+            // S / S(1): I becomes 1 (NaN when S(1) is 0 or not finite).
+            const T s0 = ns_[0];
+            const T one = s0 / s0;
+            bool ok = isfinite(one);
+            if (NMAT > 1) {
+                q = ns_[1] / s0; u = ns_[2] / s0;
+                ok = ok && isfinite(q) && isfinite(u) && sqrt(q * q + u * u) <= one + T(1e-2);
+            }
+            if (!ok) { atomicOr(failure, kInvalidStokes); P.pid[slot] = kNone; continue; }
+            const T so = sqrt(fmax(T(0), T(1) - cos_out * cos_out));
+            T spo, cpo;
+            sincos(phi_out, &spo, &cpo);
+            a = cpo * so; b = spo * so; c = cos_out;
+            fresh_path = true;
+        }
+        T x = P.x[slot], y = P.y[slot], z = P.z[slot];
+        if (a * a0 < T(0)) x = fmax(T(0), s.xunit - x);
+        if (b * b0 < T(0)) y = fmax(T(0), s.yunit - y);
+        if (c * c0 < T(0)) {
+            int k, k1, wmin, wmax;
+            unpack_layers(P.layers[slot], k, k1, wmin, wmax);
+            z = fmax(T(0), __ldg(s.zunit + k) - z);
+        }
+        P.x[slot] = x; P.y[slot] = y; P.z[slot] = z;
+        P.a[slot] = a; P.b[slot] = b; P.c[slot] = c;
+        P.phi[slot] = phi_out;
+        P.q[slot] = q; P.u[slot] = u;
+        if (fresh_path) P.remains[slot] = -log(fmax(T(rng.next()), eps));
+        P.draw[slot] = rng.draw;
+    }
+}
+
+// ----------------------------------------------------------------------------------
+// FP64 flush of the wavefront tallies into RawTallies order, with the prefix sums of
+// the straight initial-descent and detector-ray layers. info: zunit[nz] (km),
+// 1/|mu0|, then 1/mu per view, then mu0/mu per view.
+// ----------------------------------------------------------------------------------
+template <typename TA>
+__global__ void wf_flush(const TA* __restrict__ banks, WaveTally L, int nmat, int nx, int ny, int nz, int angles,
+                         const double* __restrict__ info, uint32_t rounds, uint32_t out_count, bool paths,
+                         double* __restrict__ out) {
+    const uint32_t pixels = uint32_t(nx * ny * angles);
+    const uint32_t stokes_out = uint32_t(nmat) * pixels;
+    const uint64_t total = uint64_t(out_count) * rounds;
+    const double* zunit = info;
+    const double inv_mu0 = info[nz];
+    const double* inv_mu = info + nz + 1;
+    const double* mu0mu = info + nz + 1 + angles;
+    for (uint64_t e = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; e < total; e += uint64_t(gridDim.x) * blockDim.x) {
+        const uint32_t r = uint32_t(e / out_count);
+        const uint32_t o = uint32_t(e % out_count);
+        const TA* base = banks + size_t(r) * L.shards * L.count;
+        auto sum = [&](uint32_t index) {
+            double acc = 0.0;
+            for (uint32_t sh = 0; sh < L.shards; ++sh) acc += double(base[size_t(sh) * L.count + index]);
+            return acc;
+        };
+        double value;
+        if (o < stokes_out) {
+            const uint32_t ia = o / uint32_t(nmat * nx * ny);
+            value = sum(o) * mu0mu[ia];
+        } else if (paths && o < stokes_out + pixels * uint32_t(nz)) {
+            const uint32_t q = o - stokes_out;  // i + nx * (j + ny * (k + nz * ia))
+            const uint32_t i = q % nx;
+            uint32_t t = q / nx;
+            const uint32_t j = t % ny; t /= ny;
+            const int k = int(t % nz);
+            const uint32_t ia = t / nz;
+            const uint32_t pixel = i + nx * (j + ny * ia);
+            value = sum(L.stokes + pixel * nz + k);
+            double first = 0.0;
+            for (int s = 0; s <= k; ++s) first += sum(L.stokes + L.layer + pixel * (nz + 1) + s);
+            value += zunit[k] * inv_mu0 * first;
+            if (k < nz - 1) {
+                double view = 0.0;
+                for (int s = 0; s < k; ++s) view += sum(L.stokes + L.layer + L.first + pixel * nz + s);
+                value += zunit[k] * inv_mu[ia] * view;
+            }
+        } else {
+            const uint32_t pixel = o - stokes_out - pixels * uint32_t(nz);
+            value = sum(L.stokes + L.layer + L.first + L.view + pixel);
+        }
+        out[e] = value;
+    }
+}
+
+}  // namespace monki

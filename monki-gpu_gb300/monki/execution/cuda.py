@@ -44,6 +44,8 @@ class CUDA(Backend):
         max_steps: int = 100_000,
         precision: str = "fp32",
         block: int = 256,
+        engine: str = "wavefront",
+        pool: int = 1 << 20,
         library=None,
     ):
         for name, value, minimum, maximum in (
@@ -69,6 +71,12 @@ class CUDA(Backend):
         if block % 32:
             raise ValueError("block must be a multiple of 32")
 
+        if engine not in ("wavefront", "megakernel"):
+            raise ValueError("engine must be 'wavefront' or 'megakernel'")
+
+        if type(pool) is not int or not 1024 <= pool <= 1 << 26:
+            raise ValueError("pool must be an integer in [1024, 2**26]")
+
         self.device = device
         self.save_path = save_path
         self.profile = profile
@@ -78,6 +86,8 @@ class CUDA(Backend):
         self.max_steps = max_steps
         self.precision = precision
         self.block = block
+        self.engine = engine
+        self.pool = pool
         self.library = library or _native.LIBRARY
         self.metadata = None
         self.provenance: dict = {}
@@ -131,7 +141,10 @@ class CUDA(Backend):
         )
         native = _native.load(self.library)
         error = ctypes.create_string_buffer(8192)
-        config = f"precision={self.precision},shards={self.tally_shards},block={self.block}".encode()
+        config = (
+            f"precision={self.precision},shards={self.tally_shards},block={self.block},"
+            f"engine={self.engine},pool={self.pool}"
+        ).encode()
         handle = native.monki_cuda_create(
             self.device,
             tables.ctypes.data_as(_native.F64P),
@@ -175,6 +188,8 @@ class CUDA(Backend):
             "round_capacity": capacity,
             "max_steps": self.max_steps,
             "block": self.block,
+            "engine": self.engine,
+            "pool": self.pool,
             "library_sha256": hashlib.sha256(open(self.library, "rb").read()).hexdigest(),
             "tables_sha256": hashlib.sha256(tables.tobytes()).hexdigest(),
             "machine": platform.machine(),
@@ -236,6 +251,8 @@ class CUDA(Backend):
             self.tally_shards,
             self.precision,
             self.block,
+            self.engine,
+            self.pool,
         )
 
     def _validate_requests(self, controls: list) -> None:

@@ -112,6 +112,8 @@ def test_backend_is_abstract_and_closes_on_failure():
         {"precision": "bf16"},
         {"block": 48},
         {"device": -1},
+        {"engine": "triton"},
+        {"pool": 10},
     ],
 )
 def test_invalid_settings_fail_before_any_device_work(settings):

@@ -92,10 +92,10 @@ def _controls(scene, rounds, seed, first_round=1):
     return [per_round * rounds, 0, first_round, seed, 100000, 0, per_round, rounds]
 
 
-def _gpu_rounds(scene, rounds, seed, precision):
+def _gpu_rounds(scene, rounds, seed, precision, **kw):
     from monki.execution import BatchControls
 
-    with _session(scene, precision, seed=seed) as backend:
+    with _session(scene, precision, seed=seed, **kw) as backend:
         batches = backend.run_batches([BatchControls(i, scene.photons_per_column) for i in range(1, rounds + 1)])
         return batches, dict(backend.provenance)
 
@@ -107,13 +107,14 @@ def _flat(batch):
     return np.concatenate(parts)
 
 
+@pytest.mark.parametrize("engine", ["wavefront", "megakernel"])
 @pytest.mark.parametrize("name", ["clear_sky", "layered_cloud", "box_cloud"])
-def test_fp64_transport_reproduces_oracle_histories(oracle, device, name):
+def test_fp64_transport_reproduces_oracle_histories(oracle, device, name, engine):
     import monki.scenes as scenes
 
     builder = getattr(scenes, name)
     scene = builder(8, 2, nx=10, ny=8) if name != "box_cloud" else builder(8, 2, nx=12, ny=10, box_x=(3, 8), box_y=(2, 6))
-    batches, provenance = _gpu_rounds(scene, 2, 23274, "fp64")
+    batches, provenance = _gpu_rounds(scene, 2, 23274, "fp64", engine=engine)
     expected, counters = oracle.run(scene.tables, _controls(scene, 2, 23274), 8)
     actual = np.stack([_flat(b) for b in batches])
     assert provenance["scatters"] == counters["scatters"]
@@ -137,7 +138,8 @@ def test_fp32_transport_agrees_with_oracle_within_combined_se(oracle, device, na
 
     builder = getattr(scenes, name)
     rounds = 32
-    scene = builder(10, rounds, nx=10, ny=8) if name != "box_cloud" else builder(10, rounds, nx=12, ny=10, box_x=(3, 8), box_y=(2, 6))
+    # Full 30 x 20 grids: the mean-z criterion needs many (nearly independent) pixels.
+    scene = builder(12, rounds)
     batches, _ = _gpu_rounds(scene, rounds, 881, "fp32")
     gpu = np.stack([_flat(b) for b in batches])
     cpu, _ = oracle.run(scene.tables, _controls(scene, rounds, 23274), 16)
@@ -153,7 +155,7 @@ def test_dispatch_chunking_and_shards_preserve_streams(device):
     scene = scenes.layered_cloud(6, 1, nx=8, ny=6)
     results = []
 
-    for settings in ({"photons_per_dispatch": 97, "tally_shards": 1}, {"tally_shards": 32}):
+    for settings in ({"photons_per_dispatch": 97, "tally_shards": 1}, {"tally_shards": 32, "pool": 1024}):
         with _session(scene, "fp64", **settings) as backend:
             results.append(backend.run_batch(BatchControls(1, 6)))
 
