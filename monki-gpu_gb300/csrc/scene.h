@@ -31,6 +31,7 @@ enum Failure : uint32_t {
     kSamplingCap = 4u,
     kInvalidStokes = 8u,
     kHistoryCap = 16u,
+    kQueueCorrupt = 32u,  // a queue entry outside the photon pool (internal error)
 };
 
 template <typename T>

@@ -87,15 +87,17 @@ struct DrawStream {
     }
 };
 
-// Reserve `n` consecutive entries of a counter for the lanes that call this together.
-__device__ __forceinline__ uint32_t warp_reserve(uint32_t* counter) {
+// Reserve one entry of counters[key] per calling lane. Lanes that arrive together are
+// grouped by key, so each counter advances only by the lanes that write to its queue.
+__device__ __forceinline__ uint32_t warp_reserve(uint32_t* counters, int key = 0) {
     const uint32_t active = __activemask();
-    const int leader = __ffs(active) - 1;
+    const uint32_t group = __match_any_sync(active, key);
+    const int leader = __ffs(group) - 1;
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t base = 0;
-    if (int(lane) == leader) base = atomicAdd(counter, uint32_t(__popc(active)));
-    base = __shfl_sync(active, base, leader);
-    return base + uint32_t(__popc(active & ((1u << lane) - 1u)));
+    if (int(lane) == leader) base = atomicAdd(counters + key, uint32_t(__popc(group)));
+    base = __shfl_sync(group, base, leader);
+    return base + uint32_t(__popc(group & ((1u << lane) - 1u)));
 }
 
 // Add v to the wander entry of layer kk, keeping [wmin, wmax] the only valid range:
@@ -255,7 +257,7 @@ wf_transit(SceneView<T> s, Controls ctl, Pool<T> P, uint32_t* __restrict__ failu
             }
             ++scatters;
             const int queue = kind == 255 ? kQueueSurface : (kind == 0 ? kQueueGas : kQueueParticle);
-            const uint32_t at = warp_reserve(P.counts + queue);
+            const uint32_t at = warp_reserve(P.counts, queue);
             P.queue[queue][at] = slot;
             P.kind[slot] = uint8_t(kind);
             break;
@@ -316,8 +318,10 @@ wf_peel(SceneView<T> s, Controls ctl, Pool<T> P, TA* __restrict__ banks, WaveTal
         if (e < ns) { slot = P.queue[kQueueSurface][e]; surface = true; }
         else if (e < ns + ng) slot = P.queue[kQueueGas][e - ns];
         else slot = P.queue[kQueueParticle][e - ns - ng];
+        if (slot >= P.capacity) { atomicOr(failure, kQueueCorrupt); continue; }
 
         const uint32_t pid = P.pid[slot];
+        if (pid == kNone) { atomicOr(failure, kQueueCorrupt); continue; }
         const uint32_t cell = P.cell[slot];
         const int i = int(cell & 0xFFFF), j = int(cell >> 16);
         int k, k1, wmin, wmax;
@@ -434,7 +438,9 @@ wf_scatter(SceneView<T> s, Controls ctl, Pool<T> P, uint32_t* __restrict__ failu
         if (e < ns) { slot = P.queue[kQueueSurface][e]; surface = true; }
         else if (e < ns + ng) slot = P.queue[kQueueGas][e - ns];
         else slot = P.queue[kQueueParticle][e - ns - ng];
+        if (slot >= P.capacity) { atomicOr(failure, kQueueCorrupt); continue; }
         const uint32_t pid = P.pid[slot];
+        if (pid == kNone) { atomicOr(failure, kQueueCorrupt); continue; }
         uint32_t photon, round;
         photon_origin(s, ctl, pid, photon, round);
         DrawStream rng;
