@@ -278,8 +278,8 @@ def main():
     out = np.zeros(tally_count)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
     timing = (ctypes.c_float * 2)()
-    counters_before = (ctypes.c_uint64 * 5)()
-    counters_after = (ctypes.c_uint64 * 5)()
+    counters_before = (ctypes.c_uint64 * 6)()
+    counters_after = (ctypes.c_uint64 * 6)()
 
     def step(index):
         # Ranks run disjoint rounds: round = rank * steps_total + index + 1.
@@ -315,7 +315,7 @@ def main():
 
     native.monki_cuda_counters(handle, counters_after)
     delta = [int(a) - int(b) for a, b in zip(counters_after, counters_before, strict=True)]
-    scatters, visits_fp, visits_det, updates, photons = delta
+    scatters, visits_fp, visits_det, updates, photons, launches = delta
     device_seconds = sum(run_ms) / 1e3
 
     if world > 1:
@@ -346,7 +346,7 @@ def main():
         backend.prepare(e2e_scene)
         batches = backend.run_batches([BatchControls(i, ppc) for i in range(1, args.steps + 1)])
         e2e_scatters = backend.provenance["scatters"]
-        dispatches = backend.provenance["gpu_dispatches"]
+        e2e_launches = backend.provenance["kernel_launches"]
 
     wall_e2e = time.perf_counter() - wall_e2e
     assert len(batches) == args.steps
@@ -400,8 +400,8 @@ def main():
             "wall_s": wall_e2e,
             "note": "CUDA.prepare (table upload) + run_batches of all steps, tallies copied to host",
         },
-        "gpu_launches": 2 * args.steps,
-        "e2e_gpu_launches": 2 * dispatches,
+        "gpu_launches": launches,
+        "e2e_gpu_launches": e2e_launches,
         "clocks": clocks.summary(),
     }
 

@@ -55,9 +55,9 @@ double monki_cuda_gpu_seconds(void *session);
  * counterpart. */
 int monki_cuda_last_timing(void *session, float out[2]);
 
-/* Session totals: scatters, free-path cell visits, detector cell visits, tally updates,
- * photons. No reference counterpart (the scatter count is mc.f90's nscat). */
-int monki_cuda_counters(void *session, uint64_t out[5]);
+/* Session totals: scatters, free-path walk steps, detector cell visits, tally updates,
+ * photons, kernel launches. No reference counterpart (the scatter count is mc.f90's nscat). */
+int monki_cuda_counters(void *session, uint64_t out[6]);
 
 /* Number of float64 values per round in a run's output; no reference counterpart. */
 size_t monki_cuda_tally_count(void *session);

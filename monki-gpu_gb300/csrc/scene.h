@@ -11,6 +11,9 @@
 //   zunit[nz], zsum[nz + 1]  layer thickness and its running sum from the surface
 //   ssalb_gas[nz], albedo[nx * ny]
 //   tau_above[nz]            optical depth of the horizontally uniform layers above k
+//   layer_beta[nz]           extinction of a horizontally uniform layer, -1 where it varies
+//   vprefix[nz + 1]          vertical optical depth of the uniform layers below each level
+//   run_lo[nz], run_hi[nz]   first / last layer of the uniform run containing k (ints)
 //   lut_f[4 * n]             {F11, F22, F33, F12} per scattering angle, per species
 //   lut_cos[n], lut_cdf[n]   ascending cosine grid and the bound-function CDF
 //   guide[kGuide + 1]        CDF guide table: largest i with cdf[i] <= g / kGuide
@@ -48,6 +51,10 @@ struct SceneView {
     const T* ssalb_gas;
     const T* albedo;
     const T* tau_above;
+    const T* layer_beta;
+    const T* vprefix;
+    const int* run_lo;
+    const int* run_hi;
     const T* lut_f[kMaxSpecies];
     const T* lut_cos[kMaxSpecies];
     const T* lut_cdf[kMaxSpecies];

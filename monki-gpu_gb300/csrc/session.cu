@@ -32,6 +32,7 @@ struct Config {
     bool uniform_prefix = true;
     uint32_t pool = 1u << 20;    // wavefront photon slots
     uint32_t check_every = 8;    // wavefront iterations between host checks
+    uint32_t walk = 24;          // walk steps per photon per transit launch
 };
 
 Config parse_config(const char* text) {
@@ -68,6 +69,7 @@ Config parse_config(const char* text) {
             else throw std::runtime_error("engine must be wavefront or megakernel");
         } else if (key == "pool") c.pool = uint32_t(as_int(1024, 1l << 26));
         else if (key == "check_every") c.check_every = uint32_t(as_int(1, 1024));
+        else if (key == "walk") c.walk = uint32_t(as_int(1, 1 << 20));
         else throw std::runtime_error("Unknown config key: " + key);
     }
     if (c.block % 32) throw std::runtime_error("block must be a multiple of 32");
@@ -173,7 +175,7 @@ template <typename T>
 struct Packed {
     std::vector<T> values;
     std::vector<int> guides;
-    size_t cells, zunit, zsum, ssalb_gas, albedo, tau_above;
+    size_t cells, zunit, zsum, ssalb_gas, albedo, tau_above, layer_beta, vprefix, run_lo, run_hi;
     size_t lut_f[kMaxSpecies], lut_cos[kMaxSpecies], lut_cdf[kMaxSpecies], guide[kMaxSpecies];
     int uniform_top;
 };
@@ -226,6 +228,38 @@ Packed<T> pack(const Prepared& p, bool uniform_prefix) {
             v[k.tau_above + z] = acc;
         }
     }
+    // Horizontally uniform layers (equal extinction in every cell at transport precision)
+    // and the runs of consecutive uniform layers; the vacuum layer is uniform and clear.
+    k.layer_beta = reserve(p.nz);
+    k.vprefix = reserve(p.nz + 1);
+    std::vector<bool> uniform(size_t(p.nz), true);
+    for (int z = 0; z < p.nz - 1; ++z) {
+        T b0 = T(p.beta[size_t(z) * cols]);
+        for (size_t c = 1; c < cols && uniform[size_t(z)]; ++c)
+            if (T(p.beta[size_t(z) * cols + c]) != b0) uniform[size_t(z)] = false;
+        v[k.layer_beta + z] = uniform[size_t(z)] ? b0 : T(-1);
+    }
+    v[k.layer_beta + p.nz - 1] = T(0);
+    {
+        T acc = T(0);
+        v[k.vprefix] = T(0);
+        for (int z = 0; z < p.nz; ++z) {
+            if (uniform[size_t(z)]) acc += T(v[k.layer_beta + z]) * T(p.zunit[size_t(z)]);
+            v[k.vprefix + z + 1] = acc;
+        }
+    }
+    k.run_lo = k.guides.size();
+    for (int z = 0; z < p.nz; ++z) {
+        int lo = z;
+        while (uniform[size_t(z)] && lo > 0 && uniform[size_t(lo - 1)]) --lo;
+        k.guides.push_back(lo);
+    }
+    k.run_hi = k.guides.size();
+    for (int z = 0; z < p.nz; ++z) {
+        int hi = z;
+        while (uniform[size_t(z)] && hi < p.nz - 1 && uniform[size_t(hi + 1)]) ++hi;
+        k.guides.push_back(hi);
+    }
     for (int s = 0; s < p.ntypes; ++s) {
         const auto& l = p.luts[s];
         k.lut_f[s] = reserve(4 * size_t(l.n));
@@ -274,8 +308,9 @@ struct Session {
     SceneView<double> view64{};
     int grid = 0;
     double gpu_seconds = 0.0;
-    // scatters, free-path cell visits, detector cell visits, tally updates, photons
-    uint64_t totals[5] = {0, 0, 0, 0, 0};
+    // scatters, free-path cell visits, detector cell visits, tally updates, photons,
+    // kernel launches
+    uint64_t totals[6] = {0, 0, 0, 0, 0, 0};
     float last_kernel_ms = 0.f;   // transport kernel
     float last_run_ms = 0.f;      // transport kernel + FP64 flush
     std::string name;
@@ -303,6 +338,8 @@ SceneView<T> make_view(const Prepared& p, const Packed<T>& k, void* base) {
     }
     s.cells = tv + k.cells; s.zunit = tv + k.zunit; s.zsum = tv + k.zsum; s.ssalb_gas = tv + k.ssalb_gas;
     s.albedo = tv + k.albedo; s.tau_above = tv + k.tau_above;
+    s.layer_beta = tv + k.layer_beta; s.vprefix = tv + k.vprefix;
+    s.run_lo = gv + k.run_lo; s.run_hi = gv + k.run_hi;
     for (int sp = 0; sp < p.ntypes; ++sp) {
         s.lut_n[sp] = p.luts[sp].n; s.ssalb_aer[sp] = T(p.luts[sp].ssalb);
         s.lut_f[sp] = tv + k.lut_f[sp]; s.lut_cos[sp] = tv + k.lut_cos[sp]; s.lut_cdf[sp] = tv + k.lut_cdf[sp];
@@ -371,7 +408,7 @@ template <typename T, int NMAT, bool PATHS>
 void wave_iteration(Session& s, const SceneView<T>& v, Pool<T>& P, const Controls& c, int grid) {
     T* banks = static_cast<T*>(s.banks);
     check(cudaMemsetAsync(P.counts, 0, 3 * sizeof(uint32_t), s.stream), "memset(queues)");
-    wf_transit<T, PATHS><<<grid, s.cfg.block, 0, s.stream>>>(v, c, P, s.failure, s.counters);
+    wf_transit<T, PATHS><<<grid, s.cfg.block, 0, s.stream>>>(v, c, P, s.cfg.walk, s.failure, s.counters);
     wf_peel<T, T, NMAT, PATHS><<<grid, s.cfg.block, 0, s.stream>>>(v, c, P, banks, s.wave, s.failure, s.counters);
     wf_scatter<T, NMAT><<<grid, s.cfg.block, 0, s.stream>>>(v, c, P, s.failure);
 }
@@ -408,6 +445,7 @@ void run_wavefront(Session& s, const Controls& c) {
         if (it > limit * 4 + 1024 && it > 1000000) throw std::runtime_error("wavefront did not drain");
     }
     s.iterations += it;
+    s.totals[5] += 3 * it;
 }
 
 template <typename T>
@@ -560,6 +598,7 @@ int monki_cuda_run(void* handle, const uint32_t controls[8], double* out, char* 
             } else {
                 if (s->cfg.fp64) launch_transport<double>(*s, c, std::max(needed, 1));
                 else launch_transport<float>(*s, c, std::max(needed, 1));
+                s->totals[5] += 1;
             }
             check(cudaGetLastError(), "transport launch");
         }
@@ -588,6 +627,7 @@ int monki_cuda_run(void* handle, const uint32_t controls[8], double* out, char* 
             check(cudaGetLastError(), "flush launch");
         }
         check(cudaEventRecord(s->t2, s->stream), "event");
+        s->totals[5] += 1;  // the flush
         uint32_t flag = 0;
         unsigned long long cnt[4] = {0, 0, 0, 0};
         check(cudaMemcpyAsync(&flag, s->failure, sizeof(flag), cudaMemcpyDeviceToHost, s->stream), "copy(failure)");
@@ -626,10 +666,10 @@ int monki_cuda_last_timing(void* handle, float out[2]) {
     return 0;
 }
 
-int monki_cuda_counters(void* handle, uint64_t out[5]) {
+int monki_cuda_counters(void* handle, uint64_t out[6]) {
     if (!handle || !out) return 1;
     Session* s = static_cast<Session*>(handle);
-    for (int q = 0; q < 5; ++q) out[q] = s->totals[q];
+    for (int q = 0; q < 6; ++q) out[q] = s->totals[q];
     return 0;
 }
 

@@ -120,6 +120,106 @@ __device__ __forceinline__ void wander_add(T* w, int kk, T v, int& wmin, int& wm
     }
 }
 
+// Move a distance h >= 0 along one horizontal axis of the periodic grid: x is the distance
+// to the next face in direction sgn. Equivalent to the face-by-face walk of ADVANCE.
+template <typename T>
+__device__ __forceinline__ void slide(int& i, T& x, int sgn, T h, T unit, int n) {
+    if (h < x) { x = x - h; return; }
+    T rest = h - x;
+    T whole = floor(rest / unit);
+    rest -= whole * unit;
+    if (rest < T(0)) rest = T(0);
+    long long cross = 1 + (long long)whole;
+    if (rest >= unit) { rest -= unit; ++cross; }
+    int step = int(cross % n);
+    i += sgn * step;
+    i %= n;
+    if (i < 0) i += n;
+    x = unit - rest;
+}
+
+// One jump through the horizontally uniform run that contains layer k, from the current
+// position (z: vertical distance to the exit face in direction ks). Returns 0 for an
+// interaction inside the run, 1 for the surface, 2 for escape through the top, and -1
+// when the photon enters a horizontally varying layer (at its face, z = zunit). Path
+// lengths per layer go to the wander array when `record`; an escaping photon needs none.
+template <typename T, bool PATHS>
+__device__ __forceinline__ int uniform_jump(const SceneView<T>& s, int& k, T& z, T& remains, int ks, T ca, T ci,
+                                            bool record, T* wander, int& wmin, int& wmax,
+                                            int& i, T& x, int is, T aa, int& j, T& y, int js, T ba) {
+    const T eps = Tol<T>::eps;
+    const int top = s.nz - 1;
+    int outcome;
+    T travelled;
+    const T bk = __ldg(s.layer_beta + k);
+    const T seg = z * ci;
+    if (bk > eps && remains / bk < seg) {
+        const T de = remains / bk;
+        travelled = de;
+        z = fmax(T(0), z - ca * de);
+        if (record) wander_add(wander, k, de, wmin, wmax);
+        outcome = 0;
+    } else {
+        remains -= seg * bk;
+        travelled = seg;
+        if (record) wander_add(wander, k, seg, wmin, wmax);
+        const int m0 = k + ks;
+        // Layers m0 .. end of the run, in the direction of travel.
+        const int end = ks > 0 ? __ldg(s.run_hi + k) : __ldg(s.run_lo + k);
+        const T* V = s.vprefix;   // V[m] = vertical optical depth of uniform layers below m
+        const T* Z = s.zsum;      // Z[m] = height of the bottom of layer m
+        const bool inside = ks > 0 ? m0 <= end : m0 >= end;
+        const T run_tau = !inside ? T(0) : (ks > 0 ? __ldg(V + end + 1) - __ldg(V + m0) : __ldg(V + m0 + 1) - __ldg(V + end));
+        if (!inside || remains * ca >= run_tau) {
+            // Leaves the run: every remaining layer of it is crossed whole.
+            if (inside) {
+                remains -= run_tau * ci;
+                const T height = ks > 0 ? __ldg(Z + end + 1) - __ldg(Z + m0) : __ldg(Z + m0 + 1) - __ldg(Z + end);
+                travelled += height * ci;
+            }
+            k = inside ? end + ks : m0;
+            if (k > top) outcome = 2;
+            else if (k < 0) outcome = 1;
+            else {
+                if (record && inside)
+                    for (int m = m0; m != end + ks; m += ks) wander_add(wander, m, __ldg(s.zunit + m) * ci, wmin, wmax);
+                z = __ldg(s.zunit + k);
+                outcome = -1;
+            }
+            if (outcome == 1 && record && inside)
+                for (int m = m0; m != end + ks; m += ks) wander_add(wander, m, __ldg(s.zunit + m) * ci, wmin, wmax);
+        } else {
+            // The interaction lies inside the run: find its layer.
+            const T need = remains * ca;
+            int m = m0;
+            T before = T(0);  // vertical optical depth of the whole layers crossed before m
+            for (;;) {
+                const T bm = __ldg(s.layer_beta + m) * __ldg(s.zunit + m);
+                if (before + bm > need || m == end) break;
+                before += bm;
+                m += ks;
+            }
+            const T slant_before = (ks > 0 ? __ldg(Z + m) - __ldg(Z + m0) : __ldg(Z + m0 + 1) - __ldg(Z + m + 1)) * ci;
+            remains -= before * ci;
+            const T bm = __ldg(s.layer_beta + m);
+            const T de = bm > eps ? remains / bm : T(0);
+            travelled += slant_before + de;
+            if (record) {
+                for (int q = m0; q != m; q += ks) wander_add(wander, q, __ldg(s.zunit + q) * ci, wmin, wmax);
+                wander_add(wander, m, de, wmin, wmax);
+            }
+            k = m;
+            z = fmax(T(0), __ldg(s.zunit + m) - ca * de);
+            outcome = 0;
+        }
+    }
+    if (outcome != 2) {
+        slide(i, x, is, aa * travelled, s.xunit, s.nx);
+        slide(j, y, js, ba * travelled, s.yunit, s.ny);
+    }
+    return outcome;
+}
+
 template <typename T>
 __device__ __forceinline__ void photon_origin(const SceneView<T>& s, const Controls& ctl, uint32_t pid,
                                               uint32_t& photon, uint32_t& round) {
@@ -132,7 +232,7 @@ __device__ __forceinline__ void photon_origin(const SceneView<T>& s, const Contr
 // ----------------------------------------------------------------------------------
 template <typename T, bool PATHS>
 __global__ void __launch_bounds__(256)
-wf_transit(SceneView<T> s, Controls ctl, Pool<T> P, uint32_t* __restrict__ failure,
+wf_transit(SceneView<T> s, Controls ctl, Pool<T> P, uint32_t walk, uint32_t* __restrict__ failure,
            unsigned long long* __restrict__ counters) {
     const T eps = Tol<T>::eps;
     const int top = s.nz - 1;
@@ -145,7 +245,7 @@ wf_transit(SceneView<T> s, Controls ctl, Pool<T> P, uint32_t* __restrict__ failu
         DrawStream rng;
         int i = 0, j = 0, k = 0, k1 = -2, wmin = 255, wmax = 0;
         T x = 0, y = 0, z = 0, a = 0, b = 0, c = 0, weight = 0, remains = 0, init_part = 0;
-        uint32_t steps = 0;
+        uint32_t steps = 0, budget = walk;
         bool fresh = false;
 
         if (pid != kNone) {
@@ -192,20 +292,31 @@ wf_transit(SceneView<T> s, Controls ctl, Pool<T> P, uint32_t* __restrict__ failu
             const T ai = T(1) / fmax(aa, eps), bi = T(1) / fmax(ba, eps), ci = T(1) / fmax(ca, eps);
             // Path length of the current layer, added to the wander array on layer change.
             T* wander = PATHS ? P.wander + size_t(slot) * s.nz : nullptr;
+            const bool record = PATHS && k1 > -2;
             int acc_k = -1;
             T acc = T(0);
-            int outcome = -1;  // 0 atmosphere, 1 surface, 2 escaped, 3 step limit
+            int outcome = -1;  // 0 atmosphere, 1 surface, 2 escaped, 3 step limit, 4 paused
             for (;;) {
+                if (budget == 0) { outcome = 4; break; }
+                --budget;
                 if (++steps > ctl.max_steps) { outcome = 3; break; }
                 ++visits;
-                const T bv = (k < top && k >= 0) ? beta_at(s, i, j, k) : T(0);
+                if (__ldg(s.layer_beta + k) >= T(0)) {
+                    // Horizontally uniform run: x/y faces change no extinction, so the walk
+                    // jumps to the layer of the event (or out of the run) with the vertical
+                    // optical-depth prefix; the horizontal position follows at the end.
+                    outcome = uniform_jump<T, PATHS>(s, k, z, remains, ks, ca, ci, record, wander, wmin, wmax, i, x, is, aa, j, y, js, ba);
+                    if (outcome >= 0) break;
+                    continue;
+                }
+                const T bv = k < top ? beta_at(s, i, j, k) : T(0);
                 if (bv > eps) {
                     const T de = remains / bv;
                     if (de < x * ai && de < y * bi && de < z * ci) {
                         x = fmax(T(0), x - aa * de);
                         y = fmax(T(0), y - ba * de);
                         z = fmax(T(0), z - ca * de);
-                        if (PATHS && k1 > -2) {
+                        if (record) {
                             if (acc_k != k) {
                                 if (acc_k >= 0) wander_add(wander, acc_k, acc, wmin, wmax);
                                 acc_k = k; acc = T(0);
@@ -218,7 +329,7 @@ wf_transit(SceneView<T> s, Controls ctl, Pool<T> P, uint32_t* __restrict__ failu
                 }
                 const int k_old = k;
                 const T dist = advance(s, i, j, k, x, y, z, is, js, ks, aa, ba, ca, ai, bi, ci);
-                if (PATHS && k1 > -2) {
+                if (record) {
                     if (acc_k != k_old) {
                         if (acc_k >= 0) wander_add(wander, acc_k, acc, wmin, wmax);
                         acc_k = k_old; acc = T(0);
@@ -231,6 +342,7 @@ wf_transit(SceneView<T> s, Controls ctl, Pool<T> P, uint32_t* __restrict__ failu
                 break;
             }
             if (PATHS && acc_k >= 0) wander_add(wander, acc_k, acc, wmin, wmax);
+            if (outcome == 4) break;  // budget spent: the walk resumes next iteration
             if (outcome == 3) { atomicOr(failure, kHistoryCap); pid = kNone; continue; }
             if (outcome == 2) { pid = kNone; continue; }
             int kind;

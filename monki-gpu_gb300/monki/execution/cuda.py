@@ -197,6 +197,7 @@ class CUDA(Backend):
             "gpu_dispatches": 0,
             "scatters": 0,
             "photons": 0,
+            "kernel_launches": 0,
         }
 
     def run_batch(self, controls: object) -> RawTallies:
@@ -307,10 +308,11 @@ class CUDA(Backend):
                 total += scratch
                 self.provenance["gpu_dispatches"] += 1
 
-            counters = (ctypes.c_uint64 * 5)()
+            counters = (ctypes.c_uint64 * 6)()
             self._native.monki_cuda_counters(self._handle, counters)
             self.provenance["scatters"] = int(counters[0])
             self.provenance["photons"] = int(counters[4])
+            self.provenance["kernel_launches"] = int(counters[5])
 
             if self.profile:
                 self.provenance["gpu_seconds"] = self._native.monki_cuda_gpu_seconds(self._handle)
