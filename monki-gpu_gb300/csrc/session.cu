@@ -363,27 +363,28 @@ void upload(Session& s) {
 
 template <typename T>
 Pool<T> allocate_pool(Session& s) {
-    const uint32_t n = s.cfg.pool;
+    const size_t n = s.cfg.pool;
     const size_t nz = size_t(s.prep.nz);
-    const size_t u32 = size_t(n) * sizeof(uint32_t), tv = size_t(n) * sizeof(T);
-    const size_t bytes = 5 * u32 + align_up(n, 16) + 12 * tv + size_t(n) * nz * sizeof(T) + 3 * u32 + 256;
-    check(cudaMalloc(&s.pool_memory, bytes + 64 * 16), "cudaMalloc(pool)");
+    const size_t quad = n * sizeof(Quad<T>);
+    const size_t parts[] = {quad, quad, quad, n * sizeof(uint4), n * sizeof(uint32_t), n,
+                            n * nz * sizeof(T), 3 * n * sizeof(uint32_t), 16 * sizeof(uint32_t)};
+    size_t bytes = 0;
+    for (size_t part : parts) bytes += align_up(part, 256);
+    check(cudaMalloc(&s.pool_memory, bytes), "cudaMalloc(pool)");
     char* p = static_cast<char*>(s.pool_memory);
     auto take = [&](size_t b) { char* q = p; p += align_up(b, 256); return q; };
     Pool<T> P{};
-    P.capacity = n;
-    P.pid = reinterpret_cast<uint32_t*>(take(u32));
-    P.draw = reinterpret_cast<uint32_t*>(take(u32));
-    P.steps = reinterpret_cast<uint32_t*>(take(u32));
-    P.cell = reinterpret_cast<uint32_t*>(take(u32));
-    P.layers = reinterpret_cast<uint32_t*>(take(u32));
+    P.capacity = uint32_t(n);
+    P.pos = reinterpret_cast<Quad<T>*>(take(quad));
+    P.dir = reinterpret_cast<Quad<T>*>(take(quad));
+    P.pol = reinterpret_cast<Quad<T>*>(take(quad));
+    P.meta = reinterpret_cast<uint4*>(take(n * sizeof(uint4)));
+    P.steps = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
     P.kind = reinterpret_cast<uint8_t*>(take(n));
-    T** fields[] = {&P.x, &P.y, &P.z, &P.a, &P.b, &P.c, &P.phi, &P.q, &P.u, &P.weight, &P.remains, &P.init_part};
-    for (T** f : fields) *f = reinterpret_cast<T*>(take(tv));
-    P.wander = reinterpret_cast<T*>(take(size_t(n) * nz * sizeof(T)));
-    for (int q = 0; q < 3; ++q) P.queue[q] = reinterpret_cast<uint32_t*>(take(u32));
+    P.wander = reinterpret_cast<T*>(take(n * nz * sizeof(T)));
+    uint32_t* queues = reinterpret_cast<uint32_t*>(take(3 * n * sizeof(uint32_t)));
+    for (int q = 0; q < 3; ++q) P.queue[q] = queues + size_t(q) * n;
     P.counts = reinterpret_cast<uint32_t*>(take(16 * sizeof(uint32_t)));
-    if (size_t(p - static_cast<char*>(s.pool_memory)) > bytes + 64 * 16) throw std::runtime_error("pool layout overflow");
     return P;
 }
 
@@ -405,12 +406,12 @@ void launch_transport(Session& s, const Controls& c, int grid) {
 }
 
 template <typename T, int NMAT, bool PATHS>
-void wave_iteration(Session& s, const SceneView<T>& v, Pool<T>& P, const Controls& c, int grid) {
+void wave_iteration(Session& s, const SceneView<T>& v, Pool<T>& P, const Controls& c, const Divisors& dv, int grid) {
     T* banks = static_cast<T*>(s.banks);
     check(cudaMemsetAsync(P.counts, 0, 3 * sizeof(uint32_t), s.stream), "memset(queues)");
-    wf_transit<T, PATHS><<<grid, s.cfg.block, 0, s.stream>>>(v, c, P, s.cfg.walk, s.failure, s.counters);
-    wf_peel<T, T, NMAT, PATHS><<<grid, s.cfg.block, 0, s.stream>>>(v, c, P, banks, s.wave, s.failure, s.counters);
-    wf_scatter<T, NMAT><<<grid, s.cfg.block, 0, s.stream>>>(v, c, P, s.failure);
+    wf_transit<T, PATHS><<<grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, s.cfg.walk, s.failure, s.counters);
+    wf_peel<T, T, NMAT, PATHS><<<grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, banks, s.wave, s.failure, s.counters);
+    wf_scatter<T, NMAT><<<grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, s.failure);
 }
 
 template <typename T>
@@ -424,7 +425,9 @@ void run_wavefront(Session& s, const Controls& c) {
     // Small groups scan only as many slots as they have photons.
     P.capacity = uint32_t(std::min<uint64_t>(P.capacity, (uint64_t(c.count) + 255) / 256 * 256));
     check(cudaMemsetAsync(P.counts, 0, 16 * sizeof(uint32_t), s.stream), "memset(counts)");
-    check(cudaMemsetAsync(P.pid, 0xFF, size_t(P.capacity) * sizeof(uint32_t), s.stream), "memset(pool)");
+    check(cudaMemsetAsync(P.meta, 0xFF, size_t(P.capacity) * sizeof(uint4), s.stream), "memset(pool)");
+    Divisors dv{FastDiv::make(c.per_round), FastDiv::make(uint32_t(s.prep.nx)), FastDiv::make(uint32_t(s.prep.ny)),
+                FastDiv::make(uint32_t(s.prep.nx * s.prep.ny))};
     const int grid = s.grid;
     const int nm = s.prep.nmat;
     const bool paths = s.prep.paths;
@@ -432,10 +435,10 @@ void run_wavefront(Session& s, const Controls& c) {
     uint64_t it = 0;
     for (;;) {
         for (uint32_t b = 0; b < s.cfg.check_every; ++b, ++it) {
-            if (nm == 1 && !paths) wave_iteration<T, 1, false>(s, v, P, c, grid);
-            else if (nm == 1) wave_iteration<T, 1, true>(s, v, P, c, grid);
-            else if (!paths) wave_iteration<T, 3, false>(s, v, P, c, grid);
-            else wave_iteration<T, 3, true>(s, v, P, c, grid);
+            if (nm == 1 && !paths) wave_iteration<T, 1, false>(s, v, P, c, dv, grid);
+            else if (nm == 1) wave_iteration<T, 1, true>(s, v, P, c, dv, grid);
+            else if (!paths) wave_iteration<T, 3, false>(s, v, P, c, dv, grid);
+            else wave_iteration<T, 3, true>(s, v, P, c, dv, grid);
         }
         check(cudaGetLastError(), "wavefront launch");
         check(cudaMemcpyAsync(s.host_counts, P.counts, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s.stream), "copy(counts)");
@@ -520,12 +523,9 @@ void* monki_cuda_create(uint32_t device, const double* tables, size_t table_coun
         L.shards = cfg.shards;
         const uint32_t pixels = uint32_t(p.nx * p.ny * p.angles);
         WaveTally& W = s->wave;
-        W.stokes = L.stokes;
-        W.layer = p.paths ? pixels * uint32_t(p.nz) : 0u;
-        W.first = p.paths ? pixels * uint32_t(p.nz + 1) : 0u;
-        W.view = p.paths ? pixels * uint32_t(p.nz) : 0u;
-        W.weights = p.paths ? pixels : 0u;
-        W.count = W.stokes + W.layer + W.first + W.view + W.weights;
+        W.pixels = pixels;
+        W.layers = p.paths ? pixels * uint32_t(p.nz + 1) * 4u : 0u;
+        W.count = 4u * pixels + W.layers;
         W.shards = cfg.shards;
         const size_t elem = cfg.fp64 ? sizeof(double) : sizeof(float);
         const size_t per_round = cfg.wavefront ? W.count : L.count;

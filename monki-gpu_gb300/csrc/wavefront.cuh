@@ -7,11 +7,16 @@
 //            albedo (mc.f90:1028-1074) or the surface albedo (mc.f90:681-728), and appends
 //            the photon to the surface / gas / particle queue. Slots whose photon escaped or
 //            died claim the next photon of the round group, so the pool stays full.
-//   peel     one thread per (event, view): phase matrix and rotations, optical depth to the
-//            top along the view (calc_radiances_and_paths_pol,
-//            mc_routines_cartesian_mod.f90:849-1222) and the tallies.
+//            Horizontally uniform layer runs are crossed in one jump with a vertical
+//            optical-depth prefix; a per-launch step budget keeps the lanes of a warp in step.
+//   peel     one thread per event, all views: phase matrix and rotations, optical depth to
+//            the top along each view (calc_radiances_and_paths_pol,
+//            mc_routines_cartesian_mod.f90:849-1222) and the tallies, as 128-bit atomics.
 //   scatter  Lambertian reflection (GROUND_LAMB2) or polarized rejection sampling of the
 //            new direction with the Stokes update (mc.f90:1266-1431).
+//
+// Photon state is stored as 16-byte records per slot (position, direction, polarization,
+// bookkeeping), one load or store per record.
 //
 // Each photon's random stream is addressed by a draw index, so the draw sequence of a
 // history is the same as in one thread (and as in the CPU oracle) however the stages split.
@@ -31,28 +36,54 @@ constexpr uint32_t kNone = 0xFFFFFFFFu;
 
 enum Queue : int { kQueueSurface = 0, kQueueGas = 1, kQueueParticle = 2 };
 
-// Device tally layout of one round and one shard for the wavefront engine.
+template <typename T>
+struct alignas(4 * sizeof(T)) Quad { T x, y, z, w; };
+
+// Unsigned division by a launch constant with one multiply-high and two shifts
+// (round-up method; d == 1 handled separately).
+struct FastDiv {
+    uint32_t d, m, l;
+    __host__ static FastDiv make(uint32_t d) {
+        FastDiv f{d, 0u, 0u};
+        if (d > 1) {
+            uint32_t l = 0;
+            while ((uint64_t(1) << l) < d) ++l;
+            f.l = l;
+            f.m = uint32_t((((uint64_t(1) << 32) * ((uint64_t(1) << l) - d)) / d) + 1);
+        }
+        return f;
+    }
+    __device__ __forceinline__ uint32_t div(uint32_t n) const {
+        if (d == 1) return n;
+        const uint32_t t = __umulhi(m, n);
+        return (t + ((n - t) >> 1)) >> (l - 1);
+    }
+    __device__ __forceinline__ uint32_t mod(uint32_t n) const { return n - div(n) * d; }
+};
+
+struct Divisors { FastDiv per_round, nx, ny, ncol; };
+
+// Device tally layout of one round and one shard (element counts of TA):
+//   pixel records  [pixel]                  {I, Q, U, detected weight}
+//   layer records  [pixel * (nz + 1) + k]   {layer path, view-ray weight, first-event weight, 0}
+//   (record k = nz holds the first-event weight of histories that met the surface first)
 struct WaveTally {
-    uint32_t stokes;   // nmat * pixels,        [m + nmat * pixel]
-    uint32_t layer;    // pixels * nz,          wandering + partial pieces, [pixel * nz + k]
-    uint32_t first;    // pixels * (nz + 1),    weight by first-event slot k1 + 1
-    uint32_t view;     // pixels * nz,          weight by event layer (detector-ray prefix)
-    uint32_t weights;  // pixels
-    uint32_t count;    // sum of the above
+    uint32_t pixels;   // nx * ny * angles
+    uint32_t layers;   // pixels * (nz + 1) * 4 when paths are tallied, else 0
+    uint32_t count;    // 4 * pixels + layers
     uint32_t shards;
 };
 
 template <typename T>
 struct Pool {
     uint32_t capacity;
-    uint32_t* pid;     // flattened photon identity in the round group, kNone when empty
-    uint32_t* draw;    // index of the next random draw of the photon's stream
-    uint32_t* steps;   // cell visits so far (history step limit)
-    uint32_t* cell;    // i | j << 16
-    uint32_t* layers;  // k + 1 | (k1 + 2) << 8 | wmin << 16 | wmax << 24
-    uint8_t* kind;     // species of the pending event: 0 gas, 1 + s particle s, 255 surface
-    T *x, *y, *z, *a, *b, *c, *phi, *q, *u, *weight, *remains, *init_part;
-    T* wander;         // capacity * nz path lengths after the first event
+    Quad<T>* pos;    // x, y, z, weight
+    Quad<T>* dir;    // a, b, c, phi
+    Quad<T>* pol;    // q, u, remains, init_part
+    uint4* meta;     // pid (kNone when empty), next draw, i | j << 16, packed layers
+    uint32_t* steps; // walk steps so far (history step limit)
+    uint8_t* kind;   // pending event: 0 gas, 1 + s particle s, 255 surface
+    T* wander;       // capacity * nz path lengths after the first event
     uint32_t* queue[3];
     uint32_t* counts;  // [0..2] queue sizes, [3] next photon to claim
 };
@@ -143,7 +174,7 @@ __device__ __forceinline__ void slide(int& i, T& x, int sgn, T h, T unit, int n)
 // interaction inside the run, 1 for the surface, 2 for escape through the top, and -1
 // when the photon enters a horizontally varying layer (at its face, z = zunit). Path
 // lengths per layer go to the wander array when `record`; an escaping photon needs none.
-template <typename T, bool PATHS>
+template <typename T>
 __device__ __forceinline__ int uniform_jump(const SceneView<T>& s, int& k, T& z, T& remains, int ks, T ca, T ci,
                                             bool record, T* wander, int& wmin, int& wmax,
                                             int& i, T& x, int is, T aa, int& j, T& y, int js, T ba) {
@@ -179,15 +210,10 @@ __device__ __forceinline__ int uniform_jump(const SceneView<T>& s, int& k, T& z,
             }
             k = inside ? end + ks : m0;
             if (k > top) outcome = 2;
-            else if (k < 0) outcome = 1;
-            else {
-                if (record && inside)
-                    for (int m = m0; m != end + ks; m += ks) wander_add(wander, m, __ldg(s.zunit + m) * ci, wmin, wmax);
-                z = __ldg(s.zunit + k);
-                outcome = -1;
-            }
-            if (outcome == 1 && record && inside)
+            else outcome = k < 0 ? 1 : -1;
+            if (outcome != 2 && record && inside)
                 for (int m = m0; m != end + ks; m += ks) wander_add(wander, m, __ldg(s.zunit + m) * ci, wmin, wmax);
+            if (outcome == -1) z = __ldg(s.zunit + k);
         } else {
             // The interaction lies inside the run: find its layer.
             const T need = remains * ca;
@@ -220,47 +246,39 @@ __device__ __forceinline__ int uniform_jump(const SceneView<T>& s, int& k, T& z,
     return outcome;
 }
 
-template <typename T>
-__device__ __forceinline__ void photon_origin(const SceneView<T>& s, const Controls& ctl, uint32_t pid,
-                                              uint32_t& photon, uint32_t& round) {
-    photon = pid % ctl.per_round;
-    round = ctl.first_round + pid / ctl.per_round;
-}
-
 // ----------------------------------------------------------------------------------
 // transit: free path to the next interaction for every pooled photon.
 // ----------------------------------------------------------------------------------
 template <typename T, bool PATHS>
 __global__ void __launch_bounds__(256)
-wf_transit(SceneView<T> s, Controls ctl, Pool<T> P, uint32_t walk, uint32_t* __restrict__ failure,
+wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, uint32_t* __restrict__ failure,
            unsigned long long* __restrict__ counters) {
     const T eps = Tol<T>::eps;
     const int top = s.nz - 1;
-    const uint32_t ncol = uint32_t(s.nx * s.ny);
     const uint32_t stride = gridDim.x * blockDim.x;
     uint64_t scatters = 0, visits = 0;
 
     for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < P.capacity; slot += stride) {
-        uint32_t pid = P.pid[slot];
+        const uint4 meta = P.meta[slot];
+        uint32_t pid = meta.x;
         DrawStream rng;
         int i = 0, j = 0, k = 0, k1 = -2, wmin = 255, wmax = 0;
-        T x = 0, y = 0, z = 0, a = 0, b = 0, c = 0, weight = 0, remains = 0, init_part = 0;
+        Quad<T> pos{}, dir{}, pol{};
         uint32_t steps = 0, budget = walk;
         bool fresh = false;
 
         if (pid != kNone) {
-            uint32_t photon, round;
-            photon_origin(s, ctl, pid, photon, round);
-            rng.init(photon, round, ctl.seed, P.draw[slot]);
-            const uint32_t cell = P.cell[slot];
-            i = int(cell & 0xFFFF); j = int(cell >> 16);
-            unpack_layers(P.layers[slot], k, k1, wmin, wmax);
-            x = P.x[slot]; y = P.y[slot]; z = P.z[slot];
-            a = P.a[slot]; b = P.b[slot]; c = P.c[slot];
-            weight = P.weight[slot]; remains = P.remains[slot];
+            const uint32_t ro = dv.per_round.div(pid);
+            rng.init(pid - ro * ctl.per_round, ctl.first_round + ro, ctl.seed, meta.y);
+            i = int(meta.z & 0xFFFF); j = int(meta.z >> 16);
+            unpack_layers(meta.w, k, k1, wmin, wmax);
+            pos = P.pos[slot];
+            dir = P.dir[slot];
+            pol = P.pol[slot];
             steps = P.steps[slot];
-            if (PATHS) init_part = P.init_part[slot];
         }
+        T& x = pos.x; T& y = pos.y; T& z = pos.z; T& weight = pos.w;
+        T& remains = pol.z; T& init_part = pol.w;
 
         for (;;) {
             if (pid == kNone) {
@@ -269,24 +287,26 @@ wf_transit(SceneView<T> s, Controls ctl, Pool<T> P, uint32_t walk, uint32_t* __r
                 const uint32_t n = warp_reserve(P.counts + 3);
                 if (n >= ctl.count) break;
                 pid = ctl.first + n;
-                uint32_t photon, round;
-                photon_origin(s, ctl, pid, photon, round);
-                rng.init(photon, round, ctl.seed, 0u);
-                const uint32_t column = photon % ncol;
-                i = int(column % uint32_t(s.nx));
-                j = int(column / uint32_t(s.nx));
-                if (j > s.ny - 1) j = s.ny - 1;
+                const uint32_t ro = dv.per_round.div(pid);
+                const uint32_t photon = pid - ro * ctl.per_round;
+                rng.init(photon, ctl.first_round + ro, ctl.seed, 0u);
+                const uint32_t column = dv.ncol.mod(photon);
+                const uint32_t row = dv.nx.div(column);
+                i = int(column - row * uint32_t(s.nx));
+                j = min(int(row), s.ny - 1);
                 k = top;
                 x = s.xunit * T(rng.next());
                 y = s.yunit * T(rng.next());
                 z = __ldg(s.zunit + k);
-                a = s.a0; b = s.b0; c = s.c0;
                 weight = T(1);
+                dir = Quad<T>{s.a0, s.b0, s.c0, s.phi0};
+                pol.x = T(0); pol.y = T(0);
                 steps = 0;
                 k1 = -2; wmin = 255; wmax = 0; init_part = T(0);
                 remains = -log(fmax(T(rng.next()), eps));
                 fresh = true;
             }
+            const T a = dir.x, b = dir.y, c = dir.z;
             const int is = signbit(a) ? -1 : 1, js = signbit(b) ? -1 : 1, ks = signbit(c) ? -1 : 1;
             const T aa = fabs(a), ba = fabs(b), ca = fabs(c);
             const T ai = T(1) / fmax(aa, eps), bi = T(1) / fmax(ba, eps), ci = T(1) / fmax(ca, eps);
@@ -302,10 +322,8 @@ wf_transit(SceneView<T> s, Controls ctl, Pool<T> P, uint32_t walk, uint32_t* __r
                 if (++steps > ctl.max_steps) { outcome = 3; break; }
                 ++visits;
                 if (__ldg(s.layer_beta + k) >= T(0)) {
-                    // Horizontally uniform run: x/y faces change no extinction, so the walk
-                    // jumps to the layer of the event (or out of the run) with the vertical
-                    // optical-depth prefix; the horizontal position follows at the end.
-                    outcome = uniform_jump<T, PATHS>(s, k, z, remains, ks, ca, ci, record, wander, wmin, wmax, i, x, is, aa, j, y, js, ba);
+                    outcome = uniform_jump<T>(s, k, z, remains, ks, ca, ci, record, wander, wmin, wmax,
+                                              i, x, is, aa, j, y, js, ba);
                     if (outcome >= 0) break;
                     continue;
                 }
@@ -376,22 +394,14 @@ wf_transit(SceneView<T> s, Controls ctl, Pool<T> P, uint32_t walk, uint32_t* __r
         }
 
         if (pid == kNone) {
-            P.pid[slot] = kNone;
+            if (meta.x != kNone) P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u);
             continue;
         }
-        if (fresh) P.pid[slot] = pid;
-        P.draw[slot] = rng.draw;
+        P.meta[slot] = make_uint4(pid, rng.draw, uint32_t(i) | (uint32_t(j) << 16), pack_layers(k, k1, wmin, wmax));
         P.steps[slot] = steps;
-        P.cell[slot] = uint32_t(i) | (uint32_t(j) << 16);
-        P.layers[slot] = pack_layers(k, k1, wmin, wmax);
-        P.x[slot] = x; P.y[slot] = y; P.z[slot] = z;
-        P.weight[slot] = weight;
-        P.remains[slot] = remains;
-        if (fresh) {
-            P.a[slot] = a; P.b[slot] = b; P.c[slot] = c;
-            P.phi[slot] = s.phi0; P.q[slot] = T(0); P.u[slot] = T(0);
-        }
-        if (PATHS) P.init_part[slot] = init_part;
+        P.pos[slot] = pos;
+        P.pol[slot] = pol;
+        if (fresh) P.dir[slot] = dir;
     }
 
     unsigned long long v0 = scatters, v1 = visits;
@@ -406,120 +416,147 @@ wf_transit(SceneView<T> s, Controls ctl, Pool<T> P, uint32_t walk, uint32_t* __r
     }
 }
 
+// 128-bit tally update (FP32: one vector atomic; FP64: per nonzero element).
+__device__ __forceinline__ void quad_add(Quad<float>* p, float x, float y, float z, float w) {
+    atomicAdd(reinterpret_cast<float4*>(p), make_float4(x, y, z, w));
+}
+__device__ __forceinline__ void quad_add(Quad<double>* p, double x, double y, double z, double w) {
+    if (x != 0.0) atomicAdd(&p->x, x);
+    if (y != 0.0) atomicAdd(&p->y, y);
+    if (z != 0.0) atomicAdd(&p->z, z);
+    if (w != 0.0) atomicAdd(&p->w, w);
+}
+
+__device__ __forceinline__ uint32_t queue_entry(uint32_t* const* queue, uint32_t e, uint32_t ns, uint32_t ng,
+                                                bool& surface) {
+    surface = e < ns;
+    if (surface) return queue[kQueueSurface][e];
+    if (e < ns + ng) return queue[kQueueGas][e - ns];
+    return queue[kQueueParticle][e - ns - ng];
+}
+
 // ----------------------------------------------------------------------------------
-// peel: one (event, view) pair per thread.
+// peel: one event per thread, every view.
 // ----------------------------------------------------------------------------------
 template <typename T, typename TA, int NMAT, bool PATHS>
 __global__ void __launch_bounds__(256)
-wf_peel(SceneView<T> s, Controls ctl, Pool<T> P, TA* __restrict__ banks, WaveTally L,
+wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ banks, WaveTally L,
         uint32_t* __restrict__ failure, unsigned long long* __restrict__ counters) {
     const T eps = Tol<T>::eps;
     const int top = s.nz - 1;
     const uint32_t ns = P.counts[0], ng = P.counts[1], np = P.counts[2];
-    const uint32_t views = uint32_t(s.angles);
-    const uint64_t total = uint64_t(ns + ng + np) * views;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t total = ns + ng + np;
+    const uint32_t shard = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) % L.shards;
     uint64_t visits = 0, updates = 0;
 
-    for (uint64_t t = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; t < total;
-         t += uint64_t(gridDim.x) * blockDim.x) {
-        const uint32_t e = uint32_t(t / views);
-        const int ia = int(t % views);
-        uint32_t slot;
-        bool surface = false;
-        if (e < ns) { slot = P.queue[kQueueSurface][e]; surface = true; }
-        else if (e < ns + ng) slot = P.queue[kQueueGas][e - ns];
-        else slot = P.queue[kQueueParticle][e - ns - ng];
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        bool surface;
+        const uint32_t slot = queue_entry(P.queue, e, ns, ng, surface);
         if (slot >= P.capacity) { atomicOr(failure, kQueueCorrupt); continue; }
-
-        const uint32_t pid = P.pid[slot];
+        const uint4 meta = P.meta[slot];
+        const uint32_t pid = meta.x;
         if (pid == kNone) { atomicOr(failure, kQueueCorrupt); continue; }
-        const uint32_t cell = P.cell[slot];
-        const int i = int(cell & 0xFFFF), j = int(cell >> 16);
+        const int i = int(meta.z & 0xFFFF), j = int(meta.z >> 16);
         int k, k1, wmin, wmax;
-        unpack_layers(P.layers[slot], k, k1, wmin, wmax);
-        const T x = P.x[slot], y = P.y[slot], z = P.z[slot];
-        const T a = P.a[slot], b = P.b[slot], c = P.c[slot];
-        const T weight = P.weight[slot];
-        T prob[3] = {T(0), T(0), T(0)};
-        const T vc = s.vc[ia];
-        if (surface) {
-            prob[0] = vc > T(0) ? vc * weight : T(0);
-        } else {
-            const int sp = int(P.kind[slot]) - 1;
-            const T phi = P.phi[slot];
-            const T st[3] = {T(1), P.q[slot], P.u[slot]};
-            const T cs = c * vc + sqrt(fmax(eps, T(1) - c * c)) * sqrt(fmax(eps, T(1) - vc * vc)) *
-                                     cos(phi - s.vphi[ia]);
-            const Rot<T> r = NMAT > 1 ? rotation<T>(cs, c, vc, phi, s.vphi[ia]) : Rot<T>{T(1), T(0), T(1), T(0)};
-            const Phase<T> f = phase<T>(s, sp, cs, NMAT);
-            T back[3];
-            scatter_stokes<T>(f, r, NMAT, st, back);
-            for (int m = 0; m < NMAT; ++m) prob[m] = back[m] * weight;
-            if (prob[0] < Tol<T>::negligible) for (int m = 0; m < NMAT; ++m) prob[m] = T(0);
-        }
-        bool finite = true;
-        for (int m = 0; m < NMAT; ++m) finite = finite && isfinite(prob[m]);
-        if (!finite) { atomicOr(failure, kNonfinite); continue; }
-        if (!(prob[0] > eps)) continue;
+        unpack_layers(meta.w, k, k1, wmin, wmax);
+        const Quad<T> pos = P.pos[slot];
+        const Quad<T> dir = P.dir[slot];
+        const Quad<T> pol = P.pol[slot];
+        const int sp = surface ? -1 : int(P.kind[slot]) - 1;
+        const T x = pos.x, y = pos.y, z = pos.z, weight = pos.w;
+        const T a = dir.x, b = dir.y, c = dir.z, phi = dir.w;
+        const T st[3] = {T(1), pol.x, pol.y};
+        const uint32_t round_offset = dv.per_round.div(pid);
+        TA* bank = banks + (size_t(round_offset) * L.shards + shard) * L.count;
+        Quad<TA>* pixrec = reinterpret_cast<Quad<TA>*>(bank);
+        Quad<TA>* layrec = reinterpret_cast<Quad<TA>*>(bank + 4 * size_t(L.pixels));
+        const T* wander = PATHS ? P.wander + size_t(slot) * s.nz : nullptr;
+        const T sin_c = sqrt(fmax(eps, T(1) - c * c));
+        for (int ia = 0; ia < s.angles; ++ia) {
+            const T vc = s.vc[ia];
+            T prob[3] = {T(0), T(0), T(0)};
+            if (surface) {
+                prob[0] = vc > T(0) ? vc * weight : T(0);
+            } else {
+                const T cs = c * vc + sin_c * sqrt(fmax(eps, T(1) - vc * vc)) * cos(phi - s.vphi[ia]);
+                const Rot<T> r = NMAT > 1 ? rotation<T>(cs, c, vc, phi, s.vphi[ia]) : Rot<T>{T(1), T(0), T(1), T(0)};
+                const Phase<T> f = phase<T>(s, sp, cs, NMAT);
+                T back[3];
+                scatter_stokes<T>(f, r, NMAT, st, back);
+                for (int m = 0; m < NMAT; ++m) prob[m] = back[m] * weight;
+                if (prob[0] < Tol<T>::negligible) for (int m = 0; m < NMAT; ++m) prob[m] = T(0);
+            }
+            bool finite = true;
+            for (int m = 0; m < NMAT; ++m) finite = finite && isfinite(prob[m]);
+            if (!finite) { atomicOr(failure, kNonfinite); break; }
+            if (!(prob[0] > eps)) continue;
 
-        // Detector ray (as detector() in transport.cuh) with the decomposed path tallies.
-        const T va = s.va[ia], vb = s.vb[ia];
-        T rx = x, ry = y, rz = z;
-        if (va * a < T(0)) rx = fmax(T(0), s.xunit - rx);
-        if (vb * b < T(0)) ry = fmax(T(0), s.yunit - ry);
-        if (vc * c < T(0)) rz = fmax(T(0), __ldg(s.zunit + k) - rz);
-        const int is = signbit(va) ? -1 : 1, js = signbit(vb) ? -1 : 1, ks = signbit(vc) ? -1 : 1;
-        const T aa = fabs(va), ba = fabs(vb), ca = fabs(vc);
-        const T ai = T(1) / fmax(aa, eps), bi = T(1) / fmax(ba, eps), ci = T(1) / fmax(ca, eps);
-        const T x_old = rx, y_old = ry, z_old = rz;
-        T tau = T(0);
-        int ri = i, rj = j, rk = k;
-        uint32_t rsteps = 0;
-        bool capped = false;
-        while (rk >= 0 && rk < top) {
-            if (rk >= s.uniform_top) {
-                tau += (rz * beta_at(s, ri, rj, rk) + __ldg(s.tau_above + rk)) * ci;
+            // Detector ray: explicit cell walk below the uniform top, then the prefix.
+            const T va = s.va[ia], vb = s.vb[ia];
+            T rx = x, ry = y, rz = z;
+            if (va * a < T(0)) rx = fmax(T(0), s.xunit - rx);
+            if (vb * b < T(0)) ry = fmax(T(0), s.yunit - ry);
+            if (vc * c < T(0)) rz = fmax(T(0), __ldg(s.zunit + k) - rz);
+            const int is = signbit(va) ? -1 : 1, js = signbit(vb) ? -1 : 1, ks = signbit(vc) ? -1 : 1;
+            const T aa = fabs(va), ba = fabs(vb), ca = fabs(vc);
+            const T ai = T(1) / fmax(aa, eps), bi = T(1) / fmax(ba, eps), ci = T(1) / fmax(ca, eps);
+            const T x_old = rx, y_old = ry, z_old = rz;
+            T tau = T(0);
+            int ri = i, rj = j, rk = k;
+            uint32_t rsteps = 0;
+            bool capped = false;
+            while (rk >= 0 && rk < top) {
+                if (rk >= s.uniform_top) {
+                    tau += (rz * beta_at(s, ri, rj, rk) + __ldg(s.tau_above + rk)) * ci;
+                    ++visits;
+                    break;
+                }
+                if (++rsteps > ctl.max_steps) { capped = true; break; }
+                const T bv = beta_at(s, ri, rj, rk);
+                const T dist = advance(s, ri, rj, rk, rx, ry, rz, is, js, ks, aa, ba, ca, ai, bi, ci);
+                tau += dist * bv;
                 ++visits;
-                break;
             }
-            if (++rsteps > ctl.max_steps) { capped = true; break; }
-            const T bv = beta_at(s, ri, rj, rk);
-            const T dist = advance(s, ri, rj, rk, rx, ry, rz, is, js, ks, aa, ba, ca, ai, bi, ci);
-            tau += dist * bv;
-            ++visits;
-        }
-        if (capped) { atomicOr(failure, kDetectorCap); continue; }
-        T height = __ldg(s.zsum + k) + (ks > 0 ? __ldg(s.zunit + k) - z_old : z_old);
-        height = __ldg(s.zsum + top) - height;
-        const T dxp = aa * height / ca, dyp = ba * height / ca;
-        const int di = int(((s.xunit - x_old) + dxp) / s.xunit);
-        const int dj = int(((s.yunit - y_old) + dyp) / s.yunit);
-        int pi_ = (i + is * (di % s.nx)) % s.nx; pi_ = pi_ < 0 ? pi_ + s.nx : pi_;
-        int pj_ = (j + js * (dj % s.ny)) % s.ny; pj_ = pj_ < 0 ? pj_ + s.ny : pj_;
-        const uint32_t pixel = uint32_t(pi_ + s.nx * (pj_ + s.ny * ia));
-        const T att = exp(-tau);
-        const uint32_t round_offset = pid / ctl.per_round;
-        TA* bank = banks + (size_t(round_offset) * L.shards + (warp % L.shards)) * L.count;
-#pragma unroll
-        for (int m = 0; m < NMAT; ++m) tally_add(bank + NMAT * pixel + m, TA(prob[m] * att));
-        updates += NMAT;
-        if (PATHS) {
+            if (capped) { atomicOr(failure, kDetectorCap); break; }
+            T height = __ldg(s.zsum + k) + (ks > 0 ? __ldg(s.zunit + k) - z_old : z_old);
+            height = __ldg(s.zsum + top) - height;
+            const T dxp = aa * height / ca, dyp = ba * height / ca;
+            const uint32_t di = uint32_t(((s.xunit - x_old) + dxp) / s.xunit);
+            const uint32_t dj = uint32_t(((s.yunit - y_old) + dyp) / s.yunit);
+            int pi_ = i + is * int(dv.nx.mod(di));
+            pi_ = pi_ < 0 ? pi_ + s.nx : (pi_ >= s.nx ? pi_ - s.nx : pi_);
+            int pj_ = j + js * int(dv.ny.mod(dj));
+            pj_ = pj_ < 0 ? pj_ + s.ny : (pj_ >= s.ny ? pj_ - s.ny : pj_);
+            const uint32_t pixel = uint32_t(pi_ + s.nx * (pj_ + s.ny * ia));
+            const T att = exp(-tau);
             const T w = prob[0] * att;
-            TA* layer = bank + L.stokes + size_t(pixel) * s.nz;
-            TA* first = bank + L.stokes + L.layer + size_t(pixel) * (s.nz + 1);
-            TA* view = bank + L.stokes + L.layer + L.first + size_t(pixel) * s.nz;
-            const T* wander = P.wander + size_t(slot) * s.nz;
-            for (int kk = wmin; kk <= wmax; ++kk) {
-                const T v = w * wander[kk];
-                if (v != T(0)) { tally_add(layer + kk, TA(v)); ++updates; }
+            quad_add(pixrec + pixel, TA(w), TA(NMAT > 1 ? prob[1] * att : T(0)), TA(NMAT > 2 ? prob[2] * att : T(0)),
+                     TA(PATHS ? w : T(0)));
+            ++updates;
+            if (PATHS) {
+                Quad<TA>* rec = layrec + size_t(pixel) * (s.nz + 1);
+                // Layers touched: the wander range, the event layer k (partial view ray and
+                // the view prefix weight), and the first-event layer k1 (partial descent and
+                // the descent prefix weight; record nz when the surface came first).
+                int lo = k, hi = k;
+                if (wmin <= wmax) { lo = min(lo, wmin); hi = max(hi, wmax); }
+                if (k1 >= 0) { lo = min(lo, k1); hi = max(hi, k1); }
+                const T init_piece = k1 >= 0 ? w * pol.w : T(0);
+                for (int kk = lo; kk <= hi; ++kk) {
+                    T px = (kk >= wmin && kk <= wmax) ? w * wander[kk] : T(0);
+                    T py = T(0), pz = T(0);
+                    if (kk == k) { px += w * z_old * ci; py = w; }
+                    if (kk == k1) { px += init_piece; pz = w; }
+                    if (px != T(0) || py != T(0) || pz != T(0)) {
+                        quad_add(rec + kk, TA(px), TA(py), TA(pz), TA(0));
+                        ++updates;
+                    }
+                }
+                if (k1 < 0) {
+                    quad_add(rec + s.nz, TA(0), TA(0), TA(w), TA(0));
+                    ++updates;
+                }
             }
-            tally_add(first + (k1 + 1), TA(w));
-            if (k1 >= 0) tally_add(layer + k1, TA(w * P.init_part[slot]));
-            tally_add(view + k, TA(w));
-            tally_add(layer + k, TA(w * z_old * ci));
-            tally_add(bank + L.stokes + L.layer + L.first + L.view + pixel, TA(w));
-            updates += 5;
         }
     }
     unsigned long long v2 = visits, v3 = updates;
@@ -539,27 +576,26 @@ wf_peel(SceneView<T> s, Controls ctl, Pool<T> P, TA* __restrict__ banks, WaveTal
 // ----------------------------------------------------------------------------------
 template <typename T, int NMAT>
 __global__ void __launch_bounds__(256)
-wf_scatter(SceneView<T> s, Controls ctl, Pool<T> P, uint32_t* __restrict__ failure) {
+wf_scatter(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t* __restrict__ failure) {
     const T eps = Tol<T>::eps;
     const T pi = pi_v<T>();
     const uint32_t ns = P.counts[0], ng = P.counts[1], np = P.counts[2];
     const uint32_t total = ns + ng + np;
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
-        uint32_t slot;
-        bool surface = false;
-        if (e < ns) { slot = P.queue[kQueueSurface][e]; surface = true; }
-        else if (e < ns + ng) slot = P.queue[kQueueGas][e - ns];
-        else slot = P.queue[kQueueParticle][e - ns - ng];
+        bool surface;
+        const uint32_t slot = queue_entry(P.queue, e, ns, ng, surface);
         if (slot >= P.capacity) { atomicOr(failure, kQueueCorrupt); continue; }
-        const uint32_t pid = P.pid[slot];
+        uint4 meta = P.meta[slot];
+        const uint32_t pid = meta.x;
         if (pid == kNone) { atomicOr(failure, kQueueCorrupt); continue; }
-        uint32_t photon, round;
-        photon_origin(s, ctl, pid, photon, round);
+        const uint32_t ro = dv.per_round.div(pid);
         DrawStream rng;
-        rng.init(photon, round, ctl.seed, P.draw[slot]);
-        const T a0 = P.a[slot], b0 = P.b[slot], c0 = P.c[slot];
+        rng.init(pid - ro * ctl.per_round, ctl.first_round + ro, ctl.seed, meta.y);
+        Quad<T> pos = P.pos[slot];
+        const Quad<T> dir0 = P.dir[slot];
+        Quad<T> pol = P.pol[slot];
+        const T a0 = dir0.x, b0 = dir0.y, c0 = dir0.z;
         T a, b, c, phi_out, q = T(0), u = T(0);
-        bool fresh_path = false;
         if (surface) {
             const T Pd = T(rng.next()), U = T(rng.next());
             const T mu = sqrt(Pd);
@@ -570,48 +606,46 @@ wf_scatter(SceneView<T> s, Controls ctl, Pool<T> P, uint32_t* __restrict__ failu
             a = sine * cp; b = sine * sp; c = fabs(mu);
         } else {
             const int sp = int(P.kind[slot]) - 1;
-            const T phi = P.phi[slot];
-            T st[3] = {T(1), P.q[slot], P.u[slot]};
+            const T phi = dir0.w;
+            T st[3] = {T(1), pol.x, pol.y};
             T cos_out, dphi, cos_sca;
             if (!sample_direction<T>(s, sp, NMAT, st, c0, rng, cos_out, dphi, cos_sca)) {
                 atomicOr(failure, kSamplingCap);
-                P.pid[slot] = kNone;
+                P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u);
                 continue;
             }
             phi_out = phi + dphi;
             const Rot<T> r = NMAT > 1 ? rotation<T>(cos_sca, c0, cos_out, phi, phi_out) : Rot<T>{T(1), T(0), T(1), T(0)};
             const Phase<T> f = phase<T>(s, sp, cos_sca, NMAT);
-            T ns_[3];
-            scatter_stokes<T>(f, r, NMAT, st, ns_);
+            T out[3];
+            scatter_stokes<T>(f, r, NMAT, st, out);
             // S / S(1): I becomes 1 (NaN when S(1) is 0 or not finite).
-            const T s0 = ns_[0];
+            const T s0 = out[0];
             const T one = s0 / s0;
             bool ok = isfinite(one);
             if (NMAT > 1) {
-                q = ns_[1] / s0; u = ns_[2] / s0;
+                q = out[1] / s0; u = out[2] / s0;
                 ok = ok && isfinite(q) && isfinite(u) && sqrt(q * q + u * u) <= one + T(1e-2);
             }
-            if (!ok) { atomicOr(failure, kInvalidStokes); P.pid[slot] = kNone; continue; }
+            if (!ok) { atomicOr(failure, kInvalidStokes); P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u); continue; }
             const T so = sqrt(fmax(T(0), T(1) - cos_out * cos_out));
             T spo, cpo;
             sincos(phi_out, &spo, &cpo);
             a = cpo * so; b = spo * so; c = cos_out;
-            fresh_path = true;
         }
-        T x = P.x[slot], y = P.y[slot], z = P.z[slot];
-        if (a * a0 < T(0)) x = fmax(T(0), s.xunit - x);
-        if (b * b0 < T(0)) y = fmax(T(0), s.yunit - y);
+        if (a * a0 < T(0)) pos.x = fmax(T(0), s.xunit - pos.x);
+        if (b * b0 < T(0)) pos.y = fmax(T(0), s.yunit - pos.y);
         if (c * c0 < T(0)) {
-            int k, k1, wmin, wmax;
-            unpack_layers(P.layers[slot], k, k1, wmin, wmax);
-            z = fmax(T(0), __ldg(s.zunit + k) - z);
+            const int k = int(meta.w & 0xFF) - 1;
+            pos.z = fmax(T(0), __ldg(s.zunit + k) - pos.z);
         }
-        P.x[slot] = x; P.y[slot] = y; P.z[slot] = z;
-        P.a[slot] = a; P.b[slot] = b; P.c[slot] = c;
-        P.phi[slot] = phi_out;
-        P.q[slot] = q; P.u[slot] = u;
-        if (fresh_path) P.remains[slot] = -log(fmax(T(rng.next()), eps));
-        P.draw[slot] = rng.draw;
+        pol.x = q; pol.y = u;
+        if (!surface) pol.z = -log(fmax(T(rng.next()), eps));
+        meta.y = rng.draw;
+        P.pos[slot] = pos;
+        P.dir[slot] = Quad<T>{a, b, c, phi_out};
+        P.pol[slot] = pol;
+        P.meta[slot] = meta;
     }
 }
 
@@ -624,7 +658,7 @@ template <typename TA>
 __global__ void wf_flush(const TA* __restrict__ banks, WaveTally L, int nmat, int nx, int ny, int nz, int angles,
                          const double* __restrict__ info, uint32_t rounds, uint32_t out_count, bool paths,
                          double* __restrict__ out) {
-    const uint32_t pixels = uint32_t(nx * ny * angles);
+    const uint32_t pixels = L.pixels;
     const uint32_t stokes_out = uint32_t(nmat) * pixels;
     const uint64_t total = uint64_t(out_count) * rounds;
     const double* zunit = info;
@@ -635,15 +669,17 @@ __global__ void wf_flush(const TA* __restrict__ banks, WaveTally L, int nmat, in
         const uint32_t r = uint32_t(e / out_count);
         const uint32_t o = uint32_t(e % out_count);
         const TA* base = banks + size_t(r) * L.shards * L.count;
-        auto sum = [&](uint32_t index) {
+        auto sum = [&](size_t index) {
             double acc = 0.0;
             for (uint32_t sh = 0; sh < L.shards; ++sh) acc += double(base[size_t(sh) * L.count + index]);
             return acc;
         };
         double value;
         if (o < stokes_out) {
-            const uint32_t ia = o / uint32_t(nmat * nx * ny);
-            value = sum(o) * mu0mu[ia];
+            const uint32_t m = o % uint32_t(nmat);
+            const uint32_t pixel = o / uint32_t(nmat);
+            const uint32_t ia = pixel / uint32_t(nx * ny);
+            value = sum(size_t(pixel) * 4 + m) * mu0mu[ia];
         } else if (paths && o < stokes_out + pixels * uint32_t(nz)) {
             const uint32_t q = o - stokes_out;  // i + nx * (j + ny * (k + nz * ia))
             const uint32_t i = q % nx;
@@ -652,18 +688,19 @@ __global__ void wf_flush(const TA* __restrict__ banks, WaveTally L, int nmat, in
             const int k = int(t % nz);
             const uint32_t ia = t / nz;
             const uint32_t pixel = i + nx * (j + ny * ia);
-            value = sum(L.stokes + pixel * nz + k);
-            double first = 0.0;
-            for (int s = 0; s <= k; ++s) first += sum(L.stokes + L.layer + pixel * (nz + 1) + s);
+            const size_t rec = 4 * size_t(pixels) + size_t(pixel) * (nz + 1) * 4;
+            value = sum(rec + size_t(k) * 4);
+            double first = sum(rec + size_t(nz) * 4 + 2);
+            for (int s = 0; s < k; ++s) first += sum(rec + size_t(s) * 4 + 2);
             value += zunit[k] * inv_mu0 * first;
             if (k < nz - 1) {
                 double view = 0.0;
-                for (int s = 0; s < k; ++s) view += sum(L.stokes + L.layer + L.first + pixel * nz + s);
+                for (int s = 0; s < k; ++s) view += sum(rec + size_t(s) * 4 + 1);
                 value += zunit[k] * inv_mu[ia] * view;
             }
         } else {
             const uint32_t pixel = o - stokes_out - pixels * uint32_t(nz);
-            value = sum(L.stokes + L.layer + L.first + L.view + pixel);
+            value = sum(size_t(pixel) * 4 + 3);
         }
         out[e] = value;
     }
