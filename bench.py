@@ -45,8 +45,9 @@ METRIC = "time to SE/|I|<1% per scene, plain vs importance-guided MC on 1 GB300;
 UNIT = "scatters/s"
 PHOTONS_PER_COLUMN = 20_000
 WORKLOAD = "layered-cloud 30x20x35, I/Q/U + layer AMF, 20000 photons/column/round"
-TALLY_BYTES = 8  # one FP32 read-modify-write in L2
+STATE_BYTES = 64  # one event's photon state records read by the peel kernel
 CELL_BYTES = 16  # one cell record (beta + cumulative species fractions)
+TALLY_BYTES = 32  # one 128-bit tally atomic: 16 B read + 16 B written in L2
 
 
 def peaks():
@@ -269,21 +270,28 @@ def main():
     native = binding.load()
     tables = np.ascontiguousarray(scene.tables)
     err = ctypes.create_string_buffer(4096)
-    handle = native.monki_cuda_create(local, tables.ctypes.data_as(binding.F64P), tables.size, 1, b"precision=fp32", err, len(err))
+    capacity = max(args.steps, args.warmup)
+    handle = native.monki_cuda_create(
+        local, tables.ctypes.data_as(binding.F64P), tables.size, capacity, b"precision=fp32", err, len(err)
+    )
 
     if not handle:
         raise RuntimeError(err.value.decode())
 
     tally_count = int(native.monki_cuda_tally_count(handle))
-    out = np.zeros(tally_count)
+    out = np.zeros(tally_count * capacity)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
     timing = (ctypes.c_float * 2)()
     counters_before = (ctypes.c_uint64 * 6)()
     counters_after = (ctypes.c_uint64 * 6)()
 
-    def step(index):
-        # Ranks run disjoint rounds: round = rank * steps_total + index + 1.
-        controls = (ctypes.c_uint32 * 8)(per_round, 0, rank * 100000 + index + 1, 0, 100000, 0, per_round, 1)
+    def group(first_round, rounds):
+        """One round group in one dispatch, as CUDA.run_batches schedules it, with the
+        per-stage event timing on. Ranks run disjoint rounds (offset 100000 per rank)."""
+
+        controls = (ctypes.c_uint32 * 8)(
+            per_round * rounds, 0, rank * 100000 + first_round, 0, 100000, 1, per_round, rounds
+        )
 
         if native.monki_cuda_run(handle, controls, out.ctypes.data_as(binding.F64P), err, len(err)):
             raise RuntimeError(err.value.decode())
@@ -291,32 +299,27 @@ def main():
         native.monki_cuda_last_timing(handle, timing)
         return timing[0], timing[1]
 
-    for index in range(args.warmup):
-        flush.zero_()
-        torch.cuda.synchronize()
-        step(index)
-
-    kernel_ms, run_ms = [], []
+    # Warm-up: W rounds, untimed.
+    flush.zero_()
+    torch.cuda.synchronize()
+    group(1, args.warmup)
     native.monki_cuda_counters(handle, counters_before)
+    flush.zero_()  # 256 MiB write: the timed group starts with a cold L2
     barrier()
 
     with Clocks(local) as clocks:
         wall = time.perf_counter()
-
-        for index in range(args.steps):
-            flush.zero_()  # 256 MiB write: the next step starts with a cold L2
-            torch.cuda.synchronize()
-            k, r = step(args.warmup + index)
-            kernel_ms.append(k)
-            run_ms.append(r)
-
+        kernel_ms, run_ms = group(args.warmup + 1, args.steps)
         barrier()
         wall = time.perf_counter() - wall
 
     native.monki_cuda_counters(handle, counters_after)
+    stage_ms = (ctypes.c_double * 3)()
+    stage_launches = (ctypes.c_uint64 * 3)()
+    native.monki_cuda_stage_timing(handle, stage_ms, stage_launches)
     delta = [int(a) - int(b) for a, b in zip(counters_after, counters_before, strict=True)]
     scatters, visits_fp, visits_det, updates, photons, launches = delta
-    device_seconds = sum(run_ms) / 1e3
+    device_seconds = run_ms / 1e3
 
     if world > 1:
         import torch.distributed as dist
@@ -332,10 +335,15 @@ def main():
 
     native.monki_cuda_close(handle)
     value = total_scatters / device_seconds
-    bytes_per_launch = (CELL_BYTES * (visits_fp + visits_det) + TALLY_BYTES * updates) / args.steps
-    kernel_seconds = sum(kernel_ms) / 1e3 / args.steps
+    # Roofline of the dominant kernel, the peel stage: per launch, the event state it reads,
+    # the cells its detector rays visit and its 128-bit tally atomics, over its event time.
+    peel_launches = max(int(stage_launches[1]), 1)
+    peel_seconds = stage_ms[1] / 1e3 / peel_launches
+    peel_bytes = (STATE_BYTES * scatters + CELL_BYTES * visits_det + TALLY_BYTES * updates) / peel_launches
     peak, peak_kind = peaks()
-    achieved = bytes_per_launch / kernel_seconds / 1e9
+    achieved = peel_bytes / peel_seconds / 1e9
+    stage_total = max(sum(stage_ms), 1e-9)
+    stage_share = {name: stage_ms[q] / stage_total for q, name in enumerate(("transit", "peel", "scatter"))}
 
     # End to end through the public API: prepare (table upload) + every round's copy-out.
     e2e_scene = scenes.layered_cloud(ppc, args.steps)
@@ -382,15 +390,17 @@ def main():
         },
         "roofline": {
             "bound": "hbm",
+            "kernel": "wf_peel (event peel-off: phase matrix, detector ray, tallies)",
             "achieved": achieved,
             "peak": peak,
             "unit": "GB/s",
             "frac": achieved / peak,
             "traffic": recorded_traffic(),
             "peak_source": peak_kind,
-            "algorithmic_bytes_per_launch": bytes_per_launch,
-            "bytes_per_scatter": bytes_per_launch * args.steps / max(scatters, 1),
-            "kernel_ms": kernel_seconds * 1e3,
+            "algorithmic_bytes_per_launch": peel_bytes,
+            "launch_ms": peel_seconds * 1e3,
+            "launches": peel_launches,
+            "stage_share": stage_share,
         },
         "e2e": {
             "value": e2e_value,

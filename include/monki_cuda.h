@@ -59,6 +59,11 @@ int monki_cuda_last_timing(void *session, float out[2]);
  * photons, kernel launches. No reference counterpart (the scatter count is mc.f90's nscat). */
 int monki_cuda_counters(void *session, uint64_t out[6]);
 
+/* Wavefront stage timing of the last run with the profiling flag set, from CUDA events
+ * around each launch: summed milliseconds and launch counts of the transit, peel and
+ * scatter kernels. No reference counterpart. */
+int monki_cuda_stage_timing(void *session, double ms[3], uint64_t launches[3]);
+
 /* Number of float64 values per round in a run's output; no reference counterpart. */
 size_t monki_cuda_tally_count(void *session);
 

@@ -304,6 +304,11 @@ struct Session {
     double* flush_info = nullptr;
     uint32_t* host_counts = nullptr;  // pinned
     uint64_t iterations = 0;
+    // Per-stage event timing of the wavefront (runs with the profiling flag set):
+    // 4 events per iteration of one host-check batch; ms summed per stage.
+    std::vector<cudaEvent_t> stage_events;
+    double stage_ms[3] = {0, 0, 0};
+    uint64_t stage_launches[3] = {0, 0, 0};
     SceneView<float> view32{};
     SceneView<double> view64{};
     int grid = 0;
@@ -406,12 +411,17 @@ void launch_transport(Session& s, const Controls& c, int grid) {
 }
 
 template <typename T, int NMAT, bool PATHS>
-void wave_iteration(Session& s, const SceneView<T>& v, Pool<T>& P, const Controls& c, const Divisors& dv, int grid) {
+void wave_iteration(Session& s, const SceneView<T>& v, Pool<T>& P, const Controls& c, const Divisors& dv, int grid,
+                    cudaEvent_t* ev) {
     T* banks = static_cast<T*>(s.banks);
     check(cudaMemsetAsync(P.counts, 0, 3 * sizeof(uint32_t), s.stream), "memset(queues)");
+    if (ev) cudaEventRecord(ev[0], s.stream);
     wf_transit<T, PATHS><<<grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, s.cfg.walk, s.failure, s.counters);
+    if (ev) cudaEventRecord(ev[1], s.stream);
     wf_peel<T, T, NMAT, PATHS><<<grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, banks, s.wave, s.failure, s.counters);
+    if (ev) cudaEventRecord(ev[2], s.stream);
     wf_scatter<T, NMAT><<<grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, s.failure);
+    if (ev) cudaEventRecord(ev[3], s.stream);
 }
 
 template <typename T>
@@ -433,16 +443,34 @@ void run_wavefront(Session& s, const Controls& c) {
     const bool paths = s.prep.paths;
     const uint64_t limit = uint64_t(c.max_steps) + 16;  // events per photon are bounded by its steps
     uint64_t it = 0;
+    const bool profile = c.profile != 0;
+    if (profile && s.stage_events.size() < 4 * size_t(s.cfg.check_every)) {
+        for (cudaEvent_t e : s.stage_events) cudaEventDestroy(e);
+        s.stage_events.assign(4 * size_t(s.cfg.check_every), nullptr);
+        for (cudaEvent_t& e : s.stage_events) check(cudaEventCreate(&e), "cudaEventCreate");
+    }
+    if (profile) for (int q = 0; q < 3; ++q) { s.stage_ms[q] = 0; s.stage_launches[q] = 0; }
     for (;;) {
         for (uint32_t b = 0; b < s.cfg.check_every; ++b, ++it) {
-            if (nm == 1 && !paths) wave_iteration<T, 1, false>(s, v, P, c, dv, grid);
-            else if (nm == 1) wave_iteration<T, 1, true>(s, v, P, c, dv, grid);
-            else if (!paths) wave_iteration<T, 3, false>(s, v, P, c, dv, grid);
-            else wave_iteration<T, 3, true>(s, v, P, c, dv, grid);
+            cudaEvent_t* ev = profile ? s.stage_events.data() + 4 * b : nullptr;
+            if (nm == 1 && !paths) wave_iteration<T, 1, false>(s, v, P, c, dv, grid, ev);
+            else if (nm == 1) wave_iteration<T, 1, true>(s, v, P, c, dv, grid, ev);
+            else if (!paths) wave_iteration<T, 3, false>(s, v, P, c, dv, grid, ev);
+            else wave_iteration<T, 3, true>(s, v, P, c, dv, grid, ev);
         }
         check(cudaGetLastError(), "wavefront launch");
         check(cudaMemcpyAsync(s.host_counts, P.counts, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s.stream), "copy(counts)");
         check(cudaStreamSynchronize(s.stream), "wavefront");
+        if (profile) {
+            for (uint32_t b = 0; b < s.cfg.check_every; ++b) {
+                for (int q = 0; q < 3; ++q) {
+                    float ms = 0.f;
+                    check(cudaEventElapsedTime(&ms, s.stage_events[4 * b + q], s.stage_events[4 * b + q + 1]), "stage time");
+                    s.stage_ms[q] += ms;
+                    s.stage_launches[q] += 1;
+                }
+            }
+        }
         const uint32_t* h = s.host_counts;
         if (h[3] >= c.count && h[0] == 0 && h[1] == 0 && h[2] == 0) break;
         if (it > limit * 4 + 1024 && it > 1000000) throw std::runtime_error("wavefront did not drain");
@@ -472,6 +500,7 @@ void destroy(Session* s) {
     if (s->t0) cudaEventDestroy(s->t0);
     if (s->t1) cudaEventDestroy(s->t1);
     if (s->t2) cudaEventDestroy(s->t2);
+    for (cudaEvent_t e : s->stage_events) cudaEventDestroy(e);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
 }
@@ -670,6 +699,13 @@ int monki_cuda_counters(void* handle, uint64_t out[6]) {
     if (!handle || !out) return 1;
     Session* s = static_cast<Session*>(handle);
     for (int q = 0; q < 6; ++q) out[q] = s->totals[q];
+    return 0;
+}
+
+int monki_cuda_stage_timing(void* handle, double ms[3], uint64_t launches[3]) {
+    if (!handle || !ms || !launches) return 1;
+    Session* s = static_cast<Session*>(handle);
+    for (int q = 0; q < 3; ++q) { ms[q] = s->stage_ms[q]; launches[q] = s->stage_launches[q]; }
     return 0;
 }
 

@@ -39,7 +39,7 @@ class CUDA(Backend):
         save_path: bool | None = None,
         profile: bool = False,
         seed: int = 23274,
-        photons_per_dispatch: int = 1 << 26,
+        photons_per_dispatch: int = 1 << 30,
         tally_shards: int = 8,
         max_steps: int = 100_000,
         precision: str = "fp32",
@@ -130,7 +130,11 @@ class CUDA(Backend):
         paths = bool(tables[10])
         tally_count = nmat * nx * ny * angles + (nx * ny * (nz + 1) * angles if paths else 0)
         per_round = scene.photons_per_column * nx * ny
-        bytes_per_round = tally_count * self.tally_shards * (4 if self.precision == "fp32" else 8)
+        # Device tally records per round and shard: {I, Q, U, weight} per pixel, plus
+        # {layer, view, first, -} per (pixel, layer + 1) with path diagnostics.
+        pixels = nx * ny * angles
+        device_count = 4 * pixels + (4 * pixels * (nz + 1) if paths else 0)
+        bytes_per_round = device_count * self.tally_shards * (4 if self.precision == "fp32" else 8)
         capacity = max(
             1,
             min(

@@ -27,6 +27,7 @@ _SIGNATURES = {
     "monki_cuda_gpu_seconds": (ctypes.c_double, [ctypes.c_void_p]),
     "monki_cuda_last_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]),
     "monki_cuda_counters": (ctypes.c_int, [ctypes.c_void_p, _U64P]),
+    "monki_cuda_stage_timing": (ctypes.c_int, [ctypes.c_void_p, _F64P, _U64P]),
     "monki_cuda_tally_count": (ctypes.c_size_t, [ctypes.c_void_p]),
     "monki_cuda_device_name": (ctypes.c_char_p, [ctypes.c_void_p]),
     "monki_cuda_close": (None, [ctypes.c_void_p]),
