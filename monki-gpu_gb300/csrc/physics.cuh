@@ -142,8 +142,9 @@ __device__ __forceinline__ Phase<T> phase(const SceneView<T>& s, int sp, T cs, i
 template <typename T>
 struct Rot { T c1, s1, c2, s2; };
 
+// The rotations with the sines and cosines of both azimuths supplied by the caller.
 template <typename T>
-__device__ __forceinline__ Rot<T> rotation(T cs, T uo, T u1, T phio, T phi1) {
+__device__ __forceinline__ Rot<T> rotation_pre(T cs, T uo, T u1, T phio, T phi1, T cpo, T spo, T cp1, T sp1) {
     Rot<T> r{T(1), T(0), T(1), T(0)};
     const T pi = pi_v<T>();
     T dphi = fabs(phio - phi1);
@@ -157,9 +158,6 @@ __device__ __forceinline__ Rot<T> rotation(T cs, T uo, T u1, T phio, T phi1) {
     T sino = fac < Tol<T>::eps ? T(0) : sqrt(fac);
     fac = T(1) - u1 * u1;
     T sin1 = fac < Tol<T>::eps ? T(0) : sqrt(fac);
-    T cpo, spo, cp1, sp1;
-    sincos(phio, &spo, &cpo);
-    sincos(phi1, &sp1, &cp1);
     T cosi1, cosi2, q;
     if (v1) {
         cosi1 = fsign(T(1), u1);
@@ -190,6 +188,14 @@ __device__ __forceinline__ Rot<T> rotation(T cs, T uo, T u1, T phio, T phi1) {
     r.c2 = cosi2 * cosi2 - sini2 * sini2;
     r.s2 = T(2) * sini2 * cosi2;
     return r;
+}
+
+template <typename T>
+__device__ __forceinline__ Rot<T> rotation(T cs, T uo, T u1, T phio, T phi1) {
+    T cpo, spo, cp1, sp1;
+    sincos(phio, &spo, &cpo);
+    sincos(phi1, &sp1, &cp1);
+    return rotation_pre<T>(cs, uo, u1, phio, phi1, cpo, spo, cp1, sp1);
 }
 
 // S_out = L2 * F * L1 * S (matmul_stokes_rot followed by the forward-mode product).

@@ -44,6 +44,8 @@ struct SceneView {
     T xunit, yunit, depol;
     T a0, b0, c0, phi0;  // solar propagation direction cosines and azimuth (rad)
     T va[kMaxViews], vb[kMaxViews], vc[kMaxViews], vphi[kMaxViews];
+    T vsin[kMaxViews];          // sqrt(max(eps, 1 - vc^2))
+    T vcos_phi[kMaxViews], vsin_phi[kMaxViews];  // cos / sin of the view azimuth
     T ssalb_aer[kMaxSpecies];
     const T* cells;
     const T* zunit;

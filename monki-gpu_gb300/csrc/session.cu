@@ -340,6 +340,8 @@ SceneView<T> make_view(const Prepared& p, const Packed<T>& k, void* base) {
         double th = kDegToRad * p.vartheta[ia], ph = kDegToRad * p.vphi[ia];
         s.va[ia] = T(std::cos(ph) * std::sin(th)); s.vb[ia] = T(std::sin(ph) * std::sin(th));
         s.vc[ia] = T(std::cos(th)); s.vphi[ia] = T(ph);
+        s.vsin[ia] = T(std::sqrt(std::max(1e-16, 1.0 - double(s.vc[ia]) * double(s.vc[ia]))));
+        s.vcos_phi[ia] = T(std::cos(double(s.vphi[ia]))); s.vsin_phi[ia] = T(std::sin(double(s.vphi[ia])));
     }
     s.cells = tv + k.cells; s.zunit = tv + k.zunit; s.zsum = tv + k.zsum; s.ssalb_gas = tv + k.ssalb_gas;
     s.albedo = tv + k.albedo; s.tau_above = tv + k.tau_above;

@@ -250,7 +250,7 @@ __device__ __forceinline__ int uniform_jump(const SceneView<T>& s, int& k, T& z,
 // transit: free path to the next interaction for every pooled photon.
 // ----------------------------------------------------------------------------------
 template <typename T, bool PATHS>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
 wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, uint32_t* __restrict__ failure,
            unsigned long long* __restrict__ counters) {
     const T eps = Tol<T>::eps;
@@ -439,7 +439,7 @@ __device__ __forceinline__ uint32_t queue_entry(uint32_t* const* queue, uint32_t
 // peel: one event per thread, every view.
 // ----------------------------------------------------------------------------------
 template <typename T, typename TA, int NMAT, bool PATHS>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
 wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ banks, WaveTally L,
         uint32_t* __restrict__ failure, unsigned long long* __restrict__ counters) {
     const T eps = Tol<T>::eps;
@@ -472,14 +472,19 @@ wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ b
         Quad<TA>* layrec = reinterpret_cast<Quad<TA>*>(bank + 4 * size_t(L.pixels));
         const T* wander = PATHS ? P.wander + size_t(slot) * s.nz : nullptr;
         const T sin_c = sqrt(fmax(eps, T(1) - c * c));
+        T sphi, cphi;
+        sincos(phi, &sphi, &cphi);
         for (int ia = 0; ia < s.angles; ++ia) {
             const T vc = s.vc[ia];
             T prob[3] = {T(0), T(0), T(0)};
             if (surface) {
                 prob[0] = vc > T(0) ? vc * weight : T(0);
             } else {
-                const T cs = c * vc + sin_c * sqrt(fmax(eps, T(1) - vc * vc)) * cos(phi - s.vphi[ia]);
-                const Rot<T> r = NMAT > 1 ? rotation<T>(cs, c, vc, phi, s.vphi[ia]) : Rot<T>{T(1), T(0), T(1), T(0)};
+                // cos(phi - phi_view) from the sines and cosines of both azimuths.
+                const T cdphi = cphi * s.vcos_phi[ia] + sphi * s.vsin_phi[ia];
+                const T cs = c * vc + sin_c * s.vsin[ia] * cdphi;
+                const Rot<T> r = NMAT > 1 ? rotation_pre<T>(cs, c, vc, phi, s.vphi[ia], cphi, sphi, s.vcos_phi[ia], s.vsin_phi[ia])
+                                          : Rot<T>{T(1), T(0), T(1), T(0)};
                 const Phase<T> f = phase<T>(s, sp, cs, NMAT);
                 T back[3];
                 scatter_stokes<T>(f, r, NMAT, st, back);
@@ -575,7 +580,7 @@ wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ b
 // scatter: new direction (and Stokes vector) for every queued event.
 // ----------------------------------------------------------------------------------
 template <typename T, int NMAT>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
 wf_scatter(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t* __restrict__ failure) {
     const T eps = Tol<T>::eps;
     const T pi = pi_v<T>();
