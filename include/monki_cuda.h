@@ -80,6 +80,20 @@ void monki_cuda_close(void *session);
 int monki_cuda_inspect(const double *tables, size_t table_count, int fp64, int32_t *uniform_top,
                        double *tau_above, size_t tau_capacity, char *err, size_t errlen);
 
+/* Transport without device allocation; no counterpart in the reference. For callers
+ * that cannot call cudaMalloc (an application that owns all device memory through its
+ * own arena, a real-time loop that must not allocate while running, a plugin host that
+ * owns the GPU memory budget): runs one round group of the photon-history kernel like
+ * monki_cuda_run, but keeps every device scratch buffer (packed scene, FP32 tally bank,
+ * FP64 output staging, flags) in one fixed 16 MiB array inside this library, which each
+ * GPU that loads the library holds until the process exits. Inputs and outputs are the
+ * caller's host arrays, as for create + run. Scenes whose scratch exceeds 16 MiB are
+ * rejected with an error. All calls share the array: calls that overlap on the GPU race,
+ * and each call clears what must start at zero. The first call on a device looks up the
+ * array's device address; make it before any stream capture. */
+int monki_cuda_run_static(uint32_t device, const double *tables, size_t table_count,
+                          const uint32_t controls[8], double *out, char *err, size_t errlen);
+
 /* Device probes of the production helpers, the counterpart of the reference's probe
  * kernels (tests/integration/test_metal.py:23-103). */
 int monki_cuda_probe_philox(uint32_t device, const uint32_t *counters, const uint32_t *keys,

@@ -14,6 +14,7 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <mutex>
 #include <vector>
 
 #include "wavefront.cuh"
@@ -743,3 +744,140 @@ int monki_cuda_inspect(const double* tables, size_t table_count, int fp64, int32
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// Transport without device allocation.
+//
+// Some callers cannot call cudaMalloc: a host application that hands all device memory
+// out of its own arena and forbids other allocations, a real-time pipeline that must not
+// allocate (an allocation can synchronize the device or fail under memory pressure) once
+// it is running, or a plugin host that owns the GPU's memory budget. For them,
+// monki_cuda_run_static runs one round group of the photon-history kernel with every
+// scratch buffer (packed scene, FP32 tally bank, failure word, counters, FP64 output
+// staging) inside the fixed array below, so the call itself allocates nothing.
+//
+// The array is 16 MiB, and every GPU that loads this library holds it until the process
+// exits. All calls share it and it keeps the last call's contents: each call clears the
+// parts that must start at zero, and two calls that overlap on the GPU (from several host
+// threads or on several streams) race on it. The first call on a device looks up the
+// array's device address for that device, so make that first call before any stream
+// capture.
+// ---------------------------------------------------------------------------------------
+namespace monki {
+namespace {
+
+constexpr size_t kStaticScratchBytes = size_t(16) << 20;
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+constexpr int kStaticMaxDevices = 64;
+std::mutex g_static_lock;
+void* g_static_address[kStaticMaxDevices] = {};
+int g_static_grid[kStaticMaxDevices] = {};
+
+}  // namespace
+}  // namespace monki
+
+extern "C" int monki_cuda_run_static(uint32_t device, const double* tables, size_t table_count,
+                                     const uint32_t controls[8], double* out, char* err, size_t errlen) {
+    try {
+        if (!tables || !controls || !out) throw std::runtime_error("Invalid tables, controls or output buffer");
+        int count = 0;
+        if (cudaGetDeviceCount(&count) != cudaSuccess || device >= uint32_t(count) || device >= uint32_t(kStaticMaxDevices))
+            throw std::runtime_error("Requested CUDA device is unavailable");
+        check(cudaSetDevice(int(device)), "cudaSetDevice");
+        void* base = nullptr;
+        int grid = 0;
+        {
+            // Once per device, with the device current: the array's address on this device.
+            std::lock_guard<std::mutex> guard(g_static_lock);
+            if (!g_static_address[device]) {
+                void* address = nullptr;
+                check(cudaGetSymbolAddress(&address, g_static_scratch), "cudaGetSymbolAddress");
+                cudaDeviceProp prop{};
+                check(cudaGetDeviceProperties(&prop, int(device)), "cudaGetDeviceProperties");
+                if (prop.major < 10) throw std::runtime_error("This build targets sm_103a (GB300)");
+                int blocks = 0;
+                check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                          &blocks, reinterpret_cast<const void*>(&transport_kernel<float, float, 3, true>), 256, 0),
+                      "occupancy");
+                g_static_grid[device] = prop.multiProcessorCount * std::max(blocks, 1);
+                g_static_address[device] = address;
+            }
+            base = g_static_address[device];
+            grid = g_static_grid[device];
+        }
+
+        const Prepared p = parse(tables, table_count);
+        const Controls c{controls[0], controls[1], controls[2], controls[3], controls[4], controls[5], controls[6], controls[7]};
+        if (!c.per_round || !c.rounds || !c.max_steps || uint64_t(c.first) + c.count > uint64_t(c.per_round) * c.rounds)
+            throw std::runtime_error("Invalid CUDA round group");
+
+        // Layout inside the array: packed scene, tally bank (one shard per round), FP64
+        // output staging, mu0/mu per view, failure word and counters.
+        Packed<float> k = pack<float>(p, true);
+        TallyLayout L{};
+        L.stokes = uint32_t(p.nmat * p.nx * p.ny * p.angles);
+        L.paths = p.paths ? uint32_t(p.nx * p.ny * p.nz * p.angles) : 0u;
+        L.weights = p.paths ? uint32_t(p.nx * p.ny * p.angles) : 0u;
+        L.count = L.stokes + L.paths + L.weights;
+        L.shards = 1;
+        const size_t scene_bytes = align_up(k.values.size() * sizeof(float) + k.guides.size() * sizeof(int), 256);
+        const size_t bank_bytes = align_up(size_t(c.rounds) * L.count * sizeof(float), 256);
+        const size_t out_bytes = align_up(size_t(c.rounds) * L.count * sizeof(double), 256);
+        const size_t mu_bytes = align_up(size_t(p.angles) * sizeof(double), 256);
+        const size_t small_bytes = 256;  // failure word + 4 counters
+        const size_t needed = scene_bytes + bank_bytes + out_bytes + mu_bytes + small_bytes;
+        if (needed > kStaticScratchBytes) {
+            char msg[256];
+            std::snprintf(msg, sizeof msg,
+                          "Scene and round group need %zu bytes of scratch; the static scratch holds %zu (16 MiB)",
+                          needed, kStaticScratchBytes);
+            throw std::runtime_error(msg);
+        }
+        char* at = static_cast<char*>(base);
+        char* scene = at;
+        float* banks = reinterpret_cast<float*>(at + scene_bytes);
+        double* staged = reinterpret_cast<double*>(at + scene_bytes + bank_bytes);
+        double* mu0mu = reinterpret_cast<double*>(at + scene_bytes + bank_bytes + out_bytes);
+        uint32_t* failure = reinterpret_cast<uint32_t*>(at + scene_bytes + bank_bytes + out_bytes + mu_bytes);
+        unsigned long long* counters = reinterpret_cast<unsigned long long*>(
+            at + scene_bytes + bank_bytes + out_bytes + mu_bytes + 64);
+
+        std::vector<double> mu(size_t(p.angles));
+        for (int ia = 0; ia < p.angles; ++ia)
+            mu[size_t(ia)] = std::fabs(std::cos(kDegToRad * p.vartheta0)) / std::fabs(std::cos(kDegToRad * p.vartheta[size_t(ia)]));
+        check(cudaMemcpy(scene, k.values.data(), k.values.size() * sizeof(float), cudaMemcpyHostToDevice), "upload(scene)");
+        if (!k.guides.empty())
+            check(cudaMemcpy(scene + k.values.size() * sizeof(float), k.guides.data(), k.guides.size() * sizeof(int),
+                             cudaMemcpyHostToDevice), "upload(guides)");
+        check(cudaMemcpy(mu0mu, mu.data(), mu.size() * sizeof(double), cudaMemcpyHostToDevice), "upload(mu0mu)");
+        // The array keeps the previous call's contents: clear everything that accumulates.
+        check(cudaMemset(banks, 0, bank_bytes), "clear(banks)");
+        check(cudaMemset(failure, 0, small_bytes), "clear(flags)");
+        const SceneView<float> v = make_view<float>(p, k, scene);
+        const int blocks = int(std::min<uint64_t>((uint64_t(c.count) + 255) / 256, uint64_t(grid)));
+        if (c.count) {
+            if (p.nmat == 1 && !p.paths) transport_kernel<float, float, 1, false><<<std::max(blocks, 1), 256>>>(v, c, banks, L, failure, counters);
+            else if (p.nmat == 1) transport_kernel<float, float, 1, true><<<std::max(blocks, 1), 256>>>(v, c, banks, L, failure, counters);
+            else if (!p.paths) transport_kernel<float, float, 3, false><<<std::max(blocks, 1), 256>>>(v, c, banks, L, failure, counters);
+            else transport_kernel<float, float, 3, true><<<std::max(blocks, 1), 256>>>(v, c, banks, L, failure, counters);
+            check(cudaGetLastError(), "transport launch");
+        }
+        const uint64_t total = uint64_t(L.count) * c.rounds;
+        const int fgrid = int(std::min<uint64_t>((total + 255) / 256, 4096));
+        flush_kernel<float><<<std::max(fgrid, 1), 256>>>(banks, L, p.nmat, p.nx, p.ny, p.nz, p.angles, mu0mu, c.rounds, staged);
+        check(cudaGetLastError(), "flush launch");
+        uint32_t flag = 0;
+        check(cudaMemcpy(&flag, failure, sizeof(flag), cudaMemcpyDeviceToHost), "copy(failure)");
+        check(cudaMemcpy(out, staged, total * sizeof(double), cudaMemcpyDeviceToHost), "copy(tallies)");
+        if (flag) {
+            char msg[128];
+            std::snprintf(msg, sizeof msg, "CUDA transport failed (flag %u); round rejected", flag);
+            throw std::runtime_error(msg);
+        }
+        return 0;
+    } catch (const std::exception& e) {
+        monki::write_error(err, errlen, e.what());
+        return 1;
+    }
+}

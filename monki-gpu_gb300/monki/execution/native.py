@@ -35,6 +35,10 @@ _SIGNATURES = {
         ctypes.c_int,
         [_F64P, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(ctypes.c_int32), _F64P, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t],
     ),
+    "monki_cuda_run_static": (
+        ctypes.c_int,
+        [ctypes.c_uint32, _F64P, ctypes.c_size_t, _U32P, _F64P, ctypes.c_char_p, ctypes.c_size_t],
+    ),
     "monki_cuda_probe_philox": (
         ctypes.c_int,
         [ctypes.c_uint32, _U32P, _U32P, ctypes.c_uint32, _U32P, ctypes.c_char_p, ctypes.c_size_t],
