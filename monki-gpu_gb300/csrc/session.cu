@@ -375,7 +375,8 @@ Pool<T> allocate_pool(Session& s) {
     const size_t nz = size_t(s.prep.nz);
     const size_t quad = n * sizeof(Quad<T>);
     const size_t parts[] = {quad, quad, quad, n * sizeof(uint4), n * sizeof(uint32_t), n,
-                            n * nz * sizeof(T), 3 * n * sizeof(uint32_t), 16 * sizeof(uint32_t)};
+                            n * nz * sizeof(T), n * sizeof(uint32_t), 2 * n * sizeof(T),
+                            3 * n * sizeof(uint32_t), 16 * sizeof(uint32_t)};
     size_t bytes = 0;
     for (size_t part : parts) bytes += align_up(part, 256);
     check(cudaMalloc(&s.pool_memory, bytes), "cudaMalloc(pool)");
@@ -390,6 +391,8 @@ Pool<T> allocate_pool(Session& s) {
     P.steps = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
     P.kind = reinterpret_cast<uint8_t*>(take(n));
     P.wander = reinterpret_cast<T*>(take(n * nz * sizeof(T)));
+    P.runs = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
+    P.run_ci = reinterpret_cast<T*>(take(2 * n * sizeof(T)));
     uint32_t* queues = reinterpret_cast<uint32_t*>(take(3 * n * sizeof(uint32_t)));
     for (int q = 0; q < 3; ++q) P.queue[q] = queues + size_t(q) * n;
     P.counts = reinterpret_cast<uint32_t*>(take(16 * sizeof(uint32_t)));

@@ -65,7 +65,8 @@ struct Divisors { FastDiv per_round, nx, ny, ncol; };
 
 // Device tally layout of one round and one shard (element counts of TA):
 //   pixel records  [pixel]                  {I, Q, U, detected weight}
-//   layer records  [pixel * (nz + 1) + k]   {layer path, view-ray weight, first-event weight, 0}
+//   layer records  [pixel * (nz + 1) + k]   {layer path, view-ray weight, first-event weight,
+//                                            difference array of straight-run weight / |cos|}
 //   (record k = nz holds the first-event weight of histories that met the surface first)
 struct WaveTally {
     uint32_t pixels;   // nx * ny * angles
@@ -84,6 +85,8 @@ struct Pool {
     uint32_t* steps; // walk steps so far (history step limit)
     uint8_t* kind;   // pending event: 0 gas, 1 + s particle s, 255 surface
     T* wander;       // capacity * nz path lengths after the first event
+    uint32_t* runs;  // two straight runs of whole layers: lo0 | hi0 << 8 | lo1 << 16 | hi1 << 24
+    T* run_ci;       // capacity * 2: 1 / |cos| of each run
     uint32_t* queue[3];
     uint32_t* counts;  // [0..2] queue sizes, [3] next photon to claim
 };
@@ -151,6 +154,32 @@ __device__ __forceinline__ void wander_add(T* w, int kk, T v, int& wmin, int& wm
     }
 }
 
+// The layer-path record of a photon after its first event: partial-layer lengths in the
+// wander range, and up to two straight runs of whole layers crossed in uniform runs (each
+// whole layer m of a run adds zunit[m] / |cos|), tallied later as a difference array.
+// A third run falls back to the wander array.
+constexpr uint32_t kNoRuns = 0xFFFFFFFFu;
+
+template <typename T>
+struct PathRecord {
+    T* wander;
+    int wmin, wmax;
+    uint32_t runs;
+    T ci0, ci1;
+    __device__ __forceinline__ void add(int kk, T v) { wander_add(wander, kk, v, wmin, wmax); }
+    __device__ __forceinline__ void run(const T* zunit, int lo, int hi, T ci) {
+        if ((runs & 0xFFu) == 0xFFu) {
+            runs = (runs & 0xFFFF0000u) | uint32_t(lo) | (uint32_t(hi) << 8);
+            ci0 = ci;
+        } else if (((runs >> 16) & 0xFFu) == 0xFFu) {
+            runs = (runs & 0x0000FFFFu) | (uint32_t(lo) << 16) | (uint32_t(hi) << 24);
+            ci1 = ci;
+        } else {
+            for (int m = lo; m <= hi; ++m) add(m, __ldg(zunit + m) * ci);
+        }
+    }
+};
+
 // Move a distance h >= 0 along one horizontal axis of the periodic grid: x is the distance
 // to the next face in direction sgn. Equivalent to the face-by-face walk of ADVANCE.
 template <typename T>
@@ -176,7 +205,7 @@ __device__ __forceinline__ void slide(int& i, T& x, int sgn, T h, T unit, int n)
 // lengths per layer go to the wander array when `record`; an escaping photon needs none.
 template <typename T>
 __device__ __forceinline__ int uniform_jump(const SceneView<T>& s, int& k, T& z, T& remains, int ks, T ca, T ci,
-                                            bool record, T* wander, int& wmin, int& wmax,
+                                            bool record, PathRecord<T>& path,
                                             int& i, T& x, int is, T aa, int& j, T& y, int js, T ba) {
     const T eps = Tol<T>::eps;
     const int top = s.nz - 1;
@@ -188,12 +217,12 @@ __device__ __forceinline__ int uniform_jump(const SceneView<T>& s, int& k, T& z,
         const T de = remains / bk;
         travelled = de;
         z = fmax(T(0), z - ca * de);
-        if (record) wander_add(wander, k, de, wmin, wmax);
+        if (record) path.add(k, de);
         outcome = 0;
     } else {
         remains -= seg * bk;
         travelled = seg;
-        if (record) wander_add(wander, k, seg, wmin, wmax);
+        if (record) path.add(k, seg);
         const int m0 = k + ks;
         // Layers m0 .. end of the run, in the direction of travel.
         const int end = ks > 0 ? __ldg(s.run_hi + k) : __ldg(s.run_lo + k);
@@ -211,8 +240,7 @@ __device__ __forceinline__ int uniform_jump(const SceneView<T>& s, int& k, T& z,
             k = inside ? end + ks : m0;
             if (k > top) outcome = 2;
             else outcome = k < 0 ? 1 : -1;
-            if (outcome != 2 && record && inside)
-                for (int m = m0; m != end + ks; m += ks) wander_add(wander, m, __ldg(s.zunit + m) * ci, wmin, wmax);
+            if (outcome != 2 && record && inside) path.run(s.zunit, min(m0, end), max(m0, end), ci);
             if (outcome == -1) z = __ldg(s.zunit + k);
         } else {
             // The interaction lies inside the run: find its layer.
@@ -231,8 +259,8 @@ __device__ __forceinline__ int uniform_jump(const SceneView<T>& s, int& k, T& z,
             const T de = bm > eps ? remains / bm : T(0);
             travelled += slant_before + de;
             if (record) {
-                for (int q = m0; q != m; q += ks) wander_add(wander, q, __ldg(s.zunit + q) * ci, wmin, wmax);
-                wander_add(wander, m, de, wmin, wmax);
+                if (m != m0) path.run(s.zunit, min(m0, m - ks), max(m0, m - ks), ci);
+                path.add(m, de);
             }
             k = m;
             z = fmax(T(0), __ldg(s.zunit + m) - ca * de);
@@ -266,6 +294,7 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
         Quad<T> pos{}, dir{}, pol{};
         uint32_t steps = 0, budget = walk;
         bool fresh = false;
+        PathRecord<T> path{PATHS ? P.wander + size_t(slot) * s.nz : nullptr, 255, 0, kNoRuns, T(0), T(0)};
 
         if (pid != kNone) {
             const uint32_t ro = dv.per_round.div(pid);
@@ -276,7 +305,13 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
             dir = P.dir[slot];
             pol = P.pol[slot];
             steps = P.steps[slot];
+            if (PATHS) {
+                path.runs = P.runs[slot];
+                path.ci0 = P.run_ci[2 * size_t(slot)];
+                path.ci1 = P.run_ci[2 * size_t(slot) + 1];
+            }
         }
+        path.wmin = wmin; path.wmax = wmax;
         T& x = pos.x; T& y = pos.y; T& z = pos.z; T& weight = pos.w;
         T& remains = pol.z; T& init_part = pol.w;
 
@@ -302,7 +337,8 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
                 dir = Quad<T>{s.a0, s.b0, s.c0, s.phi0};
                 pol.x = T(0); pol.y = T(0);
                 steps = 0;
-                k1 = -2; wmin = 255; wmax = 0; init_part = T(0);
+                k1 = -2; init_part = T(0);
+                path.wmin = 255; path.wmax = 0; path.runs = kNoRuns;
                 remains = -log(fmax(T(rng.next()), eps));
                 fresh = true;
             }
@@ -311,7 +347,6 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
             const T aa = fabs(a), ba = fabs(b), ca = fabs(c);
             const T ai = T(1) / fmax(aa, eps), bi = T(1) / fmax(ba, eps), ci = T(1) / fmax(ca, eps);
             // Path length of the current layer, added to the wander array on layer change.
-            T* wander = PATHS ? P.wander + size_t(slot) * s.nz : nullptr;
             const bool record = PATHS && k1 > -2;
             int acc_k = -1;
             T acc = T(0);
@@ -322,8 +357,7 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
                 if (++steps > ctl.max_steps) { outcome = 3; break; }
                 ++visits;
                 if (__ldg(s.layer_beta + k) >= T(0)) {
-                    outcome = uniform_jump<T>(s, k, z, remains, ks, ca, ci, record, wander, wmin, wmax,
-                                              i, x, is, aa, j, y, js, ba);
+                    outcome = uniform_jump<T>(s, k, z, remains, ks, ca, ci, record, path, i, x, is, aa, j, y, js, ba);
                     if (outcome >= 0) break;
                     continue;
                 }
@@ -336,7 +370,7 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
                         z = fmax(T(0), z - ca * de);
                         if (record) {
                             if (acc_k != k) {
-                                if (acc_k >= 0) wander_add(wander, acc_k, acc, wmin, wmax);
+                                if (acc_k >= 0) path.add(acc_k, acc);
                                 acc_k = k; acc = T(0);
                             }
                             acc += de;
@@ -349,7 +383,7 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
                 const T dist = advance(s, i, j, k, x, y, z, is, js, ks, aa, ba, ca, ai, bi, ci);
                 if (record) {
                     if (acc_k != k_old) {
-                        if (acc_k >= 0) wander_add(wander, acc_k, acc, wmin, wmax);
+                        if (acc_k >= 0) path.add(acc_k, acc);
                         acc_k = k_old; acc = T(0);
                     }
                     acc += dist;
@@ -359,7 +393,7 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
                 outcome = k > top ? 2 : 1;
                 break;
             }
-            if (PATHS && acc_k >= 0) wander_add(wander, acc_k, acc, wmin, wmax);
+            if (PATHS && acc_k >= 0) path.add(acc_k, acc);
             if (outcome == 4) break;  // budget spent: the walk resumes next iteration
             if (outcome == 3) { atomicOr(failure, kHistoryCap); pid = kNone; continue; }
             if (outcome == 2) { pid = kNone; continue; }
@@ -397,8 +431,13 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
             if (meta.x != kNone) P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u);
             continue;
         }
-        P.meta[slot] = make_uint4(pid, rng.draw, uint32_t(i) | (uint32_t(j) << 16), pack_layers(k, k1, wmin, wmax));
+        P.meta[slot] = make_uint4(pid, rng.draw, uint32_t(i) | (uint32_t(j) << 16), pack_layers(k, k1, path.wmin, path.wmax));
         P.steps[slot] = steps;
+        if (PATHS) {
+            P.runs[slot] = path.runs;
+            P.run_ci[2 * size_t(slot)] = path.ci0;
+            P.run_ci[2 * size_t(slot) + 1] = path.ci1;
+        }
         P.pos[slot] = pos;
         P.pol[slot] = pol;
         if (fresh) P.dir[slot] = dir;
@@ -561,6 +600,16 @@ wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ b
                     quad_add(rec + s.nz, TA(0), TA(0), TA(w), TA(0));
                     ++updates;
                 }
+                // Straight runs of whole layers: +w/|cos| from the first layer, -w/|cos| past the last.
+                const uint32_t runs = P.runs[slot];
+                for (int r = 0; r < 2; ++r) {
+                    const uint32_t lh = (runs >> (16 * r)) & 0xFFFFu;
+                    if ((lh & 0xFFu) == 0xFFu) continue;
+                    const T v = w * P.run_ci[2 * size_t(slot) + r];
+                    quad_add(rec + (lh & 0xFFu), TA(0), TA(0), TA(0), TA(v));
+                    quad_add(rec + (lh >> 8) + 1, TA(0), TA(0), TA(0), TA(-v));
+                    updates += 2;
+                }
             }
         }
     }
@@ -698,6 +747,9 @@ __global__ void wf_flush(const TA* __restrict__ banks, WaveTally L, int nmat, in
             double first = sum(rec + size_t(nz) * 4 + 2);
             for (int s = 0; s < k; ++s) first += sum(rec + size_t(s) * 4 + 2);
             value += zunit[k] * inv_mu0 * first;
+            double runs = 0.0;
+            for (int s = 0; s <= k; ++s) runs += sum(rec + size_t(s) * 4 + 3);
+            value += zunit[k] * runs;
             if (k < nz - 1) {
                 double view = 0.0;
                 for (int s = 0; s < k; ++s) view += sum(rec + size_t(s) * 4 + 1);
