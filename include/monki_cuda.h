@@ -73,6 +73,22 @@ const char *monki_cuda_device_name(void *session);
 /* Replaces monki_metal_close (kernels/metal/bridge.m:145-150). Safe on NULL. */
 void monki_cuda_close(void *session);
 
+/* Guided transport (no reference counterpart: the reference's transport is analog only).
+ * Created with config items epsilon=E (detector-directed sampling probability at particle
+ * scatters, [0, 1)), roulette=W (Russian-roulette weight, [0, 1], 0 = off) and cap=C (the
+ * detector branch only for photons lighter than C, 0 = always); the estimator keeps the
+ * analog expectation exactly. This call gives the roulette weight a per-cell scale:
+ * scale holds nx * ny * nz non-negative values in Fortran cell order (i fastest, the
+ * vacuum layer included); NULL removes the map. Applies to later runs. Returns nonzero
+ * with a message in err on failure. */
+int monki_cuda_set_roulette_scale(void *session, const double *scale, size_t cells, char *err, size_t errlen);
+
+/* Importance tally of a session created with importance=1 (no reference counterpart):
+ * writes 2 * nx * ny * nz values, per cell the summed Stokes-I peel-off contribution, per
+ * unit weight at the event, of every event there and of the next seven events of its
+ * history, then the event count; reset != 0 clears the tally. */
+int monki_cuda_importance(void *session, double *out, size_t count, int reset, char *err, size_t errlen);
+
 /* Host-only check of the table packer (no GPU needed): validates the stream and returns
  * the first layer of the horizontally uniform top and the optical depth above each
  * layer, at fp32 or fp64 transport precision. The counterpart of the uniform-top prefix

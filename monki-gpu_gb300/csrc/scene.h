@@ -47,6 +47,7 @@ struct SceneView {
     T vsin[kMaxViews];          // sqrt(max(eps, 1 - vc^2))
     T vcos_phi[kMaxViews], vsin_phi[kMaxViews];  // cos / sin of the view azimuth
     T ssalb_aer[kMaxSpecies];
+    T znorm[kMaxSpecies];       // mass of the analog particle sampler (guided weights)
     const T* cells;
     const T* zunit;
     const T* zsum;
@@ -62,6 +63,21 @@ struct SceneView {
     const T* lut_cdf[kMaxSpecies];
     const int* guide[kMaxSpecies];
 };
+
+// Guided transport (detector-directed sampling at particle scatters and Russian
+// roulette; see wavefront.cuh). epsilon = 0 and roulette = 0 is the analog method.
+template <typename T>
+struct Guide {
+    T epsilon;         // probability of the detector branch at a particle scatter
+    T roulette;        // roulette weight (0 = off), times scale[cell] when a map is set
+    T cap;             // detector branch only while the weight is below cap
+    const T* scale;    // per-cell roulette scale (nx * ny * nz), or null
+};
+
+// Importance tally of a pilot run: per cell the summed Stokes-I contribution, per unit
+// weight at the event, of the event and the next kRing - 1 events of its history, then
+// the event count (2 * nx * ny * nz FP64 values).
+constexpr int kRing = 8;
 
 // Per-launch controls, the eight words of the Metal ABI v2 (kernels/metal/README.md:52-55).
 struct Controls {

@@ -34,6 +34,10 @@ struct Config {
     uint32_t pool = 1u << 20;    // wavefront photon slots
     uint32_t check_every = 8;    // wavefront iterations between host checks
     uint32_t walk = 24;          // walk steps per photon per transit launch
+    double epsilon = 0.0;        // guided: detector-branch probability at particle scatters
+    double roulette = 0.0;       // guided: roulette weight (0 = off)
+    double cap = 0.0;            // guided: detector branch only below this weight (0 = always)
+    bool importance = false;     // tally per-cell importance (pilot runs)
 };
 
 Config parse_config(const char* text) {
@@ -71,9 +75,25 @@ Config parse_config(const char* text) {
         } else if (key == "pool") c.pool = uint32_t(as_int(1024, 1l << 26));
         else if (key == "check_every") c.check_every = uint32_t(as_int(1, 1024));
         else if (key == "walk") c.walk = uint32_t(as_int(1, 1 << 20));
+        else if (key == "epsilon" || key == "roulette" || key == "cap") {
+            char* e = nullptr;
+            const double v = std::strtod(value.c_str(), &e);
+            if (!e || *e || !std::isfinite(v) || v < 0.0) throw std::runtime_error("Invalid config value: " + item);
+            if (key == "epsilon") {
+                if (v >= 1.0) throw std::runtime_error("epsilon must be in [0, 1)");
+                c.epsilon = v;
+            } else if (key == "roulette") {
+                if (v > 1.0) throw std::runtime_error("roulette must be in [0, 1]");
+                c.roulette = v;
+            } else {
+                c.cap = v;
+            }
+        } else if (key == "importance") c.importance = as_int(0, 1) != 0;
         else throw std::runtime_error("Unknown config key: " + key);
     }
     if (c.block % 32) throw std::runtime_error("block must be a multiple of 32");
+    if (!c.wavefront && (c.epsilon > 0.0 || c.roulette > 0.0 || c.importance))
+        throw std::runtime_error("guided transport and importance tallies need engine=wavefront");
     return c;
 }
 
@@ -169,6 +189,30 @@ Prepared parse(const double* raw, size_t count) {
 }
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Mass kept by the analog particle sampler: the integral over the cosine of the proposal
+// density (the bound CDF, linear between nodes) times F11 / (F11 + |F12|), four-point
+// Gauss-Legendre per table interval; exactly the CDF span when F12 = 0 or nmat = 1.
+double analog_norm(const Prepared::Lut& l, int nmat) {
+    static const double xg[4] = {-0.8611363115940526, -0.3399810435848563, 0.3399810435848563, 0.8611363115940526};
+    static const double wg[4] = {0.3478548451374538, 0.6521451548625461, 0.6521451548625461, 0.3478548451374538};
+    double z = 0.0;
+    for (int lo = 0; lo + 1 < l.n; ++lo) {
+        const double dc = l.cdf[size_t(lo) + 1] - l.cdf[size_t(lo)];
+        if (dc == 0.0) continue;
+        if (nmat == 1 || (l.f12[size_t(lo)] == 0.0 && l.f12[size_t(lo) + 1] == 0.0)) { z += dc; continue; }
+        double mean = 0.0;
+        for (int q = 0; q < 4; ++q) {
+            const double t = 0.5 * (xg[q] + 1.0);
+            const double f11 = l.f11[size_t(lo)] + t * (l.f11[size_t(lo) + 1] - l.f11[size_t(lo)]);
+            const double f12 = l.f12[size_t(lo)] + t * (l.f12[size_t(lo) + 1] - l.f12[size_t(lo)]);
+            const double b = f11 + std::fabs(f12);
+            mean += 0.5 * wg[q] * (b > 0.0 ? f11 / b : 0.0);
+        }
+        z += dc * mean;
+    }
+    return z;
+}
 
 // Host image of the device scene: element offsets into one allocation of T, plus the
 // guide tables (int) appended after the T region.
@@ -303,6 +347,8 @@ struct Session {
     Pool<float> pool32{};
     Pool<double> pool64{};
     double* flush_info = nullptr;
+    void* scale = nullptr;            // per-cell roulette scale (T), or null
+    double* importance = nullptr;     // 2 * cells, pilot runs only
     uint32_t* host_counts = nullptr;  // pinned
     uint64_t iterations = 0;
     // Per-stage event timing of the wavefront (runs with the profiling flag set):
@@ -350,6 +396,7 @@ SceneView<T> make_view(const Prepared& p, const Packed<T>& k, void* base) {
     s.run_lo = gv + k.run_lo; s.run_hi = gv + k.run_hi;
     for (int sp = 0; sp < p.ntypes; ++sp) {
         s.lut_n[sp] = p.luts[sp].n; s.ssalb_aer[sp] = T(p.luts[sp].ssalb);
+        s.znorm[sp] = T(analog_norm(p.luts[sp], p.nmat));
         s.lut_f[sp] = tv + k.lut_f[sp]; s.lut_cos[sp] = tv + k.lut_cos[sp]; s.lut_cdf[sp] = tv + k.lut_cdf[sp];
         s.guide[sp] = gv + k.guide[sp];
     }
@@ -374,9 +421,11 @@ Pool<T> allocate_pool(Session& s) {
     const size_t n = s.cfg.pool;
     const size_t nz = size_t(s.prep.nz);
     const size_t quad = n * sizeof(Quad<T>);
+    const size_t ring = s.cfg.importance ? n * kRing : 0;
     const size_t parts[] = {quad, quad, quad, n * sizeof(uint4), n * sizeof(uint32_t), n,
                             n * nz * sizeof(T), n * sizeof(uint32_t), 2 * n * sizeof(T),
-                            3 * n * sizeof(uint32_t), 16 * sizeof(uint32_t)};
+                            3 * n * sizeof(uint32_t), 16 * sizeof(uint32_t),
+                            ring * sizeof(uint32_t), ring * sizeof(T), s.cfg.importance ? n * sizeof(uint32_t) : 0};
     size_t bytes = 0;
     for (size_t part : parts) bytes += align_up(part, 256);
     check(cudaMalloc(&s.pool_memory, bytes), "cudaMalloc(pool)");
@@ -396,6 +445,12 @@ Pool<T> allocate_pool(Session& s) {
     uint32_t* queues = reinterpret_cast<uint32_t*>(take(3 * n * sizeof(uint32_t)));
     for (int q = 0; q < 3; ++q) P.queue[q] = queues + size_t(q) * n;
     P.counts = reinterpret_cast<uint32_t*>(take(16 * sizeof(uint32_t)));
+    if (s.cfg.importance) {
+        P.ring_cell = reinterpret_cast<uint32_t*>(take(ring * sizeof(uint32_t)));
+        P.ring_inv = reinterpret_cast<T*>(take(ring * sizeof(T)));
+        P.ring_n = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
+        P.importance = s.importance;
+    }
     return P;
 }
 
@@ -420,13 +475,15 @@ template <typename T, int NMAT, bool PATHS>
 void wave_iteration(Session& s, const SceneView<T>& v, Pool<T>& P, const Controls& c, const Divisors& dv, int grid,
                     cudaEvent_t* ev) {
     T* banks = static_cast<T*>(s.banks);
-    check(cudaMemsetAsync(P.counts, 0, 3 * sizeof(uint32_t), s.stream), "memset(queues)");
+    check(cudaMemsetAsync(P.counts, 0, 4 * sizeof(uint32_t), s.stream), "memset(queues)");
     if (ev) cudaEventRecord(ev[0], s.stream);
     wf_transit<T, PATHS><<<grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, s.cfg.walk, s.failure, s.counters);
     if (ev) cudaEventRecord(ev[1], s.stream);
     wf_peel<T, T, NMAT, PATHS><<<grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, banks, s.wave, s.failure, s.counters);
     if (ev) cudaEventRecord(ev[2], s.stream);
-    wf_scatter<T, NMAT><<<grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, s.failure);
+    Guide<T> g{T(s.cfg.epsilon), T(s.cfg.roulette), s.cfg.cap > 0.0 ? T(s.cfg.cap) : T(INFINITY),
+               static_cast<const T*>(s.scale)};
+    wf_scatter<T, NMAT><<<grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, g, s.failure);
     if (ev) cudaEventRecord(ev[3], s.stream);
 }
 
@@ -465,7 +522,7 @@ void run_wavefront(Session& s, const Controls& c) {
             else wave_iteration<T, 3, true>(s, v, P, c, dv, grid, ev);
         }
         check(cudaGetLastError(), "wavefront launch");
-        check(cudaMemcpyAsync(s.host_counts, P.counts, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s.stream), "copy(counts)");
+        check(cudaMemcpyAsync(s.host_counts, P.counts, 5 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s.stream), "copy(counts)");
         check(cudaStreamSynchronize(s.stream), "wavefront");
         if (profile) {
             for (uint32_t b = 0; b < s.cfg.check_every; ++b) {
@@ -478,7 +535,9 @@ void run_wavefront(Session& s, const Controls& c) {
             }
         }
         const uint32_t* h = s.host_counts;
-        if (h[3] >= c.count && h[0] == 0 && h[1] == 0 && h[2] == 0) break;
+        // Done when every photon was claimed and none is queued for an event or paused
+        // mid-walk by the per-launch step budget.
+        if (h[4] >= c.count && h[0] == 0 && h[1] == 0 && h[2] == 0 && h[3] == 0) break;
         if (it > limit * 4 + 1024 && it > 1000000) throw std::runtime_error("wavefront did not drain");
     }
     s.iterations += it;
@@ -501,7 +560,7 @@ void destroy(Session* s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     cudaFree(s->scene); cudaFree(s->banks); cudaFree(s->out); cudaFree(s->mu0mu);
     cudaFree(s->failure); cudaFree(s->counters);
-    cudaFree(s->pool_memory); cudaFree(s->flush_info);
+    cudaFree(s->pool_memory); cudaFree(s->flush_info); cudaFree(s->scale); cudaFree(s->importance);
     if (s->host_counts) cudaFreeHost(s->host_counts);
     if (s->t0) cudaEventDestroy(s->t0);
     if (s->t1) cudaEventDestroy(s->t1);
@@ -576,6 +635,11 @@ void* monki_cuda_create(uint32_t device, const double* tables, size_t table_coun
         check(cudaMalloc(&s->failure, sizeof(uint32_t)), "cudaMalloc(failure)");
         check(cudaMalloc(&s->counters, 4 * sizeof(unsigned long long)), "cudaMalloc(counters)");
         if (cfg.fp64) upload<double>(*s); else upload<float>(*s);
+        if (cfg.importance) {
+            const size_t cells = size_t(p.nx) * p.ny * p.nz;
+            check(cudaMalloc(&s->importance, 2 * cells * sizeof(double)), "cudaMalloc(importance)");
+            check(cudaMemset(s->importance, 0, 2 * cells * sizeof(double)), "cudaMemset(importance)");
+        }
         if (cfg.wavefront) {
             if (cfg.fp64) s->pool64 = allocate_pool<double>(*s); else s->pool32 = allocate_pool<float>(*s);
             std::vector<double> info(size_t(p.nz) + 1 + 2 * size_t(p.angles));
@@ -724,6 +788,55 @@ const char* monki_cuda_device_name(void* handle) {
 }
 
 void monki_cuda_close(void* handle) { destroy(static_cast<Session*>(handle)); }
+
+int monki_cuda_set_roulette_scale(void* handle, const double* scale, size_t cells, char* err, size_t errlen) {
+    Session* s = static_cast<Session*>(handle);
+    try {
+        if (!s) throw std::runtime_error("Invalid CUDA session");
+        const Prepared& p = s->prep;
+        const size_t n = size_t(p.nx) * p.ny * p.nz;
+        check(cudaSetDevice(s->device), "cudaSetDevice");
+        check(cudaStreamSynchronize(s->stream), "sync");
+        if (!scale) {
+            cudaFree(s->scale);
+            s->scale = nullptr;
+            return 0;
+        }
+        if (cells != n) throw std::runtime_error("roulette scale needs nx * ny * nz values");
+        for (size_t c = 0; c < n; ++c)
+            if (!std::isfinite(scale[c]) || scale[c] < 0.0) throw std::runtime_error("Invalid roulette scale map");
+        const size_t elem = s->cfg.fp64 ? sizeof(double) : sizeof(float);
+        if (!s->scale) check(cudaMalloc(&s->scale, n * elem), "cudaMalloc(scale)");
+        if (s->cfg.fp64) {
+            check(cudaMemcpy(s->scale, scale, n * elem, cudaMemcpyHostToDevice), "upload(scale)");
+        } else {
+            std::vector<float> f(scale, scale + n);
+            check(cudaMemcpy(s->scale, f.data(), n * elem, cudaMemcpyHostToDevice), "upload(scale)");
+        }
+        return 0;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        return 1;
+    }
+}
+
+int monki_cuda_importance(void* handle, double* out, size_t count, int reset, char* err, size_t errlen) {
+    Session* s = static_cast<Session*>(handle);
+    try {
+        if (!s || !s->importance) throw std::runtime_error("The session was created without importance=1");
+        const Prepared& p = s->prep;
+        const size_t n = 2 * size_t(p.nx) * p.ny * p.nz;
+        if (!out || count != n) throw std::runtime_error("importance needs 2 * nx * ny * nz values");
+        check(cudaSetDevice(s->device), "cudaSetDevice");
+        check(cudaStreamSynchronize(s->stream), "sync");
+        check(cudaMemcpy(out, s->importance, n * sizeof(double), cudaMemcpyDeviceToHost), "copy(importance)");
+        if (reset) check(cudaMemset(s->importance, 0, n * sizeof(double)), "memset(importance)");
+        return 0;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        return 1;
+    }
+}
 
 int monki_cuda_inspect(const double* tables, size_t table_count, int fp64, int32_t* uniform_top,
                        double* tau_above, size_t tau_capacity, char* err, size_t errlen) {

@@ -88,7 +88,15 @@ struct Pool {
     uint32_t* runs;  // two straight runs of whole layers: lo0 | hi0 << 8 | lo1 << 16 | hi1 << 24
     T* run_ci;       // capacity * 2: 1 / |cos| of each run
     uint32_t* queue[3];
-    uint32_t* counts;  // [0..2] queue sizes, [3] next photon to claim
+    // [0..2] queue sizes and [3] photons paused mid-walk, of the last transit launch
+    // (a photon is live exactly when it is queued or paused); [4] next photon to claim.
+    uint32_t* counts;
+    // Importance tally (pilot runs only; null otherwise): the cells and 1 / weight of the
+    // last kRing events of each history, and the per-cell FP64 sums.
+    uint32_t* ring_cell;  // capacity * kRing
+    T* ring_inv;          // capacity * kRing
+    uint32_t* ring_n;     // events so far
+    double* importance;   // 2 * nx * ny * nz
 };
 
 __device__ __forceinline__ uint32_t pack_layers(int k, int k1, int wmin, int wmax) {
@@ -285,6 +293,7 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
     const int top = s.nz - 1;
     const uint32_t stride = gridDim.x * blockDim.x;
     uint64_t scatters = 0, visits = 0;
+    uint32_t paused = 0;
 
     for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < P.capacity; slot += stride) {
         const uint4 meta = P.meta[slot];
@@ -318,8 +327,8 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
         for (;;) {
             if (pid == kNone) {
                 // Read first so a drained group stops reserving (the counter never wraps).
-                if (*reinterpret_cast<volatile uint32_t*>(P.counts + 3) >= ctl.count) break;
-                const uint32_t n = warp_reserve(P.counts + 3);
+                if (*reinterpret_cast<volatile uint32_t*>(P.counts + 4) >= ctl.count) break;
+                const uint32_t n = warp_reserve(P.counts + 4);
                 if (n >= ctl.count) break;
                 pid = ctl.first + n;
                 const uint32_t ro = dv.per_round.div(pid);
@@ -394,7 +403,7 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
                 break;
             }
             if (PATHS && acc_k >= 0) path.add(acc_k, acc);
-            if (outcome == 4) break;  // budget spent: the walk resumes next iteration
+            if (outcome == 4) { ++paused; break; }  // budget spent: the walk resumes next iteration
             if (outcome == 3) { atomicOr(failure, kHistoryCap); pid = kNone; continue; }
             if (outcome == 2) { pid = kNone; continue; }
             int kind;
@@ -440,18 +449,24 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
         }
         P.pos[slot] = pos;
         P.pol[slot] = pol;
-        if (fresh) P.dir[slot] = dir;
+        if (fresh) {
+            P.dir[slot] = dir;
+            if (P.ring_n) P.ring_n[slot] = 0u;
+        }
     }
 
     unsigned long long v0 = scatters, v1 = visits;
+    uint32_t v2 = paused;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         v0 += __shfl_down_sync(0xffffffffu, v0, off);
         v1 += __shfl_down_sync(0xffffffffu, v1, off);
+        v2 += __shfl_down_sync(0xffffffffu, v2, off);
     }
     if ((threadIdx.x & 31) == 0) {
         atomicAdd(counters + 0, v0);
         atomicAdd(counters + 1, v1);
+        if (v2) atomicAdd(P.counts + 3, v2);
     }
 }
 
@@ -513,6 +528,8 @@ wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ b
         const T sin_c = sqrt(fmax(eps, T(1) - c * c));
         T sphi, cphi;
         sincos(phi, &sphi, &cphi);
+        T contributed = T(0);  // Stokes-I peel-off of this event, all views
+        bool failed = false;
         for (int ia = 0; ia < s.angles; ++ia) {
             const T vc = s.vc[ia];
             T prob[3] = {T(0), T(0), T(0)};
@@ -532,7 +549,7 @@ wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ b
             }
             bool finite = true;
             for (int m = 0; m < NMAT; ++m) finite = finite && isfinite(prob[m]);
-            if (!finite) { atomicOr(failure, kNonfinite); break; }
+            if (!finite) { atomicOr(failure, kNonfinite); failed = true; break; }
             if (!(prob[0] > eps)) continue;
 
             // Detector ray: explicit cell walk below the uniform top, then the prefix.
@@ -561,7 +578,7 @@ wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ b
                 tau += dist * bv;
                 ++visits;
             }
-            if (capped) { atomicOr(failure, kDetectorCap); break; }
+            if (capped) { atomicOr(failure, kDetectorCap); failed = true; break; }
             T height = __ldg(s.zsum + k) + (ks > 0 ? __ldg(s.zunit + k) - z_old : z_old);
             height = __ldg(s.zsum + top) - height;
             const T dxp = aa * height / ca, dyp = ba * height / ca;
@@ -574,6 +591,7 @@ wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ b
             const uint32_t pixel = uint32_t(pi_ + s.nx * (pj_ + s.ny * ia));
             const T att = exp(-tau);
             const T w = prob[0] * att;
+            contributed += w;
             quad_add(pixrec + pixel, TA(w), TA(NMAT > 1 ? prob[1] * att : T(0)), TA(NMAT > 2 ? prob[2] * att : T(0)),
                      TA(PATHS ? w : T(0)));
             ++updates;
@@ -612,6 +630,23 @@ wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ b
                 }
             }
         }
+        if (P.ring_n && !failed) {
+            // Importance tally: this event enters the ring, and its contribution is credited,
+            // per unit weight, to every event of the ring (itself included).
+            const uint32_t cells = uint32_t(s.nx) * uint32_t(s.ny) * uint32_t(s.nz);
+            const uint32_t cell = uint32_t(i) + uint32_t(s.nx) * (uint32_t(j) + uint32_t(s.ny) * uint32_t(k));
+            const uint32_t n = P.ring_n[slot];
+            uint32_t* rc = P.ring_cell + size_t(slot) * kRing;
+            T* ri = P.ring_inv + size_t(slot) * kRing;
+            rc[n % kRing] = cell;
+            ri[n % kRing] = T(1) / weight;
+            P.ring_n[slot] = n + 1;
+            atomicAdd(P.importance + cells + cell, 1.0);
+            if (contributed != T(0)) {
+                const uint32_t live = min(n + 1, uint32_t(kRing));
+                for (uint32_t q = 0; q < live; ++q) atomicAdd(P.importance + rc[q], double(contributed * ri[q]));
+            }
+        }
     }
     unsigned long long v2 = visits, v3 = updates;
 #pragma unroll
@@ -628,9 +663,49 @@ wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ b
 // ----------------------------------------------------------------------------------
 // scatter: new direction (and Stokes vector) for every queued event.
 // ----------------------------------------------------------------------------------
+// Guided transport: detector directional importance sampling (DDIS) and Russian roulette,
+// the unbiased variance reduction of Buras & Mayer (2011), "Efficient unbiased variance
+// reduction techniques for Monte Carlo simulations of radiative transfer in cloudy
+// atmospheres: The solution", JQSRT 112, 434-447. At a particle scatter, with probability
+// epsilon the new direction is drawn about a detector direction (a view picked uniformly)
+// from the particle's own cosine proposal with a uniform azimuth, otherwise by the analog
+// polarized sampler; the weight is then multiplied by p_analog / q with
+// q = (1 - epsilon) p_analog + epsilon p_detector, so every estimate keeps its analog
+// expectation. After every scatter a photon lighter than the cell's roulette weight W
+// survives with probability weight / W, at weight W.
+
+// Density per unit cosine of the analog cosine proposal of species sp: the bound CDF is
+// interpolated linearly in cosine, so the density is constant between table nodes.
+template <typename T>
+__device__ __forceinline__ T proposal_density(const SceneView<T>& s, int sp, T cs) {
+    const int n = s.lut_n[sp];
+    const T* __restrict__ cosv = s.lut_cos[sp];
+    const T* __restrict__ cdf = s.lut_cdf[sp];
+    int lo = lut_bracket(cosv, n, cs);
+    if (lo > n - 2) lo = n - 2;
+    return (__ldg(cdf + lo + 1) - __ldg(cdf + lo)) / (__ldg(cosv + lo + 1) - __ldg(cosv + lo));
+}
+
+// p_analog / q for a particle scatter into (a, b, c) at scattering cosine cs; s0 is the
+// scattered intensity of the unit incident Stokes vector (the acceptance pdf).
+template <typename T, int NMAT>
+__device__ __forceinline__ T ddis_factor(const SceneView<T>& s, const Guide<T>& g, int sp, T cs, T s0, T a, T b, T c) {
+    const Phase<T> f = particle<T>(s, sp, cs, NMAT);
+    const T bound = f.f11 + fabs(f.f12);
+    const T p_an = bound > T(0) ? proposal_density<T>(s, sp, cs) * (s0 / bound) / s.znorm[sp] : T(0);
+    T p_det = T(0);
+    for (int v = 0; v < s.angles; ++v) {
+        const T cv = a * s.va[v] + b * s.vb[v] + c * s.vc[v];
+        p_det += proposal_density<T>(s, sp, fmin(T(1), fmax(T(-1), cv)));
+    }
+    p_det /= T(s.angles);
+    const T q = (T(1) - g.epsilon) * p_an + g.epsilon * p_det;
+    return q > T(0) ? p_an / q : T(0);
+}
+
 template <typename T, int NMAT>
 __global__ void __launch_bounds__(256, 4)
-wf_scatter(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t* __restrict__ failure) {
+wf_scatter(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, Guide<T> g, uint32_t* __restrict__ failure) {
     const T eps = Tol<T>::eps;
     const T pi = pi_v<T>();
     const uint32_t ns = P.counts[0], ng = P.counts[1], np = P.counts[2];
@@ -650,8 +725,15 @@ wf_scatter(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t* __res
         Quad<T> pol = P.pol[slot];
         const T a0 = dir0.x, b0 = dir0.y, c0 = dir0.z;
         T a, b, c, phi_out, q = T(0), u = T(0);
+        const int ci = int(meta.z & 0xFFFF), cj = int(meta.z >> 16), ck = int(meta.w & 0xFF) - 1;
+        T roulette = g.roulette;
+        if (g.scale) roulette *= __ldg(g.scale + ci + s.nx * (cj + s.ny * ck));
         if (surface) {
             const T Pd = T(rng.next()), U = T(rng.next());
+            if (roulette > T(0) && pos.w < roulette) {
+                if (T(rng.next()) * roulette < pos.w) pos.w = roulette;
+                else { P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u); continue; }
+            }
             const T mu = sqrt(Pd);
             phi_out = T(2) * pi * U;
             const T sine = sqrt(fmax(T(0), T(1) - mu * mu));
@@ -663,12 +745,37 @@ wf_scatter(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t* __res
             const T phi = dir0.w;
             T st[3] = {T(1), pol.x, pol.y};
             T cos_out, dphi, cos_sca;
-            if (!sample_direction<T>(s, sp, NMAT, st, c0, rng, cos_out, dphi, cos_sca)) {
-                atomicOr(failure, kSamplingCap);
-                P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u);
-                continue;
+            const bool guided = sp >= 0 && g.epsilon > T(0) && pos.w < g.cap;
+            if (guided && T(rng.next()) < g.epsilon) {
+                // Detector branch: a view, a cosine about it from the proposal, an azimuth.
+                const int v = min(int(T(rng.next()) * T(s.angles)), s.angles - 1);
+                const T cd = sample_cdf<T>(s, sp, T(rng.next()));
+                const T psi = T(2) * pi * T(rng.next());
+                const T dx = s.va[v], dy = s.vb[v], dz = s.vc[v];
+                const T h = sqrt(dx * dx + dy * dy);
+                const bool tilted = h > T(1e-12);
+                const T e1x = tilted ? -dy / h : T(1), e1y = tilted ? dx / h : T(0);
+                const T e2x = -dz * e1y, e2y = dz * e1x, e2z = dx * e1y - dy * e1x;
+                const T sd = sqrt(fmax(T(0), T(1) - cd * cd));
+                T spsi, cpsi;
+                sincos(psi, &spsi, &cpsi);
+                const T wx = cd * dx + sd * (cpsi * e1x + spsi * e2x);
+                const T wy = cd * dy + sd * (cpsi * e1y + spsi * e2y);
+                const T wz = cd * dz + sd * spsi * e2z;
+                cos_out = fmin(T(1), fmax(T(-1), wz));
+                phi_out = atan2(wy, wx);
+                const T so = sqrt(fmax(T(0), T(1) - cos_out * cos_out));
+                T sp_, cp_;
+                sincos(phi_out, &sp_, &cp_);
+                cos_sca = fmin(T(1), fmax(T(-1), a0 * (cp_ * so) + b0 * (sp_ * so) + c0 * cos_out));
+            } else {
+                if (!sample_direction<T>(s, sp, NMAT, st, c0, rng, cos_out, dphi, cos_sca)) {
+                    atomicOr(failure, kSamplingCap);
+                    P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u);
+                    continue;
+                }
+                phi_out = phi + dphi;
             }
-            phi_out = phi + dphi;
             const Rot<T> r = NMAT > 1 ? rotation<T>(cos_sca, c0, cos_out, phi, phi_out) : Rot<T>{T(1), T(0), T(1), T(0)};
             const Phase<T> f = phase<T>(s, sp, cos_sca, NMAT);
             T out[3];
@@ -686,6 +793,11 @@ wf_scatter(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t* __res
             T spo, cpo;
             sincos(phi_out, &spo, &cpo);
             a = cpo * so; b = spo * so; c = cos_out;
+            if (guided) pos.w *= ddis_factor<T, NMAT>(s, g, sp, cos_sca, s0, a, b, c);
+            if (roulette > T(0) && pos.w < roulette) {
+                if (T(rng.next()) * roulette < pos.w) pos.w = roulette;
+                else { P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u); continue; }
+            }
         }
         if (a * a0 < T(0)) pos.x = fmax(T(0), s.xunit - pos.x);
         if (b * b0 < T(0)) pos.y = fmax(T(0), s.yunit - pos.y);

@@ -6,6 +6,7 @@ Same entry points as the reference package (python/monki/__init__.py:3-9): ``sim
 """
 
 from .convergence import AMFConvergence, RadianceConvergence
+from .guided import Guided
 from .input import ReferenceCase
 from .output import SimulationResult
 from .scenes import TransportScene
@@ -13,6 +14,7 @@ from .simulation import simulate
 
 __all__ = [
     "AMFConvergence",
+    "Guided",
     "RadianceConvergence",
     "ReferenceCase",
     "SimulationResult",

@@ -16,6 +16,7 @@ import platform
 
 import numpy as np
 
+from ..guided import Guided
 from ..scenes import TransportScene
 from . import native as _native
 from .backend import Backend
@@ -30,6 +31,12 @@ class CUDA(Backend):
     ``precision="fp32"`` is the production transport. ``"fp64"`` runs the same kernels in
     double precision: it is the on-device check build against which the FP32 bias of
     each result is stated.
+
+    ``guided`` (a ``Guided``) turns on importance-guided transport: detector-directed
+    sampling at particle scatters and Russian roulette, both with exact weight correction;
+    ``set_roulette_scale`` gives the roulette weight a per-cell scale. ``importance=True``
+    makes the session tally per-cell detector importance (``importance()``), the training
+    data of the learned importance model.
     """
 
     def __init__(
@@ -46,6 +53,8 @@ class CUDA(Backend):
         block: int = 256,
         engine: str = "wavefront",
         pool: int = 1 << 20,
+        guided: Guided | None = None,
+        importance: bool = False,
         library=None,
     ):
         for name, value, minimum, maximum in (
@@ -77,6 +86,15 @@ class CUDA(Backend):
         if type(pool) is not int or not 1024 <= pool <= 1 << 26:
             raise ValueError("pool must be an integer in [1024, 2**26]")
 
+        if guided is not None and not isinstance(guided, Guided):
+            raise ValueError("guided must be a monki.Guided or None")
+
+        if type(importance) is not bool:
+            raise ValueError("importance must be a bool")
+
+        if (guided is not None or importance) and engine != "wavefront":
+            raise ValueError("guided transport and importance tallies need engine='wavefront'")
+
         self.device = device
         self.save_path = save_path
         self.profile = profile
@@ -88,6 +106,8 @@ class CUDA(Backend):
         self.block = block
         self.engine = engine
         self.pool = pool
+        self.guided = guided
+        self.importance_tally = importance
         self.library = library or _native.LIBRARY
         self.metadata = None
         self.provenance: dict = {}
@@ -148,6 +168,8 @@ class CUDA(Backend):
         config = (
             f"precision={self.precision},shards={self.tally_shards},block={self.block},"
             f"engine={self.engine},pool={self.pool}"
+            + (self.guided.config() if self.guided is not None else "")
+            + (",importance=1" if self.importance_tally else "")
         ).encode()
         handle = native.monki_cuda_create(
             self.device,
@@ -194,6 +216,7 @@ class CUDA(Backend):
             "block": self.block,
             "engine": self.engine,
             "pool": self.pool,
+            "guided": None if self.guided is None else self.guided.describe(),
             "library_sha256": hashlib.sha256(open(self.library, "rb").read()).hexdigest(),
             "tables_sha256": hashlib.sha256(tables.tobytes()).hexdigest(),
             "machine": platform.machine(),
@@ -203,6 +226,53 @@ class CUDA(Backend):
             "photons": 0,
             "kernel_launches": 0,
         }
+
+    def set_roulette_scale(self, scale) -> None:
+        """Scale the guided roulette weight per cell: ``scale`` has shape (nx, ny, nz)
+        (the vacuum layer included); None removes the map. Applies to later rounds."""
+
+        if self._handle is None:
+            raise RuntimeError("CUDA backend has no prepared scene")
+
+        error = ctypes.create_string_buffer(8192)
+
+        if scale is None:
+            status = self._native.monki_cuda_set_roulette_scale(self._handle, None, 0, error, len(error))
+        else:
+            _, nx, ny, nz, _ = self._shape
+            values = np.asarray(scale, dtype=np.float64)
+
+            if values.shape != (nx, ny, nz):
+                raise ValueError(f"roulette scale must have shape {(nx, ny, nz)}")
+
+            flat = np.ascontiguousarray(values.ravel(order="F"))
+            status = self._native.monki_cuda_set_roulette_scale(
+                self._handle, flat.ctypes.data_as(_native.F64P), flat.size, error, len(error)
+            )
+
+        if status:
+            raise RuntimeError(error.value.decode() or "setting the roulette scale failed")
+
+        self.provenance["roulette_scale"] = None if scale is None else "per-cell map"
+
+    def importance(self, reset: bool = True) -> np.ndarray:
+        """The importance tally of the rounds run so far: shape (2, nx, ny, nz), the summed
+        future Stokes-I contribution per unit weight and the event count of each cell."""
+
+        if self._handle is None:
+            raise RuntimeError("CUDA backend has no prepared scene")
+
+        _, nx, ny, nz, _ = self._shape
+        cells = nx * ny * nz
+        out = np.zeros(2 * cells)
+        error = ctypes.create_string_buffer(8192)
+
+        if self._native.monki_cuda_importance(
+            self._handle, out.ctypes.data_as(_native.F64P), out.size, int(reset), error, len(error)
+        ):
+            raise RuntimeError(error.value.decode() or "reading the importance tally failed")
+
+        return np.stack([out[:cells].reshape((nx, ny, nz), order="F"), out[cells:].reshape((nx, ny, nz), order="F")])
 
     def run_batch(self, controls: object) -> RawTallies:
         """Execute exactly one complete statistical round."""
@@ -258,6 +328,8 @@ class CUDA(Backend):
             self.block,
             self.engine,
             self.pool,
+            self.guided,
+            self.importance_tally,
         )
 
     def _validate_requests(self, controls: list) -> None:

@@ -35,6 +35,14 @@ _SIGNATURES = {
         ctypes.c_int,
         [_F64P, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(ctypes.c_int32), _F64P, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t],
     ),
+    "monki_cuda_set_roulette_scale": (
+        ctypes.c_int,
+        [ctypes.c_void_p, _F64P, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t],
+    ),
+    "monki_cuda_importance": (
+        ctypes.c_int,
+        [ctypes.c_void_p, _F64P, ctypes.c_size_t, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t],
+    ),
     "monki_cuda_run_static": (
         ctypes.c_int,
         [ctypes.c_uint32, _F64P, ctypes.c_size_t, _U32P, _F64P, ctypes.c_char_p, ctypes.c_size_t],

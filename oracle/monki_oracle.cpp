@@ -438,6 +438,78 @@ bool mie_scatter_pol_bound(int nmat, const Species& sp, const double s[3], doubl
 }
 
 // ---------------------------------------------------------------------------------
+// Guided transport: detector directional importance sampling (DDIS) and Russian
+// roulette, the unbiased variance reduction of Buras & Mayer (2011), "Efficient unbiased
+// variance reduction techniques for Monte Carlo simulations of radiative transfer in
+// cloudy atmospheres: The solution", JQSRT 112, 434-447.
+//
+// At a particle scatter, with probability epsilon the new direction is drawn about a
+// detector direction (a view picked uniformly) from the particle's own cosine proposal,
+// with a uniform azimuth; otherwise the analog polarized sampler runs. Either way the
+// weight is multiplied by p_analog / q, q = (1 - epsilon) p_analog + epsilon p_detector,
+// so every estimate keeps the analog expectation. p_analog is the density of what the
+// analog sampler draws: the bound CDF interpolated linearly in cosine (a density constant
+// between table nodes) thinned by the acceptance pdf / bound, normalized by Z.
+// Russian roulette after every scatter: a photon lighter than `roulette` survives with
+// probability weight / roulette at weight `roulette`.
+// ---------------------------------------------------------------------------------
+struct Guide {
+    double epsilon = 0.0;
+    double roulette = 0.0;
+    double cap = 1.0e300;         // DDIS only while the weight is below this
+    const double* scale = nullptr;  // per-cell roulette threshold scale (nx * ny * nz), or none
+};
+
+// Importance tally: for every event, the Stokes-I peel-off contributions of that event and
+// of the next kRing - 1 events of the same history, per unit weight at the event, summed
+// per cell with the event count. A pilot of the analog method yields the detector
+// importance of each cell (mean future contribution of a unit-weight photon there).
+constexpr int kRing = 8;
+
+// Density per unit cosine of the analog cosine proposal of species sp.
+double proposal_density(const Species& sp, double cs) {
+    int hi = int(std::upper_bound(sp.cosines.begin(), sp.cosines.end(), cs) - sp.cosines.begin());
+    hi = std::min(std::max(hi, 1), sp.n - 1);
+    const int lo = hi - 1;
+    return (sp.cdf[size_t(hi)] - sp.cdf[size_t(lo)]) / (sp.cosines[size_t(hi)] - sp.cosines[size_t(lo)]);
+}
+
+// Z = integral over the cosine of proposal density x F11 / (F11 + |F12|), the mass the
+// acceptance step keeps (the F12 term averages out over the azimuth). Four-point
+// Gauss-Legendre per table interval; exactly sum(dCDF) when F12 = 0 or nmat = 1.
+double analog_norm(const Species& sp, int nmat) {
+    static const double xg[4] = {-0.8611363115940526, -0.3399810435848563, 0.3399810435848563, 0.8611363115940526};
+    static const double wg[4] = {0.3478548451374538, 0.6521451548625461, 0.6521451548625461, 0.3478548451374538};
+    double z = 0.0;
+    for (int lo = 0; lo + 1 < sp.n; ++lo) {
+        const double dc = sp.cdf[size_t(lo) + 1] - sp.cdf[size_t(lo)];
+        if (dc == 0.0) continue;
+        bool ratio_one = nmat == 1 || (sp.f12[size_t(lo)] == 0.0 && sp.f12[size_t(lo) + 1] == 0.0);
+        if (ratio_one) { z += dc; continue; }
+        double mean = 0.0;
+        for (int q = 0; q < 4; ++q) {
+            const double t01 = 0.5 * (xg[q] + 1.0);
+            const double f11 = sp.f11[size_t(lo)] + t01 * (sp.f11[size_t(lo) + 1] - sp.f11[size_t(lo)]);
+            const double f12 = sp.f12[size_t(lo)] + t01 * (sp.f12[size_t(lo) + 1] - sp.f12[size_t(lo)]);
+            const double b = f11 + std::fabs(f12);
+            mean += 0.5 * wg[q] * (b > 0.0 ? f11 / b : 0.0);
+        }
+        z += dc * mean;
+    }
+    return z;
+}
+
+// Cosine drawn from the bound CDF (the proposal step of mie_scatter_pol_bound).
+double sample_proposal(const Species& sp, double u) {
+    int hi = int(std::upper_bound(sp.cdf.begin(), sp.cdf.end(), u) - sp.cdf.begin());
+    hi = std::min(std::max(hi, 1), sp.n - 1);
+    const int lo = hi - 1;
+    const double c2[2] = {sp.cdf[size_t(lo)], sp.cdf[size_t(hi)]};
+    const double a2[2] = {sp.cosines[size_t(lo)], sp.cosines[size_t(hi)]};
+    return linpol2(c2, a2, u);
+}
+
+// ---------------------------------------------------------------------------------
 // Per-round tallies in the RawTallies order: stokes(nmat,nx,ny,angles),
 // paths(nx,ny,nz,angles), weights(nx,ny,angles), all Fortran order, FP64.
 // ---------------------------------------------------------------------------------
@@ -452,6 +524,8 @@ struct Counters {
 struct Transport {
     const Tables& t;
     uint32_t max_steps;
+    Guide guide;
+    std::vector<double> z_norm;  // analog sampler mass per particle species
     double a0, b0, c0, phi0_rad, vartheta0_rad;
     std::vector<double> va, vb, vc, view_phi_rad, zsum;  // zsum[k] = SUM(zunit(1:k))
     size_t stokes_count, path_count, weight_count, tally_count;
@@ -475,6 +549,35 @@ struct Transport {
         path_count = t.paths ? size_t(t.nx) * t.ny * t.nz * t.angles : 0;
         weight_count = t.paths ? size_t(t.nx) * t.ny * t.angles : 0;
         tally_count = stokes_count + path_count + weight_count;
+        for (const auto& sp : t.species) z_norm.push_back(analog_norm(sp, t.nmat));
+    }
+
+    // Russian roulette; false when the photon is terminated.
+    bool roulette(double& weight, Stream& rng, int i, int j, int k) const {
+        double threshold = guide.roulette;
+        if (guide.scale) threshold *= guide.scale[size_t(i - 1) + size_t(t.nx) * (size_t(j - 1) + size_t(t.ny) * size_t(k - 1))];
+        if (!(threshold > 0.0) || !(weight < threshold)) return true;
+        if (rng.uniform() * threshold < weight) { weight = threshold; return true; }
+        return false;
+    }
+
+    // DDIS weight factor p_analog / q for a particle scatter into (a, b, c) at cos_sca;
+    // s0 is the scattered intensity (the acceptance pdf) for the unit incident Stokes vector.
+    double ddis_factor(int sp_index, double cos_sca, double s0, double a, double b, double c) const {
+        const Species& sp = t.species[size_t(sp_index)];
+        double f11, f12;
+        mie_scat_elements(cos_sca, sp, f11, f12);
+        if (t.nmat == 1) f12 = 0.0;
+        const double bound = f11 + std::fabs(f12);
+        const double p_an = bound > 0.0 ? proposal_density(sp, cos_sca) * (s0 / bound) / z_norm[size_t(sp_index)] : 0.0;
+        double p_det = 0.0;
+        for (int v = 0; v < t.angles; ++v) {
+            double cv = a * va[size_t(v)] + b * vb[size_t(v)] + c * vc[size_t(v)];
+            p_det += proposal_density(sp, std::min(1.0, std::max(-1.0, cv)));
+        }
+        p_det /= double(t.angles);
+        const double q = (1.0 - guide.epsilon) * p_an + guide.epsilon * p_det;
+        return q > 0.0 ? p_an / q : 0.0;
     }
 
     size_t stokes_index(int m, int i, int j, int ia) const {
@@ -515,8 +618,9 @@ struct Transport {
     bool peel_off(double a_bak, double b_bak, double c_bak, int i_bak, int j_bak, int k_bak,
                   double x_bak, double y_bak, double z_bak, const std::vector<double>& s_prob,
                   const std::vector<double>& path_layers, double* tally,
-                  std::vector<double>& path_angle, Counters& cnt) const {
+                  std::vector<double>& path_angle, Counters& cnt, double& contributed) const {
         const int nmat = t.nmat, nz = t.nz;
+        contributed = 0.0;
         for (int ia = 0; ia < t.angles; ++ia) {
             double p1 = s_prob[size_t(ia) * nmat];
             if (!(p1 > kEps)) continue;
@@ -554,6 +658,7 @@ struct Transport {
             int inew = int(modulo((long long)i_bak + is * (long long)di + t.nx - 1, t.nx)) + 1;
             int jnew = int(modulo((long long)j_bak + js * (long long)dj + t.ny - 1, t.ny)) + 1;
             double att = std::exp(-tau);
+            contributed += p1 * att;
             for (int m = 0; m < nmat; ++m) tally[stokes_index(m, inew, jnew, ia)] += s_prob[size_t(ia) * nmat + m] * att;
             cnt.tally_updates += nmat;
             if (t.paths) {
@@ -570,8 +675,24 @@ struct Transport {
     // One photon history (mc.f90:351-1436). Returns a failure flag (0 on success).
     uint32_t photon(uint32_t photon_id, uint32_t round, uint32_t seed, double* tally,
                     Counters& cnt, std::vector<double>& path_layers, std::vector<double>& path_angle,
-                    std::vector<double>& s_prob) const {
+                    std::vector<double>& s_prob, double* importance) const {
         const int nx = t.nx, ny = t.ny, nz = t.nz, nmat = t.nmat;
+        uint32_t ring_cell[kRing];
+        double ring_inv[kRing];
+        int ring_n = 0;
+        double contributed = 0.0;
+        // Record an event in cell (i, j, k) at weight w that contributed c.
+        auto record = [&](int ci, int cj, int ck, double w, double c) {
+            if (!importance) return;
+            const size_t cells = size_t(nx) * ny * nz;
+            const uint32_t cell = uint32_t(size_t(ci - 1) + size_t(nx) * (size_t(cj - 1) + size_t(ny) * size_t(ck - 1)));
+            ring_cell[ring_n % kRing] = cell;
+            ring_inv[ring_n % kRing] = 1.0 / w;
+            ++ring_n;
+            importance[cells + cell] += 1.0;
+            const int live = std::min(ring_n, kRing);
+            for (int e = 0; e < live; ++e) importance[ring_cell[e]] += c * ring_inv[e];
+        };
         Stream rng{photon_id, round, seed};
         ++cnt.photons;
         int column = int(photon_id % uint32_t(nx * ny));
@@ -634,10 +755,12 @@ struct Transport {
                     if (vc[ia] > 0) s_prob[size_t(ia) * nmat] = s[0] * vc[ia] * weight;
                     if (!std::isfinite(s_prob[size_t(ia) * nmat])) return 1;
                 }
-                if (!peel_off(a_int, b_int, c_int, i, j, k, x, y, z, s_prob, path_layers, tally, path_angle, cnt))
+                if (!peel_off(a_int, b_int, c_int, i, j, k, x, y, z, s_prob, path_layers, tally, path_angle, cnt, contributed))
                     return 2;
+                record(i, j, k, weight, contributed);
                 // GROUND_LAMB2: theta = acos(sqrt(P)), phi = 2 pi U.
                 double P = rng.uniform(), U = rng.uniform();
+                if (!roulette(weight, rng, i, j, k)) return 0;
                 double theta = std::acos(std::sqrt(P));
                 double phi_out = 2.0 * kPi * U;
                 a = std::sin(theta) * std::cos(phi_out);
@@ -679,12 +802,34 @@ struct Transport {
                 for (int m = 0; m < nmat; ++m)
                     if (!std::isfinite(s_prob[size_t(ia) * nmat + m])) return 1;
             }
-            if (!peel_off(a, b, c, i, j, k, x, y, z, s_prob, path_layers, tally, path_angle, cnt)) return 2;
-            double cos_in = c, cos_out, dphi, cos_sca;
-            bool ok = gas ? rayl_scatter_pol(nmat, t.depol, s, cos_in, rng, cos_out, dphi, cos_sca)
-                          : mie_scatter_pol_bound(nmat, t.species[size_t(sp - 1)], s, cos_in, rng, cos_out, dphi, cos_sca);
-            if (!ok) return 4;
-            double phi_out = phi_in + dphi;
+            if (!peel_off(a, b, c, i, j, k, x, y, z, s_prob, path_layers, tally, path_angle, cnt, contributed)) return 2;
+            record(i, j, k, weight, contributed);
+            double cos_in = c, cos_out, dphi, cos_sca, phi_out;
+            const bool guided = !gas && guide.epsilon > 0.0 && weight < guide.cap;
+            if (guided && rng.uniform() < guide.epsilon) {
+                // Detector branch: a view, a cosine about it from the proposal, an azimuth.
+                const int v = std::min(int(rng.uniform() * t.angles), t.angles - 1);
+                const double cd = sample_proposal(t.species[size_t(sp - 1)], rng.uniform());
+                const double psi = 2.0 * kPi * rng.uniform();
+                const double dx = va[size_t(v)], dy = vb[size_t(v)], dz = vc[size_t(v)];
+                const double h = std::sqrt(dx * dx + dy * dy);
+                const double e1x = h > 1e-12 ? -dy / h : 1.0, e1y = h > 1e-12 ? dx / h : 0.0;
+                const double e2x = -dz * e1y, e2y = dz * e1x, e2z = dx * e1y - dy * e1x;
+                const double sd = std::sqrt(std::max(0.0, 1.0 - cd * cd));
+                const double cp = std::cos(psi), spsi = std::sin(psi);
+                const double wx = cd * dx + sd * (cp * e1x + spsi * e2x);
+                const double wy = cd * dy + sd * (cp * e1y + spsi * e2y);
+                const double wz = cd * dz + sd * spsi * e2z;
+                cos_out = std::min(1.0, std::max(-1.0, wz));
+                phi_out = std::atan2(wy, wx);
+                const double so = std::sqrt(std::max(0.0, 1.0 - cos_out * cos_out));
+                cos_sca = std::min(1.0, std::max(-1.0, a * (std::cos(phi_out) * so) + b * (std::sin(phi_out) * so) + c * cos_out));
+            } else {
+                bool ok = gas ? rayl_scatter_pol(nmat, t.depol, s, cos_in, rng, cos_out, dphi, cos_sca)
+                              : mie_scatter_pol_bound(nmat, t.species[size_t(sp - 1)], s, cos_in, rng, cos_out, dphi, cos_sca);
+                if (!ok) return 4;
+                phi_out = phi_in + dphi;
+            }
             Rotation rot = stokes_rot_mat(cos_sca, cos_in, cos_out, phi_in, phi_out, nmat);
             Mat3 f = gas ? ray_scat_matrix(nmat, cos_sca, t.depol) : mie_scat_matrix(nmat, cos_sca, t.species[size_t(sp - 1)]);
             Mat3 p = matmul_stokes_rot(nmat, f, rot);
@@ -699,6 +844,8 @@ struct Transport {
             a = std::cos(phi_out) * std::sqrt(std::max(0.0, 1.0 - cos_out * cos_out));
             b = std::sin(phi_out) * std::sqrt(std::max(0.0, 1.0 - cos_out * cos_out));
             c = cos_out;
+            if (guided) weight *= ddis_factor(sp - 1, cos_sca, s0, a, b, c);
+            if (!roulette(weight, rng, i, j, k)) return 0;
             if (a * a_bak < 0.0) x = std::max(0.0, t.xunit - x);
             if (b * b_bak < 0.0) y = std::max(0.0, t.yunit - y);
             if (c * c_bak < 0.0) z = std::max(0.0, t.zu(k) - z);
@@ -759,9 +906,30 @@ int monki_oracle_validate(const double* tables, size_t count, char* err, size_t 
 // count FP64, each round in RawTallies order with the mu0/mu factor applied to Stokes.
 // counters (5 x u64): scatters, photons, free-path cell visits, detector cell visits,
 // tally updates. Returns the failure flag (0 on success); a nonzero flag rejects the run.
+int monki_oracle_run_guided(const double* tables, size_t table_count, const uint32_t controls[8],
+                            const double guide[3], const double* scale, int threads, double* out,
+                            uint64_t* counters, double* importance, char* err, size_t errlen);
+
 int monki_oracle_run(const double* tables, size_t table_count, const uint32_t controls[8], int threads,
                      double* out, uint64_t* counters, char* err, size_t errlen) {
+    const double plain[3] = {0.0, 0.0, 0.0};
+    return monki_oracle_run_guided(tables, table_count, controls, plain, nullptr, threads, out, counters, nullptr,
+                                   err, errlen);
+}
+
+// The same round group with guided transport: guide = {epsilon (DDIS probability at
+// particle scatters, [0, 1)), roulette weight (0 = off), DDIS weight cap (0 = none)};
+// scale (nx * ny * nz, or NULL) multiplies the roulette weight per cell. importance
+// (2 * nx * ny * nz, or NULL) receives the importance tally: per cell the summed future
+// contribution per unit weight, then the event count.
+int monki_oracle_run_guided(const double* tables, size_t table_count, const uint32_t controls[8],
+                            const double guide[3], const double* scale, int threads, double* out,
+                            uint64_t* counters, double* importance, char* err, size_t errlen) {
     try {
+        if (!guide || !(guide[0] >= 0.0 && guide[0] < 1.0) || !(guide[1] >= 0.0 && guide[1] <= 1.0)) {
+            write_error(err, errlen, "Invalid guide: epsilon must be in [0, 1), roulette in [0, 1]");
+            return 1;
+        }
         Tables t = parse_tables(tables, table_count);
         const uint32_t count = controls[0], first = controls[1], first_round = controls[2];
         const uint32_t seed = controls[3], max_steps = controls[4], per_round = controls[6];
@@ -771,6 +939,19 @@ int monki_oracle_run(const double* tables, size_t table_count, const uint32_t co
             return 1;
         }
         Transport tr(t, max_steps);
+        tr.guide.epsilon = guide[0];
+        tr.guide.roulette = guide[1];
+        if (guide[2] > 0.0) tr.guide.cap = guide[2];
+        tr.guide.scale = scale;
+        const size_t cells = size_t(t.nx) * t.ny * t.nz;
+        if (scale)
+            for (size_t c = 0; c < cells; ++c)
+                if (!(scale[c] >= 0.0) || !std::isfinite(scale[c])) {
+                    write_error(err, errlen, "Invalid roulette scale map");
+                    return 1;
+                }
+        std::vector<std::vector<double>> imp_partial(importance ? size_t(threads > 0 ? threads : 1) : 0,
+                                                     std::vector<double>(importance ? 2 * cells : 0, 0.0));
         const size_t tc = tr.tally_count;
         std::fill(out, out + tc * rounds, 0.0);
         int nthreads = threads > 0 ? threads : 1;
@@ -795,7 +976,8 @@ int monki_oracle_run(const double* tables, size_t table_count, const uint32_t co
                 double* tally = partial[size_t(tid)].data() + size_t(round_offset) * tc;
                 try {
                     uint32_t flag = tr.photon(photon_id, first_round + round_offset, seed, tally,
-                                              cnts[size_t(tid)], path_layers, path_angle, s_prob);
+                                              cnts[size_t(tid)], path_layers, path_angle, s_prob,
+                                              importance ? imp_partial[size_t(tid)].data() : nullptr);
                     if (flag) flags[size_t(tid)] |= flag;
                 } catch (const std::exception& e) {
                     errors[size_t(tid)] = e.what();
@@ -810,6 +992,10 @@ int monki_oracle_run(const double* tables, size_t table_count, const uint32_t co
             total.add(cnts[size_t(q)]);
             const std::vector<double>& p = partial[size_t(q)];
             for (size_t v = 0; v < tc * rounds; ++v) out[v] += p[v];
+            if (importance) {
+                if (q == 0) std::fill(importance, importance + 2 * cells, 0.0);
+                for (size_t v = 0; v < 2 * cells; ++v) importance[v] += imp_partial[size_t(q)][v];
+            }
         }
         // mu0/mu geometry factor on Stokes only (mc.f90:1456-1474).
         for (uint32_t r = 0; r < rounds; ++r)

@@ -45,6 +45,20 @@ def library() -> ctypes.CDLL:
             ctypes.c_size_t,
         ]
         lib.monki_oracle_run.restype = ctypes.c_int
+        lib.monki_oracle_run_guided.argtypes = [
+            _F64P,
+            ctypes.c_size_t,
+            _U32P,
+            _F64P,
+            _F64P,
+            ctypes.c_int,
+            _F64P,
+            _U64P,
+            _F64P,
+            ctypes.c_char_p,
+            ctypes.c_size_t,
+        ]
+        lib.monki_oracle_run_guided.restype = ctypes.c_int
         _library = lib
 
     return _library
@@ -84,26 +98,41 @@ def tally_count(tables) -> int:
     return nmat * nx * ny * angles + (nx * ny * (nz + 1) * angles if paths else 0)
 
 
-def run(tables, controls, threads: int | None = None):
-    """Run one round group; returns (tallies[rounds, tally_count], counters dict).
+def run(tables, controls, threads: int | None = None, guide=None, scale=None, importance: bool = False):
+    """Run one round group; returns (tallies[rounds, tally_count], counters dict[, importance]).
 
-    ``controls`` are the eight words of the CUDA run call. A failure flag raises.
+    ``controls`` are the eight words of the CUDA run call. ``guide`` = (epsilon, roulette
+    [, DDIS weight cap]) selects guided transport (detector-directed sampling at particle
+    scatters and Russian roulette); None is the analog method. ``scale`` (nx, ny, nz),
+    Fortran order, multiplies the roulette weight per cell. With ``importance`` the third
+    result is the importance tally, shape (2, nx, ny, nz): summed future contribution per
+    unit weight and event count per cell. A failure flag raises.
     """
 
     t = np.ascontiguousarray(tables, dtype=np.float64)
     ctl = np.ascontiguousarray(controls, dtype=np.uint32)
+    nx, ny, nz = (int(v) for v in t[1:4])
     rounds = int(ctl[7])
     out = np.zeros((rounds, tally_count(t)), dtype=np.float64)
     counters = np.zeros(5, dtype=np.uint64)
     err = ctypes.create_string_buffer(4096)
     threads = threads or os.cpu_count() or 1
-    status = library().monki_oracle_run(
+    g = np.zeros(3)
+    g[: len(guide or ())] = guide or ()
+    scale_arr = None if scale is None else np.ascontiguousarray(np.asarray(scale, dtype=np.float64).ravel(order="F"))
+    if scale_arr is not None and scale_arr.size != nx * ny * nz:
+        raise ValueError("scale must have nx * ny * nz cells")
+    imp = np.zeros(2 * nx * ny * nz) if importance else None
+    status = library().monki_oracle_run_guided(
         t.ctypes.data_as(_F64P),
         t.size,
         ctl.ctypes.data_as(_U32P),
+        g.ctypes.data_as(_F64P),
+        None if scale_arr is None else scale_arr.ctypes.data_as(_F64P),
         threads,
         out.ctypes.data_as(_F64P),
         counters.ctypes.data_as(_U64P),
+        None if imp is None else imp.ctypes.data_as(_F64P),
         err,
         len(err),
     )
@@ -112,7 +141,11 @@ def run(tables, controls, threads: int | None = None):
         raise RuntimeError(err.value.decode() or f"oracle failed with flag {status}")
 
     names = ("scatters", "photons", "free_path_visits", "detector_visits", "tally_updates")
-    return out, {name: int(value) for name, value in zip(names, counters, strict=True)}
+    stats = {name: int(value) for name, value in zip(names, counters, strict=True)}
+    if importance:
+        cells = nx * ny * nz
+        return out, stats, np.stack([imp[:cells].reshape((nx, ny, nz), order="F"), imp[cells:].reshape((nx, ny, nz), order="F")])
+    return out, stats
 
 
 def split(tables, values):

@@ -259,3 +259,35 @@ def test_off_plane_polarization_is_nonzero_and_bounded(device):
     stokes = batches[0].stokes
     assert np.max(np.abs(stokes[2])) > 1e-3 * np.max(stokes[0])
     assert np.all(np.hypot(stokes[1], stokes[2]) <= stokes[0] * 1.01 + 1e-12)
+
+
+def test_group_ends_only_after_paused_walks_finish(native, oracle, device):
+    """Photons paused by the per-launch walk budget are live: a round group must not end
+    while one is still walking. Single-photon groups with a one-step budget pause at
+    nearly every launch; each must reproduce the oracle's history."""
+    import monki.scenes as scenes
+    from monki.execution.native import F64P, U32P, U64P
+
+    scene = scenes.box_cloud(8, 2, nx=12, ny=10, box_x=(3, 8), box_y=(2, 6))
+    nmat, nx, ny, nz, angles = scene.shape
+    per_round = 8 * nx * ny
+    tables = np.ascontiguousarray(scene.tables)
+    err = _err()
+    handle = native.monki_cuda_create(0, tables.ctypes.data_as(F64P), tables.size, 2, b"precision=fp64,pool=1024,walk=1", err, len(err))
+    assert handle, err.value
+    try:
+        count = native.monki_cuda_tally_count(handle)
+        before = np.zeros(6, dtype=np.uint64)
+        after = np.zeros(6, dtype=np.uint64)
+        for photon in (99, 374, 5, 600):
+            controls = np.array([1, photon, 1, 5, 100000, 0, per_round, 2], dtype=np.uint32)
+            out = np.zeros(2 * count)
+            native.monki_cuda_counters(handle, before.ctypes.data_as(U64P))
+            status = native.monki_cuda_run(handle, controls.ctypes.data_as(U32P), out.ctypes.data_as(F64P), err, len(err))
+            assert status == 0, err.value
+            native.monki_cuda_counters(handle, after.ctypes.data_as(U64P))
+            expected, counters = oracle.run(tables, controls, 1)
+            assert int(after[0] - before[0]) == counters["scatters"], photon
+            np.testing.assert_allclose(out, expected.ravel(), rtol=1e-6, atol=1e-12)
+    finally:
+        native.monki_cuda_close(handle)
