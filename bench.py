@@ -1,20 +1,25 @@
 """Benchmark of the GB300 MONKI transport hot path.
 
-Workload: the layered-cloud scene (polarized I/Q/U with layer-AMF paths): 30 x 20
-periodic 1 km columns, 34 layers plus vacuum, Rayleigh 0.70 + O3 0.30 + aerosol 0.20
-(g 0.70, SSA 0.92) + a 2-3 km cloud slab of optical depth 10 (g 0.85, SSA 0.9999),
-SZA 30, views (VZA, RAA) = (0,0), (30,90), (60,180), albedo 0.05, FP32 transport with
-FP64 per-round tallies, 20,000 photons per column per round. One step = one statistical
-round (12,000,000 photon histories) through the transport kernel and the FP64 flush.
+Default workload: the 3-D box cloud (polarized I/Q/U): 30 x 20 periodic 1 km columns, 34
+layers plus vacuum, Rayleigh 0.70 + O3 0.30 + aerosol 0.20 (g 0.70, SSA 0.92), a 10 x 6
+column cloud block at 1-3 km of optical depth 20 (g 0.85, SSA 0.9999), SZA 60, views
+(VZA, RAA) = (0,0), (30,90), (60,180), albedo 0.05, FP32 transport with FP64 per-round
+tallies, 50,000 photons per column per round. One step = one statistical round
+(30,000,000 photon histories) through the transport kernels and the FP64 flush.
+``--workload layered`` runs the layered-cloud scene instead (cloud slab at 2-3 km,
+optical depth 10, SZA 30, layer AMF paths, 20,000 photons per column).
 
 Printed JSON (one line, rank 0):
-  value      scatters/s with the scene resident on the device, from CUDA events on the
-             session stream around each step (L2 flushed between steps);
-  e2e        the same metric through the public API (``CUDA.prepare`` + ``run_batches``),
-             wall clock, including the table upload and every round's tally copy-out;
-  roofline   the transport kernel's algorithmic bytes per launch (16 B per cell visit on
-             the free path and the detector rays, 8 B per FP32 tally read-modify-write)
-             over its event-timed duration, against the measured HBM copy bandwidth;
+  value      scatters/s of the analog kernels with the scene resident on the device, from
+             CUDA events on the session stream (L2 flushed before the timed group);
+  time_to_target  wall seconds of ``simulate`` through the public API until SE/|I| < 1 %
+             in every pixel and view (standard error of the round means, defined from the
+             31st round on), analog and importance-guided, from the same rounds' tallies;
+  e2e        scatters/s of that analog ``simulate`` run (host tables in, every round's
+             FP64 tallies out, statistics on the host);
+  roofline   the peel kernel's algorithmic bytes per launch (event state, cell records of
+             the detector rays, 128-bit tally atomics) over its event-timed duration,
+             against the measured HBM copy bandwidth;
   cpu_baseline  the FP64 CPU restatement of the reference transport (oracle) on a bounded
              sample of the same round, on every host core.
 
@@ -43,8 +48,12 @@ sys.path.insert(0, str(ROOT / "monki-gpu_gb300"))
 
 METRIC = "time to SE/|I|<1% per scene, plain vs importance-guided MC on 1 GB300; scatters/s"
 UNIT = "scatters/s"
-PHOTONS_PER_COLUMN = 20_000
-WORKLOAD = "layered-cloud 30x20x35, I/Q/U + layer AMF, 20000 photons/column/round"
+WORKLOADS = {
+    "box": ("box_cloud", 50_000, "box-cloud 30x20x35, I/Q/U, SZA 60, 50000 photons/column/round"),
+    "layered": ("layered_cloud", 20_000, "layered-cloud 30x20x35, I/Q/U + layer AMF, 20000 photons/column/round"),
+}
+TARGET = 0.01  # SE/|I| in every pixel and view
+GUIDED = (0.0, 1.0, 0.0)  # epsilon, roulette weight, cap: Russian roulette at unit weight
 STATE_BYTES = 64  # one event's photon state records read by the peel kernel
 CELL_BYTES = 16  # one cell record (beta + cumulative species fractions)
 TALLY_BYTES = 32  # one 128-bit tally atomic: 16 B read + 16 B written in L2
@@ -60,10 +69,11 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def recorded_traffic():
-    """Per-launch DRAM bytes of the transport kernel from the committed ncu summary."""
+def recorded_traffic(workload):
+    """Per-launch DRAM bytes of the peel kernel from the committed ncu summary."""
 
-    path = ROOT / "profiles" / "transport_kernel_layered_cloud.md"
+    name = {"box": "box_cloud", "layered": "layered_cloud"}[workload]
+    path = ROOT / "profiles" / f"transport_kernel_{name}.md"
 
     if not path.is_file():
         return None
@@ -169,19 +179,26 @@ def cpu_baseline(scene, target_seconds: float = 10.0):
     }
 
 
-def reference_arm(args):
+def build_scene(workload, photons_per_column, rounds):
     import monki.scenes as scenes
 
+    builder, _, _ = WORKLOADS[workload]
+    return getattr(scenes, builder)(photons_per_column, rounds)
+
+
+def reference_arm(args):
     world, rank, _ = distributed()
 
     if rank != 0:
         return 0
 
-    scene = scenes.layered_cloud(PHOTONS_PER_COLUMN, 1)
     from oracle import oracle
 
+    _, default_ppc, workload = WORKLOADS[args.workload]
+    ppc = args.photons_per_column or default_ppc
+    scene = build_scene(args.workload, ppc, 1)
     nmat, nx, ny, nz, angles = scene.shape
-    per_round = PHOTONS_PER_COLUMN * nx * ny
+    per_round = ppc * nx * ny
     threads = os.cpu_count() or 1
     sample = max(threads * 256, 20_000)
     scatters = 0
@@ -212,7 +229,7 @@ def reference_arm(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "step": f"{sample} photon histories of one round on the host cores"},
+        "config": {"workload": workload, "step": f"{sample} photon histories of one round on the host cores"},
         "cpu_baseline": {
             "value": value,
             "unit": UNIT,
@@ -227,14 +244,52 @@ def reference_arm(args):
     return 0
 
 
+def time_to_target(workload, ppc, device, seed, guided):
+    """Wall seconds of ``simulate`` (the public API, host tables in, every round's FP64
+    tallies out, statistics on the host) until SE/|I| < TARGET in every pixel and view."""
+
+    import tempfile
+
+    from monki import Guided, RadianceConvergence, simulate
+    from monki.execution import CUDA
+
+    scene = build_scene(workload, ppc, 256)
+    rule = RadianceConvergence(TARGET, minimum_rounds=32, check_every=1, consecutive_checks=1)
+    backend = CUDA(device=device, seed=seed, guided=Guided(*guided) if guided else None)
+
+    with tempfile.TemporaryDirectory() as tmp:
+        start = time.perf_counter()
+        result = simulate(scene, backend, f"{tmp}/run.nc", convergence=rule)
+        wall = time.perf_counter() - start
+        receipt = json.loads(Path(f"{tmp}/run.run.json").read_text())
+
+    radiance = result.values["radiance"][..., 0, 0]
+    error = result.values["std_radiance"][..., 0, 0]
+    rounds = int(receipt["completed_rounds"])
+    nmat, nx, ny, nz, angles = scene.shape
+    return {
+        "seconds": wall,
+        "status": receipt["status"],
+        "rounds": rounds,
+        "max_relative_se": float(np.max(error / np.abs(radiance))),
+        "scatters": int(receipt["scatters"]),
+        "scatters_per_s": receipt["scatters"] / wall,
+        "h2d_bytes": int(scene.tables.nbytes + 32 * rounds),
+        "d2h_bytes": int(rounds * (nmat * nx * ny * angles + (nx * ny * (nz + 1) * angles if scene.save_path else 0)) * 8),
+        "kernel_launches": int(receipt.get("kernel_launches", 0)),
+    }
+
+
 def main():
     parser = argparse.ArgumentParser()
     parser.add_argument("--gpus", type=int, default=1)
     parser.add_argument("--steps", type=int, default=8)
     parser.add_argument("--warmup", type=int, default=3)
     parser.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
+    parser.add_argument("--workload", default="box", choices=tuple(WORKLOADS))
     parser.add_argument("--no-cpu-baseline", action="store_true")
-    parser.add_argument("--photons-per-column", type=int, default=PHOTONS_PER_COLUMN)
+    parser.add_argument("--no-target", action="store_true", help="skip the time-to-target runs")
+    parser.add_argument("--photons-per-column", type=int, default=0)
     args = parser.parse_args()
 
     if args.warmup < 3:
@@ -245,8 +300,6 @@ def main():
 
     import torch
 
-    import monki.scenes as scenes
-    from monki.execution import CUDA, BatchControls
     from monki.execution import native as binding
 
     world, rank, local = distributed()
@@ -263,8 +316,9 @@ def main():
 
         torch.cuda.synchronize()
 
-    ppc = args.photons_per_column
-    scene = scenes.layered_cloud(ppc, args.warmup + args.steps)
+    _, default_ppc, workload = WORKLOADS[args.workload]
+    ppc = args.photons_per_column or default_ppc
+    scene = build_scene(args.workload, ppc, args.warmup + args.steps)
     nmat, nx, ny, nz, angles = scene.shape
     per_round = ppc * nx * ny
     native = binding.load()
@@ -345,21 +399,14 @@ def main():
     stage_total = max(sum(stage_ms), 1e-9)
     stage_share = {name: stage_ms[q] / stage_total for q, name in enumerate(("transit", "peel", "scatter"))}
 
-    # End to end through the public API: prepare (table upload) + every round's copy-out.
-    e2e_scene = scenes.layered_cloud(ppc, args.steps)
-    torch.cuda.synchronize()
-    wall_e2e = time.perf_counter()
-
-    with CUDA(device=local, seed=rank) as backend:
-        backend.prepare(e2e_scene)
-        batches = backend.run_batches([BatchControls(i, ppc) for i in range(1, args.steps + 1)])
-        e2e_scatters = backend.provenance["scatters"]
-        e2e_launches = backend.provenance["kernel_launches"]
-
-    wall_e2e = time.perf_counter() - wall_e2e
-    assert len(batches) == args.steps
-    e2e_value = e2e_scatters * world / wall_e2e
-    tally_bytes = tally_count * 8
+    # Time to the precision target through the public API, analog then guided, on every
+    # rank (independent seeds); the analog run is also the end-to-end throughput.
+    target = None
+    if not args.no_target:
+        barrier()
+        plain = time_to_target(args.workload, ppc, local, 23274 + rank, None)
+        guided = time_to_target(args.workload, ppc, local, 23274 + rank, GUIDED)
+        target = {"analog": plain, "guided": guided}
 
     if rank != 0:
         if world > 1:
@@ -381,10 +428,11 @@ def main():
         "dtype": "f32",
         "data": "synthetic",
         "config": {
-            "workload": WORKLOAD,
+            "workload": workload,
             "photons_per_step": per_round,
             "scatters_per_step": scatters / args.steps,
-            "l2": "flushed between steps by a 256 MiB device write",
+            "l2": "flushed before the timed round group by a 256 MiB device write; the scene "
+            "tables (< 2 MB) stay L2-resident by design",
             "parallelism": f"{world} independent round streams" if world > 1 else "1 GPU",
             "wall_s": wall,
         },
@@ -395,28 +443,40 @@ def main():
             "peak": peak,
             "unit": "GB/s",
             "frac": achieved / peak,
-            "traffic": recorded_traffic(),
+            "traffic": recorded_traffic(args.workload),
             "peak_source": peak_kind,
             "algorithmic_bytes_per_launch": peel_bytes,
             "launch_ms": peel_seconds * 1e3,
             "launches": peel_launches,
             "stage_share": stage_share,
         },
-        "e2e": {
-            "value": e2e_value,
-            "unit": UNIT,
-            "h2d_bytes_per_step": tables.nbytes / args.steps + 32,
-            "d2h_bytes_per_step": tally_bytes,
-            "wall_s": wall_e2e,
-            "note": "CUDA.prepare (table upload) + run_batches of all steps, tallies copied to host",
-        },
         "gpu_launches": launches,
-        "e2e_gpu_launches": e2e_launches,
         "clocks": clocks.summary(),
     }
 
+    if target is not None:
+        plain, guided = target["analog"], target["guided"]
+        line["time_to_target"] = {
+            "target": f"SE/|I| < {TARGET:g} in every pixel and view, first checked at round 32",
+            "analog_s": plain["seconds"],
+            "guided_s": guided["seconds"],
+            "guided_speedup": plain["seconds"] / guided["seconds"],
+            "guided_method": {"epsilon": GUIDED[0], "roulette": GUIDED[1], "cap": GUIDED[2]},
+            "analog": plain,
+            "guided": guided,
+        }
+        line["e2e"] = {
+            "value": plain["scatters_per_s"] * world,
+            "unit": UNIT,
+            "h2d_bytes_per_step": plain["h2d_bytes"] / plain["rounds"],
+            "d2h_bytes_per_step": plain["d2h_bytes"] / plain["rounds"],
+            "wall_s": plain["seconds"],
+            "note": "the analog time-to-target run: simulate() with CUDA(), table upload, "
+            "every round's FP64 tallies copied to the host, statistics and NetCDF output",
+        }
+
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(scenes.layered_cloud(ppc, 1))
+        line["cpu_baseline"] = cpu_baseline(build_scene(args.workload, ppc, 1))
 
     print(json.dumps(line))
 

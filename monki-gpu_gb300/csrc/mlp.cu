@@ -1,0 +1,601 @@
+// Learned detector importance: a BF16 multilayer perceptron trained and evaluated on the
+// GB300 by the tcgen05 GEMM of umma.cuh, with the small elementwise kernels around it.
+//
+// Network: F <= 64 input features (zero-padded to 64) -> 256 -> 256 -> 256 -> 1, GELU
+// after each hidden layer, BF16 weights and activations, FP32 accumulation, FP32 master
+// weights updated by Adam. Loss: weighted mean squared error. All row-major.
+//
+// Parameter vector (FP32), the layout of monki_mlp_get_params / set_params:
+//   W1[256 x 64], b1[256], W2[256 x 256], b2[256], W3[256 x 256], b3[256], w4[256], b4[1]
+//
+// Per layer l with input X (rows x K) and weights W (256 x K):
+//   forward   Z = X W^T + b (tcgen05, epilogue adds b, writes Z, H = GELU(Z), H^T)
+//   backward  dW += dZ^T X (tcgen05 split-K over the rows, A = dZ^T, B = X^T)
+//             dX' = (dZ W) * GELU'(Z_prev) (tcgen05, B = W^T, epilogue applies GELU')
+// so every operand is K-major and the transposed activations come from the epilogues.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "physics.cuh"
+#include "umma.cuh"
+
+namespace monki {
+namespace mlp {
+
+constexpr int kIn = 64;       // padded input width
+constexpr int kHidden = 256;
+constexpr size_t kW1 = size_t(kHidden) * kIn, kW2 = size_t(kHidden) * kHidden;
+constexpr size_t kParams = kW1 + kHidden + 2 * (kW2 + kHidden) + kHidden + 1;
+// Offsets into the parameter vector.
+constexpr size_t oW1 = 0, ob1 = kW1, oW2 = ob1 + kHidden, ob2 = oW2 + kW2, oW3 = ob2 + kHidden, ob3 = oW3 + kW2,
+                 ow4 = ob3 + kHidden, ob4 = ow4 + kHidden;
+
+using bf16 = __nv_bfloat16;
+
+void check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void write_error(char* err, size_t n, const std::string& msg) {
+    if (err && n) std::snprintf(err, n, "%s", msg.c_str());
+}
+
+// ----------------------------------------------------------------------------------
+// Elementwise kernels.
+// ----------------------------------------------------------------------------------
+
+// Rows of FP32 features (gathered through idx when given) into the padded BF16 input and
+// its transpose; rows >= n and columns >= F are zero.
+__global__ void pack_input(const float* __restrict__ x, const uint32_t* __restrict__ idx, int n, int F, int R,
+                           bf16* __restrict__ X, bf16* __restrict__ XT) {
+    const int total = R * kIn;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        const int m = e / kIn, c = e % kIn;
+        float v = 0.f;
+        if (m < n && c < F) v = x[size_t(idx ? idx[m] : uint32_t(m)) * F + c];
+        const bf16 b = __float2bfloat16(v);
+        X[size_t(m) * kIn + c] = b;
+        XT[size_t(c) * R + m] = b;
+    }
+}
+
+__global__ void gather_targets(const float* __restrict__ t, const float* __restrict__ w, const uint32_t* __restrict__ idx,
+                               int n, int R, float* __restrict__ tb, float* __restrict__ wb) {
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < R; m += gridDim.x * blockDim.x) {
+        tb[m] = m < n ? t[idx ? idx[m] : uint32_t(m)] : 0.f;
+        wb[m] = m < n ? w[idx ? idx[m] : uint32_t(m)] : 0.f;
+    }
+}
+
+// Minibatch indices: Philox4x32-10 counter (step, i / 4, 1, 0), key (seed, 0).
+__global__ void sample_indices(uint32_t step, uint32_t seed, int batch, uint32_t n, uint32_t* __restrict__ idx) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < batch; i += gridDim.x * blockDim.x) {
+        const uint4 w = philox4x32_10(make_uint4(step, uint32_t(i) >> 2, 1u, 0u), make_uint2(seed, 0u));
+        const uint32_t lane = uint32_t(i) & 3u;
+        const uint32_t r = lane == 0 ? w.x : lane == 1 ? w.y : lane == 2 ? w.z : w.w;
+        idx[i] = uint32_t((uint64_t(r) * n) >> 32);
+    }
+}
+
+// y = H3 w4 + b4, one warp per row.
+__global__ void head_forward(const bf16* __restrict__ H, const float* __restrict__ w4, const float* __restrict__ b4,
+                             int rows, float* __restrict__ y) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= rows) return;
+    const bf16* h = H + size_t(warp) * kHidden + lane * 8;
+    float acc = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc += __bfloat162float(h[q]) * w4[lane * 8 + q];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if (lane == 0) y[warp] = acc + b4[0];
+}
+
+// dy = 2 w (y - t) / sum(w); loss accumulates sum w (y - t)^2 / sum(w).
+__global__ void loss_grad(const float* __restrict__ y, const float* __restrict__ t, const float* __restrict__ w,
+                          int rows, float inv_weight, float* __restrict__ dy, float* __restrict__ loss) {
+    float part = 0.f;
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < rows; m += gridDim.x * blockDim.x) {
+        const float d = y[m] - t[m];
+        dy[m] = 2.f * w[m] * d * inv_weight;
+        part += w[m] * d * d * inv_weight;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+    if ((threadIdx.x & 31) == 0 && part != 0.f) atomicAdd(loss, part);
+}
+
+// Output layer backward: dw4 += dy^T H3, db4 += sum dy, and dZ3 = dy w4^T * GELU'(Z3).
+// Block: 256 threads (one per hidden unit) over a slab of 64 rows.
+__global__ void head_backward(const float* __restrict__ dy, const bf16* __restrict__ H, const float* __restrict__ w4,
+                              const float* __restrict__ Z, int R, float* __restrict__ grads, bf16* __restrict__ G) {
+    const int n = threadIdx.x;
+    const int m0 = blockIdx.x * 64;
+    float acc = 0.f, bias = 0.f;
+    const float wn = w4[n];
+    for (int m = m0; m < min(m0 + 64, R); ++m) {
+        const float d = dy[m];
+        const size_t at = size_t(m) * kHidden + n;
+        acc += d * __bfloat162float(H[at]);
+        bias += d;
+        G[at] = __float2bfloat16(d * wn * umma::gelu_grad(Z[at]));
+    }
+    atomicAdd(grads + ow4 + n, acc);
+    if (n == 0) atomicAdd(grads + ob4, bias);
+}
+
+// out (cols x R) = in^T for a BF16 rows x cols matrix (row-major), 32 x 32 tiles.
+__global__ void transpose(const bf16* __restrict__ in, int rows, int cols, int R, bf16* __restrict__ out) {
+    __shared__ bf16 tile[32][33];
+    const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int m = by + r, c = bx + threadIdx.x;
+        tile[r][threadIdx.x] = (m < rows && c < cols) ? in[size_t(m) * cols + c] : __float2bfloat16(0.f);
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int c = bx + r, m = by + threadIdx.x;
+        if (c < cols && m < R) out[size_t(c) * R + m] = tile[threadIdx.x][r];
+    }
+}
+
+// out[n] += sum over m < rows of GT[n * R + m] (bias gradients from a transposed matrix).
+__global__ void row_sums(const bf16* __restrict__ GT, int rows, int R, float* __restrict__ out) {
+    const int n = blockIdx.x;
+    float acc = 0.f;
+    for (int m = threadIdx.x; m < rows; m += blockDim.x) acc += __bfloat162float(GT[size_t(n) * R + m]);
+    __shared__ float part[32];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float s = 0.f;
+        for (int q = 0; q < int(blockDim.x >> 5); ++q) s += part[q];
+        out[n] += s;
+    }
+}
+
+__global__ void adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1, float* __restrict__ m2,
+                     size_t count, float lr, float c1, float c2) {
+    for (size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x; e < count; e += size_t(gridDim.x) * blockDim.x) {
+        const float gi = g[e];
+        const float a = 0.9f * m1[e] + 0.1f * gi;
+        const float b = 0.999f * m2[e] + 0.001f * gi * gi;
+        m1[e] = a;
+        m2[e] = b;
+        p[e] -= lr * (a * c1) / (sqrtf(b * c2) + 1e-8f);
+    }
+}
+
+// BF16 working copies of the weights and the transposes the backward pass needs.
+__global__ void refresh(const float* __restrict__ p, bf16* __restrict__ W1, bf16* __restrict__ W2, bf16* __restrict__ W3,
+                        bf16* __restrict__ W2T, bf16* __restrict__ W3T) {
+    for (size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x; e < kW2; e += size_t(gridDim.x) * blockDim.x) {
+        const size_t r = e / kHidden, c = e % kHidden;
+        if (e < kW1) W1[e] = __float2bfloat16(p[oW1 + e]);
+        const bf16 w2 = __float2bfloat16(p[oW2 + e]), w3 = __float2bfloat16(p[oW3 + e]);
+        W2[e] = w2;
+        W3[e] = w3;
+        W2T[c * kHidden + r] = w2;
+        W3T[c * kHidden + r] = w3;
+    }
+}
+
+// ----------------------------------------------------------------------------------
+// Session.
+// ----------------------------------------------------------------------------------
+struct Net {
+    int device = 0, features = 0, R = 0;  // R: rows per pass, a multiple of 128
+    cudaStream_t stream = nullptr;
+    float *params = nullptr, *grads = nullptr, *m1 = nullptr, *m2 = nullptr;
+    bf16 *W1 = nullptr, *W2 = nullptr, *W3 = nullptr, *W2T = nullptr, *W3T = nullptr;
+    bf16 *X = nullptr, *XT = nullptr, *H1 = nullptr, *H2 = nullptr, *H3 = nullptr, *H1T = nullptr, *H2T = nullptr;
+    bf16 *G3 = nullptr, *G3T = nullptr, *G2 = nullptr, *G2T = nullptr, *G1 = nullptr, *G1T = nullptr;
+    float *Z1 = nullptr, *Z2 = nullptr, *Z3 = nullptr, *y = nullptr, *dy = nullptr, *tb = nullptr, *wb = nullptr;
+    float* loss = nullptr;
+    uint32_t* failure = nullptr;
+    uint32_t* idx = nullptr;
+    float *data_x = nullptr, *data_t = nullptr, *data_w = nullptr;
+    uint32_t data_n = 0;
+    uint32_t step = 0, seed = 0;
+    std::vector<void*> owned;
+
+    template <typename P>
+    P* alloc(size_t count) {
+        void* p = nullptr;
+        check(cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(P)), "cudaMalloc");
+        owned.push_back(p);
+        return static_cast<P*>(p);
+    }
+    ~Net() {
+        if (stream) cudaStreamSynchronize(stream);
+        for (void* p : owned) cudaFree(p);
+        cudaFree(data_x); cudaFree(data_t); cudaFree(data_w);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+std::mutex g_attr_lock;
+bool g_attr_done[64] = {};
+
+void configure(int device) {
+    std::lock_guard<std::mutex> guard(g_attr_lock);
+    if (device < 0 || device >= 64 || g_attr_done[device]) return;
+    check(cudaFuncSetAttribute(umma::gemm<umma::kStore>, cudaFuncAttributeMaxDynamicSharedMemorySize, umma::kSmemBytes), "attr");
+    check(cudaFuncSetAttribute(umma::gemm<umma::kForward>, cudaFuncAttributeMaxDynamicSharedMemorySize, umma::kSmemBytes), "attr");
+    check(cudaFuncSetAttribute(umma::gemm<umma::kBackward>, cudaFuncAttributeMaxDynamicSharedMemorySize, umma::kSmemBytes), "attr");
+    check(cudaFuncSetAttribute(umma::gemm<umma::kAccumulate>, cudaFuncAttributeMaxDynamicSharedMemorySize, umma::kSmemBytes), "attr");
+    g_attr_done[device] = true;
+}
+
+template <int EPI>
+void gemm(const umma::Params& p, int splits, cudaStream_t stream) {
+    if (p.K % umma::kBlockK || p.k_chunk % umma::kBlockK || p.N % 16 || p.N < 16 || p.N > 256 || p.rows_a < 1)
+        throw std::runtime_error("GEMM shape outside the kernel's tiling");
+    dim3 grid((p.rows_a + umma::kBlockM - 1) / umma::kBlockM, splits);
+    umma::gemm<EPI><<<grid, umma::kThreads, umma::kSmemBytes, stream>>>(p);
+    check(cudaGetLastError(), "gemm launch");
+}
+
+umma::Params params_for(const bf16* A, const bf16* B, int rows, int N, int K, uint32_t* failure) {
+    umma::Params p{};
+    p.A = A; p.B = B; p.rows_a = rows; p.N = N; p.K = K; p.lda = K; p.ldb = K; p.k_chunk = K;
+    p.failure = failure;
+    return p;
+}
+
+// Zero the columns [rows, rows rounded up to 64) of a transposed (height x R) matrix: the
+// split-K weight-gradient GEMMs read whole 64-column slices.
+void clear_tail(bf16* T, int rows, int R, int height, cudaStream_t stream) {
+    const int end = std::min(R, (rows + 63) / 64 * 64);
+    if (end > rows)
+        check(cudaMemset2DAsync(T + rows, size_t(R) * sizeof(bf16), 0, size_t(end - rows) * sizeof(bf16), size_t(height), stream),
+              "memset(tail)");
+}
+
+// Forward pass of the first `rows` rows (<= R) of the packed input.
+void forward(Net& n, int rows) {
+    const int R = n.R;
+    umma::Params p = params_for(n.X, n.W1, rows, kHidden, kIn, n.failure);
+    p.C = n.Z1; p.bias = n.params + ob1; p.H = n.H1; p.HT = n.H1T; p.rows_ht = R;
+    gemm<umma::kForward>(p, 1, n.stream);
+    p = params_for(n.H1, n.W2, rows, kHidden, kHidden, n.failure);
+    p.C = n.Z2; p.bias = n.params + ob2; p.H = n.H2; p.HT = n.H2T; p.rows_ht = R;
+    gemm<umma::kForward>(p, 1, n.stream);
+    p = params_for(n.H2, n.W3, rows, kHidden, kHidden, n.failure);
+    p.C = n.Z3; p.bias = n.params + ob3; p.H = n.H3; p.HT = nullptr; p.rows_ht = R;
+    gemm<umma::kForward>(p, 1, n.stream);
+    clear_tail(n.H1T, rows, R, kHidden, n.stream);
+    clear_tail(n.H2T, rows, R, kHidden, n.stream);
+    head_forward<<<(rows * 32 + 255) / 256, 256, 0, n.stream>>>(n.H3, n.params + ow4, n.params + ob4, rows, n.y);
+    check(cudaGetLastError(), "head launch");
+}
+
+// Loss and gradients of the first `rows` rows against tb / wb (gradients accumulate into
+// n.grads, which the caller clears).
+void backward(Net& n, int rows, float inv_weight, float* loss) {
+    const int R = n.R;
+    loss_grad<<<256, 256, 0, n.stream>>>(n.y, n.tb, n.wb, rows, inv_weight, n.dy, loss);
+    check(cudaMemsetAsync(n.G3, 0, size_t(R) * kHidden * sizeof(bf16), n.stream), "memset");
+    head_backward<<<(rows + 63) / 64, kHidden, 0, n.stream>>>(n.dy, n.H3, n.params + ow4, n.Z3, rows, n.grads, n.G3);
+    transpose<<<dim3(kHidden / 32, (R + 31) / 32), dim3(32, 8), 0, n.stream>>>(n.G3, R, kHidden, R, n.G3T);
+    row_sums<<<kHidden, 256, 0, n.stream>>>(n.G3T, rows, R, n.grads + ob3);
+    check(cudaGetLastError(), "head backward launch");
+    // Split-K over the rows for the weight gradients: 64-row multiples, 512 rows per slice.
+    const int chunk = 512, K = (rows + 63) / 64 * 64, splits = (K + chunk - 1) / chunk;
+    umma::Params p = params_for(n.G3T, n.H2T, kHidden, kHidden, K, n.failure);
+    p.lda = R; p.ldb = R; p.k_chunk = chunk; p.C = n.grads + oW3;
+    gemm<umma::kAccumulate>(p, splits, n.stream);
+    p = params_for(n.G3, n.W3T, rows, kHidden, kHidden, n.failure);
+    p.zprev = n.Z2; p.H = n.G2; p.HT = n.G2T; p.rows_ht = R;
+    gemm<umma::kBackward>(p, 1, n.stream);
+    clear_tail(n.G2T, rows, R, kHidden, n.stream);
+    row_sums<<<kHidden, 256, 0, n.stream>>>(n.G2T, rows, R, n.grads + ob2);
+    p = params_for(n.G2T, n.H1T, kHidden, kHidden, K, n.failure);
+    p.lda = R; p.ldb = R; p.k_chunk = chunk; p.C = n.grads + oW2;
+    gemm<umma::kAccumulate>(p, splits, n.stream);
+    p = params_for(n.G2, n.W2T, rows, kHidden, kHidden, n.failure);
+    p.zprev = n.Z1; p.H = n.G1; p.HT = n.G1T; p.rows_ht = R;
+    gemm<umma::kBackward>(p, 1, n.stream);
+    clear_tail(n.G1T, rows, R, kHidden, n.stream);
+    row_sums<<<kHidden, 256, 0, n.stream>>>(n.G1T, rows, R, n.grads + ob1);
+    p = params_for(n.G1T, n.XT, kHidden, kIn, K, n.failure);
+    p.lda = R; p.ldb = R; p.k_chunk = chunk; p.C = n.grads + oW1;
+    gemm<umma::kAccumulate>(p, splits, n.stream);
+    check(cudaGetLastError(), "backward launch");
+}
+
+void refresh_weights(Net& n) {
+    refresh<<<256, 256, 0, n.stream>>>(n.params, n.W1, n.W2, n.W3, n.W2T, n.W3T);
+    check(cudaGetLastError(), "refresh launch");
+}
+
+void check_failure(Net& n) {
+    uint32_t flag = 0;
+    check(cudaMemcpyAsync(&flag, n.failure, sizeof(flag), cudaMemcpyDeviceToHost, n.stream), "copy(failure)");
+    check(cudaStreamSynchronize(n.stream), "mlp");
+    if (flag) throw std::runtime_error("tensor-core GEMM wait gave up (flag " + std::to_string(flag) + ")");
+}
+
+}  // namespace mlp
+}  // namespace monki
+
+using monki::mlp::Net;
+using namespace monki::mlp;
+namespace umma = monki::umma;
+
+extern "C" {
+
+size_t monki_mlp_param_count(void) { return kParams; }
+
+void* monki_mlp_create(uint32_t device, uint32_t features, uint32_t rows, uint32_t seed, char* err, size_t errlen) {
+    Net* n = nullptr;
+    try {
+        if (features < 1 || features > uint32_t(kIn)) throw std::runtime_error("features must be in [1, 64]");
+        if (rows < 1 || rows > (1u << 20)) throw std::runtime_error("rows must be in [1, 2^20]");
+        int count = 0;
+        if (cudaGetDeviceCount(&count) != cudaSuccess || device >= uint32_t(count))
+            throw std::runtime_error("Requested CUDA device is unavailable");
+        check(cudaSetDevice(int(device)), "cudaSetDevice");
+        cudaDeviceProp prop{};
+        check(cudaGetDeviceProperties(&prop, int(device)), "cudaGetDeviceProperties");
+        if (prop.major != 10 || prop.minor != 3) throw std::runtime_error("The learned importance kernels need an sm_103 GPU");
+        configure(int(device));
+        n = new Net();
+        n->device = int(device);
+        n->features = int(features);
+        n->R = int((rows + 127) / 128 * 128);
+        n->seed = seed;
+        check(cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking), "stream");
+        const size_t R = size_t(n->R), H = size_t(kHidden);
+        n->params = n->alloc<float>(kParams); n->grads = n->alloc<float>(kParams);
+        n->m1 = n->alloc<float>(kParams); n->m2 = n->alloc<float>(kParams);
+        n->W1 = n->alloc<bf16>(kW1); n->W2 = n->alloc<bf16>(kW2); n->W3 = n->alloc<bf16>(kW2);
+        n->W2T = n->alloc<bf16>(kW2); n->W3T = n->alloc<bf16>(kW2);
+        n->X = n->alloc<bf16>(R * kIn); n->XT = n->alloc<bf16>(R * kIn);
+        for (bf16** b : {&n->H1, &n->H2, &n->H3, &n->H1T, &n->H2T, &n->G3, &n->G3T, &n->G2, &n->G2T, &n->G1, &n->G1T})
+            *b = n->alloc<bf16>(R * H);
+        n->Z1 = n->alloc<float>(R * H); n->Z2 = n->alloc<float>(R * H); n->Z3 = n->alloc<float>(R * H);
+        n->y = n->alloc<float>(R); n->dy = n->alloc<float>(R); n->tb = n->alloc<float>(R); n->wb = n->alloc<float>(R);
+        n->loss = n->alloc<float>(1);
+        n->failure = n->alloc<uint32_t>(1);
+        n->idx = n->alloc<uint32_t>(R);
+        check(cudaMemset(n->params, 0, kParams * sizeof(float)), "memset");
+        check(cudaMemset(n->m1, 0, kParams * sizeof(float)), "memset");
+        check(cudaMemset(n->m2, 0, kParams * sizeof(float)), "memset");
+        check(cudaMemset(n->failure, 0, sizeof(uint32_t)), "memset");
+        // Transposed activations are read in 64-row slices; the padding rows stay zero.
+        for (bf16* b : {n->XT, n->H1T, n->H2T, n->G3T, n->G2T, n->G1T})
+            check(cudaMemset(b, 0, R * (b == n->XT ? size_t(kIn) : H) * sizeof(bf16)), "memset");
+        refresh_weights(*n);
+        check(cudaStreamSynchronize(n->stream), "create");
+        return n;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        delete n;
+        return nullptr;
+    }
+}
+
+int monki_mlp_set_params(void* handle, const float* params, size_t count, char* err, size_t errlen) {
+    Net* n = static_cast<Net*>(handle);
+    try {
+        if (!n || !params || count != kParams) throw std::runtime_error("set_params needs the full parameter vector");
+        for (size_t e = 0; e < count; ++e)
+            if (!std::isfinite(params[e])) throw std::runtime_error("Nonfinite parameter");
+        check(cudaSetDevice(n->device), "cudaSetDevice");
+        check(cudaMemcpyAsync(n->params, params, kParams * sizeof(float), cudaMemcpyHostToDevice, n->stream), "upload");
+        check(cudaMemsetAsync(n->m1, 0, kParams * sizeof(float), n->stream), "memset");
+        check(cudaMemsetAsync(n->m2, 0, kParams * sizeof(float), n->stream), "memset");
+        n->step = 0;
+        refresh_weights(*n);
+        check(cudaStreamSynchronize(n->stream), "set_params");
+        return 0;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        return 1;
+    }
+}
+
+int monki_mlp_get_params(void* handle, float* params, size_t count, char* err, size_t errlen) {
+    Net* n = static_cast<Net*>(handle);
+    try {
+        if (!n || !params || count != kParams) throw std::runtime_error("get_params needs the full parameter vector");
+        check(cudaSetDevice(n->device), "cudaSetDevice");
+        check(cudaMemcpyAsync(params, n->params, kParams * sizeof(float), cudaMemcpyDeviceToHost, n->stream), "download");
+        check(cudaStreamSynchronize(n->stream), "get_params");
+        return 0;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        return 1;
+    }
+}
+
+// y[rows] = network(x[rows x features]), any number of rows (processed R at a time).
+int monki_mlp_forward(void* handle, const float* x, uint32_t rows, float* y, char* err, size_t errlen) {
+    Net* n = static_cast<Net*>(handle);
+    try {
+        if (!n || (!x && rows) || (!y && rows)) throw std::runtime_error("Invalid network or buffers");
+        check(cudaSetDevice(n->device), "cudaSetDevice");
+        float* dx = nullptr;
+        check(cudaMalloc(&dx, std::max<size_t>(1, size_t(std::min<uint32_t>(rows, uint32_t(n->R))) * n->features * sizeof(float))), "cudaMalloc");
+        try {
+            for (uint32_t r0 = 0; r0 < rows; r0 += uint32_t(n->R)) {
+                const int m = int(std::min<uint32_t>(uint32_t(n->R), rows - r0));
+                check(cudaMemcpyAsync(dx, x + size_t(r0) * n->features, size_t(m) * n->features * sizeof(float),
+                                      cudaMemcpyHostToDevice, n->stream), "upload");
+                pack_input<<<1024, 256, 0, n->stream>>>(dx, nullptr, m, n->features, n->R, n->X, n->XT);
+                forward(*n, m);
+                check(cudaMemcpyAsync(y + r0, n->y, size_t(m) * sizeof(float), cudaMemcpyDeviceToHost, n->stream), "download");
+                check_failure(*n);
+            }
+        } catch (...) {
+            cudaFree(dx);
+            throw;
+        }
+        cudaFree(dx);
+        return 0;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        return 1;
+    }
+}
+
+// Loss and gradient (the parameter vector's layout) of one batch of rows <= R.
+int monki_mlp_gradients(void* handle, const float* x, const float* target, const float* weight, uint32_t rows,
+                        float* grads, float* loss, char* err, size_t errlen) {
+    Net* n = static_cast<Net*>(handle);
+    try {
+        if (!n || !x || !target || !weight || !grads || !loss || rows < 1 || rows > uint32_t(n->R))
+            throw std::runtime_error("Invalid network, buffers or row count");
+        double total = 0.0;
+        for (uint32_t m = 0; m < rows; ++m) total += weight[m];
+        if (!(total > 0.0)) throw std::runtime_error("Weights must have a positive sum");
+        check(cudaSetDevice(n->device), "cudaSetDevice");
+        float *dx = nullptr, *dt = nullptr, *dw = nullptr;
+        check(cudaMalloc(&dx, size_t(rows) * n->features * sizeof(float)), "cudaMalloc");
+        check(cudaMalloc(&dt, rows * sizeof(float)), "cudaMalloc");
+        check(cudaMalloc(&dw, rows * sizeof(float)), "cudaMalloc");
+        check(cudaMemcpyAsync(dx, x, size_t(rows) * n->features * sizeof(float), cudaMemcpyHostToDevice, n->stream), "upload");
+        check(cudaMemcpyAsync(dt, target, rows * sizeof(float), cudaMemcpyHostToDevice, n->stream), "upload");
+        check(cudaMemcpyAsync(dw, weight, rows * sizeof(float), cudaMemcpyHostToDevice, n->stream), "upload");
+        pack_input<<<1024, 256, 0, n->stream>>>(dx, nullptr, int(rows), n->features, n->R, n->X, n->XT);
+        gather_targets<<<256, 256, 0, n->stream>>>(dt, dw, nullptr, int(rows), n->R, n->tb, n->wb);
+        check(cudaMemsetAsync(n->grads, 0, kParams * sizeof(float), n->stream), "memset");
+        check(cudaMemsetAsync(n->loss, 0, sizeof(float), n->stream), "memset");
+        forward(*n, int(rows));
+        backward(*n, int(rows), float(1.0 / total), n->loss);
+        check(cudaMemcpyAsync(grads, n->grads, kParams * sizeof(float), cudaMemcpyDeviceToHost, n->stream), "download");
+        check(cudaMemcpyAsync(loss, n->loss, sizeof(float), cudaMemcpyDeviceToHost, n->stream), "download");
+        check_failure(*n);
+        cudaFree(dx); cudaFree(dt); cudaFree(dw);
+        return 0;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        return 1;
+    }
+}
+
+// Keep a training set on the device: rows x features inputs, targets and weights.
+int monki_mlp_set_data(void* handle, const float* x, const float* target, const float* weight, uint32_t rows,
+                       char* err, size_t errlen) {
+    Net* n = static_cast<Net*>(handle);
+    try {
+        if (!n || !x || !target || !weight || rows < 1) throw std::runtime_error("Invalid network or training set");
+        check(cudaSetDevice(n->device), "cudaSetDevice");
+        check(cudaStreamSynchronize(n->stream), "sync");
+        cudaFree(n->data_x); cudaFree(n->data_t); cudaFree(n->data_w);
+        n->data_x = n->data_t = n->data_w = nullptr;
+        n->data_n = 0;
+        check(cudaMalloc(&n->data_x, size_t(rows) * n->features * sizeof(float)), "cudaMalloc");
+        check(cudaMalloc(&n->data_t, rows * sizeof(float)), "cudaMalloc");
+        check(cudaMalloc(&n->data_w, rows * sizeof(float)), "cudaMalloc");
+        check(cudaMemcpy(n->data_x, x, size_t(rows) * n->features * sizeof(float), cudaMemcpyHostToDevice), "upload");
+        check(cudaMemcpy(n->data_t, target, rows * sizeof(float), cudaMemcpyHostToDevice), "upload");
+        check(cudaMemcpy(n->data_w, weight, rows * sizeof(float), cudaMemcpyHostToDevice), "upload");
+        n->data_n = rows;
+        return 0;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        return 1;
+    }
+}
+
+// Adam steps on minibatches of `batch` rows (<= R) drawn with replacement from the
+// device training set; losses[steps] receives each step's minibatch loss.
+int monki_mlp_train(void* handle, uint32_t steps, uint32_t batch, float lr, float* losses, char* err, size_t errlen) {
+    Net* n = static_cast<Net*>(handle);
+    try {
+        if (!n || !n->data_n) throw std::runtime_error("No training set on the device");
+        if (batch < 1 || batch > uint32_t(n->R)) throw std::runtime_error("batch must be in [1, rows of the network]");
+        if (!(lr > 0.f) || !std::isfinite(lr)) throw std::runtime_error("Invalid learning rate");
+        check(cudaSetDevice(n->device), "cudaSetDevice");
+        std::vector<float> host_loss(steps, 0.f);
+        float* dloss = nullptr;
+        check(cudaMalloc(&dloss, std::max<size_t>(steps, 1) * sizeof(float)), "cudaMalloc");
+        try {
+            check(cudaMemsetAsync(dloss, 0, std::max<size_t>(steps, 1) * sizeof(float), n->stream), "memset");
+            for (uint32_t s = 0; s < steps; ++s) {
+                const uint32_t t = ++n->step;
+                sample_indices<<<(batch + 255) / 256, 256, 0, n->stream>>>(t, n->seed, int(batch), n->data_n, n->idx);
+                pack_input<<<1024, 256, 0, n->stream>>>(n->data_x, n->idx, int(batch), n->features, n->R, n->X, n->XT);
+                gather_targets<<<256, 256, 0, n->stream>>>(n->data_t, n->data_w, n->idx, int(batch), n->R, n->tb, n->wb);
+                check(cudaMemsetAsync(n->grads, 0, kParams * sizeof(float), n->stream), "memset");
+                forward(*n, int(batch));
+                // Weighted mean over the minibatch: normalised by the batch size (the
+                // targets' weights average to about one), so the gradient scale does not
+                // depend on the batch.
+                backward(*n, int(batch), 1.0f / float(batch), dloss + s);
+                const float c1 = 1.f / (1.f - std::pow(0.9f, float(t))), c2 = 1.f / (1.f - std::pow(0.999f, float(t)));
+                adam<<<592, 256, 0, n->stream>>>(n->params, n->grads, n->m1, n->m2, kParams, lr, c1, c2);
+                refresh_weights(*n);
+                check(cudaGetLastError(), "train launch");
+            }
+            check(cudaMemcpyAsync(host_loss.data(), dloss, steps * sizeof(float), cudaMemcpyDeviceToHost, n->stream), "download");
+            check_failure(*n);
+        } catch (...) {
+            cudaFree(dloss);
+            throw;
+        }
+        cudaFree(dloss);
+        if (losses) std::copy(host_loss.begin(), host_loss.end(), losses);
+        return 0;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        return 1;
+    }
+}
+
+void monki_mlp_close(void* handle) {
+    Net* n = static_cast<Net*>(handle);
+    if (!n) return;
+    cudaSetDevice(n->device);
+    delete n;
+}
+
+// Test hook: C (M x N, FP32) = A (M x K) B^T (N x K), BF16 bits in, through the tcgen05
+// GEMM; splits > 1 runs split-K into a zeroed C with the accumulating epilogue.
+int monki_mlp_gemm_probe(uint32_t device, const uint16_t* a, const uint16_t* b, int M, int N, int K, int splits,
+                         float* c, char* err, size_t errlen) {
+    try {
+        if (!a || !b || !c || M < 1 || splits < 1 || K % 64 || N % 16 || N < 16 || N > 256 || (K / 64) % splits)
+            throw std::runtime_error("Invalid GEMM probe shape");
+        check(cudaSetDevice(int(device)), "cudaSetDevice");
+        configure(int(device));
+        bf16 *da = nullptr, *db = nullptr;
+        float* dc = nullptr;
+        uint32_t* flag = nullptr;
+        check(cudaMalloc(&da, size_t(M) * K * 2), "cudaMalloc");
+        check(cudaMalloc(&db, size_t(N) * K * 2), "cudaMalloc");
+        check(cudaMalloc(&dc, size_t(M) * N * 4), "cudaMalloc");
+        check(cudaMalloc(&flag, 4), "cudaMalloc");
+        check(cudaMemcpy(da, a, size_t(M) * K * 2, cudaMemcpyHostToDevice), "upload");
+        check(cudaMemcpy(db, b, size_t(N) * K * 2, cudaMemcpyHostToDevice), "upload");
+        check(cudaMemset(dc, 0, size_t(M) * N * 4), "memset");
+        check(cudaMemset(flag, 0, 4), "memset");
+        umma::Params p = params_for(da, db, M, N, K, flag);
+        p.C = dc;
+        p.k_chunk = K / splits;
+        if (splits == 1) gemm<umma::kStore>(p, 1, nullptr);
+        else gemm<umma::kAccumulate>(p, splits, nullptr);
+        uint32_t f = 0;
+        check(cudaMemcpy(&f, flag, 4, cudaMemcpyDeviceToHost), "download");
+        check(cudaMemcpy(c, dc, size_t(M) * N * 4, cudaMemcpyDeviceToHost), "download");
+        cudaFree(da); cudaFree(db); cudaFree(dc); cudaFree(flag);
+        if (f) throw std::runtime_error("tensor-core GEMM wait gave up");
+        return 0;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        return 1;
+    }
+}
+
+}  // extern "C"

@@ -17,6 +17,9 @@
 //   lut_f[4 * n]             {F11, F22, F33, F12} per scattering angle, per species
 //   lut_cos[n], lut_cdf[n]   ascending cosine grid and the bound-function CDF
 //   guide[kGuide + 1]        CDF guide table: largest i with cdf[i] <= g / kGuide
+//   band[nx * ny * uniform_top]  extinction of every cell below the horizontally uniform
+//                            top (the only cells a cell walk visits), 16-byte aligned and
+//                            padded, staged whole into shared memory when it fits
 #pragma once
 #include <stdint.h>
 
@@ -26,6 +29,7 @@ constexpr int kMaxViews = 16;
 constexpr int kMaxSpecies = 3;
 constexpr int kMaxLayers = 64;   // including the vacuum layer
 constexpr int kGuide = 4096;
+constexpr uint32_t kBandMaxBytes = 48u * 1024u;  // largest band staged in shared memory
 
 // Failure flags shared with the Python host (kernels/metal/README.md:57-59).
 enum Failure : uint32_t {
@@ -35,6 +39,7 @@ enum Failure : uint32_t {
     kInvalidStokes = 8u,
     kHistoryCap = 16u,
     kQueueCorrupt = 32u,  // a queue entry outside the photon pool (internal error)
+    kStageTimeout = 64u,  // the shared-memory staging copy did not complete in time
 };
 
 template <typename T>
@@ -62,6 +67,8 @@ struct SceneView {
     const T* lut_cos[kMaxSpecies];
     const T* lut_cdf[kMaxSpecies];
     const int* guide[kMaxSpecies];
+    const T* band;          // extinction below the uniform top, i + nx * (j + ny * k)
+    uint32_t band_bytes;    // padded size when staged in shared memory, else 0
 };
 
 // Guided transport (detector-directed sampling at particle scatters and Russian

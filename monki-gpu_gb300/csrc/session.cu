@@ -222,6 +222,7 @@ struct Packed {
     std::vector<int> guides;
     size_t cells, zunit, zsum, ssalb_gas, albedo, tau_above, layer_beta, vprefix, run_lo, run_hi;
     size_t lut_f[kMaxSpecies], lut_cos[kMaxSpecies], lut_cdf[kMaxSpecies], guide[kMaxSpecies];
+    size_t band, band_count;
     int uniform_top;
 };
 
@@ -261,6 +262,10 @@ Packed<T> pack(const Prepared& p, bool uniform_prefix) {
             if (T(p.beta[size_t(z) * cols + c]) != b0) { varying = z; break; }
     }
     k.uniform_top = uniform_prefix ? varying + 1 : p.nz;
+    // Extinction of the cells below the uniform top: the cell walks read nothing else.
+    k.band_count = cols * size_t(std::min(k.uniform_top, p.nz - 1));
+    k.band = reserve(k.band_count + 4);
+    for (size_t c = 0; c < k.band_count; ++c) v[k.band + c] = T(p.beta[c]);
     k.tau_above = reserve(p.nz);
     {
         // tau_above[k] = sum over physical layers above k of thickness * extinction,
@@ -394,6 +399,9 @@ SceneView<T> make_view(const Prepared& p, const Packed<T>& k, void* base) {
     s.albedo = tv + k.albedo; s.tau_above = tv + k.tau_above;
     s.layer_beta = tv + k.layer_beta; s.vprefix = tv + k.vprefix;
     s.run_lo = gv + k.run_lo; s.run_hi = gv + k.run_hi;
+    s.band = tv + k.band;
+    const size_t band_bytes = align_up(k.band_count * sizeof(T), 16);
+    s.band_bytes = (k.band_count && band_bytes <= kBandMaxBytes) ? uint32_t(band_bytes) : 0u;
     for (int sp = 0; sp < p.ntypes; ++sp) {
         s.lut_n[sp] = p.luts[sp].n; s.ssalb_aer[sp] = T(p.luts[sp].ssalb);
         s.znorm[sp] = T(analog_norm(p.luts[sp], p.nmat));
@@ -477,9 +485,9 @@ void wave_iteration(Session& s, const SceneView<T>& v, Pool<T>& P, const Control
     T* banks = static_cast<T*>(s.banks);
     check(cudaMemsetAsync(P.counts, 0, 4 * sizeof(uint32_t), s.stream), "memset(queues)");
     if (ev) cudaEventRecord(ev[0], s.stream);
-    wf_transit<T, PATHS><<<grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, s.cfg.walk, s.failure, s.counters);
+    wf_transit<T, PATHS><<<grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, s.cfg.walk, s.failure, s.counters);
     if (ev) cudaEventRecord(ev[1], s.stream);
-    wf_peel<T, T, NMAT, PATHS><<<grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, banks, s.wave, s.failure, s.counters);
+    wf_peel<T, T, NMAT, PATHS><<<grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, banks, s.wave, s.failure, s.counters);
     if (ev) cudaEventRecord(ev[2], s.stream);
     Guide<T> g{T(s.cfg.epsilon), T(s.cfg.roulette), s.cfg.cap > 0.0 ? T(s.cfg.cap) : T(INFINITY),
                static_cast<const T*>(s.scale)};

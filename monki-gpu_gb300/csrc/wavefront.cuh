@@ -109,6 +109,44 @@ __device__ __forceinline__ void unpack_layers(uint32_t v, int& k, int& k1, int& 
     wmax = int(v >> 24);
 }
 
+// Stage the extinction band (every cell below the uniform top) into this block's shared
+// memory with one bulk asynchronous copy (TMA engine) completing on an mbarrier. Returns
+// the shared copy, or null when the band is not staged (too large, or absent) or the copy
+// did not complete within the wait limit (then kStageTimeout is raised and the caller
+// reads global memory). Every thread of the block must call it.
+template <typename T>
+__device__ __forceinline__ const T* stage_band(const SceneView<T>& s, unsigned char* smem, uint32_t* failure) {
+    if (!s.band_bytes) return nullptr;
+    __shared__ __align__(8) uint64_t barrier;
+    const uint32_t bar = uint32_t(__cvta_generic_to_shared(&barrier));
+    const uint32_t dst = uint32_t(__cvta_generic_to_shared(smem));
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(s.band_bytes) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(dst), "l"(s.band), "r"(s.band_bytes), "r"(bar) : "memory");
+    }
+    __syncthreads();
+    uint32_t done = 0;
+    for (uint32_t attempt = 0; attempt < (1u << 22) && !done; ++attempt) {
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.b32 %0, 1, 0, p;\n}"
+            : "=r"(done) : "r"(bar) : "memory");
+    }
+    if (!done) {
+        if (threadIdx.x == 0) atomicOr(failure, kStageTimeout);
+        return nullptr;
+    }
+    return reinterpret_cast<const T*>(smem);
+}
+
+// Extinction of a cell below the uniform top: the staged copy when there is one.
+template <typename T>
+__device__ __forceinline__ T band_beta(const SceneView<T>& s, const T* band, int i, int j, int k) {
+    return band ? band[i + s.nx * (j + s.ny * k)] : beta_at(s, i, j, k);
+}
+
 // A photon's Philox stream addressed by draw index: draw d is word d % 4 of block d / 4.
 struct DrawStream {
     uint32_t photon, round, seed, draw, loaded;
@@ -289,6 +327,8 @@ template <typename T, bool PATHS>
 __global__ void __launch_bounds__(256, 4)
 wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, uint32_t* __restrict__ failure,
            unsigned long long* __restrict__ counters) {
+    extern __shared__ __align__(16) unsigned char staged[];
+    const T* band = stage_band<T>(s, staged, failure);
     const T eps = Tol<T>::eps;
     const int top = s.nz - 1;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -370,7 +410,7 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
                     if (outcome >= 0) break;
                     continue;
                 }
-                const T bv = k < top ? beta_at(s, i, j, k) : T(0);
+                const T bv = k < top ? band_beta<T>(s, band, i, j, k) : T(0);
                 if (bv > eps) {
                     const T de = remains / bv;
                     if (de < x * ai && de < y * bi && de < z * ci) {
@@ -496,6 +536,8 @@ template <typename T, typename TA, int NMAT, bool PATHS>
 __global__ void __launch_bounds__(256, 3)
 wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ banks, WaveTally L,
         uint32_t* __restrict__ failure, unsigned long long* __restrict__ counters) {
+    extern __shared__ __align__(16) unsigned char staged[];
+    const T* band = stage_band<T>(s, staged, failure);
     const T eps = Tol<T>::eps;
     const int top = s.nz - 1;
     const uint32_t ns = P.counts[0], ng = P.counts[1], np = P.counts[2];
@@ -568,12 +610,13 @@ wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ b
             bool capped = false;
             while (rk >= 0 && rk < top) {
                 if (rk >= s.uniform_top) {
-                    tau += (rz * beta_at(s, ri, rj, rk) + __ldg(s.tau_above + rk)) * ci;
+                    // Uniform layers: one extinction per layer, the same in every cell.
+                    tau += (rz * __ldg(s.layer_beta + rk) + __ldg(s.tau_above + rk)) * ci;
                     ++visits;
                     break;
                 }
                 if (++rsteps > ctl.max_steps) { capped = true; break; }
-                const T bv = beta_at(s, ri, rj, rk);
+                const T bv = band_beta<T>(s, band, ri, rj, rk);
                 const T dist = advance(s, ri, rj, rk, rx, ry, rz, is, js, ks, aa, ba, ca, ai, bi, ci);
                 tau += dist * bv;
                 ++visits;

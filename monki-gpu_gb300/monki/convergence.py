@@ -137,7 +137,13 @@ class RadianceMoments:
 
 
 class AMFStopping:
-    """Schedule rounds in groups of ``check_every`` and stop after sustained precision."""
+    """Schedule rounds in groups of ``check_every`` and stop after sustained precision.
+
+    The rounds before the first check (the first group end at or after
+    ``minimum_rounds``) are requested as one group: the checks, and so every result, are
+    those of the reference schedule, and a GPU backend runs them in one dispatch instead
+    of draining its photon pool once per group.
+    """
 
     def __init__(self, policy: AMFConvergence, thickness):
         self.policy = policy
@@ -155,9 +161,16 @@ class AMFStopping:
         self.moments.add(batch)
 
     def batches(self, backend, case):
+        first = 1
+
         for start in range(1, case.rounds + 1, self.policy.check_every):
             end = min(start + self.policy.check_every - 1, case.rounds)
-            requests = [BatchControls(i, case.photons_per_column) for i in range(start, end + 1)]
+
+            if end < self.policy.minimum_rounds and end < case.rounds:
+                continue  # no check before the minimum: extend the first group
+
+            requests = [BatchControls(i, case.photons_per_column) for i in range(first, end + 1)]
+            first = end + 1
             batches = backend.run_batches(requests)
 
             if len(batches) != len(requests):

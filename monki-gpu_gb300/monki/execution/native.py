@@ -43,6 +43,32 @@ _SIGNATURES = {
         ctypes.c_int,
         [ctypes.c_void_p, _F64P, ctypes.c_size_t, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t],
     ),
+    "monki_mlp_param_count": (ctypes.c_size_t, []),
+    "monki_mlp_create": (
+        ctypes.c_void_p,
+        [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_size_t],
+    ),
+    "monki_mlp_set_params": (ctypes.c_int, [ctypes.c_void_p, _F32P, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t]),
+    "monki_mlp_get_params": (ctypes.c_int, [ctypes.c_void_p, _F32P, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t]),
+    "monki_mlp_forward": (ctypes.c_int, [ctypes.c_void_p, _F32P, ctypes.c_uint32, _F32P, ctypes.c_char_p, ctypes.c_size_t]),
+    "monki_mlp_gradients": (
+        ctypes.c_int,
+        [ctypes.c_void_p, _F32P, _F32P, _F32P, ctypes.c_uint32, _F32P, _F32P, ctypes.c_char_p, ctypes.c_size_t],
+    ),
+    "monki_mlp_set_data": (
+        ctypes.c_int,
+        [ctypes.c_void_p, _F32P, _F32P, _F32P, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_size_t],
+    ),
+    "monki_mlp_train": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, _F32P, ctypes.c_char_p, ctypes.c_size_t],
+    ),
+    "monki_mlp_close": (None, [ctypes.c_void_p]),
+    "monki_mlp_gemm_probe": (
+        ctypes.c_int,
+        [ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint16), ctypes.POINTER(ctypes.c_uint16), ctypes.c_int, ctypes.c_int,
+         ctypes.c_int, ctypes.c_int, _F32P, ctypes.c_char_p, ctypes.c_size_t],
+    ),
     "monki_cuda_run_static": (
         ctypes.c_int,
         [ctypes.c_uint32, _F64P, ctypes.c_size_t, _U32P, _F64P, ctypes.c_char_p, ctypes.c_size_t],

@@ -16,8 +16,8 @@ GOLDEN = ROOT / "tests" / "golden"
 
 
 def header_symbols():
-    text = (ROOT / "include" / "monki_cuda.h").read_text()
-    return sorted(set(re.findall(r"\b(monki_cuda_[a-z_0-9]+)\s*\(", text)))
+    text = "".join(path.read_text() for path in sorted((ROOT / "include").glob("*.h")))
+    return sorted(set(re.findall(r"\b(monki_(?:cuda|mlp)_[a-z_0-9]+)\s*\(", text)))
 
 
 def test_library_exports_every_declared_symbol(native):
@@ -259,6 +259,37 @@ def test_radiance_stopping_uses_intensity_relative_error():
     stopping = RadianceStopping(RadianceConvergence(0.01, minimum_rounds=32, check_every=32, consecutive_checks=2), 100)
     batches = list(stopping.batches(Synthetic(), case()))
     assert stopping.converged and len(batches) == 64
+
+
+@pytest.mark.parametrize("minimum, every, rounds", [(32, 5, 60), (128, 32, 256), (32, 1, 40), (64, 16, 40)])
+def test_rounds_before_the_first_check_run_as_one_group(minimum, every, rounds):
+    """The first request covers every round up to the first check; the checks (rounds and
+    values) are those of the reference schedule of groups of check_every."""
+    from monki import AMFConvergence
+    from monki.convergence import AMFStopping
+    from monki.execution.tallies import RawTallies
+
+    rng = np.random.default_rng(3)
+    groups = []
+
+    class Synthetic:
+        def run_batches(self, requests):
+            groups.append([r.round_index for r in requests])
+            return [
+                RawTallies(r, np.ones((3, 1, 1, 1)), 1 + 0.3 * rng.random((1, 1, 2, 1)), np.ones((1, 1, 1)))
+                for r in requests
+            ]
+
+    case = type("Case", (), {"rounds": rounds, "photons_per_column": 100})
+    policy = AMFConvergence(relative_error=0.5, minimum_rounds=minimum, check_every=every, consecutive_checks=100)
+    stopping = AMFStopping(policy, np.array([1.0]))
+    assert len(list(stopping.batches(Synthetic(), case()))) == rounds
+    ends = [min(start + every - 1, rounds) for start in range(1, rounds + 1, every)]
+    checked = [e for e in ends if e >= minimum]
+    assert [h["rounds"] for h in stopping.history] == checked
+    first = checked[0] if checked else rounds
+    assert groups[0] == list(range(1, first + 1))
+    assert [g[-1] for g in groups] == [first] + [e for e in ends if e > first]
 
 
 @pytest.mark.parametrize("builder", ["clear_sky", "layered_cloud", "box_cloud"])
