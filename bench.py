@@ -244,7 +244,7 @@ def reference_arm(args):
     return 0
 
 
-def time_to_target(workload, ppc, device, seed, guided):
+def time_to_target(workload, ppc, device, seed, guided, scale=None):
     """Wall seconds of ``simulate`` (the public API, host tables in, every round's FP64
     tallies out, statistics on the host) until SE/|I| < TARGET in every pixel and view."""
 
@@ -255,7 +255,7 @@ def time_to_target(workload, ppc, device, seed, guided):
 
     scene = build_scene(workload, ppc, 256)
     rule = RadianceConvergence(TARGET, minimum_rounds=32, check_every=1, consecutive_checks=1)
-    backend = CUDA(device=device, seed=seed, guided=Guided(*guided) if guided else None)
+    backend = CUDA(device=device, seed=seed, guided=Guided(*guided) if guided else None, roulette_scale=scale)
 
     with tempfile.TemporaryDirectory() as tmp:
         start = time.perf_counter()
@@ -289,6 +289,7 @@ def main():
     parser.add_argument("--workload", default="box", choices=tuple(WORKLOADS))
     parser.add_argument("--no-cpu-baseline", action="store_true")
     parser.add_argument("--no-target", action="store_true", help="skip the time-to-target runs")
+    parser.add_argument("--no-learned", action="store_true", help="skip the learned-importance run")
     parser.add_argument("--photons-per-column", type=int, default=0)
     args = parser.parse_args()
 
@@ -408,6 +409,21 @@ def main():
         guided = time_to_target(args.workload, ppc, local, 23274 + rank, GUIDED)
         target = {"analog": plain, "guided": guided}
 
+        if not args.no_learned:
+            # The learned roulette map: train the importance network on the device from
+            # analog importance tallies of the training family, then apply it.
+            from monki.importance import learned_scale, train_model, training_scenes
+
+            start = time.perf_counter()
+            model, losses, rows = train_model(training_scenes(24), device=local)
+            trained = time.perf_counter() - start
+            with model:
+                scale = learned_scale(model, build_scene(args.workload, ppc, 1))
+            learned = time_to_target(args.workload, ppc, local, 23274 + rank, GUIDED, scale)
+            learned["training"] = {"seconds": trained, "rows": rows, "steps": len(losses),
+                                   "loss_first": float(losses[:20].mean()), "loss_last": float(losses[-50:].mean())}
+            target["guided_learned"] = learned
+
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
@@ -465,6 +481,9 @@ def main():
             "analog": plain,
             "guided": guided,
         }
+        if "guided_learned" in target:
+            line["time_to_target"]["guided_learned_s"] = target["guided_learned"]["seconds"]
+            line["time_to_target"]["guided_learned"] = target["guided_learned"]
         line["e2e"] = {
             "value": plain["scatters_per_s"] * world,
             "unit": UNIT,

@@ -89,6 +89,12 @@ int monki_cuda_set_roulette_scale(void *session, const double *scale, size_t cel
  * history, then the event count; reset != 0 clears the tally. */
 int monki_cuda_importance(void *session, double *out, size_t count, int reset, char *err, size_t errlen);
 
+/* Weights of the importance tally's contributions per output pixel (nx * ny * angles,
+ * Fortran order, non-negative; NULL restores 1): a contribution to pixel p counts
+ * weights[p] times, so the tally measures importance for a weighted objective (for
+ * example the pixels whose relative error limits a precision target). */
+int monki_cuda_set_importance_weights(void *session, const double *weights, size_t pixels, char *err, size_t errlen);
+
 /* Host-only check of the table packer (no GPU needed): validates the stream and returns
  * the first layer of the horizontally uniform top and the optical depth above each
  * layer, at fp32 or fp64 transport precision. The counterpart of the uniform-top prefix

@@ -354,6 +354,7 @@ struct Session {
     double* flush_info = nullptr;
     void* scale = nullptr;            // per-cell roulette scale (T), or null
     double* importance = nullptr;     // 2 * cells, pilot runs only
+    void* pixel_weight = nullptr;     // nx * ny * angles (T), or null
     uint32_t* host_counts = nullptr;  // pinned
     uint64_t iterations = 0;
     // Per-stage event timing of the wavefront (runs with the profiling flag set):
@@ -503,6 +504,7 @@ void run_wavefront(Session& s, const Controls& c) {
     Pool<T> P = [&]() -> Pool<T>& {
         if constexpr (sizeof(T) == 4) return s.pool32; else return s.pool64;
     }();
+    P.pixel_weight = static_cast<const T*>(s.pixel_weight);
     // Small groups scan only as many slots as they have photons.
     P.capacity = uint32_t(std::min<uint64_t>(P.capacity, (uint64_t(c.count) + 255) / 256 * 256));
     check(cudaMemsetAsync(P.counts, 0, 16 * sizeof(uint32_t), s.stream), "memset(counts)");
@@ -568,7 +570,7 @@ void destroy(Session* s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     cudaFree(s->scene); cudaFree(s->banks); cudaFree(s->out); cudaFree(s->mu0mu);
     cudaFree(s->failure); cudaFree(s->counters);
-    cudaFree(s->pool_memory); cudaFree(s->flush_info); cudaFree(s->scale); cudaFree(s->importance);
+    cudaFree(s->pool_memory); cudaFree(s->flush_info); cudaFree(s->scale); cudaFree(s->importance); cudaFree(s->pixel_weight);
     if (s->host_counts) cudaFreeHost(s->host_counts);
     if (s->t0) cudaEventDestroy(s->t0);
     if (s->t1) cudaEventDestroy(s->t1);
@@ -820,6 +822,37 @@ int monki_cuda_set_roulette_scale(void* handle, const double* scale, size_t cell
         } else {
             std::vector<float> f(scale, scale + n);
             check(cudaMemcpy(s->scale, f.data(), n * elem, cudaMemcpyHostToDevice), "upload(scale)");
+        }
+        return 0;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        return 1;
+    }
+}
+
+int monki_cuda_set_importance_weights(void* handle, const double* weights, size_t pixels, char* err, size_t errlen) {
+    Session* s = static_cast<Session*>(handle);
+    try {
+        if (!s || !s->importance) throw std::runtime_error("The session was created without importance=1");
+        const Prepared& p = s->prep;
+        const size_t n = size_t(p.nx) * p.ny * p.angles;
+        check(cudaSetDevice(s->device), "cudaSetDevice");
+        check(cudaStreamSynchronize(s->stream), "sync");
+        if (!weights) {
+            cudaFree(s->pixel_weight);
+            s->pixel_weight = nullptr;
+            return 0;
+        }
+        if (pixels != n) throw std::runtime_error("importance weights need nx * ny * angles values");
+        for (size_t c = 0; c < n; ++c)
+            if (!std::isfinite(weights[c]) || weights[c] < 0.0) throw std::runtime_error("Invalid importance weights");
+        const size_t elem = s->cfg.fp64 ? sizeof(double) : sizeof(float);
+        if (!s->pixel_weight) check(cudaMalloc(&s->pixel_weight, n * elem), "cudaMalloc(weights)");
+        if (s->cfg.fp64) {
+            check(cudaMemcpy(s->pixel_weight, weights, n * elem, cudaMemcpyHostToDevice), "upload(weights)");
+        } else {
+            std::vector<float> f(weights, weights + n);
+            check(cudaMemcpy(s->pixel_weight, f.data(), n * elem, cudaMemcpyHostToDevice), "upload(weights)");
         }
         return 0;
     } catch (const std::exception& e) {

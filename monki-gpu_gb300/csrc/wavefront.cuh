@@ -97,6 +97,7 @@ struct Pool {
     T* ring_inv;          // capacity * kRing
     uint32_t* ring_n;     // events so far
     double* importance;   // 2 * nx * ny * nz
+    const T* pixel_weight;  // nx * ny * angles weights of the contributions, or null (all 1)
 };
 
 __device__ __forceinline__ uint32_t pack_layers(int k, int k1, int wmin, int wmax) {
@@ -634,7 +635,7 @@ wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ b
             const uint32_t pixel = uint32_t(pi_ + s.nx * (pj_ + s.ny * ia));
             const T att = exp(-tau);
             const T w = prob[0] * att;
-            contributed += w;
+            contributed += P.pixel_weight ? w * __ldg(P.pixel_weight + pixel) : w;
             quad_add(pixrec + pixel, TA(w), TA(NMAT > 1 ? prob[1] * att : T(0)), TA(NMAT > 2 ? prob[2] * att : T(0)),
                      TA(PATHS ? w : T(0)));
             ++updates;

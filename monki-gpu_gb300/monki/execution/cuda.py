@@ -55,6 +55,7 @@ class CUDA(Backend):
         pool: int = 1 << 20,
         guided: Guided | None = None,
         importance: bool = False,
+        roulette_scale=None,
         library=None,
     ):
         for name, value, minimum, maximum in (
@@ -108,6 +109,9 @@ class CUDA(Backend):
         self.pool = pool
         self.guided = guided
         self.importance_tally = importance
+        # Per-cell roulette scale (nx, ny, nz) applied at every prepare; set_roulette_scale
+        # changes it for the prepared session only.
+        self.roulette_scale = None if roulette_scale is None else np.asarray(roulette_scale, dtype=np.float64)
         self.library = library or _native.LIBRARY
         self.metadata = None
         self.provenance: dict = {}
@@ -227,6 +231,13 @@ class CUDA(Backend):
             "kernel_launches": 0,
         }
 
+        if self.roulette_scale is not None:
+            try:
+                self.set_roulette_scale(self.roulette_scale)
+            except Exception:
+                self.close()
+                raise
+
     def set_roulette_scale(self, scale) -> None:
         """Scale the guided roulette weight per cell: ``scale`` has shape (nx, ny, nz)
         (the vacuum layer included); None removes the map. Applies to later rounds."""
@@ -254,6 +265,32 @@ class CUDA(Backend):
             raise RuntimeError(error.value.decode() or "setting the roulette scale failed")
 
         self.provenance["roulette_scale"] = None if scale is None else "per-cell map"
+
+    def set_importance_weights(self, weights) -> None:
+        """Weight the importance tally's contributions per output pixel: ``weights`` has
+        shape (nx, ny, angles); None restores equal weights."""
+
+        if self._handle is None:
+            raise RuntimeError("CUDA backend has no prepared scene")
+
+        error = ctypes.create_string_buffer(8192)
+
+        if weights is None:
+            status = self._native.monki_cuda_set_importance_weights(self._handle, None, 0, error, len(error))
+        else:
+            _, nx, ny, _, angles = self._shape
+            values = np.asarray(weights, dtype=np.float64)
+
+            if values.shape != (nx, ny, angles):
+                raise ValueError(f"importance weights must have shape {(nx, ny, angles)}")
+
+            flat = np.ascontiguousarray(values.ravel(order="F"))
+            status = self._native.monki_cuda_set_importance_weights(
+                self._handle, flat.ctypes.data_as(_native.F64P), flat.size, error, len(error)
+            )
+
+        if status:
+            raise RuntimeError(error.value.decode() or "setting the importance weights failed")
 
     def importance(self, reset: bool = True) -> np.ndarray:
         """The importance tally of the rounds run so far: shape (2, nx, ny, nz), the summed

@@ -43,6 +43,10 @@ _SIGNATURES = {
         ctypes.c_int,
         [ctypes.c_void_p, _F64P, ctypes.c_size_t, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t],
     ),
+    "monki_cuda_set_importance_weights": (
+        ctypes.c_int,
+        [ctypes.c_void_p, _F64P, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t],
+    ),
     "monki_mlp_param_count": (ctypes.c_size_t, []),
     "monki_mlp_create": (
         ctypes.c_void_p,

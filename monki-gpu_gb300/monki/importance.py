@@ -189,10 +189,11 @@ def importance_targets(tally, minimum_events: int = 16, floor: float = 1e-8):
     return flat(target), flat(weight)
 
 
-def roulette_scale(log_importance, shape, *, exponent: float = 0.5, low: float = 0.25, high: float = 1.0):
+def roulette_scale(log_importance, shape, *, exponent: float = 0.5, low: float = 0.5, high: float = 2.0):
     """Per-cell roulette scale (nx, ny, nz) from predicted log importance: cells more
-    important than the median get a lower roulette weight (fewer photons killed there),
-    (importance / median) ** -exponent clipped to [low, high]."""
+    important than the median get a lower roulette weight (fewer photons killed there) and
+    less important ones a higher one, (importance / median) ** -exponent clipped to
+    [low, high]."""
 
     values = np.asarray(log_importance, dtype=np.float64).reshape(shape, order="F")
     reference = np.median(values)
@@ -322,13 +323,94 @@ def initial_params(seed: int = 0, features: int = FEATURES) -> np.ndarray:
     return np.concatenate(parts).astype(np.float32)
 
 
-def pilot(scene, device: int = 0, rounds: int = 2, photons_per_column: int | None = None, seed: int = 7):
-    """Importance tally of a short analog run: shape (2, nx, ny, nz)."""
+def pilot(scene, device: int = 0, rounds: int = 2, photons_per_column: int | None = None, seed: int = 7,
+          pixel_weights=None):
+    """Importance tally of a short analog run, shape (2, nx, ny, nz); contributions are
+    weighted per output pixel by ``pixel_weights`` (nx, ny, angles) when given."""
 
     from .execution import CUDA, BatchControls
 
     ppc = photons_per_column or scene.photons_per_column
     with CUDA(device=device, seed=seed, importance=True) as backend:
         backend.prepare(scene)
-        backend.run_batches([BatchControls(i, ppc) for i in range(1, rounds + 1)])
-        return backend.importance()
+        if pixel_weights is not None:
+            backend.set_importance_weights(pixel_weights)
+        batches = backend.run_batches([BatchControls(i, ppc) for i in range(1, rounds + 1)])
+        tally = backend.importance()
+    return tally, batches
+
+
+def objective_weights(batches, photons_per_column: int, power: float = 2.0):
+    """Per-pixel weights (nx, ny, angles) for the precision target SE/|I| < r in every
+    pixel and view: (relative error / the largest relative error) ** power from the
+    rounds of a pilot, so contributions to the pixels that set the time count most."""
+
+    intensity = np.stack([b.stokes[0] for b in batches]) / photons_per_column
+    mean = intensity.mean(axis=0)
+    spread = intensity.std(axis=0, ddof=1) if len(batches) > 1 else np.abs(mean)
+    relative = np.divide(spread, np.abs(mean), out=np.zeros_like(mean), where=np.abs(mean) > 0)
+    top = relative.max()
+    return (relative / top) ** power if top > 0 else np.ones_like(mean)
+
+
+# ------------------------------------------------------------------------------------
+# Training set, training and evaluation.
+# ------------------------------------------------------------------------------------
+def training_rows(scene, *, device: int = 0, rounds: int = 2, photons_per_column: int = 300, seed: int = 7,
+                  limit: int = 40000, rng=None):
+    """(features, target, weight) of the cells of one scene with enough pilot events, at
+    most ``limit`` of them (drawn at random)."""
+
+    tally, _ = pilot(scene, device=device, rounds=rounds, photons_per_column=photons_per_column, seed=seed)
+    target, weight = importance_targets(tally)
+    keep = np.flatnonzero(weight > 0)
+    if keep.size > limit:
+        keep = (rng or np.random.default_rng(seed)).choice(keep, size=limit, replace=False)
+    features = cell_features(scene.tables)
+    return features[keep], target[keep], weight[keep]
+
+
+def r_squared(prediction, target, weight) -> float:
+    """Weighted coefficient of determination of a prediction."""
+
+    w = np.asarray(weight, dtype=np.float64)
+    t = np.asarray(target, dtype=np.float64)
+    mean = np.sum(w * t) / np.sum(w)
+    residual = np.sum(w * (np.asarray(prediction) - t) ** 2)
+    total = np.sum(w * (t - mean) ** 2)
+    return float(1.0 - residual / total) if total > 0 else 0.0
+
+
+def training_scenes(count: int = 24):
+    """The training family: scenes of the batched generator (seeds 10000 on, photons
+    scaled down) and box clouds placed at random (seeds 2000 on, disjoint from the
+    held-out box-cloud seeds 1000-1015)."""
+
+    from . import scenes
+
+    return [scenes.batched_scene(10000 + s, photons_scale=0.01) for s in range(count)] + [
+        scenes.box_cloud_variant(2000 + s, 300, 2) for s in range(count)
+    ]
+
+
+def train_model(training, *, device: int = 0, steps: int = 3000, batch: int = 16384, learning_rate: float = 1e-3,
+                photons_per_column: int = 300, rows_per_scene: int = 20000, seed: int = 1):
+    """Pilot every training scene, then train a network on the device. Returns
+    (model, per-step losses, training rows)."""
+
+    rng = np.random.default_rng(seed)
+    parts = [training_rows(scene, device=device, photons_per_column=photons_per_column, limit=rows_per_scene, rng=rng)
+             for scene in training]
+    x = np.concatenate([p[0] for p in parts])
+    t = np.concatenate([p[1] for p in parts])
+    w = np.concatenate([p[2] for p in parts])
+    model = ImportanceModel(device, rows=batch, seed=seed)
+    losses = model.fit(x, t, w, steps=steps, batch=batch, learning_rate=learning_rate)
+    return model, losses, len(t)
+
+
+def learned_scale(model, scene, **transform):
+    """The roulette scale (nx, ny, nz) a trained network gives a scene."""
+
+    _, nx, ny, nz, _ = scene.shape
+    return roulette_scale(model.predict(cell_features(scene.tables)), (nx, ny, nz), **transform)

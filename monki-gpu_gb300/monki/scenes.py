@@ -480,6 +480,21 @@ def box_cloud(
     )
 
 
+def box_cloud_variant(seed: int, photons_per_column: int = 50000, rounds: int = 256) -> TransportScene:
+    """A box cloud of the held-out family of the learned-importance workload: the box-cloud
+    scene with a 10 x 6-column block placed at random and a log-uniform optical depth in
+    [10, 40], drawn from ``numpy.random.default_rng(seed)``."""
+
+    rng = np.random.default_rng(seed)
+    x0 = int(rng.integers(0, 20))
+    y0 = int(rng.integers(0, 14))
+    depth = float(np.exp(rng.uniform(np.log(10.0), np.log(40.0))))
+    scene = box_cloud(photons_per_column, rounds, box_x=(x0, x0 + 10), box_y=(y0, y0 + 6), optical_depth=depth)
+    scene.name = f"box-cloud-{seed}"
+    scene.description = {"config": 4, "seed": seed, "box": [x0, y0], "optical_depth": depth}
+    return scene
+
+
 def batched_scene(seed: int, *, photons_scale: float = 1.0) -> TransportScene:
     """One scene of the batched workload, drawn from ``numpy.random.default_rng(seed)``.
 

@@ -526,6 +526,7 @@ struct Transport {
     uint32_t max_steps;
     Guide guide;
     std::vector<double> z_norm;  // analog sampler mass per particle species
+    const double* pixel_weight = nullptr;  // importance-tally weight per output pixel, or none
     double a0, b0, c0, phi0_rad, vartheta0_rad;
     std::vector<double> va, vb, vc, view_phi_rad, zsum;  // zsum[k] = SUM(zunit(1:k))
     size_t stokes_count, path_count, weight_count, tally_count;
@@ -658,7 +659,8 @@ struct Transport {
             int inew = int(modulo((long long)i_bak + is * (long long)di + t.nx - 1, t.nx)) + 1;
             int jnew = int(modulo((long long)j_bak + js * (long long)dj + t.ny - 1, t.ny)) + 1;
             double att = std::exp(-tau);
-            contributed += p1 * att;
+            contributed += pixel_weight ? p1 * att * pixel_weight[size_t(inew - 1) + size_t(t.nx) * (size_t(jnew - 1) + size_t(t.ny) * size_t(ia))]
+                                        : p1 * att;
             for (int m = 0; m < nmat; ++m) tally[stokes_index(m, inew, jnew, ia)] += s_prob[size_t(ia) * nmat + m] * att;
             cnt.tally_updates += nmat;
             if (t.paths) {
@@ -908,23 +910,26 @@ int monki_oracle_validate(const double* tables, size_t count, char* err, size_t 
 // tally updates. Returns the failure flag (0 on success); a nonzero flag rejects the run.
 int monki_oracle_run_guided(const double* tables, size_t table_count, const uint32_t controls[8],
                             const double guide[3], const double* scale, int threads, double* out,
-                            uint64_t* counters, double* importance, char* err, size_t errlen);
+                            uint64_t* counters, double* importance, const double* pixel_weight,
+                            char* err, size_t errlen);
 
 int monki_oracle_run(const double* tables, size_t table_count, const uint32_t controls[8], int threads,
                      double* out, uint64_t* counters, char* err, size_t errlen) {
     const double plain[3] = {0.0, 0.0, 0.0};
     return monki_oracle_run_guided(tables, table_count, controls, plain, nullptr, threads, out, counters, nullptr,
-                                   err, errlen);
+                                   nullptr, err, errlen);
 }
 
 // The same round group with guided transport: guide = {epsilon (DDIS probability at
 // particle scatters, [0, 1)), roulette weight (0 = off), DDIS weight cap (0 = none)};
 // scale (nx * ny * nz, or NULL) multiplies the roulette weight per cell. importance
 // (2 * nx * ny * nz, or NULL) receives the importance tally: per cell the summed future
-// contribution per unit weight, then the event count.
+// contribution per unit weight, then the event count; pixel_weight (nx * ny * angles, or
+// NULL) weights each contribution by its output pixel.
 int monki_oracle_run_guided(const double* tables, size_t table_count, const uint32_t controls[8],
                             const double guide[3], const double* scale, int threads, double* out,
-                            uint64_t* counters, double* importance, char* err, size_t errlen) {
+                            uint64_t* counters, double* importance, const double* pixel_weight,
+                            char* err, size_t errlen) {
     try {
         if (!guide || !(guide[0] >= 0.0 && guide[0] < 1.0) || !(guide[1] >= 0.0 && guide[1] <= 1.0)) {
             write_error(err, errlen, "Invalid guide: epsilon must be in [0, 1), roulette in [0, 1]");
@@ -943,6 +948,7 @@ int monki_oracle_run_guided(const double* tables, size_t table_count, const uint
         tr.guide.roulette = guide[1];
         if (guide[2] > 0.0) tr.guide.cap = guide[2];
         tr.guide.scale = scale;
+        tr.pixel_weight = pixel_weight;
         const size_t cells = size_t(t.nx) * t.ny * t.nz;
         if (scale)
             for (size_t c = 0; c < cells; ++c)

@@ -55,6 +55,7 @@ def library() -> ctypes.CDLL:
             _F64P,
             _U64P,
             _F64P,
+            _F64P,
             ctypes.c_char_p,
             ctypes.c_size_t,
         ]
@@ -98,7 +99,8 @@ def tally_count(tables) -> int:
     return nmat * nx * ny * angles + (nx * ny * (nz + 1) * angles if paths else 0)
 
 
-def run(tables, controls, threads: int | None = None, guide=None, scale=None, importance: bool = False):
+def run(tables, controls, threads: int | None = None, guide=None, scale=None, importance: bool = False,
+        pixel_weights=None):
     """Run one round group; returns (tallies[rounds, tally_count], counters dict[, importance]).
 
     ``controls`` are the eight words of the CUDA run call. ``guide`` = (epsilon, roulette
@@ -106,7 +108,8 @@ def run(tables, controls, threads: int | None = None, guide=None, scale=None, im
     scatters and Russian roulette); None is the analog method. ``scale`` (nx, ny, nz),
     Fortran order, multiplies the roulette weight per cell. With ``importance`` the third
     result is the importance tally, shape (2, nx, ny, nz): summed future contribution per
-    unit weight and event count per cell. A failure flag raises.
+    unit weight and event count per cell, each contribution weighted by ``pixel_weights``
+    (nx, ny, angles) of its output pixel when given. A failure flag raises.
     """
 
     t = np.ascontiguousarray(tables, dtype=np.float64)
@@ -123,6 +126,12 @@ def run(tables, controls, threads: int | None = None, guide=None, scale=None, im
     if scale_arr is not None and scale_arr.size != nx * ny * nz:
         raise ValueError("scale must have nx * ny * nz cells")
     imp = np.zeros(2 * nx * ny * nz) if importance else None
+    angles = int(t[5])
+    weights_arr = None
+    if pixel_weights is not None:
+        weights_arr = np.ascontiguousarray(np.asarray(pixel_weights, dtype=np.float64).ravel(order="F"))
+        if weights_arr.size != nx * ny * angles:
+            raise ValueError("pixel_weights must have nx * ny * angles values")
     status = library().monki_oracle_run_guided(
         t.ctypes.data_as(_F64P),
         t.size,
@@ -133,6 +142,7 @@ def run(tables, controls, threads: int | None = None, guide=None, scale=None, im
         out.ctypes.data_as(_F64P),
         counters.ctypes.data_as(_U64P),
         None if imp is None else imp.ctypes.data_as(_F64P),
+        None if weights_arr is None else weights_arr.ctypes.data_as(_F64P),
         err,
         len(err),
     )

@@ -95,6 +95,26 @@ def test_fp64_importance_tally_matches_oracle(oracle, device):
     np.testing.assert_allclose(importance[0].sum(), tally[0].sum(), rtol=1e-5)
 
 
+def test_fp64_weighted_importance_tally_matches_oracle(oracle, device):
+    from monki.execution import CUDA, BatchControls
+
+    scene = _box(8, 2)
+    nmat, nx, ny, nz, angles = scene.shape
+    weights = np.random.default_rng(8).uniform(0.0, 2.0, size=(nx, ny, angles))
+    with CUDA(precision="fp64", seed=23274, importance=True) as backend:
+        backend.prepare(scene)
+        backend.set_importance_weights(weights)
+        backend.run_batches([BatchControls(i, 8) for i in (1, 2)])
+        importance = backend.importance()
+    _, _, tally = oracle.run(scene.tables, _controls(scene, 2, 23274), 8, importance=True, pixel_weights=weights)
+    close = np.isclose(importance[0], tally[0], rtol=1e-6, atol=1e-12)
+    assert close.mean() >= 0.995
+    np.testing.assert_allclose(importance[0].sum(), tally[0].sum(), rtol=1e-5)
+    # Weighting changes the tally (the same histories, other weights).
+    _, _, plain = oracle.run(scene.tables, _controls(scene, 2, 23274), 8, importance=True)
+    assert not np.allclose(plain[0], tally[0])
+
+
 @pytest.mark.parametrize("guide", GUIDES[:2])
 def test_fp32_guided_transport_agrees_with_analog_oracle(oracle, device, guide):
     import monki.scenes as scenes
