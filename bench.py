@@ -267,6 +267,13 @@ def time_to_target(workload, ppc, device, seed, guided, scale=None):
     error = result.values["std_radiance"][..., 0, 0]
     rounds = int(receipt["completed_rounds"])
     nmat, nx, ny, nz, angles = scene.shape
+    checks = len(receipt.get("radiance_convergence", {}).get("checks", []))
+    tallies = nmat * nx * ny * angles + (nx * ny * (nz + 1) * angles if scene.save_path else 0)
+    # Device statistics: per round nmat pixel sums come back; the FP64 statistics (three
+    # Stokes blocks, plus path and weight moments with path diagnostics) at each check
+    # and once at the end.
+    statistics = 3 * nmat * nx * ny * angles + (4 * nx * ny * nz * angles + 3 * nx * ny * angles if scene.save_path else 0)
+    d2h = rounds * nmat * 8 + (checks + 1) * statistics * 8 if backend.device_statistics else rounds * tallies * 8
     return {
         "seconds": wall,
         "status": receipt["status"],
@@ -275,7 +282,8 @@ def time_to_target(workload, ppc, device, seed, guided, scale=None):
         "scatters": int(receipt["scatters"]),
         "scatters_per_s": receipt["scatters"] / wall,
         "h2d_bytes": int(scene.tables.nbytes + 32 * rounds),
-        "d2h_bytes": int(rounds * (nmat * nx * ny * angles + (nx * ny * (nz + 1) * angles if scene.save_path else 0)) * 8),
+        "d2h_bytes": int(d2h),
+        "statistics": "FP64 on the device" if backend.device_statistics else "FP64 on the host",
         "kernel_launches": int(receipt.get("kernel_launches", 0)),
     }
 
@@ -490,8 +498,9 @@ def main():
             "h2d_bytes_per_step": plain["h2d_bytes"] / plain["rounds"],
             "d2h_bytes_per_step": plain["d2h_bytes"] / plain["rounds"],
             "wall_s": plain["seconds"],
-            "note": "the analog time-to-target run: simulate() with CUDA(), table upload, "
-            "every round's FP64 tallies copied to the host, statistics and NetCDF output",
+            "note": "the analog time-to-target run: simulate() with CUDA(), table upload, FP64 round "
+            "statistics on the device, per-round pixel sums and the statistics at each check copied "
+            "to the host, NetCDF output",
         }
 
     if not args.no_cpu_baseline:

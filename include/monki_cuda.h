@@ -73,6 +73,28 @@ const char *monki_cuda_device_name(void *session);
 /* Replaces monki_metal_close (kernels/metal/bridge.m:145-150). Safe on NULL. */
 void monki_cuda_close(void *session);
 
+/* Device round statistics (no reference counterpart: the reference driver sums rounds on
+ * the host, python/monki/simulation.py:86-103). Runs one round group like monki_cuda_run
+ * but keeps its tallies on the device: each round is folded, in round order and in FP64
+ * with correctly rounded operations, into the session's statistics (Stokes total, sum and
+ * sum of squares of tally / photons_per_column; path and weight sums and the Welford
+ * moments of the AMF stopping rule, python/monki/convergence.py:37-99). history receives
+ * rounds x nmat values: each round's sum over pixels of its normalized Stokes tallies.
+ * A failed group leaves the statistics unchanged. */
+int monki_cuda_run_accumulate(void *session, const uint32_t controls[8], double photons_per_column, double *history,
+                              char *err, size_t errlen);
+
+/* Length of the statistics vector: total, sum, squares (nmat nx ny angles each); with path
+ * diagnostics the path sum, mean, M2 and covariance (nx ny nz angles each) and the weight
+ * sum, mean and M2 (nx ny angles each); Fortran order within each block. */
+size_t monki_cuda_statistics_count(void *session);
+
+/* Copy the statistics out (count values) with the number of rounds folded in. */
+int monki_cuda_statistics(void *session, double *out, size_t count, uint64_t *rounds, char *err, size_t errlen);
+
+/* Clear the statistics; returns nonzero for a NULL session. */
+int monki_cuda_reset_statistics(void *session);
+
 /* Guided transport (no reference counterpart: the reference's transport is analog only).
  * Created with config items epsilon=E (detector-directed sampling probability at particle
  * scatters, [0, 1)), roulette=W (Russian-roulette weight, [0, 1], 0 = off) and cap=C (the

@@ -17,6 +17,7 @@
 #include <mutex>
 #include <vector>
 
+#include "statistics.cuh"
 #include "wavefront.cuh"
 
 namespace monki {
@@ -354,6 +355,9 @@ struct Session {
     double* flush_info = nullptr;
     void* scale = nullptr;            // per-cell roulette scale (T), or null
     double* importance = nullptr;     // 2 * cells, pilot runs only
+    double* stats = nullptr;          // FP64 round statistics (statistics_layout), lazily
+    double* history = nullptr;        // round_capacity x nmat spatial sums
+    uint64_t stats_rounds = 0;
     void* pixel_weight = nullptr;     // nx * ny * angles (T), or null
     uint32_t* host_counts = nullptr;  // pinned
     uint64_t iterations = 0;
@@ -571,6 +575,7 @@ void destroy(Session* s) {
     cudaFree(s->scene); cudaFree(s->banks); cudaFree(s->out); cudaFree(s->mu0mu);
     cudaFree(s->failure); cudaFree(s->counters);
     cudaFree(s->pool_memory); cudaFree(s->flush_info); cudaFree(s->scale); cudaFree(s->importance); cudaFree(s->pixel_weight);
+    cudaFree(s->stats); cudaFree(s->history);
     if (s->host_counts) cudaFreeHost(s->host_counts);
     if (s->t0) cudaEventDestroy(s->t0);
     if (s->t1) cudaEventDestroy(s->t1);
@@ -578,6 +583,122 @@ void destroy(Session* s) {
     for (cudaEvent_t e : s->stage_events) cudaEventDestroy(e);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
+}
+
+Controls group_controls(const Session& s, const uint32_t controls[8]) {
+    Controls c{controls[0], controls[1], controls[2], controls[3], controls[4], controls[5], controls[6], controls[7]};
+    if (!c.per_round || !c.rounds || c.rounds > s.round_capacity || !c.max_steps ||
+        uint64_t(c.first) + c.count > uint64_t(c.per_round) * c.rounds)
+        throw std::runtime_error("Invalid CUDA round group");
+    return c;
+}
+
+// Transport and FP64 flush of one round group into s.out, on the session stream.
+void execute(Session& s, const Controls& c) {
+    check(cudaSetDevice(s.device), "cudaSetDevice");
+    check(cudaMemsetAsync(s.failure, 0, sizeof(uint32_t), s.stream), "memset(failure)");
+    check(cudaMemsetAsync(s.counters, 0, 4 * sizeof(unsigned long long), s.stream), "memset(counters)");
+    const int needed = int(std::min<uint64_t>((uint64_t(c.count) + s.cfg.block - 1) / s.cfg.block, uint64_t(s.grid)));
+    check(cudaEventRecord(s.t0, s.stream), "event");
+    if (c.count) {
+        if (s.cfg.wavefront) {
+            if (s.cfg.fp64) run_wavefront<double>(s, c); else run_wavefront<float>(s, c);
+        } else {
+            if (s.cfg.fp64) launch_transport<double>(s, c, std::max(needed, 1));
+            else launch_transport<float>(s, c, std::max(needed, 1));
+            s.totals[5] += 1;
+        }
+        check(cudaGetLastError(), "transport launch");
+    }
+    check(cudaEventRecord(s.t1, s.stream), "event");
+    const uint64_t total = uint64_t(s.layout.count) * c.rounds;
+    const int fgrid = int(std::min<uint64_t>((total + 255) / 256, 4096));
+    const Prepared& p = s.prep;
+    if (s.cfg.wavefront) {
+        if (s.cfg.fp64)
+            wf_flush<double><<<fgrid, 256, 0, s.stream>>>(static_cast<const double*>(s.banks), s.wave, p.nmat,
+                p.nx, p.ny, p.nz, p.angles, s.flush_info, c.rounds, s.layout.count, p.paths, s.out);
+        else
+            wf_flush<float><<<fgrid, 256, 0, s.stream>>>(static_cast<const float*>(s.banks), s.wave, p.nmat,
+                p.nx, p.ny, p.nz, p.angles, s.flush_info, c.rounds, s.layout.count, p.paths, s.out);
+        check(cudaGetLastError(), "flush launch");
+        const size_t elem = s.cfg.fp64 ? sizeof(double) : sizeof(float);
+        check(cudaMemsetAsync(s.banks, 0, size_t(c.rounds) * s.wave.shards * s.wave.count * elem, s.stream),
+              "memset(banks)");
+    } else {
+        if (s.cfg.fp64)
+            flush_kernel<double><<<fgrid, 256, 0, s.stream>>>(static_cast<double*>(s.banks), s.layout, p.nmat,
+                p.nx, p.ny, p.nz, p.angles, s.mu0mu, c.rounds, s.out);
+        else
+            flush_kernel<float><<<fgrid, 256, 0, s.stream>>>(static_cast<float*>(s.banks), s.layout, p.nmat,
+                p.nx, p.ny, p.nz, p.angles, s.mu0mu, c.rounds, s.out);
+        check(cudaGetLastError(), "flush launch");
+    }
+    check(cudaEventRecord(s.t2, s.stream), "event");
+    s.totals[5] += 1;  // the flush
+}
+
+// Wait for the group, collect timing and counters, and turn a failure flag into an error.
+void finish(Session& s, const Controls& c) {
+    uint32_t flag = 0;
+    unsigned long long cnt[4] = {0, 0, 0, 0};
+    check(cudaMemcpyAsync(&flag, s.failure, sizeof(flag), cudaMemcpyDeviceToHost, s.stream), "copy(failure)");
+    check(cudaMemcpyAsync(cnt, s.counters, sizeof(cnt), cudaMemcpyDeviceToHost, s.stream), "copy(counters)");
+    check(cudaStreamSynchronize(s.stream), "transport");
+    float ms = 0.f, run_ms = 0.f;
+    check(cudaEventElapsedTime(&ms, s.t0, s.t1), "elapsed");
+    check(cudaEventElapsedTime(&run_ms, s.t0, s.t2), "elapsed");
+    s.last_kernel_ms = ms;
+    s.last_run_ms = run_ms;
+    if (c.profile) s.gpu_seconds += run_ms * 1e-3;
+    for (int q = 0; q < 4; ++q) s.totals[q] += cnt[q];
+    s.totals[4] += c.count;
+    if (flag) {
+        char msg[128];
+        std::snprintf(msg, sizeof msg, "CUDA transport failed (flag %u); round rejected", flag);
+        throw std::runtime_error(msg);
+    }
+}
+
+StatsLayout statistics_layout(const Session& s) {
+    const Prepared& p = s.prep;
+    const uint32_t pixels = uint32_t(p.nx) * uint32_t(p.ny) * uint32_t(p.angles);
+    StatsLayout L{};
+    L.stokes = uint32_t(p.nmat) * pixels;
+    L.paths = p.paths ? pixels * uint32_t(p.nz) : 0u;
+    L.weights = p.paths ? pixels : 0u;
+    L.nz = uint32_t(p.nz);
+    L.nx = uint32_t(p.nx);
+    L.ny = uint32_t(p.ny);
+    L.count = 3 * size_t(L.stokes) + 4 * size_t(L.paths) + 3 * size_t(L.weights);
+    return L;
+}
+
+// Add the rounds of s.out to the device accumulators (FP64, rounds in order) and write the
+// per-round spatial sums of the normalized Stokes tallies to the host.
+void accumulate(Session& s, uint32_t rounds, double photons_per_column, double* history) {
+    const StatsLayout L = statistics_layout(s);
+    if (!s.stats) {
+        check(cudaMalloc(&s.stats, L.count * sizeof(double)), "cudaMalloc(statistics)");
+        check(cudaMemsetAsync(s.stats, 0, L.count * sizeof(double), s.stream), "memset(statistics)");
+        check(cudaMalloc(&s.history, size_t(s.round_capacity) * s.prep.nmat * sizeof(double)), "cudaMalloc(history)");
+    }
+    const uint32_t elements = L.stokes + L.paths + L.weights;
+    const int grid = int(std::min<uint32_t>((elements + 255) / 256, 8192));
+    // Paths read the weight means of the previous groups, so the weights update second.
+    stats_update<<<grid, 256, 0, s.stream>>>(s.out, uint32_t(s.layout.count), rounds, uint32_t(s.stats_rounds), L,
+                                            photons_per_column, s.stats, 0);
+    if (L.weights)
+        stats_update<<<grid, 256, 0, s.stream>>>(s.out, uint32_t(s.layout.count), rounds, uint32_t(s.stats_rounds), L,
+                                                photons_per_column, s.stats, 1);
+    round_sums<<<dim3(rounds, uint32_t(s.prep.nmat)), 256, 0, s.stream>>>(s.out, uint32_t(s.layout.count),
+                                                                          uint32_t(s.prep.nmat), L.stokes,
+                                                                          photons_per_column, s.history);
+    check(cudaGetLastError(), "statistics launch");
+    check(cudaMemcpyAsync(history, s.history, size_t(rounds) * s.prep.nmat * sizeof(double), cudaMemcpyDeviceToHost,
+                          s.stream), "copy(history)");
+    check(cudaStreamSynchronize(s.stream), "statistics");
+    s.stats_rounds += rounds;
 }
 
 void write_error(char* err, size_t n, const std::string& msg) {
@@ -692,75 +813,70 @@ int monki_cuda_run(void* handle, const uint32_t controls[8], double* out, char* 
     Session* s = static_cast<Session*>(handle);
     if (!s || !controls || !out) { write_error(err, errlen, "Invalid CUDA session or buffers"); return 1; }
     try {
-        Controls c{controls[0], controls[1], controls[2], controls[3], controls[4], controls[5], controls[6], controls[7]};
-        if (!c.per_round || !c.rounds || c.rounds > s->round_capacity || !c.max_steps ||
-            uint64_t(c.first) + c.count > uint64_t(c.per_round) * c.rounds)
-            throw std::runtime_error("Invalid CUDA round group");
-        check(cudaSetDevice(s->device), "cudaSetDevice");
-        check(cudaMemsetAsync(s->failure, 0, sizeof(uint32_t), s->stream), "memset(failure)");
-        check(cudaMemsetAsync(s->counters, 0, 4 * sizeof(unsigned long long), s->stream), "memset(counters)");
-        const int needed = int(std::min<uint64_t>((uint64_t(c.count) + s->cfg.block - 1) / s->cfg.block, uint64_t(s->grid)));
-        check(cudaEventRecord(s->t0, s->stream), "event");
-        if (c.count) {
-            if (s->cfg.wavefront) {
-                if (s->cfg.fp64) run_wavefront<double>(*s, c); else run_wavefront<float>(*s, c);
-            } else {
-                if (s->cfg.fp64) launch_transport<double>(*s, c, std::max(needed, 1));
-                else launch_transport<float>(*s, c, std::max(needed, 1));
-                s->totals[5] += 1;
-            }
-            check(cudaGetLastError(), "transport launch");
-        }
-        check(cudaEventRecord(s->t1, s->stream), "event");
-        const uint64_t total = uint64_t(s->layout.count) * c.rounds;
-        const int fgrid = int(std::min<uint64_t>((total + 255) / 256, 4096));
-        const Prepared& p = s->prep;
-        if (s->cfg.wavefront) {
-            if (s->cfg.fp64)
-                wf_flush<double><<<fgrid, 256, 0, s->stream>>>(static_cast<const double*>(s->banks), s->wave, p.nmat,
-                    p.nx, p.ny, p.nz, p.angles, s->flush_info, c.rounds, s->layout.count, p.paths, s->out);
-            else
-                wf_flush<float><<<fgrid, 256, 0, s->stream>>>(static_cast<const float*>(s->banks), s->wave, p.nmat,
-                    p.nx, p.ny, p.nz, p.angles, s->flush_info, c.rounds, s->layout.count, p.paths, s->out);
-            check(cudaGetLastError(), "flush launch");
-            const size_t elem = s->cfg.fp64 ? sizeof(double) : sizeof(float);
-            check(cudaMemsetAsync(s->banks, 0, size_t(c.rounds) * s->wave.shards * s->wave.count * elem, s->stream),
-                  "memset(banks)");
-        } else {
-            if (s->cfg.fp64)
-                flush_kernel<double><<<fgrid, 256, 0, s->stream>>>(static_cast<double*>(s->banks), s->layout, p.nmat,
-                    p.nx, p.ny, p.nz, p.angles, s->mu0mu, c.rounds, s->out);
-            else
-                flush_kernel<float><<<fgrid, 256, 0, s->stream>>>(static_cast<float*>(s->banks), s->layout, p.nmat,
-                    p.nx, p.ny, p.nz, p.angles, s->mu0mu, c.rounds, s->out);
-            check(cudaGetLastError(), "flush launch");
-        }
-        check(cudaEventRecord(s->t2, s->stream), "event");
-        s->totals[5] += 1;  // the flush
-        uint32_t flag = 0;
-        unsigned long long cnt[4] = {0, 0, 0, 0};
-        check(cudaMemcpyAsync(&flag, s->failure, sizeof(flag), cudaMemcpyDeviceToHost, s->stream), "copy(failure)");
-        check(cudaMemcpyAsync(cnt, s->counters, sizeof(cnt), cudaMemcpyDeviceToHost, s->stream), "copy(counters)");
-        check(cudaMemcpyAsync(out, s->out, total * sizeof(double), cudaMemcpyDeviceToHost, s->stream), "copy(tallies)");
-        check(cudaStreamSynchronize(s->stream), "transport");
-        float ms = 0.f, run_ms = 0.f;
-        check(cudaEventElapsedTime(&ms, s->t0, s->t1), "elapsed");
-        check(cudaEventElapsedTime(&run_ms, s->t0, s->t2), "elapsed");
-        s->last_kernel_ms = ms;
-        s->last_run_ms = run_ms;
-        if (controls[5]) s->gpu_seconds += run_ms * 1e-3;
-        for (int q = 0; q < 4; ++q) s->totals[q] += cnt[q];
-        s->totals[4] += c.count;
-        if (flag) {
-            char msg[128];
-            std::snprintf(msg, sizeof msg, "CUDA transport failed (flag %u); round rejected", flag);
-            throw std::runtime_error(msg);
-        }
+        const Controls c = group_controls(*s, controls);
+        execute(*s, c);
+        check(cudaMemcpyAsync(out, s->out, size_t(s->layout.count) * c.rounds * sizeof(double), cudaMemcpyDeviceToHost,
+                              s->stream), "copy(tallies)");
+        finish(*s, c);
         return 0;
     } catch (const std::exception& e) {
         write_error(err, errlen, e.what());
         return 1;
     }
+}
+
+int monki_cuda_run_accumulate(void* handle, const uint32_t controls[8], double photons_per_column, double* history,
+                              char* err, size_t errlen) {
+    Session* s = static_cast<Session*>(handle);
+    if (!s || !controls || !history) { write_error(err, errlen, "Invalid CUDA session or buffers"); return 1; }
+    try {
+        if (!(photons_per_column > 0.0)) throw std::runtime_error("photons_per_column must be positive");
+        const Controls c = group_controls(*s, controls);
+        execute(*s, c);
+        // A failed group must not touch the accumulators: check before accumulating.
+        finish(*s, c);
+        accumulate(*s, c.rounds, photons_per_column, history);
+        return 0;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        return 1;
+    }
+}
+
+size_t monki_cuda_statistics_count(void* handle) {
+    return handle ? statistics_layout(*static_cast<Session*>(handle)).count : 0;
+}
+
+int monki_cuda_statistics(void* handle, double* out, size_t count, uint64_t* rounds, char* err, size_t errlen) {
+    Session* s = static_cast<Session*>(handle);
+    try {
+        if (!s || !out || !rounds) throw std::runtime_error("Invalid CUDA session or buffers");
+        const StatsLayout L = statistics_layout(*s);
+        if (count != L.count) throw std::runtime_error("statistics buffer has the wrong size");
+        check(cudaSetDevice(s->device), "cudaSetDevice");
+        if (!s->stats) {
+            std::fill(out, out + count, 0.0);
+        } else {
+            check(cudaMemcpyAsync(out, s->stats, count * sizeof(double), cudaMemcpyDeviceToHost, s->stream), "copy(statistics)");
+            check(cudaStreamSynchronize(s->stream), "statistics");
+        }
+        *rounds = s->stats_rounds;
+        return 0;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        return 1;
+    }
+}
+
+int monki_cuda_reset_statistics(void* handle) {
+    Session* s = static_cast<Session*>(handle);
+    if (!s) return 1;
+    s->stats_rounds = 0;
+    if (s->stats) {
+        if (cudaSetDevice(s->device) != cudaSuccess) return 1;
+        if (cudaMemsetAsync(s->stats, 0, statistics_layout(*s).count * sizeof(double), s->stream) != cudaSuccess) return 1;
+    }
+    return 0;
 }
 
 double monki_cuda_gpu_seconds(void* handle) {

@@ -160,17 +160,51 @@ class AMFStopping:
     def _add(self, batch: RawTallies) -> None:
         self.moments.add(batch)
 
-    def batches(self, backend, case):
+    def groups(self, rounds: int):
+        """(first, last, checked) round groups of the schedule."""
+
         first = 1
 
-        for start in range(1, case.rounds + 1, self.policy.check_every):
-            end = min(start + self.policy.check_every - 1, case.rounds)
+        for start in range(1, rounds + 1, self.policy.check_every):
+            end = min(start + self.policy.check_every - 1, rounds)
 
-            if end < self.policy.minimum_rounds and end < case.rounds:
+            if end < self.policy.minimum_rounds and end < rounds:
                 continue  # no check before the minimum: extend the first group
 
-            requests = [BatchControls(i, case.photons_per_column) for i in range(first, end + 1)]
+            yield first, end, end >= self.policy.minimum_rounds
             first = end + 1
+
+    def check(self, end: int) -> None:
+        """Judge the moments after round ``end`` and update the streak."""
+
+        relative = self._relative()
+        maximum = float(np.max(relative))
+        passed = bool(np.all(np.isfinite(relative)) and maximum < self.policy.relative_error)
+        self.streak = self.streak + 1 if passed else 0
+        self.converged = self.streak >= self.policy.consecutive_checks
+        self.history.append(
+            {
+                "rounds": end,
+                "max_relative_se": maximum if np.isfinite(maximum) else None,
+                "below_target": passed,
+                "streak": self.streak,
+            }
+        )
+
+    def load(self, statistics: dict) -> None:
+        """Take the moments from device round statistics (``CUDA.statistics``)."""
+
+        m = self.moments
+        m.count = statistics["rounds"]
+        m.path_mean = statistics["path_mean"][:, :, :-1, :]
+        m.path_m2 = statistics["path_m2"][:, :, :-1, :]
+        m.covariance = statistics["covariance"][:, :, :-1, :]
+        m.weight_mean = statistics["weight_mean"][:, :, None, :]
+        m.weight_m2 = statistics["weight_m2"][:, :, None, :]
+
+    def batches(self, backend, case):
+        for first, end, checked in self.groups(case.rounds):
+            requests = [BatchControls(i, case.photons_per_column) for i in range(first, end + 1)]
             batches = backend.run_batches(requests)
 
             if len(batches) != len(requests):
@@ -183,25 +217,11 @@ class AMFStopping:
                 self._add(batch)
                 yield batch
 
-            if end < self.policy.minimum_rounds:
-                continue
+            if checked:
+                self.check(end)
 
-            relative = self._relative()
-            maximum = float(np.max(relative))
-            passed = bool(np.all(np.isfinite(relative)) and maximum < self.policy.relative_error)
-            self.streak = self.streak + 1 if passed else 0
-            self.converged = self.streak >= self.policy.consecutive_checks
-            self.history.append(
-                {
-                    "rounds": end,
-                    "max_relative_se": maximum if np.isfinite(maximum) else None,
-                    "below_target": passed,
-                    "streak": self.streak,
-                }
-            )
-
-            if self.converged:
-                return
+                if self.converged:
+                    return
 
 
 class RadianceStopping(AMFStopping):
@@ -210,6 +230,11 @@ class RadianceStopping(AMFStopping):
     def __init__(self, policy: RadianceConvergence, photons_per_column: int):
         super().__init__(policy, None)
         self.moments = RadianceMoments(photons_per_column)
+
+    def load(self, statistics: dict) -> None:
+        self.moments.count = statistics["rounds"]
+        self.moments.total = statistics["sum"]
+        self.moments.squares = statistics["squares"]
 
     def _relative(self):
         mean, error = self.moments.estimate()

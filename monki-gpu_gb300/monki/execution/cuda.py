@@ -56,6 +56,7 @@ class CUDA(Backend):
         guided: Guided | None = None,
         importance: bool = False,
         roulette_scale=None,
+        device_statistics: bool = True,
         library=None,
     ):
         for name, value, minimum, maximum in (
@@ -109,6 +110,8 @@ class CUDA(Backend):
         self.pool = pool
         self.guided = guided
         self.importance_tally = importance
+        # simulate() folds rounds into FP64 statistics on the device when available.
+        self.device_statistics = bool(device_statistics)
         # Per-cell roulette scale (nx, ny, nz) applied at every prepare; set_roulette_scale
         # changes it for the prepared session only.
         self.roulette_scale = None if roulette_scale is None else np.asarray(roulette_scale, dtype=np.float64)
@@ -339,6 +342,114 @@ class CUDA(Backend):
             first = last
 
         return results
+
+    # ------------------------------------------------------------------ device statistics
+    def device_statistics_available(self, photons_per_column: int) -> bool:
+        """True when whole rounds of this size fit one dispatch, so the device can fold
+        each round into its FP64 statistics (``accumulate``)."""
+
+        _, nx, ny, _, _ = self._shape
+        return self.device_statistics and photons_per_column * nx * ny <= self.photons_per_dispatch
+
+    def accumulate(self, controls: list) -> np.ndarray:
+        """Run rounds and fold their tallies into the device's FP64 round statistics
+        without copying them to the host. Returns, per round, the spatial sum of the
+        round's normalized Stokes tallies (rounds x nmat)."""
+
+        self._validate_requests(controls)
+        nmat, nx, ny, _, _ = self._shape
+        history = []
+        first = 0
+
+        while first < len(controls):
+            ppc = controls[first].photons_per_column
+            per_round = ppc * nx * ny
+
+            if per_round > self.photons_per_dispatch:
+                raise ValueError("device statistics need whole rounds in one dispatch")
+
+            capacity = max(1, min(self._round_capacity, self.photons_per_dispatch // per_round))
+            last = first + 1
+
+            while last < min(len(controls), first + capacity) and controls[last].photons_per_column == ppc:
+                last += 1
+
+            group = controls[first:last]
+            rows = np.zeros((len(group), nmat), dtype=np.float64)
+            error = ctypes.create_string_buffer(8192)
+            command = (ctypes.c_uint32 * 8)(
+                per_round * len(group), 0, group[0].round_index, self.seed, self.max_steps, int(self.profile),
+                per_round, len(group),
+            )
+
+            try:
+                status = self._native.monki_cuda_run_accumulate(
+                    self._handle, command, float(ppc), rows.ctypes.data_as(_native.F64P), error, len(error)
+                )
+
+                if status or not np.all(np.isfinite(rows)):
+                    raise RuntimeError(error.value.decode() or "Nonfinite CUDA tallies")
+            except BaseException:
+                self.close()
+                raise
+
+            self.provenance["gpu_dispatches"] += 1
+            history.append(rows)
+            self._round = group[-1].round_index
+            first = last
+
+        counters = (ctypes.c_uint64 * 6)()
+        self._native.monki_cuda_counters(self._handle, counters)
+        self.provenance["scatters"] = int(counters[0])
+        self.provenance["photons"] = int(counters[4])
+        self.provenance["kernel_launches"] = int(counters[5])
+
+        if self.profile:
+            self.provenance["gpu_seconds"] = self._native.monki_cuda_gpu_seconds(self._handle)
+
+        return np.concatenate(history) if history else np.zeros((0, nmat))
+
+    def statistics(self) -> dict:
+        """The device's FP64 round statistics: ``rounds`` and, in RawTallies shapes, the
+        Stokes ``total``, ``sum`` and ``squares`` of the normalized tallies, and with path
+        diagnostics the path and weight sums and their Welford moments (``path_mean``,
+        ``path_m2``, ``covariance``, ``weight_mean``, ``weight_m2``)."""
+
+        if self._handle is None:
+            raise RuntimeError("CUDA backend has no prepared scene")
+
+        nmat, nx, ny, nz, angles = self._shape
+        count = int(self._native.monki_cuda_statistics_count(self._handle))
+        values = np.zeros(count)
+        rounds = ctypes.c_uint64(0)
+        error = ctypes.create_string_buffer(8192)
+
+        if self._native.monki_cuda_statistics(self._handle, values.ctypes.data_as(_native.F64P), count,
+                                              ctypes.byref(rounds), error, len(error)):
+            raise RuntimeError(error.value.decode() or "reading the statistics failed")
+
+        s, p, w = nmat * nx * ny * angles, (nx * ny * nz * angles if self._paths else 0), (nx * ny * angles if self._paths else 0)
+        at = 0
+
+        def take(n, shape):
+            nonlocal at
+            out = values[at : at + n].reshape(shape, order="F").copy()
+            at += n
+            return out
+
+        out = {"rounds": int(rounds.value)}
+        for name in ("total", "sum", "squares"):
+            out[name] = take(s, (nmat, nx, ny, angles))
+        if self._paths:
+            for name in ("paths", "path_mean", "path_m2", "covariance"):
+                out[name] = take(p, (nx, ny, nz, angles))
+            for name in ("weights", "weight_mean", "weight_m2"):
+                out[name] = take(w, (nx, ny, angles))
+        return out
+
+    def reset_statistics(self) -> None:
+        if self._handle is not None:
+            self._native.monki_cuda_reset_statistics(self._handle)
 
     def close(self) -> None:
         """Release device memory; returned arrays stay valid."""

@@ -47,6 +47,16 @@ _SIGNATURES = {
         ctypes.c_int,
         [ctypes.c_void_p, _F64P, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t],
     ),
+    "monki_cuda_run_accumulate": (
+        ctypes.c_int,
+        [ctypes.c_void_p, _U32P, ctypes.c_double, _F64P, ctypes.c_char_p, ctypes.c_size_t],
+    ),
+    "monki_cuda_statistics_count": (ctypes.c_size_t, [ctypes.c_void_p]),
+    "monki_cuda_statistics": (
+        ctypes.c_int,
+        [ctypes.c_void_p, _F64P, ctypes.c_size_t, _U64P, ctypes.c_char_p, ctypes.c_size_t],
+    ),
+    "monki_cuda_reset_statistics": (ctypes.c_int, [ctypes.c_void_p]),
     "monki_mlp_param_count": (ctypes.c_size_t, []),
     "monki_mlp_create": (
         ctypes.c_void_p,

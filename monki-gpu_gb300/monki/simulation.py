@@ -26,6 +26,83 @@ def file_hash(path: Path) -> str:
     return hashlib.sha256(Path(path).read_bytes()).hexdigest()
 
 
+def _host_rounds(case, backend, stopping):
+    """Round sums from each round's host tallies (the reference driver's loop)."""
+
+    if stopping is not None:
+        batches = stopping.batches(backend, case)
+    else:
+        requests = [BatchControls(i, case.photons_per_column) for i in range(1, case.rounds + 1)]
+        batches = backend.run_batches(requests)
+
+        if len(batches) != case.rounds:
+            raise ValueError("Backend returned the wrong number of statistical rounds")
+
+    total = rounds_sum = rounds_squared = paths = weights = None
+    history = []
+
+    for index, batch in enumerate(batches, start=1):
+        if not isinstance(batch, RawTallies):
+            raise TypeError("Backend must return RawTallies")
+
+        if batch.controls != BatchControls(index, case.photons_per_column):
+            raise ValueError("Backend returned tallies for a different round")
+
+        if total is None:
+            total = np.zeros_like(batch.stokes)
+            rounds_sum = np.zeros_like(batch.stokes)
+            rounds_squared = np.zeros_like(batch.stokes)
+
+            if batch.weighted_paths is not None:
+                paths = np.zeros_like(batch.weighted_paths)
+                weights = np.zeros_like(batch.weights)
+
+        total += batch.stokes
+        normalized = batch.stokes / case.photons_per_column
+        rounds_sum += normalized
+        rounds_squared += normalized**2
+        _, nx, ny, angles = total.shape
+        # Successive spatial sums then divisions, all Stokes components kept.
+        history.append(rounds_sum.sum(axis=1).sum(axis=1).sum(axis=1) / nx / ny / angles / index)
+
+        if paths is not None:
+            if batch.weighted_paths is None or batch.weights is None:
+                raise ValueError("Backend dropped path diagnostics during a session")
+
+            paths += batch.weighted_paths
+            weights += batch.weights
+
+    return total, rounds_sum, rounds_squared, history, paths, weights
+
+
+def _device_rounds(case, backend, stopping):
+    """Round sums folded on the device in FP64 (``backend.accumulate``): the same rounds,
+    schedule and checks; only the per-round tallies stay on the GPU. The history is the
+    running pixel sum of the device's per-round sums (equal to the host's to rounding)."""
+
+    ppc = case.photons_per_column
+    groups = stopping.groups(case.rounds) if stopping is not None else [(1, case.rounds, False)]
+    rows = []
+
+    for first, end, checked in groups:
+        rows.append(backend.accumulate([BatchControls(i, ppc) for i in range(first, end + 1)]))
+
+        if checked:
+            stopping.load(backend.statistics())
+            stopping.check(end)
+
+            if stopping.converged:
+                break
+
+    statistics = backend.statistics()
+    total = statistics["total"]
+    _, nx, ny, angles = total.shape
+    running = np.cumsum(np.concatenate(rows), axis=0)
+    history = [running[r] / nx / ny / angles / (r + 1) for r in range(statistics["rounds"])]
+    return (total, statistics["sum"], statistics["squares"], history, statistics.get("paths"),
+            statistics.get("weights"))
+
+
 def simulate(case, backend: Backend, output, *, convergence: AMFConvergence | None = None) -> SimulationResult:
     """Run equally sized rounds, save the product and its receipt, return the result.
 
@@ -53,54 +130,21 @@ def simulate(case, backend: Backend, output, *, convergence: AMFConvergence | No
 
         if isinstance(convergence, RadianceConvergence):
             stopping = RadianceStopping(convergence, case.photons_per_column)
-            batches = stopping.batches(backend, case)
         elif convergence is not None:
             if "AMF_layer" not in metadata.values:
                 raise ValueError("AMF stopping requires layer path diagnostics")
 
             stopping = AMFStopping(convergence, np.diff(metadata.values["alt"]) / 1000)
-            batches = stopping.batches(backend, case)
+
+        device = getattr(backend, "device_statistics_available", None)
+
+        if device is not None and device(case.photons_per_column):
+            total, rounds_sum, rounds_squared, history, paths, weights = _device_rounds(case, backend, stopping)
         else:
-            requests = [BatchControls(i, case.photons_per_column) for i in range(1, case.rounds + 1)]
-            batches = backend.run_batches(requests)
+            total, rounds_sum, rounds_squared, history, paths, weights = _host_rounds(case, backend, stopping)
 
-            if len(batches) != case.rounds:
-                raise ValueError("Backend returned the wrong number of statistical rounds")
-
-        total = rounds_sum = rounds_squared = paths = weights = None
-        history = []
-
-        for index, batch in enumerate(batches, start=1):
-            if not isinstance(batch, RawTallies):
-                raise TypeError("Backend must return RawTallies")
-
-            if batch.controls != BatchControls(index, case.photons_per_column):
-                raise ValueError("Backend returned tallies for a different round")
-
-            if total is None:
-                total = np.zeros_like(batch.stokes)
-                rounds_sum = np.zeros_like(batch.stokes)
-                rounds_squared = np.zeros_like(batch.stokes)
-
-                if batch.weighted_paths is not None:
-                    paths = np.zeros_like(batch.weighted_paths)
-                    weights = np.zeros_like(batch.weights)
-
-            total += batch.stokes
-            normalized = batch.stokes / case.photons_per_column
-            rounds_sum += normalized
-            rounds_squared += normalized**2
-            _, nx, ny, angles = total.shape
-            # Successive spatial sums then divisions, all Stokes components kept.
-            history.append(rounds_sum.sum(axis=1).sum(axis=1).sum(axis=1) / nx / ny / angles / index)
-
-            if paths is not None:
-                if batch.weighted_paths is None or batch.weights is None:
-                    raise ValueError("Backend dropped path diagnostics during a session")
-
-                paths += batch.weighted_paths
-                weights += batch.weights
-
+        completed = len(history)
+        _, nx, ny, angles = total.shape
         completed = len(history)
         radiance = total / completed / case.photons_per_column
         uncertainty = np.full_like(radiance, 999.0)
