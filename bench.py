@@ -503,6 +503,13 @@ def main():
             "to the host, NetCDF output",
         }
 
+    if not args.no_target:
+        # FP32 bias of the product transport against the FP64 build, per Stokes component.
+        from monki.precision import fp32_bias
+
+        line["fp32_bias"] = fp32_bias(build_scene(args.workload, 2000, 8), rounds=8, photons_per_column=2000,
+                                      device=local)
+
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(build_scene(args.workload, ppc, 1))
 

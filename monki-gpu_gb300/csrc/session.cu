@@ -490,13 +490,18 @@ void wave_iteration(Session& s, const SceneView<T>& v, Pool<T>& P, const Control
     T* banks = static_cast<T*>(s.banks);
     check(cudaMemsetAsync(P.counts, 0, 4 * sizeof(uint32_t), s.stream), "memset(queues)");
     if (ev) cudaEventRecord(ev[0], s.stream);
-    wf_transit<T, PATHS><<<grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, s.cfg.walk, s.failure, s.counters);
+    // One thread per pool slot (transit) or per possible event (scatter): a thread that
+    // looped over several slots drifted away from its warp's other lanes (each slot's walk
+    // has its own length). The peel keeps the persistent grid, which measured faster.
+    const int slots_grid = int((P.capacity + uint32_t(s.cfg.block) - 1) / uint32_t(s.cfg.block));
+    wf_transit<T, PATHS><<<slots_grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, s.cfg.walk, s.failure,
+                                                                              s.counters);
     if (ev) cudaEventRecord(ev[1], s.stream);
     wf_peel<T, T, NMAT, PATHS><<<grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, banks, s.wave, s.failure, s.counters);
     if (ev) cudaEventRecord(ev[2], s.stream);
     Guide<T> g{T(s.cfg.epsilon), T(s.cfg.roulette), s.cfg.cap > 0.0 ? T(s.cfg.cap) : T(INFINITY),
                static_cast<const T*>(s.scale)};
-    wf_scatter<T, NMAT><<<grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, g, s.failure);
+    wf_scatter<T, NMAT><<<slots_grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, g, s.failure);
     if (ev) cudaEventRecord(ev[3], s.stream);
 }
 

@@ -236,9 +236,11 @@ __device__ __forceinline__ void slide(int& i, T& x, int sgn, T h, T unit, int n)
     T whole = floor(rest / unit);
     rest -= whole * unit;
     if (rest < T(0)) rest = T(0);
-    long long cross = 1 + (long long)whole;
+    // 32-bit counts: no float-to-int64 conversion or 64-bit modulo (slow conversion and
+    // FP64-pipe work on this GPU); 4e9 faces exceed any travel a float position resolves.
+    uint32_t cross = 1u + uint32_t(fmin(whole, T(4.0e9)));
     if (rest >= unit) { rest -= unit; ++cross; }
-    int step = int(cross % n);
+    int step = int(cross % uint32_t(n));
     i += sgn * step;
     i %= n;
     if (i < 0) i += n;
