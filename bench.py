@@ -57,6 +57,9 @@ GUIDED = (0.0, 1.0, 0.0)  # epsilon, roulette weight, cap: Russian roulette at u
 STATE_BYTES = 64  # one event's photon state records read by the peel kernel
 CELL_BYTES = 16  # one cell record (beta + cumulative species fractions)
 TALLY_BYTES = 32  # one 128-bit tally atomic: 16 B read + 16 B written in L2
+SLOT_SCAN_BYTES = 16  # transit reads every slot's bookkeeping record
+TRANSIT_EVENT_BYTES = 109  # per event: state read (52 B) and written (52 B), queue entry and kind (5 B)
+SCATTER_EVENT_BYTES = 116  # per event: queue entry (4 B), state read (64 B) and written (48 B)
 
 
 def peaks():
@@ -69,8 +72,9 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def recorded_traffic(workload):
-    """Per-launch DRAM bytes of the peel kernel from the committed ncu summary."""
+def recorded_traffic(workload, kernel):
+    """Per-launch DRAM bytes (read + write) of one wavefront kernel from the committed ncu
+    summary of the workload, or None."""
 
     name = {"box": "box_cloud", "layered": "layered_cloud"}[workload]
     path = ROOT / "profiles" / f"transport_kernel_{name}.md"
@@ -78,7 +82,10 @@ def recorded_traffic(workload):
     if not path.is_file():
         return None
 
-    match = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", path.read_text())
+    text = path.read_text()
+    match = re.search(rf"traffic_{kernel}_bytes_per_launch:\s*([0-9.eE+]+)", text)
+    if match is None and kernel == "peel":
+        match = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", text)
     return float(match.group(1)) if match else None
 
 
@@ -398,15 +405,37 @@ def main():
 
     native.monki_cuda_close(handle)
     value = total_scatters / device_seconds
-    # Roofline of the dominant kernel, the peel stage: per launch, the event state it reads,
-    # the cells its detector rays visit and its 128-bit tally atomics, over its event time.
-    peel_launches = max(int(stage_launches[1]), 1)
-    peel_seconds = stage_ms[1] / 1e3 / peel_launches
-    peel_bytes = (STATE_BYTES * scatters + CELL_BYTES * visits_det + TALLY_BYTES * updates) / peel_launches
+    # Roofline per wavefront kernel: algorithmic bytes per launch over the event-timed
+    # launch duration; the line reports the kernel with the largest share of device time.
+    #   transit  every slot's bookkeeping record, each event's state read and written and
+    #            its queue entry, 16 B per free-path cell visit
+    #   peel     each event's state, 16 B per detector-ray cell visit, 32 B per tally atomic
+    #   scatter  each event's queue entry and state read and written
     peak, peak_kind = peaks()
-    achieved = peel_bytes / peel_seconds / 1e9
     stage_total = max(sum(stage_ms), 1e-9)
-    stage_share = {name: stage_ms[q] / stage_total for q, name in enumerate(("transit", "peel", "scatter"))}
+    names = ("transit", "peel", "scatter")
+    stage_share = {name: stage_ms[q] / stage_total for q, name in enumerate(names)}
+    pool = 1 << 20
+    algorithmic = {
+        "transit": SLOT_SCAN_BYTES * pool * int(stage_launches[0]) + TRANSIT_EVENT_BYTES * scatters + CELL_BYTES * visits_fp,
+        "peel": STATE_BYTES * scatters + CELL_BYTES * visits_det + TALLY_BYTES * updates,
+        "scatter": SCATTER_EVENT_BYTES * scatters,
+    }
+    kernels = {}
+    for q, name in enumerate(names):
+        launches_q = max(int(stage_launches[q]), 1)
+        seconds = stage_ms[q] / 1e3 / launches_q
+        per_launch = algorithmic[name] / launches_q
+        kernels[name] = {
+            "algorithmic_bytes_per_launch": per_launch,
+            "launch_ms": seconds * 1e3,
+            "launches": launches_q,
+            "achieved_gbs": per_launch / seconds / 1e9,
+            "frac": per_launch / seconds / 1e9 / peak,
+            "traffic": recorded_traffic(args.workload, name),
+            "share": stage_share[name],
+        }
+    dominant = max(names, key=lambda name: stage_share[name])
 
     # Time to the precision target through the public API, analog then guided, on every
     # rank (independent seeds); the analog run is also the end-to-end throughput.
@@ -425,11 +454,20 @@ def main():
             start = time.perf_counter()
             model, losses, rows = train_model(training_scenes(24), device=local)
             trained = time.perf_counter() - start
+            fit_seconds = model.fit_seconds
             with model:
                 scale = learned_scale(model, build_scene(args.workload, ppc, 1))
             learned = time_to_target(args.workload, ppc, local, 23274 + rank, GUIDED, scale)
-            learned["training"] = {"seconds": trained, "rows": rows, "steps": len(losses),
-                                   "loss_first": float(losses[:20].mean()), "loss_last": float(losses[-50:].mean())}
+            # Dense-contraction roofline of the network's training: FLOPs of the tcgen05
+            # GEMMs per step (forward 3 layers, backward weight and input gradients).
+            flops = len(losses) * 16384 * 2 * (3 * (64 * 256 + 2 * 256 * 256) - 64 * 256)
+            tensor_peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("bf16_tflops") \
+                if (ROOT / "MEASURED_PEAKS.json").is_file() else 1900.0
+            learned["training"] = {"seconds_with_pilots": trained, "fit_seconds": fit_seconds, "rows": rows,
+                                   "steps": len(losses), "batch": 16384,
+                                   "loss_first": float(losses[:20].mean()), "loss_last": float(losses[-50:].mean()),
+                                   "gemm_tflops": flops / fit_seconds / 1e12,
+                                   "frac_of_bf16_peak": flops / fit_seconds / 1e12 / tensor_peak}
             target["guided_learned"] = learned
 
     if rank != 0:
@@ -462,17 +500,18 @@ def main():
         },
         "roofline": {
             "bound": "hbm",
-            "kernel": "wf_peel (event peel-off: phase matrix, detector ray, tallies)",
-            "achieved": achieved,
+            "kernel": f"wf_{dominant}",
+            "achieved": kernels[dominant]["achieved_gbs"],
             "peak": peak,
             "unit": "GB/s",
-            "frac": achieved / peak,
-            "traffic": recorded_traffic(args.workload),
+            "frac": kernels[dominant]["frac"],
+            "traffic": kernels[dominant]["traffic"],
             "peak_source": peak_kind,
-            "algorithmic_bytes_per_launch": peel_bytes,
-            "launch_ms": peel_seconds * 1e3,
-            "launches": peel_launches,
+            "algorithmic_bytes_per_launch": kernels[dominant]["algorithmic_bytes_per_launch"],
+            "launch_ms": kernels[dominant]["launch_ms"],
+            "launches": kernels[dominant]["launches"],
             "stage_share": stage_share,
+            "kernels": kernels,
         },
         "gpu_launches": launches,
         "clocks": clocks.summary(),

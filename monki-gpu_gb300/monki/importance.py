@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import ctypes
 import math
+import time
 from dataclasses import dataclass
 
 import numpy as np
@@ -289,8 +290,10 @@ class ImportanceModel:
         self._check(self._native.monki_mlp_set_data(self._handle, x.ctypes.data_as(_native.F32P), t.ctypes.data_as(_native.F32P),
                                                     w.ctypes.data_as(_native.F32P), x.shape[0], error, len(error)), error)
         losses = np.zeros(steps, dtype=np.float32)
+        start = time.perf_counter()
         self._check(self._native.monki_mlp_train(self._handle, steps, batch, learning_rate,
                                                  losses.ctypes.data_as(_native.F32P), error, len(error)), error)
+        self.fit_seconds = time.perf_counter() - start
         return losses
 
     def close(self) -> None:
