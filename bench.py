@@ -160,6 +160,29 @@ def distributed():
     return world, rank, local
 
 
+ROUNDS_PER_RANK = 100000  # rank r runs statistical rounds from r * 100000 + 1: disjoint streams
+
+
+def first_round(rank: int, round_in_rank: int) -> int:
+    """The global round index of a rank's round: ranks never share a Philox stream."""
+
+    return rank * ROUNDS_PER_RANK + round_in_rank
+
+
+def combine_ranks(seconds: float, scatters: float, device):
+    """Whole-job timing and work over the ranks of the process group: the slowest rank's
+    device seconds and the summed scatters (the only exchange; no data-path collective)."""
+
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([seconds], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    s = torch.tensor([float(scatters)], device=device, dtype=torch.float64)
+    dist.all_reduce(s)
+    return float(t.item()), float(s.item())
+
+
 def cpu_baseline(scene, target_seconds: float = 10.0):
     """Scatters/s of the FP64 CPU restatement on a bounded sample of one round."""
 
@@ -355,12 +378,12 @@ def main():
     counters_before = (ctypes.c_uint64 * 6)()
     counters_after = (ctypes.c_uint64 * 6)()
 
-    def group(first_round, rounds):
+    def group(start, rounds):
         """One round group in one dispatch, as CUDA.run_batches schedules it, with the
         per-stage event timing on. Ranks run disjoint rounds (offset 100000 per rank)."""
 
         controls = (ctypes.c_uint32 * 8)(
-            per_round * rounds, 0, rank * 100000 + first_round, 0, 100000, 1, per_round, rounds
+            per_round * rounds, 0, first_round(rank, start), 0, 100000, 1, per_round, rounds
         )
 
         if native.monki_cuda_run(handle, controls, out.ctypes.data_as(binding.F64P), err, len(err)):
@@ -392,14 +415,7 @@ def main():
     device_seconds = run_ms / 1e3
 
     if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([device_seconds], device=f"cuda:{local}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        device_seconds = float(t.item())
-        s = torch.tensor([float(scatters)], device=f"cuda:{local}", dtype=torch.float64)
-        dist.all_reduce(s)
-        total_scatters = float(s.item())
+        device_seconds, total_scatters = combine_ranks(device_seconds, scatters, f"cuda:{local}")
     else:
         total_scatters = float(scatters)
 
