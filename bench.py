@@ -318,6 +318,32 @@ def time_to_target(workload, ppc, device, seed, guided, scale=None):
     }
 
 
+def batched_scenes(device, scale):
+    """The batched workload: 64 seeded scenes of uneven size (grids 8-128 columns a side,
+    20-60 layers, log-uniform photon budgets scaled by ``scale``, lognormal cloud fields),
+    one round each, with launch shapes from the autotuner (tuned once per size class),
+    concurrent sessions on one GPU."""
+
+    import monki.scenes as scenes
+    from monki.batched import run_batched
+    from monki.tuning import autotune
+
+    batch = [scenes.batched_scene(seed, photons_scale=scale) for seed in range(64)]
+
+    def size_class(scene):
+        _, nx, ny, _, _ = scene.shape
+        photons = scene.photons_per_column * nx * ny
+        return 0 if photons < 1 << 20 else (1 if photons < 8 << 20 else 2)
+
+    tuned = {}
+    for scene in batch:
+        tuned.setdefault(size_class(scene), autotune(scene, device=device))
+    _, summary = run_batched(batch, device=device, concurrency=4, tune=lambda s: tuned[size_class(s)].options())
+    summary["photons_scale"] = scale
+    summary["tuned"] = {str(k): v.options() for k, v in tuned.items()}
+    return summary
+
+
 def main():
     parser = argparse.ArgumentParser()
     parser.add_argument("--gpus", type=int, default=1)
@@ -328,6 +354,9 @@ def main():
     parser.add_argument("--no-cpu-baseline", action="store_true")
     parser.add_argument("--no-target", action="store_true", help="skip the time-to-target runs")
     parser.add_argument("--no-learned", action="store_true", help="skip the learned-importance run")
+    parser.add_argument("--no-batched", action="store_true", help="skip the batched-scenes run")
+    parser.add_argument("--batched-scale", type=float, default=0.05,
+                        help="photon budgets of the batched scenes, as a fraction of the workload's")
     parser.add_argument("--photons-per-column", type=int, default=0)
     args = parser.parse_args()
 
@@ -363,7 +392,7 @@ def main():
     native = binding.load()
     tables = np.ascontiguousarray(scene.tables)
     err = ctypes.create_string_buffer(4096)
-    capacity = max(args.steps, args.warmup)
+    capacity = max(args.steps, args.warmup)  # every group has at most this many rounds
     handle = native.monki_cuda_create(
         local, tables.ctypes.data_as(binding.F64P), tables.size, capacity, b"precision=fp32", err, len(err)
     )
@@ -378,12 +407,13 @@ def main():
     counters_before = (ctypes.c_uint64 * 6)()
     counters_after = (ctypes.c_uint64 * 6)()
 
-    def group(start, rounds):
-        """One round group in one dispatch, as CUDA.run_batches schedules it, with the
-        per-stage event timing on. Ranks run disjoint rounds (offset 100000 per rank)."""
+    def group(start, rounds, profile=0):
+        """One round group in one dispatch, as CUDA.run_batches schedules it (iteration
+        batches replayed as CUDA graphs); ``profile`` adds per-stage event timing instead.
+        Ranks run disjoint rounds (offset 100000 per rank)."""
 
         controls = (ctypes.c_uint32 * 8)(
-            per_round * rounds, 0, first_round(rank, start), 0, 100000, 1, per_round, rounds
+            per_round * rounds, 0, first_round(rank, start), 0, 100000, profile, per_round, rounds
         )
 
         if native.monki_cuda_run(handle, controls, out.ctypes.data_as(binding.F64P), err, len(err)):
@@ -407,11 +437,23 @@ def main():
         wall = time.perf_counter() - wall
 
     native.monki_cuda_counters(handle, counters_after)
+    delta = [int(a) - int(b) for a, b in zip(counters_after, counters_before, strict=True)]
+    scatters, visits_fp, visits_det, updates, photons, launches = delta
+    # Per-stage timing for the roofline: a separate group of the same size with CUDA events
+    # around every kernel (no graphs); its counters give the per-launch work.
+    profiled_before = (ctypes.c_uint64 * 6)()
+    profiled_after = (ctypes.c_uint64 * 6)()
+    native.monki_cuda_counters(handle, profiled_before)
+    flush.zero_()
+    torch.cuda.synchronize()
+    group(args.warmup + args.steps + 1, args.steps, profile=1)
+    native.monki_cuda_counters(handle, profiled_after)
     stage_ms = (ctypes.c_double * 3)()
     stage_launches = (ctypes.c_uint64 * 3)()
     native.monki_cuda_stage_timing(handle, stage_ms, stage_launches)
-    delta = [int(a) - int(b) for a, b in zip(counters_after, counters_before, strict=True)]
-    scatters, visits_fp, visits_det, updates, photons, launches = delta
+    p_scatters, p_visits_fp, p_visits_det, p_updates, _, _ = (
+        int(a) - int(b) for a, b in zip(profiled_after, profiled_before, strict=True)
+    )
     device_seconds = run_ms / 1e3
 
     if world > 1:
@@ -433,9 +475,9 @@ def main():
     stage_share = {name: stage_ms[q] / stage_total for q, name in enumerate(names)}
     pool = 1 << 20
     algorithmic = {
-        "transit": SLOT_SCAN_BYTES * pool * int(stage_launches[0]) + TRANSIT_EVENT_BYTES * scatters + CELL_BYTES * visits_fp,
-        "peel": STATE_BYTES * scatters + CELL_BYTES * visits_det + TALLY_BYTES * updates,
-        "scatter": SCATTER_EVENT_BYTES * scatters,
+        "transit": SLOT_SCAN_BYTES * pool * int(stage_launches[0]) + TRANSIT_EVENT_BYTES * p_scatters + CELL_BYTES * p_visits_fp,
+        "peel": STATE_BYTES * p_scatters + CELL_BYTES * p_visits_det + TALLY_BYTES * p_updates,
+        "scatter": SCATTER_EVENT_BYTES * p_scatters,
     }
     kernels = {}
     for q, name in enumerate(names):
@@ -557,6 +599,9 @@ def main():
             "statistics on the device, per-round pixel sums and the statistics at each check copied "
             "to the host, NetCDF output",
         }
+
+    if not args.no_batched:
+        line["batched"] = batched_scenes(local, args.batched_scale)
 
     if not args.no_target:
         # FP32 bias of the product transport against the FP64 build, per Stokes component.

@@ -39,6 +39,7 @@ struct Config {
     double roulette = 0.0;       // guided: roulette weight (0 = off)
     double cap = 0.0;            // guided: detector branch only below this weight (0 = always)
     bool importance = false;     // tally per-cell importance (pilot runs)
+    bool graphs = true;          // replay each batch of wavefront iterations as a CUDA graph
 };
 
 Config parse_config(const char* text) {
@@ -90,6 +91,7 @@ Config parse_config(const char* text) {
                 c.cap = v;
             }
         } else if (key == "importance") c.importance = as_int(0, 1) != 0;
+        else if (key == "graphs") c.graphs = as_int(0, 1) != 0;
         else throw std::runtime_error("Unknown config key: " + key);
     }
     if (c.block % 32) throw std::runtime_error("block must be a multiple of 32");
@@ -532,16 +534,48 @@ void run_wavefront(Session& s, const Controls& c) {
         for (cudaEvent_t& e : s.stage_events) check(cudaEventCreate(&e), "cudaEventCreate");
     }
     if (profile) for (int q = 0; q < 3; ++q) { s.stage_ms[q] = 0; s.stage_launches[q] = 0; }
-    for (;;) {
-        for (uint32_t b = 0; b < s.cfg.check_every; ++b, ++it) {
+    auto batch = [&]() {
+        for (uint32_t b = 0; b < s.cfg.check_every; ++b) {
             cudaEvent_t* ev = profile ? s.stage_events.data() + 4 * b : nullptr;
             if (nm == 1 && !paths) wave_iteration<T, 1, false>(s, v, P, c, dv, grid, ev);
             else if (nm == 1) wave_iteration<T, 1, true>(s, v, P, c, dv, grid, ev);
             else if (!paths) wave_iteration<T, 3, false>(s, v, P, c, dv, grid, ev);
             else wave_iteration<T, 3, true>(s, v, P, c, dv, grid, ev);
         }
+        check(cudaMemcpyAsync(s.host_counts, P.counts, 5 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s.stream),
+              "copy(counts)");
+    };
+    // Without per-stage timing, the batch of check_every iterations (3 launches and a queue
+    // reset each, then the counts read-back) is captured once per run and replayed as one
+    // CUDA graph: the host submits one launch per batch instead of 4 * check_every.
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    if (s.cfg.graphs && !profile) {
+        check(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        try {
+            batch();
+        } catch (...) {
+            cudaGraph_t partial = nullptr;
+            cudaStreamEndCapture(s.stream, &partial);  // leave capture mode before reporting
+            if (partial) cudaGraphDestroy(partial);
+            throw;
+        }
+        check(cudaStreamEndCapture(s.stream, &graph), "end capture");
+        const cudaError_t inst = cudaGraphInstantiate(&exec, graph, 0);
+        if (inst != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            check(inst, "graph instantiate");
+        }
+    }
+    struct GraphGuard {
+        cudaGraph_t g; cudaGraphExec_t e;
+        ~GraphGuard() { if (e) cudaGraphExecDestroy(e); if (g) cudaGraphDestroy(g); }
+    } guard{graph, exec};
+    for (;;) {
+        if (exec) check(cudaGraphLaunch(exec, s.stream), "graph launch");
+        else batch();
+        it += s.cfg.check_every;
         check(cudaGetLastError(), "wavefront launch");
-        check(cudaMemcpyAsync(s.host_counts, P.counts, 5 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s.stream), "copy(counts)");
         check(cudaStreamSynchronize(s.stream), "wavefront");
         if (profile) {
             for (uint32_t b = 0; b < s.cfg.check_every; ++b) {

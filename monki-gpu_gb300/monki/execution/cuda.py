@@ -53,6 +53,7 @@ class CUDA(Backend):
         block: int = 256,
         engine: str = "wavefront",
         pool: int = 1 << 20,
+        walk: int = 24,
         guided: Guided | None = None,
         importance: bool = False,
         roulette_scale=None,
@@ -88,6 +89,9 @@ class CUDA(Backend):
         if type(pool) is not int or not 1024 <= pool <= 1 << 26:
             raise ValueError("pool must be an integer in [1024, 2**26]")
 
+        if type(walk) is not int or not 1 <= walk <= 1 << 20:
+            raise ValueError("walk must be an integer in [1, 2**20]")
+
         if guided is not None and not isinstance(guided, Guided):
             raise ValueError("guided must be a monki.Guided or None")
 
@@ -108,6 +112,7 @@ class CUDA(Backend):
         self.block = block
         self.engine = engine
         self.pool = pool
+        self.walk = walk
         self.guided = guided
         self.importance_tally = importance
         # simulate() folds rounds into FP64 statistics on the device when available.
@@ -174,7 +179,7 @@ class CUDA(Backend):
         error = ctypes.create_string_buffer(8192)
         config = (
             f"precision={self.precision},shards={self.tally_shards},block={self.block},"
-            f"engine={self.engine},pool={self.pool}"
+            f"engine={self.engine},pool={self.pool},walk={self.walk}"
             + (self.guided.config() if self.guided is not None else "")
             + (",importance=1" if self.importance_tally else "")
         ).encode()
@@ -223,6 +228,7 @@ class CUDA(Backend):
             "block": self.block,
             "engine": self.engine,
             "pool": self.pool,
+            "walk": self.walk,
             "guided": None if self.guided is None else self.guided.describe(),
             "library_sha256": hashlib.sha256(open(self.library, "rb").read()).hexdigest(),
             "tables_sha256": hashlib.sha256(tables.tobytes()).hexdigest(),
@@ -476,6 +482,7 @@ class CUDA(Backend):
             self.block,
             self.engine,
             self.pool,
+            self.walk,
             self.guided,
             self.importance_tally,
         )

@@ -1,0 +1,65 @@
+"""CUDA-graph replay, batched scenes and the autotuner on the GB300.
+
+* a round group replayed as CUDA graphs gives the tallies of the same group launched
+  kernel by kernel (FP64 transport; only the device's atomic summation order differs);
+* scenes of uneven size run concurrently from host threads give each scene exactly what
+  running it alone gives;
+* the autotuner times its candidates and returns the fastest.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _flat(batches):
+    return np.concatenate([b.stokes.ravel(order="F") for b in batches])
+
+
+def test_graph_replay_equals_kernel_launches(native, device):
+    import monki.scenes as scenes
+    from monki.execution.native import F64P
+
+    scene = scenes.box_cloud(20, 2, nx=12, ny=10, box_x=(3, 8), box_y=(2, 6))
+    tables = np.ascontiguousarray(scene.tables)
+    per_round = 20 * 120
+    results = []
+    for graphs in (1, 0):
+        err = ctypes.create_string_buffer(1024)
+        handle = native.monki_cuda_create(0, tables.ctypes.data_as(F64P), tables.size, 2,
+                                          f"precision=fp64,pool=1024,graphs={graphs}".encode(), err, len(err))
+        assert handle, err.value
+        out = np.zeros(2 * native.monki_cuda_tally_count(handle))
+        controls = (ctypes.c_uint32 * 8)(2 * per_round, 0, 1, 9, 100000, 0, per_round, 2)
+        assert native.monki_cuda_run(handle, controls, out.ctypes.data_as(F64P), err, len(err)) == 0, err.value
+        native.monki_cuda_close(handle)
+        results.append(out)
+    np.testing.assert_allclose(results[0], results[1], rtol=1e-9, atol=1e-15)
+
+
+def test_batched_scenes_equal_scenes_run_alone(device):
+    import monki.scenes as scenes
+    from monki.batched import run_batched, run_scene
+
+    batch = [scenes.batched_scene(seed, photons_scale=0.002) for seed in range(4)]
+    results, summary = run_batched(batch, concurrency=4, tune=lambda s: {"precision": "fp64"})
+    assert summary["scenes"] == 4 and summary["scatters"] > 0
+    for scene, (batches, provenance) in zip(batch, results, strict=True):
+        alone, alone_provenance = run_scene(scene, options={"precision": "fp64"})
+        assert provenance["scatters"] == alone_provenance["scatters"]
+        np.testing.assert_allclose(_flat(batches), _flat(alone), rtol=1e-9, atol=1e-15)
+
+
+def test_autotuner_returns_the_fastest_candidate(device):
+    import monki.scenes as scenes
+    from monki.tuning import autotune
+
+    tuned = autotune(scenes.box_cloud(500, 1), photons_per_round=300_000)
+    rates = [rate for _, rate in tuned.trials]
+    assert tuned.scatters_per_second == max(rates) > 0
+    assert set(tuned.options()) == {"pool", "block", "walk"}
