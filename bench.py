@@ -518,11 +518,11 @@ def main():
             learned = time_to_target(args.workload, ppc, local, 23274 + rank, GUIDED, scale)
             # Dense-contraction roofline of the network's training: FLOPs of the tcgen05
             # GEMMs per step (forward 3 layers, backward weight and input gradients).
-            flops = len(losses) * 16384 * 2 * (3 * (64 * 256 + 2 * 256 * 256) - 64 * 256)
+            flops = len(losses) * model.rows * 2 * (3 * (64 * 256 + 2 * 256 * 256) - 64 * 256)
             tensor_peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("bf16_tflops") \
                 if (ROOT / "MEASURED_PEAKS.json").is_file() else 1900.0
             learned["training"] = {"seconds_with_pilots": trained, "fit_seconds": fit_seconds, "rows": rows,
-                                   "steps": len(losses), "batch": 16384,
+                                   "steps": len(losses), "batch": model.rows,
                                    "loss_first": float(losses[:20].mean()), "loss_last": float(losses[-50:].mean()),
                                    "gemm_tflops": flops / fit_seconds / 1e12,
                                    "frac_of_bf16_peak": flops / fit_seconds / 1e12 / tensor_peak}

@@ -1,11 +1,13 @@
 // Fifth-generation tensor-core GEMM for sm_103a: C = A * B^T with BF16 operands staged
 // in shared memory (128-byte swizzled, K-major), FP32 accumulation in tensor memory
-// (TMEM), one elected thread issuing tcgen05.mma, completion tracked by an mbarrier, and a
+// (TMEM), one elected thread issuing tcgen05.mma, completion tracked by mbarriers, and a
 // fused epilogue read back from TMEM with tcgen05.ld.
 //
 // Tile: 128 rows of C per CTA (the MMA's M), all N <= 256 columns (one MMA covers them),
 // K in steps of 64 (one 128-byte swizzle row of BF16), four MMAs of K = 16 per step.
-// The K range of a CTA is blockIdx.y's slice (split-K for the weight gradients).
+// Two shared-memory stages: the 256 threads load step s + 1 while the tensor core runs
+// step s; a stage is refilled only after the MMAs that read it have committed. The K
+// range of a CTA is blockIdx.y's slice (split-K for the weight gradients).
 //
 // Shared-memory matrix layout (K-major, SWIZZLE_128B): row r of a tile occupies bytes
 // [128 r, 128 r + 128); its 16-byte chunk c sits at chunk c ^ (r % 8). Eight rows form a
@@ -20,10 +22,11 @@ namespace umma {
 
 constexpr int kBlockM = 128;
 constexpr int kBlockK = 64;
-constexpr int kThreads = 128;                    // four warps: loaders, then epilogue
+constexpr int kThreads = 256;                    // eight warps: loaders, then epilogue
 constexpr uint32_t kSmemA = kBlockM * kBlockK * 2;   // 16 KB
 constexpr uint32_t kSmemB = 256 * kBlockK * 2;       // 32 KB (N <= 256)
-// 100 KB of dynamic shared memory: the tiles plus alignment, and at most two CTAs per SM
+constexpr uint32_t kStage = kSmemA + kSmemB;         // 48 KB, 1024-byte multiple
+// 100 KB of dynamic shared memory: two stages plus alignment, and at most two CTAs per SM
 // so their TMEM allocations (256 columns each of the SM's 512) never wait on each other.
 constexpr uint32_t kSmemBytes = 100u * 1024u;
 constexpr uint32_t kWaitLimit = 1u << 24;          // mbarrier polls before giving up
@@ -106,19 +109,17 @@ __device__ __forceinline__ bool wait_parity(uint32_t bar, uint32_t parity) {
 template <int EPI>
 __global__ void __launch_bounds__(kThreads, 1) gemm(Params p) {
     extern __shared__ __align__(1024) unsigned char raw[];
-    __shared__ __align__(8) uint64_t mma_bar;
+    __shared__ __align__(8) uint64_t mma_bar[2];
     __shared__ uint32_t tmem_base;
     __shared__ int aborted;
     unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(raw) + 1023) & ~uintptr_t(1023));
-    unsigned char* tile_a = base;
-    unsigned char* tile_b = base + kSmemA;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int row0 = blockIdx.x * kBlockM;
     const int k_begin = blockIdx.y * p.k_chunk;
     const int k_end = min(p.K, k_begin + p.k_chunk);
     const int N = p.N;
     const uint32_t columns = N <= 32 ? 32u : (N <= 64 ? 64u : (N <= 128 ? 128u : 256u));
-    const uint32_t bar = smem_u32(&mma_bar);
+    const uint32_t bar[2] = {smem_u32(&mma_bar[0]), smem_u32(&mma_bar[1])};
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
@@ -127,7 +128,8 @@ __global__ void __launch_bounds__(kThreads, 1) gemm(Params p) {
     }
     if (threadIdx.x == 0) {
         aborted = 0;
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar[0]) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar[1]) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -136,13 +138,27 @@ __global__ void __launch_bounds__(kThreads, 1) gemm(Params p) {
     const uint32_t tmem = tmem_base;
     const uint32_t idesc = instr_desc(kBlockM, N);
 
-    uint32_t phase = 0;
-    for (int k0 = k_begin; k0 < k_end; k0 += kBlockK) {
+    // Commits issued and completions observed per stage barrier (uniform in the CTA).
+    uint32_t issued[2] = {0u, 0u}, seen[2] = {0u, 0u};
+    int step = 0;
+    for (int k0 = k_begin; k0 < k_end; k0 += kBlockK, ++step) {
+        const int b = step & 1;
+        unsigned char* tile_a = base + b * kStage;
+        unsigned char* tile_b = tile_a + kSmemA;
+        if (issued[b] > seen[b]) {
+            // The MMAs of step - 2 read this stage: wait for their commit before refilling.
+            if (!wait_parity(bar[b], seen[b] & 1u)) {
+                aborted = 1;
+                if (threadIdx.x == 0) atomicOr(p.failure, 1u);
+            }
+            ++seen[b];
+        }
         load_tile(tile_a, p.A, p.lda, row0, kBlockM, p.rows_a, k0);
         load_tile(tile_b, p.B, p.ldb, 0, N, N, k0);
         // Make the generic-proxy stores visible to the tensor core (async proxy).
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
+        if (aborted) break;
         if (threadIdx.x == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t a_addr = smem_u32(tile_a), b_addr = smem_u32(tile_b);
@@ -155,31 +171,33 @@ __global__ void __launch_bounds__(kThreads, 1) gemm(Params p) {
                     " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
                     ::"r"(tmem), "l"(da), "l"(db), "r"(idesc), "r"(accumulate) : "memory");
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar[b])
                          : "memory");
         }
-        // Every thread waits for the MMAs before the tiles are overwritten.
-        if (!wait_parity(bar, phase)) {
-            aborted = 1;
-            if (threadIdx.x == 0) atomicOr(p.failure, 1u);
-        }
-        __syncthreads();
-        if (aborted) {
-            // Give the MMAs still in flight one more bounded wait before TMEM is released.
-            wait_parity(bar, phase);
-            break;
-        }
-        phase ^= 1u;
+        ++issued[b];
     }
+    // Drain: every commit issued is waited for (bounded) before TMEM is read or released.
+    for (int b = 0; b < 2; ++b) {
+        while (seen[b] < issued[b]) {
+            if (!wait_parity(bar[b], seen[b] & 1u)) {
+                aborted = 1;
+                if (threadIdx.x == 0) atomicOr(p.failure, 1u);
+            }
+            ++seen[b];
+        }
+    }
+    __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
     if (!aborted && k_end > k_begin) {
-        // Epilogue: warp w owns TMEM lanes (rows) 32 w .. 32 w + 31; one row per thread.
-        const int m = row0 + warp * 32 + lane;
+        // Epilogue: warp w reads TMEM lanes (rows) 32 (w % 4) .. + 31 (the lane quarter its
+        // position in the warpgroup allows) and every other 32-column chunk, from 32 (w / 4).
+        const int quarter = warp & 3, half = warp >> 2;
+        const int m = row0 + quarter * 32 + lane;
         const bool valid = m < p.rows_a;
-        for (int c0 = 0; c0 < N; c0 += 32) {
+        for (int c0 = 32 * half; c0 < N; c0 += 64) {
             uint32_t r[32];
-            const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0);
+            const uint32_t taddr = tmem + (uint32_t(quarter * 32) << 16) + uint32_t(c0);
             asm volatile(
                 "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
                 "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
@@ -191,25 +209,75 @@ __global__ void __launch_bounds__(kThreads, 1) gemm(Params p) {
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             if (!valid) continue;
             const int width = min(32, N - c0);
+            const size_t at = size_t(m) * N + c0;
+            // Each thread owns 32 consecutive columns of its row: 16-byte stores (and loads)
+            // instead of scalar ones, whose warp-wide pattern touched 32 rows per instruction.
+            if (width == 32 && (N & 7) == 0) {
+                float v[32];
+#pragma unroll
+                for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
+                if (EPI == kStore) {
+#pragma unroll
+                    for (int q = 0; q < 32; q += 4)
+                        *reinterpret_cast<float4*>(p.C + at + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+                } else if (EPI == kAccumulate) {
+#pragma unroll
+                    for (int q = 0; q < 32; q += 4)
+                        atomicAdd(reinterpret_cast<float4*>(p.C + at + q), make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]));
+                } else {
+                    if (EPI == kForward) {
+#pragma unroll
+                        for (int q = 0; q < 32; q += 4) {
+                            const float4 b = *reinterpret_cast<const float4*>(p.bias + c0 + q);
+                            v[q] += b.x; v[q + 1] += b.y; v[q + 2] += b.z; v[q + 3] += b.w;
+                            *reinterpret_cast<float4*>(p.C + at + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+                        }
+#pragma unroll
+                        for (int q = 0; q < 32; ++q) v[q] = gelu(v[q]);
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < 32; q += 4) {
+                            const float4 z = *reinterpret_cast<const float4*>(p.zprev + at + q);
+                            v[q] *= gelu_grad(z.x); v[q + 1] *= gelu_grad(z.y);
+                            v[q + 2] *= gelu_grad(z.z); v[q + 3] *= gelu_grad(z.w);
+                        }
+                    }
+                    uint32_t packed[16];
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) {
+                        const __nv_bfloat162 h2 = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+                        packed[q] = *reinterpret_cast<const uint32_t*>(&h2);
+                    }
+#pragma unroll
+                    for (int q = 0; q < 16; q += 4)
+                        *reinterpret_cast<uint4*>(p.H + at + 2 * q) = make_uint4(packed[q], packed[q + 1], packed[q + 2], packed[q + 3]);
+                    if (p.HT) {
+#pragma unroll
+                        for (int q = 0; q < 32; ++q)
+                            p.HT[size_t(c0 + q) * p.rows_ht + m] = __float2bfloat16(v[q]);
+                    }
+                }
+                continue;
+            }
 #pragma unroll
             for (int q = 0; q < 32; ++q) {
                 if (q >= width) break;
                 const int n = c0 + q;
                 const float acc = __uint_as_float(r[q]);
-                const size_t at = size_t(m) * N + n;
+                const size_t e = size_t(m) * N + n;
                 if (EPI == kStore) {
-                    p.C[at] = acc;
+                    p.C[e] = acc;
                 } else if (EPI == kAccumulate) {
-                    atomicAdd(p.C + at, acc);
+                    atomicAdd(p.C + e, acc);
                 } else if (EPI == kForward) {
                     const float z = acc + p.bias[n];
-                    p.C[at] = z;
+                    p.C[e] = z;
                     const __nv_bfloat16 h = __float2bfloat16(gelu(z));
-                    p.H[at] = h;
+                    p.H[e] = h;
                     if (p.HT) p.HT[size_t(n) * p.rows_ht + m] = h;
                 } else {
-                    const __nv_bfloat16 g = __float2bfloat16(acc * gelu_grad(p.zprev[at]));
-                    p.H[at] = g;
+                    const __nv_bfloat16 g = __float2bfloat16(acc * gelu_grad(p.zprev[e]));
+                    p.H[e] = g;
                     if (p.HT) p.HT[size_t(n) * p.rows_ht + m] = g;
                 }
             }

@@ -396,7 +396,7 @@ def training_scenes(count: int = 24):
     ]
 
 
-def train_model(training, *, device: int = 0, steps: int = 3000, batch: int = 16384, learning_rate: float = 1e-3,
+def train_model(training, *, device: int = 0, steps: int = 3000, batch: int = 65536, learning_rate: float = 1e-3,
                 photons_per_column: int = 300, rows_per_scene: int = 20000, seed: int = 1):
     """Pilot every training scene, then train a network on the device. Returns
     (model, per-step losses, training rows)."""
