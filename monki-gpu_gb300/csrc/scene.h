@@ -98,6 +98,10 @@ struct Controls {
 struct TallyLayout {
     uint32_t stokes, paths, weights, count;  // element counts; count = sum
     uint32_t shards;
+    uint32_t orders;  // scattering-order diagnostics after the weights (0 = off):
+                      // single-scattering Stokes (stokes elements), then the contribution of
+                      // every event location and its single-scattering part
+                      // (nmat * nx * ny * nz * angles each, layer 0 = the surface)
 };
 
 }  // namespace monki

@@ -40,6 +40,7 @@ struct Config {
     double cap = 0.0;            // guided: detector branch only below this weight (0 = always)
     bool importance = false;     // tally per-cell importance (pilot runs)
     bool graphs = true;          // replay each batch of wavefront iterations as a CUDA graph
+    bool orders = false;         // scattering-order diagnostics (single scattering, locations)
 };
 
 Config parse_config(const char* text) {
@@ -92,11 +93,12 @@ Config parse_config(const char* text) {
             }
         } else if (key == "importance") c.importance = as_int(0, 1) != 0;
         else if (key == "graphs") c.graphs = as_int(0, 1) != 0;
+        else if (key == "orders") c.orders = as_int(0, 1) != 0;
         else throw std::runtime_error("Unknown config key: " + key);
     }
     if (c.block % 32) throw std::runtime_error("block must be a multiple of 32");
-    if (!c.wavefront && (c.epsilon > 0.0 || c.roulette > 0.0 || c.importance))
-        throw std::runtime_error("guided transport and importance tallies need engine=wavefront");
+    if (!c.wavefront && (c.epsilon > 0.0 || c.roulette > 0.0 || c.importance || c.orders))
+        throw std::runtime_error("guided transport, importance and scattering-order tallies need engine=wavefront");
     return c;
 }
 
@@ -440,7 +442,8 @@ Pool<T> allocate_pool(Session& s) {
     const size_t parts[] = {quad, quad, quad, n * sizeof(uint4), n * sizeof(uint32_t), n,
                             n * nz * sizeof(T), n * sizeof(uint32_t), 2 * n * sizeof(T),
                             3 * n * sizeof(uint32_t), 16 * sizeof(uint32_t),
-                            ring * sizeof(uint32_t), ring * sizeof(T), s.cfg.importance ? n * sizeof(uint32_t) : 0};
+                            ring * sizeof(uint32_t), ring * sizeof(T), s.cfg.importance ? n * sizeof(uint32_t) : 0,
+                            s.cfg.orders ? n * sizeof(uint32_t) : 0};
     size_t bytes = 0;
     for (size_t part : parts) bytes += align_up(part, 256);
     check(cudaMalloc(&s.pool_memory, bytes), "cudaMalloc(pool)");
@@ -466,6 +469,7 @@ Pool<T> allocate_pool(Session& s) {
         P.ring_n = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
         P.importance = s.importance;
     }
+    if (s.cfg.orders) P.order = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
     return P;
 }
 
@@ -783,13 +787,17 @@ void* monki_cuda_create(uint32_t device, const double* tables, size_t table_coun
         L.stokes = uint32_t(p.nmat * p.nx * p.ny * p.angles);
         L.paths = p.paths ? uint32_t(p.nx * p.ny * p.nz * p.angles) : 0u;
         L.weights = p.paths ? uint32_t(p.nx * p.ny * p.angles) : 0u;
-        L.count = L.stokes + L.paths + L.weights;
+        L.orders = cfg.orders ? L.stokes + 2u * uint32_t(p.nmat * p.nx * p.ny * p.nz * p.angles) : 0u;
+        L.count = L.stokes + L.paths + L.weights + L.orders;
         L.shards = cfg.shards;
         const uint32_t pixels = uint32_t(p.nx * p.ny * p.angles);
         WaveTally& W = s->wave;
         W.pixels = pixels;
         W.layers = p.paths ? pixels * uint32_t(p.nz + 1) * 4u : 0u;
         W.count = 4u * pixels + W.layers;
+        W.locations = uint32_t(p.nx * p.ny * p.nz * p.angles);
+        W.orders = cfg.orders ? W.count : 0u;
+        if (cfg.orders) W.count += 4u * (pixels + 2u * W.locations);
         W.shards = cfg.shards;
         const size_t elem = cfg.fp64 ? sizeof(double) : sizeof(float);
         const size_t per_round = cfg.wavefront ? W.count : L.count;

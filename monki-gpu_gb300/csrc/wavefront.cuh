@@ -71,8 +71,14 @@ struct Divisors { FastDiv per_round, nx, ny, ncol; };
 struct WaveTally {
     uint32_t pixels;   // nx * ny * angles
     uint32_t layers;   // pixels * (nz + 1) * 4 when paths are tallied, else 0
-    uint32_t count;    // 4 * pixels + layers
+    uint32_t count;    // 4 * pixels + layers (+ the order records)
     uint32_t shards;
+    // Scattering-order diagnostics (0 = off): element offset of the single-scattering
+    // pixel records {I, Q, U, -} (pixels), followed by the location records {I, Q, U, -} of
+    // every (column, layer, view), cell = i + nx (j + ny (layer + nz view)), layer 0 = the
+    // surface, then their single-scattering part.
+    uint32_t orders;
+    uint32_t locations;  // nx * ny * nz * angles
 };
 
 template <typename T>
@@ -98,6 +104,7 @@ struct Pool {
     uint32_t* ring_n;     // events so far
     double* importance;   // 2 * nx * ny * nz
     const T* pixel_weight;  // nx * ny * angles weights of the contributions, or null (all 1)
+    uint32_t* order;      // events so far of each slot's history (scattering-order tallies), or null
 };
 
 __device__ __forceinline__ uint32_t pack_layers(int k, int k1, int wmin, int wmax) {
@@ -344,7 +351,7 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
         DrawStream rng;
         int i = 0, j = 0, k = 0, k1 = -2, wmin = 255, wmax = 0;
         Quad<T> pos{}, dir{}, pol{};
-        uint32_t steps = 0, budget = walk;
+        uint32_t steps = 0, budget = walk, order = 0;
         bool fresh = false;
         PathRecord<T> path{PATHS ? P.wander + size_t(slot) * s.nz : nullptr, 255, 0, kNoRuns, T(0), T(0)};
 
@@ -357,6 +364,7 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
             dir = P.dir[slot];
             pol = P.pol[slot];
             steps = P.steps[slot];
+            if (P.order) order = P.order[slot];
             if (PATHS) {
                 path.runs = P.runs[slot];
                 path.ci0 = P.run_ci[2 * size_t(slot)];
@@ -386,6 +394,7 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
                 y = s.yunit * T(rng.next());
                 z = __ldg(s.zunit + k);
                 weight = T(1);
+                order = 0;
                 dir = Quad<T>{s.a0, s.b0, s.c0, s.phi0};
                 pol.x = T(0); pol.y = T(0);
                 steps = 0;
@@ -472,6 +481,7 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
                 kind = sp + 1;
             }
             ++scatters;
+            ++order;
             const int queue = kind == 255 ? kQueueSurface : (kind == 0 ? kQueueGas : kQueueParticle);
             const uint32_t at = warp_reserve(P.counts, queue);
             P.queue[queue][at] = slot;
@@ -485,6 +495,7 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
         }
         P.meta[slot] = make_uint4(pid, rng.draw, uint32_t(i) | (uint32_t(j) << 16), pack_layers(k, k1, path.wmin, path.wmax));
         P.steps[slot] = steps;
+        if (P.order) P.order[slot] = order;
         if (PATHS) {
             P.runs[slot] = path.runs;
             P.run_ci[2 * size_t(slot)] = path.ci0;
@@ -575,6 +586,10 @@ wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ b
         sincos(phi, &sphi, &cphi);
         T contributed = T(0);  // Stokes-I peel-off of this event, all views
         bool failed = false;
+        // Scattering-order diagnostics: the event's history order and its location record
+        // (layer 0 = an event on the surface).
+        const uint32_t order = P.order ? P.order[slot] : 0u;
+        const uint32_t location_layer = (k == 0 && z < eps) ? 0u : uint32_t(k + 1);
         for (int ia = 0; ia < s.angles; ++ia) {
             const T vc = s.vc[ia];
             T prob[3] = {T(0), T(0), T(0)};
@@ -638,6 +653,17 @@ wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ b
             const T att = exp(-tau);
             const T w = prob[0] * att;
             contributed += P.pixel_weight ? w * __ldg(P.pixel_weight + pixel) : w;
+            if (L.orders) {
+                const T q1 = NMAT > 1 ? prob[1] * att : T(0), q2 = NMAT > 2 ? prob[2] * att : T(0);
+                Quad<TA>* single = reinterpret_cast<Quad<TA>*>(bank + L.orders);
+                Quad<TA>* located = single + L.pixels;
+                const uint32_t cell = uint32_t(i) + uint32_t(s.nx) * (uint32_t(j) + uint32_t(s.ny) * (location_layer + uint32_t(s.nz) * uint32_t(ia)));
+                quad_add(located + cell, TA(w), TA(q1), TA(q2), TA(0));
+                if (order == 1u) {
+                    quad_add(single + pixel, TA(w), TA(q1), TA(q2), TA(0));
+                    quad_add(located + L.locations + cell, TA(w), TA(q1), TA(q2), TA(0));
+                }
+            }
             quad_add(pixrec + pixel, TA(w), TA(NMAT > 1 ? prob[1] * att : T(0)), TA(NMAT > 2 ? prob[2] * att : T(0)),
                      TA(PATHS ? w : T(0)));
             ++updates;
@@ -913,9 +939,18 @@ __global__ void wf_flush(const TA* __restrict__ banks, WaveTally L, int nmat, in
                 for (int s = 0; s < k; ++s) view += sum(rec + size_t(s) * 4 + 1);
                 value += zunit[k] * inv_mu[ia] * view;
             }
-        } else {
+        } else if (!L.orders || o < stokes_out + (paths ? pixels * uint32_t(nz + 1) : 0u)) {
             const uint32_t pixel = o - stokes_out - pixels * uint32_t(nz);
             value = sum(size_t(pixel) * 4 + 3);
+        } else {
+            // Order diagnostics: single-scattering Stokes, then the location records (all
+            // orders, then single scattering), each times mu0/mu of its view.
+            const uint32_t q = o - stokes_out - (paths ? pixels * uint32_t(nz + 1) : 0u);
+            const uint32_t m = q % uint32_t(nmat);
+            const uint32_t record = q / uint32_t(nmat);
+            const uint32_t ia = record < pixels ? record / uint32_t(nx * ny)
+                                                : ((record - pixels) % L.locations) / uint32_t(nx * ny * nz);
+            value = sum(size_t(L.orders) + size_t(record) * 4 + m) * mu0mu[ia];
         }
         out[e] = value;
     }

@@ -58,6 +58,7 @@ class CUDA(Backend):
         importance: bool = False,
         roulette_scale=None,
         device_statistics: bool = True,
+        orders: bool = False,
         library=None,
     ):
         for name, value, minimum, maximum in (
@@ -101,6 +102,12 @@ class CUDA(Backend):
         if (guided is not None or importance) and engine != "wavefront":
             raise ValueError("guided transport and importance tallies need engine='wavefront'")
 
+        if type(orders) is not bool:
+            raise ValueError("orders must be a bool")
+
+        if orders and engine != "wavefront":
+            raise ValueError("scattering-order diagnostics need engine='wavefront'")
+
         self.device = device
         self.save_path = save_path
         self.profile = profile
@@ -117,6 +124,9 @@ class CUDA(Backend):
         self.importance_tally = importance
         # simulate() folds rounds into FP64 statistics on the device when available.
         self.device_statistics = bool(device_statistics)
+        # Scattering-order diagnostics (single / multiple scattering, contribution by event
+        # location), the reference's save_scats outputs.
+        self.orders = orders
         # Per-cell roulette scale (nx, ny, nz) applied at every prepare; set_roulette_scale
         # changes it for the prepared session only.
         self.roulette_scale = None if roulette_scale is None else np.asarray(roulette_scale, dtype=np.float64)
@@ -161,11 +171,15 @@ class CUDA(Backend):
         nx, ny, nz, nmat, angles = (int(v) for v in tables[1:6])
         paths = bool(tables[10])
         tally_count = nmat * nx * ny * angles + (nx * ny * (nz + 1) * angles if paths else 0)
+        if self.orders:
+            tally_count += nmat * nx * ny * angles + 2 * nmat * nx * ny * nz * angles
         per_round = scene.photons_per_column * nx * ny
         # Device tally records per round and shard: {I, Q, U, weight} per pixel, plus
         # {layer, view, first, -} per (pixel, layer + 1) with path diagnostics.
         pixels = nx * ny * angles
         device_count = 4 * pixels + (4 * pixels * (nz + 1) if paths else 0)
+        if self.orders:
+            device_count += 4 * (pixels + 2 * nx * ny * nz * angles)
         bytes_per_round = device_count * self.tally_shards * (4 if self.precision == "fp32" else 8)
         capacity = max(
             1,
@@ -182,6 +196,7 @@ class CUDA(Backend):
             f"engine={self.engine},pool={self.pool},walk={self.walk}"
             + (self.guided.config() if self.guided is not None else "")
             + (",importance=1" if self.importance_tally else "")
+            + (",orders=1" if self.orders else "")
         ).encode()
         handle = native.monki_cuda_create(
             self.device,
@@ -355,7 +370,8 @@ class CUDA(Backend):
         each round into its FP64 statistics (``accumulate``)."""
 
         _, nx, ny, _, _ = self._shape
-        return self.device_statistics and photons_per_column * nx * ny <= self.photons_per_dispatch
+        return (self.device_statistics and not self.orders
+                and photons_per_column * nx * ny <= self.photons_per_dispatch)
 
     def accumulate(self, controls: list) -> np.ndarray:
         """Run rounds and fold their tallies into the device's FP64 round statistics
@@ -483,6 +499,7 @@ class CUDA(Backend):
             self.engine,
             self.pool,
             self.walk,
+            self.orders,
             self.guided,
             self.importance_tally,
         )
@@ -562,9 +579,28 @@ class CUDA(Backend):
                         .reshape((nx, ny, nz, angles), order="F")
                         .copy()
                     )
-                    weights = values[stokes_count + path_count :].reshape((nx, ny, angles), order="F").copy()
+                    weights = (
+                        values[stokes_count + path_count : stokes_count + path_count + nx * ny * angles]
+                        .reshape((nx, ny, angles), order="F")
+                        .copy()
+                    )
 
-                results.append(RawTallies(request, stokes, paths, weights))
+                orders = None
+
+                if self.orders:
+                    at = stokes_count + ((nx * ny * nz * angles + nx * ny * angles) if self._paths else 0)
+                    locations = nmat * nx * ny * nz * angles
+                    orders = {
+                        "single": values[at : at + stokes_count].reshape((nmat, nx, ny, angles), order="F").copy(),
+                        "locations": values[at + stokes_count : at + stokes_count + locations]
+                        .reshape((nmat, nx, ny, nz, angles), order="F")
+                        .copy(),
+                        "single_locations": values[at + stokes_count + locations :]
+                        .reshape((nmat, nx, ny, nz, angles), order="F")
+                        .copy(),
+                    }
+
+                results.append(RawTallies(request, stokes, paths, weights, orders))
 
             self._round = controls[-1].round_index
             return results

@@ -25,10 +25,14 @@ class RawTallies:
     """Unnormalized Fortran-order sums owned by the caller.
 
     ``stokes`` is (component, x, y, angle); ``weighted_paths`` is (x, y, layer, angle)
-    including the vacuum layer; ``weights`` is (x, y, angle).
+    including the vacuum layer; ``weights`` is (x, y, angle). ``orders`` (scattering-order
+    diagnostics, when requested) holds ``single`` (component, x, y, angle) and
+    ``locations`` / ``single_locations`` (component, x, y, layer, angle; layer 0 = the
+    surface, then the physical layers).
     """
 
     controls: BatchControls
     stokes: np.ndarray
     weighted_paths: np.ndarray | None = None
     weights: np.ndarray | None = None
+    orders: dict | None = None

@@ -40,6 +40,7 @@ def _host_rounds(case, backend, stopping):
 
     total = rounds_sum = rounds_squared = paths = weights = None
     history = []
+    orders = None
 
     for index, batch in enumerate(batches, start=1):
         if not isinstance(batch, RawTallies):
@@ -72,6 +73,14 @@ def _host_rounds(case, backend, stopping):
             paths += batch.weighted_paths
             weights += batch.weights
 
+        if getattr(batch, "orders", None) is not None:
+            if orders is None:
+                orders = {name: np.zeros_like(value) for name, value in batch.orders.items()}
+            for name, value in batch.orders.items():
+                orders[name] += value
+
+    if orders is not None:
+        backend.provenance["scattering_orders"] = orders  # summed over rounds, raw
     return total, rounds_sum, rounds_squared, history, paths, weights
 
 
@@ -187,6 +196,31 @@ def simulate(case, backend: Backend, output, *, convergence: AMFConvergence | No
 
         dimensions = dict(metadata.dimensions)
         attributes = dict(metadata.attributes)
+        orders = backend.provenance.pop("scattering_orders", None) if hasattr(backend, "provenance") else None
+
+        if orders is not None:
+            # Scattering-order diagnostics with the reference product's names
+            # (kernels/cpu/worker.f90:1462-1492): single and multiple scattering, and the
+            # contribution of each event location (layer axis: surface, then the physical
+            # layers), normalized like the radiance.
+            scale = 1.0 / completed / case.photons_per_column
+            single = orders["single"] * scale
+            located = orders["locations"] * scale  # layer axis: surface + physical layers
+            located_single = orders["single_locations"] * scale
+            pixel_axes = (3, 2, 1, 0)
+            location_axes = (4, 3, 2, 1, 0)
+            values["radiance_sing"] = single.transpose(pixel_axes)[..., None]
+            values["radiance_mult"] = (radiance - single).transpose(pixel_axes)[..., None]
+            values["contrib_radiance_3D"] = located.transpose(location_axes)[..., None]
+            values["contrib_radiance_3D_sing"] = located_single.transpose(location_axes)[..., None]
+            values["contrib_radiance_3D_mult"] = (located - located_single).transpose(location_axes)[..., None]
+            for name, label in (("radiance_sing", "single scattering"), ("radiance_mult", "multiple scattering")):
+                dimensions[name] = ("nvza", "ny", "nx", "nmat", "nwavs")
+                attributes[name] = {"long_name": f"TOA radiance, {label} only", "units": "-, assuming E0=pi"}
+            for suffix, label in (("", ""), ("_sing", ", single scattering"), ("_mult", ", multiple scattering")):
+                dimensions["contrib_radiance_3D" + suffix] = ("nvza", "nz_withsurf", "ny", "nx", "nmat", "nwavs")
+                attributes["contrib_radiance_3D" + suffix] = {
+                    "long_name": f"TOA radiance 3D contribution by event location{label}", "units": "-"}
 
         if isinstance(stopping, AMFStopping) and not isinstance(stopping, RadianceStopping):
             _, amf_error = stopping.moments.estimate(stopping.thickness)

@@ -527,6 +527,8 @@ struct Transport {
     Guide guide;
     std::vector<double> z_norm;  // analog sampler mass per particle species
     const double* pixel_weight = nullptr;  // importance-tally weight per output pixel, or none
+    bool orders = false;     // scattering-order diagnostics (calc_radiances_and_scats)
+    size_t orders_offset = 0, locations = 0;
     double a0, b0, c0, phi0_rad, vartheta0_rad;
     std::vector<double> va, vb, vc, view_phi_rad, zsum;  // zsum[k] = SUM(zunit(1:k))
     size_t stokes_count, path_count, weight_count, tally_count;
@@ -551,6 +553,19 @@ struct Transport {
         weight_count = t.paths ? size_t(t.nx) * t.ny * t.angles : 0;
         tally_count = stokes_count + path_count + weight_count;
         for (const auto& sp : t.species) z_norm.push_back(analog_norm(sp, t.nmat));
+    }
+
+    // Scattering-order diagnostics after the weights: single-scattering Stokes, then the
+    // contribution per event location (nmat, nx, ny, 0:nz-1, angles; layer 0 = surface) of
+    // all orders and of single scattering (mc_routines_cartesian_mod.f90:405-836).
+    void enable_orders() {
+        orders = true;
+        orders_offset = tally_count;
+        locations = size_t(t.nx) * t.ny * t.nz * t.angles;
+        tally_count += stokes_count + 2 * size_t(t.nmat) * locations;
+    }
+    size_t location_index(int m, int i, int j, int layer, int ia) const {
+        return size_t(m) + size_t(t.nmat) * (size_t(i - 1) + size_t(t.nx) * (size_t(j - 1) + size_t(t.ny) * (size_t(layer) + size_t(t.nz) * size_t(ia))));
     }
 
     // Russian roulette; false when the photon is terminated.
@@ -619,7 +634,8 @@ struct Transport {
     bool peel_off(double a_bak, double b_bak, double c_bak, int i_bak, int j_bak, int k_bak,
                   double x_bak, double y_bak, double z_bak, const std::vector<double>& s_prob,
                   const std::vector<double>& path_layers, double* tally,
-                  std::vector<double>& path_angle, Counters& cnt, double& contributed) const {
+                  std::vector<double>& path_angle, Counters& cnt, double& contributed,
+                  uint32_t nscat = 0) const {
         const int nmat = t.nmat, nz = t.nz;
         contributed = 0.0;
         for (int ia = 0; ia < t.angles; ++ia) {
@@ -663,6 +679,17 @@ struct Transport {
                                         : p1 * att;
             for (int m = 0; m < nmat; ++m) tally[stokes_index(m, inew, jnew, ia)] += s_prob[size_t(ia) * nmat + m] * att;
             cnt.tally_updates += nmat;
+            if (orders) {
+                const int layer = (k_bak == 1 && z_bak < kEps) ? 0 : k_bak;
+                for (int m = 0; m < nmat; ++m) {
+                    const double v = s_prob[size_t(ia) * nmat + m] * att;
+                    tally[orders_offset + stokes_count + location_index(m, i_bak, j_bak, layer, ia)] += v;
+                    if (nscat == 1) {
+                        tally[orders_offset + stokes_index(m, inew, jnew, ia)] += v;
+                        tally[orders_offset + stokes_count + size_t(nmat) * locations + location_index(m, i_bak, j_bak, layer, ia)] += v;
+                    }
+                }
+            }
             if (t.paths) {
                 double c1 = p1 * att;
                 for (int kk = 1; kk <= nz; ++kk)
@@ -683,6 +710,7 @@ struct Transport {
         double ring_inv[kRing];
         int ring_n = 0;
         double contributed = 0.0;
+        uint32_t nscat = 0;  // events of this history so far (its scattering order)
         // Record an event in cell (i, j, k) at weight w that contributed c.
         auto record = [&](int ci, int cj, int ck, double w, double c) {
             if (!importance) return;
@@ -752,12 +780,14 @@ struct Transport {
                 weight *= t.albedo[size_t(i - 1) + size_t(nx) * size_t(j - 1)];
                 if (weight < kEps) return 0;
                 ++cnt.scatters;
+                ++nscat;
                 for (int ia = 0; ia < t.angles; ++ia) {
                     for (int m = 0; m < nmat; ++m) s_prob[size_t(ia) * nmat + m] = 0.0;
                     if (vc[ia] > 0) s_prob[size_t(ia) * nmat] = s[0] * vc[ia] * weight;
                     if (!std::isfinite(s_prob[size_t(ia) * nmat])) return 1;
                 }
-                if (!peel_off(a_int, b_int, c_int, i, j, k, x, y, z, s_prob, path_layers, tally, path_angle, cnt, contributed))
+                if (!peel_off(a_int, b_int, c_int, i, j, k, x, y, z, s_prob, path_layers, tally, path_angle, cnt, contributed,
+                              nscat))
                     return 2;
                 record(i, j, k, weight, contributed);
                 // GROUND_LAMB2: theta = acos(sqrt(P)), phi = 2 pi U.
@@ -789,6 +819,7 @@ struct Transport {
             weight *= gas ? t.ssalb_gas[size_t(k - 1)] : t.species[size_t(sp - 1)].ssalb;
             if (weight < kEps) return 0;
             ++cnt.scatters;
+            ++nscat;
             for (int ia = 0; ia < t.angles; ++ia) {
                 double cs = c * vc[ia] + std::sqrt(std::max(kEps, 1.0 - c * c)) *
                                              std::sqrt(std::max(kEps, 1.0 - vc[ia] * vc[ia])) *
@@ -804,7 +835,8 @@ struct Transport {
                 for (int m = 0; m < nmat; ++m)
                     if (!std::isfinite(s_prob[size_t(ia) * nmat + m])) return 1;
             }
-            if (!peel_off(a, b, c, i, j, k, x, y, z, s_prob, path_layers, tally, path_angle, cnt, contributed)) return 2;
+            if (!peel_off(a, b, c, i, j, k, x, y, z, s_prob, path_layers, tally, path_angle, cnt, contributed, nscat))
+                return 2;
             record(i, j, k, weight, contributed);
             double cos_in = c, cos_out, dphi, cos_sca, phi_out;
             const bool guided = !gas && guide.epsilon > 0.0 && weight < guide.cap;
@@ -911,13 +943,13 @@ int monki_oracle_validate(const double* tables, size_t count, char* err, size_t 
 int monki_oracle_run_guided(const double* tables, size_t table_count, const uint32_t controls[8],
                             const double guide[3], const double* scale, int threads, double* out,
                             uint64_t* counters, double* importance, const double* pixel_weight,
-                            char* err, size_t errlen);
+                            uint32_t options, char* err, size_t errlen);
 
 int monki_oracle_run(const double* tables, size_t table_count, const uint32_t controls[8], int threads,
                      double* out, uint64_t* counters, char* err, size_t errlen) {
     const double plain[3] = {0.0, 0.0, 0.0};
     return monki_oracle_run_guided(tables, table_count, controls, plain, nullptr, threads, out, counters, nullptr,
-                                   nullptr, err, errlen);
+                                   nullptr, 0u, err, errlen);
 }
 
 // The same round group with guided transport: guide = {epsilon (DDIS probability at
@@ -925,11 +957,12 @@ int monki_oracle_run(const double* tables, size_t table_count, const uint32_t co
 // scale (nx * ny * nz, or NULL) multiplies the roulette weight per cell. importance
 // (2 * nx * ny * nz, or NULL) receives the importance tally: per cell the summed future
 // contribution per unit weight, then the event count; pixel_weight (nx * ny * angles, or
-// NULL) weights each contribution by its output pixel.
+// NULL) weights each contribution by its output pixel. options bit 0 adds the
+// scattering-order diagnostics to each round's tallies.
 int monki_oracle_run_guided(const double* tables, size_t table_count, const uint32_t controls[8],
                             const double guide[3], const double* scale, int threads, double* out,
                             uint64_t* counters, double* importance, const double* pixel_weight,
-                            char* err, size_t errlen) {
+                            uint32_t options, char* err, size_t errlen) {
     try {
         if (!guide || !(guide[0] >= 0.0 && guide[0] < 1.0) || !(guide[1] >= 0.0 && guide[1] <= 1.0)) {
             write_error(err, errlen, "Invalid guide: epsilon must be in [0, 1), roulette in [0, 1]");
@@ -949,6 +982,7 @@ int monki_oracle_run_guided(const double* tables, size_t table_count, const uint
         if (guide[2] > 0.0) tr.guide.cap = guide[2];
         tr.guide.scale = scale;
         tr.pixel_weight = pixel_weight;
+        if (options & 1u) tr.enable_orders();
         const size_t cells = size_t(t.nx) * t.ny * t.nz;
         if (scale)
             for (size_t c = 0; c < cells; ++c)
@@ -1009,7 +1043,17 @@ int monki_oracle_run_guided(const double* tables, size_t table_count, const uint
                 double f = std::fabs(std::cos(tr.vartheta0_rad)) / std::fabs(std::cos(kDegToRad * t.vartheta[ia]));
                 for (int j = 1; j <= t.ny; ++j)
                     for (int i = 1; i <= t.nx; ++i)
-                        for (int m = 0; m < t.nmat; ++m) out[size_t(r) * tc + tr.stokes_index(m, i, j, ia)] *= f;
+                        for (int m = 0; m < t.nmat; ++m) {
+                            out[size_t(r) * tc + tr.stokes_index(m, i, j, ia)] *= f;
+                            if (tr.orders) {
+                                out[size_t(r) * tc + tr.orders_offset + tr.stokes_index(m, i, j, ia)] *= f;
+                                for (int layer = 0; layer < t.nz; ++layer) {
+                                    const size_t at = size_t(r) * tc + tr.orders_offset + tr.stokes_count + tr.location_index(m, i, j, layer, ia);
+                                    out[at] *= f;
+                                    out[at + size_t(t.nmat) * tr.locations] *= f;
+                                }
+                            }
+                        }
             }
         if (counters) {
             counters[0] = total.scatters; counters[1] = total.photons; counters[2] = total.free_path_visits;

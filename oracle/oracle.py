@@ -56,6 +56,7 @@ def library() -> ctypes.CDLL:
             _U64P,
             _F64P,
             _F64P,
+            ctypes.c_uint32,
             ctypes.c_char_p,
             ctypes.c_size_t,
         ]
@@ -93,14 +94,17 @@ def validate(tables) -> str | None:
     return err.value.decode() if status else None
 
 
-def tally_count(tables) -> int:
+def tally_count(tables, orders: bool = False) -> int:
     nx, ny, nz, nmat, angles = (int(v) for v in tables[1:6])
     paths = bool(tables[10])
-    return nmat * nx * ny * angles + (nx * ny * (nz + 1) * angles if paths else 0)
+    count = nmat * nx * ny * angles + (nx * ny * (nz + 1) * angles if paths else 0)
+    if orders:
+        count += nmat * nx * ny * angles + 2 * nmat * nx * ny * nz * angles
+    return count
 
 
 def run(tables, controls, threads: int | None = None, guide=None, scale=None, importance: bool = False,
-        pixel_weights=None):
+        pixel_weights=None, orders: bool = False):
     """Run one round group; returns (tallies[rounds, tally_count], counters dict[, importance]).
 
     ``controls`` are the eight words of the CUDA run call. ``guide`` = (epsilon, roulette
@@ -109,14 +113,15 @@ def run(tables, controls, threads: int | None = None, guide=None, scale=None, im
     Fortran order, multiplies the roulette weight per cell. With ``importance`` the third
     result is the importance tally, shape (2, nx, ny, nz): summed future contribution per
     unit weight and event count per cell, each contribution weighted by ``pixel_weights``
-    (nx, ny, angles) of its output pixel when given. A failure flag raises.
+    (nx, ny, angles) of its output pixel when given. ``orders`` appends the scattering-order
+    diagnostics to each round (see ``split_orders``). A failure flag raises.
     """
 
     t = np.ascontiguousarray(tables, dtype=np.float64)
     ctl = np.ascontiguousarray(controls, dtype=np.uint32)
     nx, ny, nz = (int(v) for v in t[1:4])
     rounds = int(ctl[7])
-    out = np.zeros((rounds, tally_count(t)), dtype=np.float64)
+    out = np.zeros((rounds, tally_count(t, orders)), dtype=np.float64)
     counters = np.zeros(5, dtype=np.uint64)
     err = ctypes.create_string_buffer(4096)
     threads = threads or os.cpu_count() or 1
@@ -143,6 +148,7 @@ def run(tables, controls, threads: int | None = None, guide=None, scale=None, im
         counters.ctypes.data_as(_U64P),
         None if imp is None else imp.ctypes.data_as(_F64P),
         None if weights_arr is None else weights_arr.ctypes.data_as(_F64P),
+        1 if orders else 0,
         err,
         len(err),
     )
@@ -156,6 +162,21 @@ def run(tables, controls, threads: int | None = None, guide=None, scale=None, im
         cells = nx * ny * nz
         return out, stats, np.stack([imp[:cells].reshape((nx, ny, nz), order="F"), imp[cells:].reshape((nx, ny, nz), order="F")])
     return out, stats
+
+
+def split_orders(tables, values):
+    """The scattering-order block of one round: (single-scattering Stokes (nmat, nx, ny,
+    angles), contributions by event location and of single scattering (nmat, nx, ny, nz,
+    angles each, layer 0 = the surface))."""
+
+    nx, ny, nz, nmat, angles = (int(v) for v in tables[1:6])
+    at = tally_count(tables)
+    s = nmat * nx * ny * angles
+    loc = nmat * nx * ny * nz * angles
+    single = values[at : at + s].reshape((nmat, nx, ny, angles), order="F")
+    located = values[at + s : at + s + loc].reshape((nmat, nx, ny, nz, angles), order="F")
+    located_single = values[at + s + loc : at + s + 2 * loc].reshape((nmat, nx, ny, nz, angles), order="F")
+    return single, located, located_single
 
 
 def split(tables, values):

@@ -112,3 +112,20 @@ def test_guide_settings_are_validated(oracle):
             Guided(**kwargs)
     assert Guided(0.25, 0.5, 1.5).oracle() == (0.25, 0.5, 1.5)
     assert "epsilon=0.25" in Guided(0.25, 0.5, 1.5).config()
+
+
+def test_scattering_order_tallies_add_up(oracle):
+    """Single scattering is part of the total; every contribution is booked once by its
+    pixel and once by its event location (layer 0 = the surface)."""
+    scene = _small_box(ppc=10, rounds=1)
+    nmat, nx, ny, nz, angles = scene.shape
+    out, _ = oracle.run(scene.tables, _controls(scene, 1, 13), 4, orders=True)
+    plain, _ = oracle.run(scene.tables, _controls(scene, 1, 13), 4)
+    stokes = oracle.split(scene.tables, out[0])[0]
+    np.testing.assert_allclose(stokes, oracle.split(scene.tables, plain[0])[0], rtol=1e-12, atol=1e-15)
+    single, located, located_single = oracle.split_orders(scene.tables, out[0])
+    assert np.all(single[0] <= stokes[0] + 1e-15) and single[0].sum() > 0
+    np.testing.assert_allclose(located.sum(axis=(1, 2, 3)), stokes.sum(axis=(1, 2)), rtol=1e-12)
+    np.testing.assert_allclose(located_single.sum(axis=(1, 2, 3)), single.sum(axis=(1, 2)), rtol=1e-12)
+    assert located[0][:, :, 0, :].sum() > 0  # surface reflections
+    assert located.shape[3] == nz  # the surface and the nz - 1 physical layers
