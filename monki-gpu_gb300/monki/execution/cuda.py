@@ -12,11 +12,13 @@ from __future__ import annotations
 
 import ctypes
 import hashlib
+import os
 import platform
 
 import numpy as np
 
 from ..guided import Guided
+from ..input import ReferenceCase
 from ..scenes import TransportScene
 from . import native as _native
 from .backend import Backend
@@ -59,6 +61,7 @@ class CUDA(Backend):
         roulette_scale=None,
         device_statistics: bool = True,
         orders: bool = False,
+        monki_home=None,
         library=None,
     ):
         for name, value, minimum, maximum in (
@@ -127,6 +130,7 @@ class CUDA(Backend):
         # Scattering-order diagnostics (single / multiple scattering, contribution by event
         # location), the reference's save_scats outputs.
         self.orders = orders
+        self.monki_home = monki_home
         # Per-cell roulette scale (nx, ny, nz) applied at every prepare; set_roulette_scale
         # changes it for the prepared session only.
         self.roulette_scale = None if roulette_scale is None else np.asarray(roulette_scale, dtype=np.float64)
@@ -148,14 +152,20 @@ class CUDA(Backend):
 
         self.close()
 
-        if not isinstance(scene, TransportScene):
-            if type(scene).__name__ == "ReferenceCase":
-                raise NotImplementedError(
-                    "CUDA.prepare needs prepared tables (monki.scenes.TransportScene); "
-                    "fixture preparation from INPUT files is not implemented"
-                )
+        if isinstance(scene, ReferenceCase):
+            # A reference fixture: prepare its tables on the host (monki.preparation), from
+            # the MONKI home directory that holds INPUT/ and DATA/.
+            home = self.monki_home or os.environ.get("MONKI_HOME")
 
-            raise TypeError("CUDA.prepare expects a TransportScene")
+            if not home:
+                raise ValueError("preparing a ReferenceCase needs monki_home= or MONKI_HOME (the directory with INPUT/ and DATA/)")
+
+            from ..preparation import prepare_reference_case
+
+            scene = prepare_reference_case(scene, home)
+
+        if not isinstance(scene, TransportScene):
+            raise TypeError("CUDA.prepare expects a TransportScene or a ReferenceCase")
 
         if scene.backward:
             raise NotImplementedError("CUDA backward transport is not implemented")

@@ -167,7 +167,7 @@ def build_tables(
     particles: list[Particle],
     particle_optical_depth: np.ndarray,
     depolarization: float = 0.0279,
-    pixel_km: float = 1.0,
+    pixel_km=1.0,
 ) -> np.ndarray:
     """Assemble a version-2 table stream.
 
@@ -204,7 +204,8 @@ def build_tables(
     )
     surface_albedo = np.broadcast_to(np.asarray(albedo, dtype=float), (nx, ny))
     header = [2, nx, ny, nz, nmat, len(views), species, nz, nz, nz, int(save_path), 0]
-    geometry = [pixel_km, pixel_km, depolarization, 180.0 - solar_zenith, solar_azimuth, azimuths[0]]
+    x_km, y_km = (pixel_km, pixel_km) if np.isscalar(pixel_km) else pixel_km
+    geometry = [x_km, y_km, depolarization, 180.0 - solar_zenith, solar_azimuth, azimuths[0]]
     parts = [
         np.asarray(header, dtype=float),
         np.asarray(geometry, dtype=float),
@@ -220,8 +221,12 @@ def build_tables(
     ]
 
     for particle in particles:
-        cosines, cdf, f11, f22, f33, f12 = henyey_greenstein_table(particle.asymmetry)
-        parts += [np.array([len(cosines), particle.albedo]), cosines, cdf, f11, f22, f33, f12]
+        if isinstance(particle, Particle):
+            cosines, cdf, f11, f22, f33, f12 = henyey_greenstein_table(particle.asymmetry)
+            albedo_p = particle.albedo
+        else:  # a tabulated species: (cosines, cdf, F11, F22, F33, F12, albedo)
+            cosines, cdf, f11, f22, f33, f12, albedo_p = particle
+        parts += [np.array([len(cosines), albedo_p]), cosines, cdf, f11, f22, f33, f12]
 
     return np.concatenate(parts).astype(np.float64)
 
@@ -242,7 +247,7 @@ def scene_metadata(
     gas_absorption,
     particle_optical_depth,
     save_path: bool,
-    pixel_km: float = 1.0,
+    pixel_km=1.0,
     wavelength_nm: float = 340.0,
 ) -> SimulationResult:
     """Labels and optical fields with the reference product's names (worker.f90:1272-1600)."""
@@ -260,8 +265,8 @@ def scene_metadata(
         "theta": np.asarray(view_zeniths, dtype=float),
         "phi0": np.array([float(solar_azimuth)]),
         "phi": np.asarray(view_azimuths, dtype=float),
-        "x_unit": np.array([pixel_km]),
-        "y_unit": np.array([pixel_km]),
+        "x_unit": np.array([pixel_km if np.isscalar(pixel_km) else pixel_km[0]]),
+        "y_unit": np.array([pixel_km if np.isscalar(pixel_km) else pixel_km[1]]),
         "z_unit": np.diff(alt) / 1000.0,
         "alt": alt,
         "bmabs": np.append(gas_absorption, 0.0)[None, :],

@@ -341,8 +341,25 @@ def driver_statistics(ref, Dataset):
     return results
 
 
+def prepared_fixture():
+    """The 2boxclouds fixture prepared by monki.preparation from the reference's INPUT and
+    DATA files (Mie LUT with F12, Rayleigh with King factors, O3 absorption): the tables
+    and the optical depths, so GPU tests can run the scene where the fixtures are absent."""
+
+    sys.path.insert(0, str(REPO / "monki-gpu_gb300"))
+    from monki import ReferenceCase
+    from monki.preparation import prepare_reference_case
+
+    case = ReferenceCase("2boxclouds", "testrun/MONKI_MLS_2boxclouds_340_340_test.in", photons_per_column=100,
+                         rounds=32, solar_zenith=45.0)
+    scene = prepare_reference_case(case, REFERENCE / "fortran" / "monki" / "upstream")
+    return {"tables": scene.tables, "bmsca": scene.metadata.values["bmsca"], "bmabs": scene.metadata.values["bmabs"],
+            "alt": scene.metadata.values["alt"], "depolarization": np.array(scene.description["depolarization"])}
+
+
 def main():
     ref, Dataset = reference_package()
+    np.savez_compressed(HERE / "prepared_2boxclouds.npz", **prepared_fixture())
     (HERE / "philox_kat.json").write_text(json.dumps(philox_kat(), indent=1) + "\n")
     (HERE / "polarization_probe.json").write_text(json.dumps(polarization_probe(), indent=1) + "\n")
     np.savez_compressed(HERE / "amf_moments.npz", **amf_moments(ref))

@@ -133,13 +133,17 @@ def test_cuda_rejects_cloud_and_unprepared_use():
         CUDA().run_batch(BatchControls(1, 10))
 
 
-def test_reference_case_needs_a_preparer():
+def test_reference_case_needs_the_fixture_home(monkeypatch, tmp_path):
     from monki import ReferenceCase
     from monki.execution import CUDA
 
+    monkeypatch.delenv("MONKI_HOME", raising=False)
     case = ReferenceCase("clear", "testrun/MONKI_MLS_cloudfree_340_340_test.in")
-    with pytest.raises(NotImplementedError):
+    with pytest.raises(ValueError, match="MONKI_HOME"):
         CUDA().prepare(case)
+    # A home without the fixture fails before any device work.
+    with pytest.raises(FileNotFoundError):
+        CUDA(monki_home=tmp_path).prepare(case)
 
 
 def test_amf_moments_match_reference_implementation():
