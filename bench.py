@@ -318,6 +318,47 @@ def time_to_target(workload, ppc, device, seed, guided, scale=None):
     }
 
 
+# The reference's published time to AMF SE < 1 % (validation/README.md:230-233; Apple M4,
+# end to end, median of three seeds, 8,000 photons per column, AMFConvergence defaults).
+PUBLISHED_AMF = {
+    "clear": {"metal_m4_s": 0.466, "cpu_m4_4_threads_s": 2.074},
+    "layered_cloud": {"metal_m4_s": 26.160, "cpu_m4_4_threads_s": 232.839},
+}
+
+
+def reference_benchmark(device):
+    """The reference's own benchmark on GB300: its clear and layered-cloud fixtures (prepared
+    from its INPUT/DATA files, kept in tests/golden/), 8,000 photons per column, the
+    AMFConvergence defaults, seeds 23274, 714103 and 19088743, one warm-up run, wall time of
+    simulate() through the public API."""
+
+    import tempfile
+    from dataclasses import replace
+
+    from monki import AMFConvergence, simulate
+    from monki.execution import CUDA
+    from monki.preparation import scene_from_arrays
+
+    out = {}
+    for name, published in PUBLISHED_AMF.items():
+        scene = scene_from_arrays(np.load(ROOT / "tests" / "golden" / f"prepared_{name}.npz"))
+        runs = []
+        with tempfile.TemporaryDirectory() as tmp:
+            simulate(replace(scene, rounds=2), CUDA(device=device), f"{tmp}/warmup.nc")
+            for seed in (23274, 714103, 19088743):
+                start = time.perf_counter()
+                simulate(scene, CUDA(device=device, seed=seed), f"{tmp}/{seed}.nc", convergence=AMFConvergence())
+                elapsed = time.perf_counter() - start
+                receipt = json.loads(Path(f"{tmp}/{seed}.run.json").read_text())
+                runs.append({"seed": seed, "seconds": elapsed, "status": receipt["status"],
+                             "rounds": receipt["completed_rounds"], "scatters": receipt["scatters"]})
+        median = statistics.median(r["seconds"] for r in runs)
+        out[name] = {"median_s": median, "runs": runs, **published,
+                     "speedup_vs_metal_m4": published["metal_m4_s"] / median,
+                     "speedup_vs_cpu_m4": published["cpu_m4_4_threads_s"] / median}
+    return out
+
+
 def batched_scenes(device, scale):
     """The batched workload: 64 seeded scenes of uneven size (grids 8-128 columns a side,
     20-60 layers, log-uniform photon budgets scaled by ``scale``, lognormal cloud fields),
@@ -355,6 +396,8 @@ def main():
     parser.add_argument("--no-target", action="store_true", help="skip the time-to-target runs")
     parser.add_argument("--no-learned", action="store_true", help="skip the learned-importance run")
     parser.add_argument("--no-batched", action="store_true", help="skip the batched-scenes run")
+    parser.add_argument("--no-reference-benchmark", action="store_true",
+                        help="skip the reference's time-to-AMF-precision benchmark")
     parser.add_argument("--batched-scale", type=float, default=0.05,
                         help="photon budgets of the batched scenes, as a fraction of the workload's")
     parser.add_argument("--photons-per-column", type=int, default=0)
@@ -602,6 +645,9 @@ def main():
 
     if not args.no_batched:
         line["batched"] = batched_scenes(local, args.batched_scale)
+
+    if not args.no_reference_benchmark:
+        line["reference_benchmark"] = reference_benchmark(local)
 
     if not args.no_target:
         # FP32 bias of the product transport against the FP64 build, per Stokes component.

@@ -322,3 +322,39 @@ def prepare_reference_case(case: ReferenceCase, home) -> TransportScene:
     return TransportScene(case.name, tables, metadata, case.photons_per_column, case.rounds, case.backward,
                           {"fixture": case.input_file, "depolarization": depol,
                            "rayleigh_optical_depth": float(bmsca.sum()), "o3_optical_depth": float(bmabs.sum())})
+
+
+def scene_arrays(scene: TransportScene, fixture_description: dict) -> dict:
+    """Arrays that rebuild a prepared fixture scene without the fixture files
+    (``scene_from_arrays``): the table stream and the product metadata's inputs."""
+
+    v = scene.metadata.values
+    return {
+        "tables": scene.tables,
+        "levels_km": v["alt"] / 1000.0,
+        "bmsca": v["bmsca"][0],
+        "bmabs": v["bmabs"][0],
+        "baer": v["baer"][..., 0].transpose(3, 2, 1, 0),
+        "geometry": np.array([v["theta0"][0], v["phi0"][0], v["asurf"][0], v["x_unit"][0], v["y_unit"][0], v["wav"][0]]),
+        "view_zeniths": v["theta"],
+        "view_azimuths": v["phi"],
+        "sizes": np.array([scene.photons_per_column, scene.rounds]),
+        "name": np.array(scene.name),
+    }
+
+
+def scene_from_arrays(arrays) -> TransportScene:
+    """The TransportScene of ``scene_arrays``."""
+
+    tables = np.asarray(arrays["tables"])
+    nx, ny, nz, nmat = (int(v) for v in tables[1:5])
+    sza, saa, albedo, x_unit, y_unit, wavelength = (float(v) for v in arrays["geometry"])
+    metadata = scene_metadata(
+        str(arrays["name"]), np.asarray(arrays["levels_km"]), nx=nx, ny=ny, nmat=nmat, solar_zenith=sza,
+        solar_azimuth=saa, view_zeniths=list(arrays["view_zeniths"]), view_azimuths=list(arrays["view_azimuths"]),
+        albedo=albedo, gas_scattering=np.asarray(arrays["bmsca"]), gas_absorption=np.asarray(arrays["bmabs"]),
+        particle_optical_depth=np.asarray(arrays["baer"]), save_path=bool(tables[10]), pixel_km=(x_unit, y_unit),
+        wavelength_nm=wavelength,
+    )
+    ppc, rounds = (int(v) for v in arrays["sizes"])
+    return TransportScene(str(arrays["name"]), tables, metadata, ppc, rounds, False, {})

@@ -357,9 +357,31 @@ def prepared_fixture():
             "alt": scene.metadata.values["alt"], "depolarization": np.array(scene.description["depolarization"])}
 
 
+def benchmark_scenes():
+    """The two cases of the reference's time-to-AMF-precision benchmark
+    (validation/benchmark_amf_convergence.py: validation/cases/{clear,layered-cloud}.json at
+    8,000 photons per column and an 8,192-round cap), prepared by monki.preparation."""
+
+    sys.path.insert(0, str(REPO / "monki-gpu_gb300"))
+    from dataclasses import replace
+
+    from monki import ReferenceCase
+    from monki.preparation import prepare_reference_case, scene_arrays
+
+    out = {}
+    for name in ("clear", "layered-cloud"):
+        spec = json.loads((REFERENCE / "validation" / "cases" / f"{name}.json").read_text())
+        case = replace(ReferenceCase(**spec), photons_per_column=8000, rounds=8192)
+        scene = prepare_reference_case(case, REFERENCE / "fortran" / "monki" / "upstream")
+        out[name] = scene_arrays(scene, {})
+    return out
+
+
 def main():
     ref, Dataset = reference_package()
     np.savez_compressed(HERE / "prepared_2boxclouds.npz", **prepared_fixture())
+    for name, arrays in benchmark_scenes().items():
+        np.savez_compressed(HERE / f"prepared_{name.replace('-', '_')}.npz", **arrays)
     (HERE / "philox_kat.json").write_text(json.dumps(philox_kat(), indent=1) + "\n")
     (HERE / "polarization_probe.json").write_text(json.dumps(polarization_probe(), indent=1) + "\n")
     np.savez_compressed(HERE / "amf_moments.npz", **amf_moments(ref))
