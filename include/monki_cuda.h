@@ -124,6 +124,15 @@ int monki_cuda_set_importance_weights(void *session, const double *weights, size
 int monki_cuda_inspect(const double *tables, size_t table_count, int fp64, int32_t *uniform_top,
                        double *tau_above, size_t tau_capacity, char *err, size_t errlen);
 
+/* Host-only check of the equal-extinction rectangles (no GPU needed; no counterpart in
+ * the reference, whose walks step face by face). Writes, for every cell below the
+ * uniform top (i + nx * (j + ny * k)), the word the cell walks read: bytes 0-3 are the
+ * cells of its rectangle before it along -x, after it along +x, before it along -y and
+ * after it along +y (each at most 255). *written receives the cell count (0 when the
+ * scene has no horizontally varying layer). */
+int monki_cuda_inspect_rectangles(const double *tables, size_t table_count, int fp64, uint32_t *extent,
+                                  size_t capacity, size_t *written, char *err, size_t errlen);
+
 /* Transport without device allocation; no counterpart in the reference. For callers
  * that cannot call cudaMalloc (an application that owns all device memory through its
  * own arena, a real-time loop that must not allocate while running, a plugin host that

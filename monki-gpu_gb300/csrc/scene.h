@@ -20,6 +20,12 @@
 //   band[nx * ny * uniform_top]  extinction of every cell below the horizontally uniform
 //                            top (the only cells a cell walk visits), 16-byte aligned and
 //                            padded, staged whole into shared memory when it fits
+//   extent[nx * ny * uniform_top]  per band cell, the rectangle of equal-extinction cells
+//                            of its layer that holds it (uint32: bytes 0-3 = cells of the
+//                            rectangle before it in -x, after it in +x, before it in -y,
+//                            after it in +y, each at most 255), from a greedy partition of
+//                            every band layer; a straight path inside one rectangle sees a
+//                            single extinction, so the free-path walk crosses it in one step
 #pragma once
 #include <stdint.h>
 
@@ -69,6 +75,7 @@ struct SceneView {
     const int* guide[kMaxSpecies];
     const T* band;          // extinction below the uniform top, i + nx * (j + ny * k)
     uint32_t band_bytes;    // padded size when staged in shared memory, else 0
+    const uint32_t* extent; // equal-extinction rectangles of the band cells, or null
 };
 
 // Guided transport (detector-directed sampling at particle scatters and Russian

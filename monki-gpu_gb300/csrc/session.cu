@@ -41,6 +41,7 @@ struct Config {
     bool importance = false;     // tally per-cell importance (pilot runs)
     bool graphs = true;          // replay each batch of wavefront iterations as a CUDA graph
     bool orders = false;         // scattering-order diagnostics (single scattering, locations)
+    bool rectangles = true;      // cross equal-extinction rectangles of the band in one step
 };
 
 Config parse_config(const char* text) {
@@ -94,6 +95,7 @@ Config parse_config(const char* text) {
         } else if (key == "importance") c.importance = as_int(0, 1) != 0;
         else if (key == "graphs") c.graphs = as_int(0, 1) != 0;
         else if (key == "orders") c.orders = as_int(0, 1) != 0;
+        else if (key == "rectangles") c.rectangles = as_int(0, 1) != 0;
         else throw std::runtime_error("Unknown config key: " + key);
     }
     if (c.block % 32) throw std::runtime_error("block must be a multiple of 32");
@@ -227,12 +229,12 @@ struct Packed {
     std::vector<int> guides;
     size_t cells, zunit, zsum, ssalb_gas, albedo, tau_above, layer_beta, vprefix, run_lo, run_hi;
     size_t lut_f[kMaxSpecies], lut_cos[kMaxSpecies], lut_cdf[kMaxSpecies], guide[kMaxSpecies];
-    size_t band, band_count;
+    size_t band, band_count, extent;
     int uniform_top;
 };
 
 template <typename T>
-Packed<T> pack(const Prepared& p, bool uniform_prefix) {
+Packed<T> pack(const Prepared& p, bool uniform_prefix, bool rectangles = true) {
     Packed<T> k{};
     auto& v = k.values;
     const size_t cols = size_t(p.nx) * p.ny, ncell = cols * p.nz;
@@ -271,6 +273,42 @@ Packed<T> pack(const Prepared& p, bool uniform_prefix) {
     k.band_count = cols * size_t(std::min(k.uniform_top, p.nz - 1));
     k.band = reserve(k.band_count + 4);
     for (size_t c = 0; c < k.band_count; ++c) v[k.band + c] = T(p.beta[c]);
+    // Equal-extinction rectangles of every band layer (greedy: from the first unassigned
+    // cell in row order, widen along +x while the extinction is equal, then grow along +y
+    // while the whole row segment is equal), stored per cell as its distances in cells to
+    // the rectangle's faces, clamped to 255 (a clamped rectangle is still uniform).
+    k.extent = SIZE_MAX;
+    if (rectangles && k.band_count) {
+        k.extent = k.guides.size();
+        k.guides.resize(k.extent + k.band_count, 0);
+        std::vector<char> taken(cols);
+        for (size_t layer = 0; layer < k.band_count / cols; ++layer) {
+            const T* b = v.data() + k.band + layer * cols;
+            std::fill(taken.begin(), taken.end(), 0);
+            for (int j0 = 0; j0 < p.ny; ++j0)
+                for (int i0 = 0; i0 < p.nx; ++i0) {
+                    const size_t c0 = size_t(i0) + size_t(p.nx) * j0;
+                    if (taken[c0]) continue;
+                    const T b0 = b[c0];
+                    int i1 = i0;
+                    while (i1 + 1 < p.nx && !taken[c0 + (i1 + 1 - i0)] && b[c0 + (i1 + 1 - i0)] == b0) ++i1;
+                    int j1 = j0;
+                    for (bool grow = true; grow && j1 + 1 < p.ny;) {
+                        const size_t row = size_t(p.nx) * (j1 + 1);
+                        for (int i = i0; i <= i1 && grow; ++i) grow = !taken[row + i] && b[row + i] == b0;
+                        if (grow) ++j1;
+                    }
+                    for (int j = j0; j <= j1; ++j)
+                        for (int i = i0; i <= i1; ++i) {
+                            const size_t c = size_t(i) + size_t(p.nx) * j;
+                            taken[c] = 1;
+                            const uint32_t word = uint32_t(std::min(i - i0, 255)) | (uint32_t(std::min(i1 - i, 255)) << 8) |
+                                                  (uint32_t(std::min(j - j0, 255)) << 16) | (uint32_t(std::min(j1 - j, 255)) << 24);
+                            k.guides[k.extent + layer * cols + c] = int(word);
+                        }
+                }
+        }
+    }
     k.tau_above = reserve(p.nz);
     {
         // tau_above[k] = sum over physical layers above k of thickness * extinction,
@@ -411,6 +449,7 @@ SceneView<T> make_view(const Prepared& p, const Packed<T>& k, void* base) {
     s.band = tv + k.band;
     const size_t band_bytes = align_up(k.band_count * sizeof(T), 16);
     s.band_bytes = (k.band_count && band_bytes <= kBandMaxBytes) ? uint32_t(band_bytes) : 0u;
+    s.extent = k.extent == SIZE_MAX ? nullptr : reinterpret_cast<const uint32_t*>(gv + k.extent);
     for (int sp = 0; sp < p.ntypes; ++sp) {
         s.lut_n[sp] = p.luts[sp].n; s.ssalb_aer[sp] = T(p.luts[sp].ssalb);
         s.znorm[sp] = T(analog_norm(p.luts[sp], p.nmat));
@@ -422,7 +461,7 @@ SceneView<T> make_view(const Prepared& p, const Packed<T>& k, void* base) {
 
 template <typename T>
 void upload(Session& s) {
-    Packed<T> k = pack<T>(s.prep, s.cfg.uniform_prefix);
+    Packed<T> k = pack<T>(s.prep, s.cfg.uniform_prefix, s.cfg.rectangles);
     size_t bytes = k.values.size() * sizeof(T) + k.guides.size() * sizeof(int);
     check(cudaMalloc(&s.scene, std::max<size_t>(bytes, 16)), "cudaMalloc(scene)");
     check(cudaMemcpy(s.scene, k.values.data(), k.values.size() * sizeof(T), cudaMemcpyHostToDevice), "upload(scene)");
@@ -1056,6 +1095,25 @@ int monki_cuda_inspect(const double* tables, size_t table_count, int fp64, int32
             *uniform_top = k.uniform_top;
             for (int z = 0; z < p.nz; ++z) tau_above[z] = double(k.values[k.tau_above + z]);
         }
+        return 0;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        return 1;
+    }
+}
+
+int monki_cuda_inspect_rectangles(const double* tables, size_t table_count, int fp64, uint32_t* extent,
+                                  size_t capacity, size_t* written, char* err, size_t errlen) {
+    try {
+        Prepared p = parse(tables, table_count);
+        auto copy = [&](const auto& k) {
+            const size_t n = k.extent == SIZE_MAX ? 0 : k.band_count;
+            if (n > capacity) throw std::runtime_error("extent needs one word per band cell");
+            for (size_t c = 0; c < n; ++c) extent[c] = uint32_t(k.guides[k.extent + c]);
+            *written = n;
+        };
+        if (fp64) copy(pack<double>(p, true));
+        else copy(pack<float>(p, true));
         return 0;
     } catch (const std::exception& e) {
         write_error(err, errlen, e.what());

@@ -254,6 +254,58 @@ __device__ __forceinline__ void slide(int& i, T& x, int sgn, T h, T unit, int n)
     x = unit - rest;
 }
 
+// Along one horizontal axis inside an equal-extinction rectangle: a slide when the
+// rectangle reaches beyond the current cell (extra > 0), else the in-cell step of advance.
+template <typename T>
+__device__ __forceinline__ void move_within(int& i, T& x, int sgn, T h, T unit, int n, int extra) {
+    if (extra) slide(i, x, sgn, h, unit, n);
+    else x = fmax(T(0), x - h);
+}
+
+// Whole cells of the equal-extinction rectangle around band cell (i, j, k) beyond the
+// current one in the direction of travel: ex along x, ey along y (0 without rectangles).
+template <typename T>
+__device__ __forceinline__ void rectangle_reach(const SceneView<T>& s, int i, int j, int k, int is, int js, int& ex,
+                                                int& ey) {
+    ex = 0; ey = 0;
+    if (s.extent) {
+        const uint32_t w = __ldg(s.extent + i + s.nx * (j + s.ny * k));
+        ex = int((w >> (is > 0 ? 8 : 0)) & 0xFFu);
+        ey = int((w >> (js > 0 ? 24 : 16)) & 0xFFu);
+    }
+}
+
+// advance through an equal-extinction rectangle: to its nearest face in one step. A
+// straight path inside the rectangle meets one extinction, so this is the face-by-face
+// walk of ADVANCE with the interior faces skipped; with ex = ey = 0 it is advance exactly.
+template <typename T>
+__device__ __forceinline__ T advance_rectangle(const SceneView<T>& s, int& i, int& j, int& k, T& x, T& y, T& z,
+                                               int is, int js, int ks, T aa, T ba, T ca, T ai, T bi, T ci, int ex,
+                                               int ey) {
+    const T dx = (ex ? x + T(ex) * s.xunit : x) * ai;
+    const T dy = (ey ? y + T(ey) * s.yunit : y) * bi;
+    const T dz = z * ci;
+    const T dist = fmin(dx, fmin(dy, dz));
+    if (dx == dist) {
+        // The rectangle lies inside the grid, so one wrap brings i back into [0, nx).
+        i += is * (ex + 1); i = i < 0 ? i + s.nx : (i >= s.nx ? i - s.nx : i);
+        x = s.xunit;
+        move_within(j, y, js, ba * dist, s.yunit, s.ny, ey);
+        z = fmax(T(0), z - ca * dist);
+    } else if (dy == dist) {
+        j += js * (ey + 1); j = j < 0 ? j + s.ny : (j >= s.ny ? j - s.ny : j);
+        move_within(i, x, is, aa * dist, s.xunit, s.nx, ex);
+        y = s.yunit;
+        z = fmax(T(0), z - ca * dist);
+    } else {
+        k += ks;
+        move_within(i, x, is, aa * dist, s.xunit, s.nx, ex);
+        move_within(j, y, js, ba * dist, s.yunit, s.ny, ey);
+        if (k >= 0 && k < s.nz) z = __ldg(s.zunit + k);
+    }
+    return dist;
+}
+
 // One jump through the horizontally uniform run that contains layer k, from the current
 // position (z: vertical distance to the exit face in direction ks). Returns 0 for an
 // interaction inside the run, 1 for the surface, 2 for escape through the top, and -1
@@ -299,15 +351,34 @@ __device__ __forceinline__ int uniform_jump(const SceneView<T>& s, int& k, T& z,
             if (outcome != 2 && record && inside) path.run(s.zunit, min(m0, end), max(m0, end), ci);
             if (outcome == -1) z = __ldg(s.zunit + k);
         } else {
-            // The interaction lies inside the run: find its layer.
+            // The interaction lies inside the run: find its layer m, the first one (from
+            // m0 in the direction of travel) whose vertical optical depth, summed from m0,
+            // exceeds need. A binary search over the prefix V: about log2 of the run
+            // length steps for every lane, where a layer-by-layer scan diverged across
+            // the warp with runs of up to nz layers.
             const T need = remains * ca;
-            int m = m0;
-            T before = T(0);  // vertical optical depth of the whole layers crossed before m
-            for (;;) {
-                const T bm = __ldg(s.layer_beta + m) * __ldg(s.zunit + m);
-                if (before + bm > need || m == end) break;
-                before += bm;
-                m += ks;
+            int m;
+            T before;  // vertical optical depth of the whole layers crossed before m
+            if (ks > 0) {
+                const T v0 = __ldg(V + m0);
+                int lo = m0, hi = end;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (__ldg(V + mid + 1) - v0 > need) hi = mid;
+                    else lo = mid + 1;
+                }
+                m = lo;
+                before = __ldg(V + m) - v0;
+            } else {
+                const T v0 = __ldg(V + m0 + 1);
+                int lo = end, hi = m0;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (v0 - __ldg(V + mid) > need) lo = mid;
+                    else hi = mid - 1;
+                }
+                m = lo;
+                before = v0 - __ldg(V + m + 1);
             }
             const T slant_before = (ks > 0 ? __ldg(Z + m) - __ldg(Z + m0) : __ldg(Z + m0 + 1) - __ldg(Z + m + 1)) * ci;
             remains -= before * ci;
@@ -423,11 +494,14 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
                     continue;
                 }
                 const T bv = k < top ? band_beta<T>(s, band, i, j, k) : T(0);
+                int ex = 0, ey = 0;
+                if (k < top) rectangle_reach(s, i, j, k, is, js, ex, ey);
                 if (bv > eps) {
                     const T de = remains / bv;
-                    if (de < x * ai && de < y * bi && de < z * ci) {
-                        x = fmax(T(0), x - aa * de);
-                        y = fmax(T(0), y - ba * de);
+                    if (de < (ex ? x + T(ex) * s.xunit : x) * ai && de < (ey ? y + T(ey) * s.yunit : y) * bi &&
+                        de < z * ci) {
+                        move_within(i, x, is, aa * de, s.xunit, s.nx, ex);
+                        move_within(j, y, js, ba * de, s.yunit, s.ny, ey);
                         z = fmax(T(0), z - ca * de);
                         if (record) {
                             if (acc_k != k) {
@@ -441,7 +515,7 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
                     }
                 }
                 const int k_old = k;
-                const T dist = advance(s, i, j, k, x, y, z, is, js, ks, aa, ba, ca, ai, bi, ci);
+                const T dist = advance_rectangle(s, i, j, k, x, y, z, is, js, ks, aa, ba, ca, ai, bi, ci, ex, ey);
                 if (record) {
                     if (acc_k != k_old) {
                         if (acc_k >= 0) path.add(acc_k, acc);
@@ -634,6 +708,8 @@ wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ b
                     break;
                 }
                 if (++rsteps > ctl.max_steps) { capped = true; break; }
+                // Face by face: view rays cross few band cells, and the rectangle
+                // lookup costs more than it skips here (measured on the box cloud).
                 const T bv = band_beta<T>(s, band, ri, rj, rk);
                 const T dist = advance(s, ri, rj, rk, rx, ry, rz, is, js, ks, aa, ba, ca, ai, bi, ci);
                 tau += dist * bv;

@@ -61,6 +61,7 @@ class CUDA(Backend):
         roulette_scale=None,
         device_statistics: bool = True,
         orders: bool = False,
+        rectangles: bool = True,
         monki_home=None,
         library=None,
     ):
@@ -111,6 +112,9 @@ class CUDA(Backend):
         if orders and engine != "wavefront":
             raise ValueError("scattering-order diagnostics need engine='wavefront'")
 
+        if type(rectangles) is not bool:
+            raise ValueError("rectangles must be a bool")
+
         self.device = device
         self.save_path = save_path
         self.profile = profile
@@ -130,6 +134,10 @@ class CUDA(Backend):
         # Scattering-order diagnostics (single / multiple scattering, contribution by event
         # location), the reference's save_scats outputs.
         self.orders = orders
+        # The free-path walk crosses each rectangle of equal-extinction cells of a horizontally
+        # varying layer in one step (the same path in exact arithmetic as the face-by-face
+        # walk); False keeps the face-by-face walk.
+        self.rectangles = rectangles
         self.monki_home = monki_home
         # Per-cell roulette scale (nx, ny, nz) applied at every prepare; set_roulette_scale
         # changes it for the prepared session only.
@@ -207,6 +215,7 @@ class CUDA(Backend):
             + (self.guided.config() if self.guided is not None else "")
             + (",importance=1" if self.importance_tally else "")
             + (",orders=1" if self.orders else "")
+            + ("" if self.rectangles else ",rectangles=0")
         ).encode()
         handle = native.monki_cuda_create(
             self.device,
@@ -510,6 +519,7 @@ class CUDA(Backend):
             self.pool,
             self.walk,
             self.orders,
+            self.rectangles,
             self.guided,
             self.importance_tally,
         )

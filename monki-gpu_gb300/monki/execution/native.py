@@ -35,6 +35,10 @@ _SIGNATURES = {
         ctypes.c_int,
         [_F64P, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(ctypes.c_int32), _F64P, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t],
     ),
+    "monki_cuda_inspect_rectangles": (
+        ctypes.c_int,
+        [_F64P, ctypes.c_size_t, ctypes.c_int, _U32P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t), ctypes.c_char_p, ctypes.c_size_t],
+    ),
     "monki_cuda_set_roulette_scale": (
         ctypes.c_int,
         [ctypes.c_void_p, _F64P, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t],

@@ -58,6 +58,60 @@ def test_uniform_top_prefix_matches_reference_packer(native, name, fp64):
     np.testing.assert_allclose(tau, case["tau_above"], rtol=1e-6 if not fp64 else 1e-6, atol=1e-9)
 
 
+def _rectangle_reach(native, scene, fp64):
+    """(layers, reach[4, layers, ny, nx]) from the packer: cells before / after along x, y."""
+
+    from monki.execution.native import F64P, U32P
+
+    tables = np.ascontiguousarray(scene.tables)
+    nmat, nx, ny, nz, angles = scene.shape
+    extent = np.zeros(nx * ny * nz, dtype=np.uint32)
+    written = ctypes.c_size_t(0)
+    err = ctypes.create_string_buffer(512)
+    status = native.monki_cuda_inspect_rectangles(tables.ctypes.data_as(F64P), tables.size, fp64, extent.ctypes.data_as(U32P),
+                                                  extent.size, ctypes.byref(written), err, len(err))
+    assert status == 0, err.value
+    layers = written.value // (nx * ny)
+    words = extent[: written.value].reshape((layers, ny, nx))
+    return layers, np.stack([(words >> shift) & 0xFF for shift in (0, 8, 16, 24)]).astype(int)
+
+
+@pytest.mark.parametrize("name", ["box_cloud", "layered_cloud", "clear_sky"])
+@pytest.mark.parametrize("fp64", [0, 1])
+def test_equal_extinction_rectangles_tile_each_band_layer(native, name, fp64):
+    """Every band cell's rectangle holds it and lies inside the grid, all of its cells
+    report the same rectangle (so the rectangles tile the layer), and it has a single
+    extinction at transport precision, the only property a cell walk relies on."""
+
+    import monki.scenes as scenes
+    from monki.importance import parse_tables
+
+    scene = getattr(scenes, name)(2, 1)
+    nmat, nx, ny, nz, angles = scene.shape
+    beta = parse_tables(scene.tables).beta.astype(np.float64 if fp64 else np.float32)
+    layers, reach = _rectangle_reach(native, scene, fp64)
+    rectangles = []
+    for k in range(layers):
+        seen = set()
+        for j in range(ny):
+            for i in range(nx):
+                i0, i1 = i - reach[0, k, j, i], i + reach[1, k, j, i]
+                j0, j1 = j - reach[2, k, j, i], j + reach[3, k, j, i]
+                assert 0 <= i0 <= i1 < nx and 0 <= j0 <= j1 < ny
+                for jj in range(j0, j1 + 1):
+                    for ii in range(i0, i1 + 1):
+                        r = reach[:, k, jj, ii]
+                        assert (ii - r[0], ii + r[1], jj - r[2], jj + r[3]) == (i0, i1, j0, j1)
+                assert np.all(beta[i0 : i1 + 1, j0 : j1 + 1, k] == beta[i, j, k])
+                seen.add((i0, j0))
+        rectangles.append(len(seen))
+    if name == "box_cloud":
+        # A cloud layer: the cloud block and four clear rectangles around it.
+        assert max(rectangles) == 5
+    if name == "clear_sky":
+        assert layers == 0
+
+
 @pytest.mark.parametrize("field,value", [(0, 3), (4, 4), (7, 1), (11, 1), (6, 4)])
 def test_packer_rejects_unsupported_tables(native, field, value):
     import monki.scenes as scenes
