@@ -53,6 +53,7 @@ struct SceneView {
     int nx, ny, nz, nmat, angles, ntypes, paths, uniform_top;
     int lut_n[kMaxSpecies];
     T xunit, yunit, depol;
+    T xinv, yinv;        // 1 / xunit, 1 / yunit
     T a0, b0, c0, phi0;  // solar propagation direction cosines and azimuth (rad)
     T va[kMaxViews], vb[kMaxViews], vc[kMaxViews], vphi[kMaxViews];
     T vsin[kMaxViews];          // sqrt(max(eps, 1 - vc^2))

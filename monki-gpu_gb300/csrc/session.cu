@@ -432,6 +432,7 @@ SceneView<T> make_view(const Prepared& p, const Packed<T>& k, void* base) {
     s.nx = p.nx; s.ny = p.ny; s.nz = p.nz; s.nmat = p.nmat; s.angles = p.angles; s.ntypes = p.ntypes;
     s.paths = p.paths; s.uniform_top = k.uniform_top;
     s.xunit = T(p.xunit); s.yunit = T(p.yunit); s.depol = T(p.depol);
+    s.xinv = T(1) / s.xunit; s.yinv = T(1) / s.yunit;
     const double th0 = kDegToRad * p.vartheta0, ph0 = kDegToRad * p.phi0;
     s.a0 = T(std::sin(th0) * std::cos(ph0)); s.b0 = T(std::sin(th0) * std::sin(ph0)); s.c0 = T(std::cos(th0));
     s.phi0 = T(ph0);

@@ -235,30 +235,31 @@ struct PathRecord {
 };
 
 // Move a distance h >= 0 along one horizontal axis of the periodic grid: x is the distance
-// to the next face in direction sgn. Equivalent to the face-by-face walk of ADVANCE.
+// to the next face in direction sgn, inv = 1 / unit. Equivalent to the face-by-face walk
+// of ADVANCE: the whole cells crossed come from one multiply, corrected by one cell either
+// way, and a face hit to rounding leaves the photon on the face.
 template <typename T>
-__device__ __forceinline__ void slide(int& i, T& x, int sgn, T h, T unit, int n) {
+__device__ __forceinline__ void slide(int& i, T& x, int sgn, T h, T unit, T inv, int n) {
     if (h < x) { x = x - h; return; }
     T rest = h - x;
-    T whole = floor(rest / unit);
+    T whole = floor(rest * inv);
     rest -= whole * unit;
-    if (rest < T(0)) rest = T(0);
     // 32-bit counts: no float-to-int64 conversion or 64-bit modulo (slow conversion and
     // FP64-pipe work on this GPU); 4e9 faces exceed any travel a float position resolves.
     uint32_t cross = 1u + uint32_t(fmin(whole, T(4.0e9)));
+    if (rest < T(0)) { rest += unit; --cross; if (rest < T(0)) rest = T(0); }
     if (rest >= unit) { rest -= unit; ++cross; }
-    int step = int(cross % uint32_t(n));
+    const int step = int(cross < uint32_t(n) ? cross : cross % uint32_t(n));
     i += sgn * step;
-    i %= n;
-    if (i < 0) i += n;
+    i = i < 0 ? i + n : (i >= n ? i - n : i);
     x = unit - rest;
 }
 
 // Along one horizontal axis inside an equal-extinction rectangle: a slide when the
 // rectangle reaches beyond the current cell (extra > 0), else the in-cell step of advance.
 template <typename T>
-__device__ __forceinline__ void move_within(int& i, T& x, int sgn, T h, T unit, int n, int extra) {
-    if (extra) slide(i, x, sgn, h, unit, n);
+__device__ __forceinline__ void move_within(int& i, T& x, int sgn, T h, T unit, T inv, int n, int extra) {
+    if (extra) slide(i, x, sgn, h, unit, inv, n);
     else x = fmax(T(0), x - h);
 }
 
@@ -290,17 +291,17 @@ __device__ __forceinline__ T advance_rectangle(const SceneView<T>& s, int& i, in
         // The rectangle lies inside the grid, so one wrap brings i back into [0, nx).
         i += is * (ex + 1); i = i < 0 ? i + s.nx : (i >= s.nx ? i - s.nx : i);
         x = s.xunit;
-        move_within(j, y, js, ba * dist, s.yunit, s.ny, ey);
+        move_within(j, y, js, ba * dist, s.yunit, s.yinv, s.ny, ey);
         z = fmax(T(0), z - ca * dist);
     } else if (dy == dist) {
         j += js * (ey + 1); j = j < 0 ? j + s.ny : (j >= s.ny ? j - s.ny : j);
-        move_within(i, x, is, aa * dist, s.xunit, s.nx, ex);
+        move_within(i, x, is, aa * dist, s.xunit, s.xinv, s.nx, ex);
         y = s.yunit;
         z = fmax(T(0), z - ca * dist);
     } else {
         k += ks;
-        move_within(i, x, is, aa * dist, s.xunit, s.nx, ex);
-        move_within(j, y, js, ba * dist, s.yunit, s.ny, ey);
+        move_within(i, x, is, aa * dist, s.xunit, s.xinv, s.nx, ex);
+        move_within(j, y, js, ba * dist, s.yunit, s.yinv, s.ny, ey);
         if (k >= 0 && k < s.nz) z = __ldg(s.zunit + k);
     }
     return dist;
@@ -395,8 +396,8 @@ __device__ __forceinline__ int uniform_jump(const SceneView<T>& s, int& k, T& z,
         }
     }
     if (outcome != 2) {
-        slide(i, x, is, aa * travelled, s.xunit, s.nx);
-        slide(j, y, js, ba * travelled, s.yunit, s.ny);
+        slide(i, x, is, aa * travelled, s.xunit, s.xinv, s.nx);
+        slide(j, y, js, ba * travelled, s.yunit, s.yinv, s.ny);
     }
     return outcome;
 }
@@ -500,8 +501,8 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
                     const T de = remains / bv;
                     if (de < (ex ? x + T(ex) * s.xunit : x) * ai && de < (ey ? y + T(ey) * s.yunit : y) * bi &&
                         de < z * ci) {
-                        move_within(i, x, is, aa * de, s.xunit, s.nx, ex);
-                        move_within(j, y, js, ba * de, s.yunit, s.ny, ey);
+                        move_within(i, x, is, aa * de, s.xunit, s.xinv, s.nx, ex);
+                        move_within(j, y, js, ba * de, s.yunit, s.yinv, s.ny, ey);
                         z = fmax(T(0), z - ca * de);
                         if (record) {
                             if (acc_k != k) {
@@ -530,15 +531,18 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
             }
             if (PATHS && acc_k >= 0) path.add(acc_k, acc);
             if (outcome == 4) { ++paused; break; }  // budget spent: the walk resumes next iteration
-            if (outcome == 3) { atomicOr(failure, kHistoryCap); pid = kNone; continue; }
-            if (outcome == 2) { pid = kNone; continue; }
+            // A finished history leaves its slot empty until the next launch, where it is
+            // refilled before the walks start: claiming and walking a second photon here
+            // would make the whole warp wait on the few lanes whose photon escaped.
+            if (outcome == 3) { atomicOr(failure, kHistoryCap); pid = kNone; break; }
+            if (outcome == 2) { pid = kNone; break; }
             int kind;
             if (outcome == 1) {
                 if (PATHS && k1 == -2) { k1 = -1; init_part = T(0); }
                 k = 0;
                 z = T(0);
                 weight *= __ldg(s.albedo + i + s.nx * j);
-                if (weight < eps) { pid = kNone; continue; }
+                if (weight < eps) { pid = kNone; break; }
                 kind = 255;
             } else {
                 if (PATHS && k1 == -2) {
@@ -551,7 +555,7 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
                 for (int q = 0; q < s.ntypes; ++q)
                     if (__ldg(cellp + 1 + q) > rtemp) { sp = q; break; }
                 weight *= sp < 0 ? __ldg(s.ssalb_gas + k) : s.ssalb_aer[sp];
-                if (weight < eps) { pid = kNone; continue; }
+                if (weight < eps) { pid = kNone; break; }
                 kind = sp + 1;
             }
             ++scatters;
