@@ -256,6 +256,8 @@ class MieSpecies:
     albedo: float
     extinction_efficiency: float
     geometric_cross_section: float
+    f34: np.ndarray | None = None
+    f44: np.ndarray | None = None
 
 
 def _suffix(wavelength_nm: float) -> str:
@@ -270,7 +272,8 @@ def mie_species(mie_dir, lut_start: str, sc_start: str, wavelength_nm: float, nm
     table = np.loadtxt(Path(mie_dir) / f"{lut_start}{suffix}")
     angles = table[::-1, 0]
     cosines = np.cos(np.deg2rad(angles))
-    f11, f22, f33, f12 = (table[::-1, c] for c in (1, 2, 3, 5))
+    # Columns: angle, F11, F22, F33, F44, F12, F34 (main_routines_general_mod.f90:790).
+    f11, f22, f33, f44, f12, f34 = (table[::-1, c] for c in (1, 2, 3, 4, 5, 6))
     bound = f11 + np.abs(f12) if nmat > 1 else f11.copy()
     cdf = np.zeros_like(cosines)
     for i in range(1, len(cosines)):
@@ -280,7 +283,7 @@ def mie_species(mie_dir, lut_start: str, sc_start: str, wavelength_nm: float, nm
     albedo = float(lines[7][32:57])
     q_ext = float(lines[9][32:57])
     geometric = float(lines[11][32:57])
-    return MieSpecies(cosines, cdf, f11, f22, f33, f12, albedo, q_ext, geometric)
+    return MieSpecies(cosines, cdf, f11, f22, f33, f12, albedo, q_ext, geometric, f34, f44)
 
 
 def prepare_reference_case(case: ReferenceCase, home) -> TransportScene:
@@ -290,8 +293,6 @@ def prepare_reference_case(case: ReferenceCase, home) -> TransportScene:
     fixture = parse_input(home / "INPUT" / case.input_file)
     if (fixture.k_source, fixture.k_detector, fixture.k_register) != (1, 1, 1):
         raise NotImplementedError("only a TOA source, detector and output grid are supported")
-    if case.backward:
-        raise NotImplementedError("backward transport is not implemented")
     depol, bmsca, bmabs = molecular_optics(fixture, home / "DATA" / "abs_data" / "O3T_BP.dat")
     species = [mie_species(home / "DATA" / "Mie_data", lu, sc, fixture.wavelength_nm, fixture.nmat)
                for sc, lu in zip(fixture.species_sc, fixture.species_lu, strict=True)]
@@ -302,7 +303,7 @@ def prepare_reference_case(case: ReferenceCase, home) -> TransportScene:
     elif fixture.cloud_input != "baer":
         raise ValueError("cloud input must be baer or ncol")
     levels_km = fixture.altitude_km
-    particles = [(s.cosines, s.cdf, s.f11, s.f22, s.f33, s.f12, s.albedo) for s in species]
+    particles = [(s.cosines, s.cdf, s.f11, s.f22, s.f33, s.f12, s.albedo, s.f34, s.f44) for s in species]
     x_unit, y_unit = fixture.x_dim / fixture.nx, fixture.y_dim / fixture.ny
     tables = build_tables(
         nx=fixture.nx, ny=fixture.ny, levels_km=levels_km, nmat=fixture.nmat,
@@ -310,7 +311,7 @@ def prepare_reference_case(case: ReferenceCase, home) -> TransportScene:
         view_zeniths=list(case.view_zeniths), view_azimuths=[case.view_azimuth] * len(case.view_zeniths),
         albedo=case.surface_albedo, save_path=fixture.save_path,
         gas_scattering=bmsca, gas_absorption=bmabs, particles=particles,
-        particle_optical_depth=clouds, depolarization=depol, pixel_km=(x_unit, y_unit),
+        particle_optical_depth=clouds, depolarization=depol, pixel_km=(x_unit, y_unit), backward=case.backward,
     )
     metadata = scene_metadata(
         case.name, levels_km, nx=fixture.nx, ny=fixture.ny, nmat=fixture.nmat,

@@ -4,7 +4,10 @@ The reference prepares optical tables in Fortran (kernels/cpu/worker.f90:940-112
 fixture and exports ``transport.bin`` v1 (float64, Fortran order, layout at
 worker.f90:1102-1120). This module builds the same stream directly from the synthetic
 atmospheres of the workloads, as version 2: v1 plus one view azimuth per view, because
-the workloads pair each view zenith with its own relative azimuth.
+the workloads pair each view zenith with its own relative azimuth. Scenes with the full
+Stokes vector (nmat 4) are written as version 3: version 2 plus the F34 and F44 tables of
+each particle species, which the reference reads from its Mie files
+(fortran/.../main_routines_general_mod.f90:790-817) but leaves out of its v1 export.
 
 Stream layout (all float64):
   header   version, nx, ny, nz, nmat, angles, species, k_source, k_detector, k_register,
@@ -14,7 +17,12 @@ Stream layout (all float64):
   zunit(nz), view zeniths(angles), [v2] view azimuths(angles),
   surface type(nx,ny) = -1, albedo(nx,ny), elevation index(nx,ny) = 1,
   beta(nx,ny,nz), species fractions(species+1,nx,ny,nz), gas single-scattering albedo(nz)
-  per particle species: LUT size, albedo, cosines, bound CDF, F11, F22, F33, F12
+  per particle species: LUT size, albedo, cosines, bound CDF, F11, F22, F33, F12, [v3] F34, F44
+
+A backward scene (header backward = 1) injects photons along the sensor's line of sight:
+its "solar" angles are those of the reversed view and its views point back to the sun
+(fortran/.../worker.f90:650-702); the transport registers every contribution at the
+injection column.
 
 The layer ``nz`` is the vacuum layer above the top of the atmosphere; like the reference
 input parser (fortran/.../main_routines_cartesian_mod.f90:455-460) it is one micrometre
@@ -168,8 +176,9 @@ def build_tables(
     particle_optical_depth: np.ndarray,
     depolarization: float = 0.0279,
     pixel_km=1.0,
+    backward: bool = False,
 ) -> np.ndarray:
-    """Assemble a version-2 table stream.
+    """Assemble a version-2 table stream (version 3 with F34 and F44 when nmat is 4).
 
     ``particle_optical_depth`` has shape (species, nx, ny, layers) in layer optical depth;
     gas optical depths have shape (layers,). Extinctions are per km, the species
@@ -203,7 +212,10 @@ def build_tables(
         gas_scattering, total_gas, out=np.ones(layers), where=total_gas > 1e-16
     )
     surface_albedo = np.broadcast_to(np.asarray(albedo, dtype=float), (nx, ny))
-    header = [2, nx, ny, nz, nmat, len(views), species, nz, nz, nz, int(save_path), 0]
+    if nmat not in (1, 3, 4):
+        raise ValueError("nmat must be 1, 3 or 4")
+    version = 3 if nmat == 4 else 2
+    header = [version, nx, ny, nz, nmat, len(views), species, nz, nz, nz, int(save_path), int(bool(backward))]
     x_km, y_km = (pixel_km, pixel_km) if np.isscalar(pixel_km) else pixel_km
     geometry = [x_km, y_km, depolarization, 180.0 - solar_zenith, solar_azimuth, azimuths[0]]
     parts = [
@@ -223,10 +235,17 @@ def build_tables(
     for particle in particles:
         if isinstance(particle, Particle):
             cosines, cdf, f11, f22, f33, f12 = henyey_greenstein_table(particle.asymmetry)
+            # The non-polarizing particle: F44 = F11 and F34 = 0, like F22 = F33 = F11.
+            f34, f44 = np.zeros_like(f11), f11.copy()
             albedo_p = particle.albedo
-        else:  # a tabulated species: (cosines, cdf, F11, F22, F33, F12, albedo)
-            cosines, cdf, f11, f22, f33, f12, albedo_p = particle
+        else:  # tabulated: (cosines, cdf, F11, F22, F33, F12, albedo[, F34, F44])
+            cosines, cdf, f11, f22, f33, f12, albedo_p = particle[:7]
+            f34, f44 = particle[7:9] if len(particle) >= 9 else (None, None)
         parts += [np.array([len(cosines), albedo_p]), cosines, cdf, f11, f22, f33, f12]
+        if version == 3:
+            if f34 is None:
+                raise ValueError("nmat 4 needs the F34 and F44 tables of every tabulated species")
+            parts += [np.asarray(f34, dtype=float), np.asarray(f44, dtype=float)]
 
     return np.concatenate(parts).astype(np.float64)
 

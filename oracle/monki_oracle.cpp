@@ -32,7 +32,18 @@
 //     of kernels/metal/transport.metal:64-92 — instead of gfortran RANDOM_NUMBER.
 //   * Intermediates the Fortran keeps in REAL (float32) — the species cumulative sum
 //     (mc.f90:1028-1036) and GROUND_LAMB2's ACOS(SQRT(P)) — are carried in FP64.
-//   * Version 2 of the table stream adds one azimuth per view (the v1 stream has one).
+//   * Version 2 of the table stream adds one azimuth per view (the v1 stream has one);
+//     version 3 adds the F34 and F44 tables of each species after F12, which the
+//     reference reads from its Mie files (main_routines_general_mod.f90:790-817) but its
+//     v1 export omits, so that nmat 4 (Stokes V) runs with tabulated particles.
+//
+// Backward transport (mc.f90:377-380, 404-415, 754-758, 790-795, 894-906, 980-982,
+// 1150-1154, 1324-1336, 1393-1395; mc_routines_cartesian_mod.f90:500-520, 1034-1039):
+// the photon carries the weight matrix M (identity at injection); a peel-off registers
+// M P^T S0 (S0 = (1, 0, 0, 0); M As S0 at the surface) at the injection column for every
+// view; the continuation sets M = M P^T (M As at the surface), samples with the Stokes
+// vector (M11, M12, -M13, M14) and the + sign in the polarized sampling pdf, and divides M
+// by M11; no mu0/mu factor is applied.
 //   * Failure caps (history steps, detector steps, 4096 rejection attempts) report a
 //     flag (1 nonfinite, 2 detector cap, 4 sampling cap, 8 invalid Stokes, 16 history
 //     cap; kernels/metal/README.md:57-59) where the Fortran loops or prints.
@@ -98,7 +109,7 @@ struct Stream {
 struct Species {
     int n = 0;
     double ssalb = 0;
-    std::vector<double> cosines, cdf, f11, f22, f33, f12;
+    std::vector<double> cosines, cdf, f11, f22, f33, f12, f34, f44;
 };
 
 struct Tables {
@@ -138,7 +149,7 @@ Tables parse_tables(const double* raw, size_t count) {
         if (!std::isfinite(raw[i])) throw std::runtime_error("Invalid/nonfinite prepared transport export");
     const double* h = take(12);
     t.version = as_int(h[0], "version");
-    if (t.version != 1 && t.version != 2) throw std::runtime_error("Unsupported transport export version");
+    if (t.version < 1 || t.version > 3) throw std::runtime_error("Unsupported transport export version");
     t.nx = as_int(h[1], "nx"); t.ny = as_int(h[2], "ny"); t.nz = as_int(h[3], "nz");
     t.nmat = as_int(h[4], "nmat"); t.angles = as_int(h[5], "angles"); t.ntypes = as_int(h[6], "species");
     t.k_source = as_int(h[7], "k_source"); t.k_detector = as_int(h[8], "k_detector");
@@ -146,8 +157,9 @@ Tables parse_tables(const double* raw, size_t count) {
     t.paths = as_int(h[10], "save_path") != 0; t.backward = as_int(h[11], "backward") != 0;
     if (t.nx < 1 || t.ny < 1 || t.nz < 2 || t.angles < 1 || t.ntypes < 0)
         throw std::runtime_error("Invalid transport export dimensions");
-    if (t.nmat != 1 && t.nmat != 3) throw std::runtime_error("Only nmat 1 or 3 is supported");
-    if (t.backward) throw std::runtime_error("Backward transport is not supported");
+    if (t.nmat != 1 && t.nmat != 3 && t.nmat != 4) throw std::runtime_error("Only nmat 1, 3 or 4 is supported");
+    if (t.nmat == 4 && t.version < 3 && t.ntypes > 0)
+        throw std::runtime_error("nmat 4 with particles needs the version 3 table stream (F34, F44)");
     if (t.k_source != t.nz || t.k_detector != t.nz || t.k_register != t.nz)
         throw std::runtime_error("Only TOA source, detector and output grid are supported");
     const double* g = take(6);
@@ -155,7 +167,7 @@ Tables parse_tables(const double* raw, size_t count) {
     const size_t cells = size_t(t.nx) * t.ny * t.nz, columns = size_t(t.nx) * t.ny;
     const double* p = take(t.nz); t.zunit.assign(p, p + t.nz);
     p = take(t.angles); t.vartheta.assign(p, p + t.angles);
-    if (t.version == 2) { p = take(t.angles); t.view_phi.assign(p, p + t.angles); }
+    if (t.version >= 2) { p = take(t.angles); t.view_phi.assign(p, p + t.angles); }
     else t.view_phi.assign(t.angles, t.phi);
     p = take(columns); t.surface.assign(p, p + columns);
     p = take(columns); t.albedo.assign(p, p + columns);
@@ -172,6 +184,12 @@ Tables parse_tables(const double* raw, size_t count) {
         sp.cosines.assign(c, c + sp.n); sp.cdf.assign(c + sp.n, c + 2 * sp.n);
         sp.f11.assign(c + 2 * sp.n, c + 3 * sp.n); sp.f22.assign(c + 3 * sp.n, c + 4 * sp.n);
         sp.f33.assign(c + 4 * sp.n, c + 5 * sp.n); sp.f12.assign(c + 5 * sp.n, c + 6 * sp.n);
+        if (t.version >= 3) {
+            const double* v = take(size_t(sp.n) * 2);
+            sp.f34.assign(v, v + sp.n); sp.f44.assign(v + sp.n, v + 2 * sp.n);
+        } else {
+            sp.f34.assign(size_t(sp.n), 0.0); sp.f44.assign(size_t(sp.n), 0.0);
+        }
         t.species.push_back(std::move(sp));
     }
     if (offset != count) throw std::runtime_error("Trailing data in transport export");
@@ -193,9 +211,9 @@ Tables parse_tables(const double* raw, size_t count) {
 
 // ---------------------------------------------------------------------------------
 // Scattering helpers (mc_routines_general_mod.f90). Matrices are nmat x nmat with
-// nmat <= 3, stored row-major m[r][c] with 0-based indices.
+// nmat <= 4, stored row-major m[r][c] with 0-based indices.
 // ---------------------------------------------------------------------------------
-struct Mat3 { double m[3][3]; };
+struct Mat4 { double m[4][4]; };
 
 // interpol_sp.f:105-151 linpol_dp_single for a two-point bracket.
 double linpol2(const double x[2], const double y[2], double xp) {
@@ -207,16 +225,18 @@ double linpol2(const double x[2], const double y[2], double xp) {
 }
 
 // mc_routines_general_mod.f90:74-136
-Mat3 ray_scat_matrix(int nmat, double cs, double depol) {
-    Mat3 f{};
+Mat4 ray_scat_matrix(int nmat, double cs, double depol) {
+    Mat4 f{};
     double sin_sca = (1.0 - cs * cs < kEps) ? 0.0 : std::sqrt(1.0 - cs * cs);
     double delta = (1.0 - depol) / (1.0 + depol / 2.0);
+    double delta_prime = (1.0 - 2.0 * depol) / (1.0 - depol);
     f.m[0][0] = 3.0 / 4.0 * (1.0 + cs * cs);
     if (nmat > 1) {
         f.m[0][1] = -3.0 / 4.0 * sin_sca * sin_sca;
         f.m[1][0] = f.m[0][1];
         f.m[1][1] = 3.0 / 4.0 * (1.0 + cs * cs);
         f.m[2][2] = 3.0 / 2.0 * cs;
+        if (nmat > 3) f.m[3][3] = delta_prime * f.m[2][2];
     }
     for (auto& r : f.m) for (double& v : r) v *= delta;
     f.m[0][0] += 1.0 - delta;
@@ -257,22 +277,26 @@ int mie_bracket(const Species& sp, double cs, bool& single) {
 }
 
 // mc_routines_general_mod.f90:257-388
-Mat3 mie_scat_matrix(int nmat, double cs, const Species& sp) {
-    Mat3 f{};
+Mat4 mie_scat_matrix(int nmat, double cs, const Species& sp) {
+    Mat4 f{};
     bool single = false;
     int lo = mie_bracket(sp, cs, single);
-    double f11, f22 = 0, f33 = 0, f12 = 0;
+    double f11, f22 = 0, f33 = 0, f12 = 0, f34 = 0, f44 = 0;
     if (single) {
         f11 = sp.f11[lo - 1]; f22 = sp.f22[lo - 1]; f33 = sp.f33[lo - 1]; f12 = sp.f12[lo - 1];
+        f34 = sp.f34[lo - 1]; f44 = sp.f44[lo - 1];
     } else {
         const double x[2] = {sp.cosines[lo - 1], sp.cosines[lo]};
         const double y11[2] = {sp.f11[lo - 1], sp.f11[lo]}, y22[2] = {sp.f22[lo - 1], sp.f22[lo]};
         const double y33[2] = {sp.f33[lo - 1], sp.f33[lo]}, y12[2] = {sp.f12[lo - 1], sp.f12[lo]};
+        const double y34[2] = {sp.f34[lo - 1], sp.f34[lo]}, y44[2] = {sp.f44[lo - 1], sp.f44[lo]};
         f11 = linpol2(x, y11, cs);
         f22 = linpol2(x, y22, cs); f33 = linpol2(x, y33, cs); f12 = linpol2(x, y12, cs);
+        if (nmat > 3) { f34 = linpol2(x, y34, cs); f44 = linpol2(x, y44, cs); }
     }
     f.m[0][0] = f11;
     if (nmat > 1) { f.m[1][1] = f22; f.m[2][2] = f33; f.m[0][1] = f12; f.m[1][0] = f12; }
+    if (nmat > 3) { f.m[2][3] = f34; f.m[3][2] = -f34; f.m[3][3] = f44; }
     for (auto& r : f.m) for (double& v : r) v /= 4.0;
     return f;
 }
@@ -340,8 +364,8 @@ Rotation stokes_rot_mat(double cs, double uo, double u1, double phio, double phi
 }
 
 // mc_routines_general_mod.f90:1184-1242
-Mat3 matmul_stokes_rot(int nmat, const Mat3& a, const Rotation& r) {
-    Mat3 p{};
+Mat4 matmul_stokes_rot(int nmat, const Mat4& a, const Rotation& r) {
+    Mat4 p{};
     p.m[0][0] = a.m[0][0];
     if (nmat > 1) {
         double C1 = r.c1, S1 = r.s1, C2 = r.c2, S2 = r.s2;
@@ -353,11 +377,18 @@ Mat3 matmul_stokes_rot(int nmat, const Mat3& a, const Rotation& r) {
         p.m[2][0] = S2 * a.m[1][0];
         p.m[2][1] = C1 * S2 * a.m[1][1] + C2 * S1 * a.m[2][2];
         p.m[2][2] = C1 * C2 * a.m[2][2] - S1 * S2 * a.m[1][1];
+        if (nmat == 4) {
+            p.m[3][1] = S1 * a.m[3][2];
+            p.m[3][2] = C1 * a.m[3][2];
+            p.m[3][3] = a.m[3][3];
+            p.m[1][3] = -S2 * a.m[2][3];
+            p.m[2][3] = C2 * a.m[2][3];
+        }
     }
     return p;
 }
 
-void apply(int nmat, const Mat3& p, const double s[3], double out[3]) {
+void apply(int nmat, const Mat4& p, const double s[4], double out[4]) {
     for (int r = 0; r < nmat; ++r) {
         double acc = 0;
         for (int c = 0; c < nmat; ++c) acc += p.m[r][c] * s[c];
@@ -379,9 +410,9 @@ void outgoing_direction(double cos_in, double cos_sca, double sigma1, double& co
     dphi = -dphi;
 }
 
-// rayl_scatter_pol (forward sign = -1), with a 4096-attempt cap.
-bool rayl_scatter_pol(int nmat, double depol, const double s[3], double cos_in, Stream& rng,
-                      double& cos_out, double& dphi, double& cos_sca) {
+// rayl_scatter_pol (sign -1 forward, +1 backward), with a 4096-attempt cap.
+bool rayl_scatter_pol(int nmat, double depol, const double s[4], double cos_in, Stream& rng,
+                      double& cos_out, double& dphi, double& cos_sca, double sign = -1.0) {
     double pdf_max = ray_scat_element(1.0, depol);
     for (int attempt = 0; attempt < kMaxAttempts; ++attempt) {
         double ran1 = rng.uniform();
@@ -391,7 +422,7 @@ bool rayl_scatter_pol(int nmat, double depol, const double s[3], double cos_in, 
         double f11, f12;
         ray_scat_elements(rc, depol, f11, f12);
         if (nmat == 1) f12 = 0.0;
-        double pdf = nmat == 1 ? f11 : f11 + f12 * (s[1] * std::cos(2.0 * sigma) - s[2] * std::sin(2.0 * sigma));
+        double pdf = nmat == 1 ? f11 : f11 + f12 * (s[1] * std::cos(2.0 * sigma) + sign * s[2] * std::sin(2.0 * sigma));
         double ran3 = rng.uniform();
         if (ran3 * pdf_max > pdf) continue;
         cos_sca = rc;
@@ -401,9 +432,9 @@ bool rayl_scatter_pol(int nmat, double depol, const double s[3], double cos_in, 
     return false;
 }
 
-// mie_scatter_pol_bound (forward sign = -1), with a 4096-attempt cap.
-bool mie_scatter_pol_bound(int nmat, const Species& sp, const double s[3], double cos_in, Stream& rng,
-                           double& cos_out, double& dphi, double& cos_sca) {
+// mie_scatter_pol_bound (sign -1 forward, +1 backward), with a 4096-attempt cap.
+bool mie_scatter_pol_bound(int nmat, const Species& sp, const double s[4], double cos_in, Stream& rng,
+                           double& cos_out, double& dphi, double& cos_sca, double sign = -1.0) {
     for (int attempt = 0; attempt < kMaxAttempts; ++attempt) {
         double ran_cdf = rng.uniform();
         // Binary search of mie_scatter_pol_bound (:733-756) on 1-based indices.
@@ -426,7 +457,7 @@ bool mie_scatter_pol_bound(int nmat, const Species& sp, const double s[3], doubl
         double f11, f12;
         mie_scat_elements(rc, sp, f11, f12);
         if (nmat == 1) f12 = 0.0;
-        double pdf = nmat == 1 ? f11 : f11 + f12 * (s[1] * std::cos(2.0 * sigma) - s[2] * std::sin(2.0 * sigma));
+        double pdf = nmat == 1 ? f11 : f11 + f12 * (s[1] * std::cos(2.0 * sigma) + sign * s[2] * std::sin(2.0 * sigma));
         double ran3 = rng.uniform();
         double bound = f11 + std::fabs(f12);
         if (ran3 * bound > pdf) continue;
@@ -520,6 +551,11 @@ struct Counters {
         detector_visits += o.detector_visits; tally_updates += o.tally_updates;
     }
 };
+
+// Backward transport registers every view at the injection column (reg_i, reg_j) and
+// attributes the event to the location of the history's first event (loc_*); forward
+// transport projects each view ray to the top (reg_i = 0) and uses the event's own cell.
+struct Register { int reg_i = 0, reg_j = 0, loc_i = 0, loc_j = 0, loc_layer = -1; };
 
 struct Transport {
     const Tables& t;
@@ -635,7 +671,7 @@ struct Transport {
                   double x_bak, double y_bak, double z_bak, const std::vector<double>& s_prob,
                   const std::vector<double>& path_layers, double* tally,
                   std::vector<double>& path_angle, Counters& cnt, double& contributed,
-                  uint32_t nscat = 0) const {
+                  uint32_t nscat = 0, const Register& reg = Register()) const {
         const int nmat = t.nmat, nz = t.nz;
         contributed = 0.0;
         for (int ia = 0; ia < t.angles; ++ia) {
@@ -674,19 +710,21 @@ struct Transport {
             auto modulo = [](long long v, long long m) { long long r = v % m; return r < 0 ? r + m : r; };
             int inew = int(modulo((long long)i_bak + is * (long long)di + t.nx - 1, t.nx)) + 1;
             int jnew = int(modulo((long long)j_bak + js * (long long)dj + t.ny - 1, t.ny)) + 1;
+            if (reg.reg_i > 0) { inew = reg.reg_i; jnew = reg.reg_j; }
             double att = std::exp(-tau);
             contributed += pixel_weight ? p1 * att * pixel_weight[size_t(inew - 1) + size_t(t.nx) * (size_t(jnew - 1) + size_t(t.ny) * size_t(ia))]
                                         : p1 * att;
             for (int m = 0; m < nmat; ++m) tally[stokes_index(m, inew, jnew, ia)] += s_prob[size_t(ia) * nmat + m] * att;
             cnt.tally_updates += nmat;
             if (orders) {
-                const int layer = (k_bak == 1 && z_bak < kEps) ? 0 : k_bak;
+                int li = i_bak, lj = j_bak, layer = (k_bak == 1 && z_bak < kEps) ? 0 : k_bak;
+                if (reg.loc_layer >= 0) { li = reg.loc_i; lj = reg.loc_j; layer = reg.loc_layer; }
                 for (int m = 0; m < nmat; ++m) {
                     const double v = s_prob[size_t(ia) * nmat + m] * att;
-                    tally[orders_offset + stokes_count + location_index(m, i_bak, j_bak, layer, ia)] += v;
+                    tally[orders_offset + stokes_count + location_index(m, li, lj, layer, ia)] += v;
                     if (nscat == 1) {
                         tally[orders_offset + stokes_index(m, inew, jnew, ia)] += v;
-                        tally[orders_offset + stokes_count + size_t(nmat) * locations + location_index(m, i_bak, j_bak, layer, ia)] += v;
+                        tally[orders_offset + stokes_count + size_t(nmat) * locations + location_index(m, li, lj, layer, ia)] += v;
                     }
                 }
             }
@@ -732,8 +770,20 @@ struct Transport {
         double x = t.xunit * rng.uniform();
         double y = t.yunit * rng.uniform();
         double z = t.zu(k);
-        double s[3] = {1.0, 0.0, 0.0};
+        double s[4] = {1.0, 0.0, 0.0, 0.0};
         double weight = 1.0;
+        // Backward transport: the weight matrix (identity at injection), the injection
+        // column where every contribution registers, and the first event's location.
+        const bool backward = t.backward;
+        const double sign = backward ? 1.0 : -1.0;
+        double M[4][4] = {};
+        for (int m = 0; m < nmat; ++m) M[m][m] = 1.0;
+        Register reg;
+        if (backward) { reg.reg_i = i; reg.reg_j = j; }
+        auto locate = [&](int ei, int ej, int ek, double ez) {
+            if (!backward) return;
+            if (nscat == 1) { reg.loc_i = ei; reg.loc_j = ej; reg.loc_layer = (ek == 1 && ez < kEps) ? 0 : ek; }
+        };
         if (t.paths) std::fill(path_layers.begin(), path_layers.end(), 0.0);
         double a = a0, b = b0, c = c0, phi_in = phi0_rad;
         double remains = 0;
@@ -781,13 +831,19 @@ struct Transport {
                 if (weight < kEps) return 0;
                 ++cnt.scatters;
                 ++nscat;
+                locate(i, j, k, z);
                 for (int ia = 0; ia < t.angles; ++ia) {
                     for (int m = 0; m < nmat; ++m) s_prob[size_t(ia) * nmat + m] = 0.0;
-                    if (vc[ia] > 0) s_prob[size_t(ia) * nmat] = s[0] * vc[ia] * weight;
-                    if (!std::isfinite(s_prob[size_t(ia) * nmat])) return 1;
+                    if (vc[ia] > 0) {
+                        // Forward As S (only I survives); backward M As S0 (the first column of M).
+                        if (backward) for (int m = 0; m < nmat; ++m) s_prob[size_t(ia) * nmat + m] = M[m][0] * vc[ia] * weight;
+                        else s_prob[size_t(ia) * nmat] = s[0] * vc[ia] * weight;
+                    }
+                    for (int m = 0; m < (backward ? nmat : 1); ++m)
+                        if (!std::isfinite(s_prob[size_t(ia) * nmat + m])) return 1;
                 }
                 if (!peel_off(a_int, b_int, c_int, i, j, k, x, y, z, s_prob, path_layers, tally, path_angle, cnt, contributed,
-                              nscat))
+                              nscat, reg))
                     return 2;
                 record(i, j, k, weight, contributed);
                 // GROUND_LAMB2: theta = acos(sqrt(P)), phi = 2 pi U.
@@ -798,8 +854,17 @@ struct Transport {
                 a = std::sin(theta) * std::cos(phi_out);
                 b = std::sin(theta) * std::sin(phi_out);
                 c = std::fabs(std::cos(theta));
-                s[1] = 0.0; s[2] = 0.0;  // As * S keeps only I
+                if (backward) {
+                    // M As keeps the first column; the sampling vector is (M11, 0, 0, 0).
+                    for (int r = 0; r < nmat; ++r) for (int col = 1; col < nmat; ++col) M[r][col] = 0.0;
+                    s[0] = M[0][0];
+                }
+                s[1] = 0.0; s[2] = 0.0; s[3] = 0.0;  // As * S keeps only I
                 if (s[0] > kEps) { double s0 = s[0]; for (int m = 0; m < nmat; ++m) s[m] /= s0; }
+                if (backward) {
+                    const double m11 = M[0][0];
+                    for (int r = 0; r < nmat; ++r) for (int col = 0; col < nmat; ++col) M[r][col] /= m11;
+                }
                 if (a * a_int < 0.0) x = std::max(0.0, t.xunit - x);
                 if (b * b_int < 0.0) y = std::max(0.0, t.yunit - y);
                 if (c * c_int < 0.0) z = std::max(0.0, t.zu(k) - z);
@@ -820,22 +885,32 @@ struct Transport {
             if (weight < kEps) return 0;
             ++cnt.scatters;
             ++nscat;
+            locate(i, j, k, z);
             for (int ia = 0; ia < t.angles; ++ia) {
                 double cs = c * vc[ia] + std::sqrt(std::max(kEps, 1.0 - c * c)) *
                                              std::sqrt(std::max(kEps, 1.0 - vc[ia] * vc[ia])) *
                                              std::cos(phi_in - view_phi_rad[ia]);
                 Rotation rot = stokes_rot_mat(cs, c, vc[ia], phi_in, view_phi_rad[ia], nmat);
-                Mat3 f = gas ? ray_scat_matrix(nmat, cs, t.depol) : mie_scat_matrix(nmat, cs, t.species[size_t(sp - 1)]);
-                Mat3 p = matmul_stokes_rot(nmat, f, rot);
-                double back[3];
-                apply(nmat, p, s, back);
+                Mat4 f = gas ? ray_scat_matrix(nmat, cs, t.depol) : mie_scat_matrix(nmat, cs, t.species[size_t(sp - 1)]);
+                Mat4 p = matmul_stokes_rot(nmat, f, rot);
+                double back[4];
+                if (backward) {
+                    // M P^T S0: M times the first row of P.
+                    for (int r = 0; r < nmat; ++r) {
+                        double acc = 0.0;
+                        for (int col = 0; col < nmat; ++col) acc += M[r][col] * p.m[0][col];
+                        back[r] = acc;
+                    }
+                } else {
+                    apply(nmat, p, s, back);
+                }
                 for (int m = 0; m < nmat; ++m) s_prob[size_t(ia) * nmat + m] = back[m] * weight;
                 if (s_prob[size_t(ia) * nmat] < 1.0e-100)
                     for (int m = 0; m < nmat; ++m) s_prob[size_t(ia) * nmat + m] = 0.0;
                 for (int m = 0; m < nmat; ++m)
                     if (!std::isfinite(s_prob[size_t(ia) * nmat + m])) return 1;
             }
-            if (!peel_off(a, b, c, i, j, k, x, y, z, s_prob, path_layers, tally, path_angle, cnt, contributed, nscat))
+            if (!peel_off(a, b, c, i, j, k, x, y, z, s_prob, path_layers, tally, path_angle, cnt, contributed, nscat, reg))
                 return 2;
             record(i, j, k, weight, contributed);
             double cos_in = c, cos_out, dphi, cos_sca, phi_out;
@@ -859,21 +934,41 @@ struct Transport {
                 const double so = std::sqrt(std::max(0.0, 1.0 - cos_out * cos_out));
                 cos_sca = std::min(1.0, std::max(-1.0, a * (std::cos(phi_out) * so) + b * (std::sin(phi_out) * so) + c * cos_out));
             } else {
-                bool ok = gas ? rayl_scatter_pol(nmat, t.depol, s, cos_in, rng, cos_out, dphi, cos_sca)
-                              : mie_scatter_pol_bound(nmat, t.species[size_t(sp - 1)], s, cos_in, rng, cos_out, dphi, cos_sca);
+                bool ok = gas ? rayl_scatter_pol(nmat, t.depol, s, cos_in, rng, cos_out, dphi, cos_sca, sign)
+                              : mie_scatter_pol_bound(nmat, t.species[size_t(sp - 1)], s, cos_in, rng, cos_out, dphi, cos_sca, sign);
                 if (!ok) return 4;
                 phi_out = phi_in + dphi;
             }
             Rotation rot = stokes_rot_mat(cos_sca, cos_in, cos_out, phi_in, phi_out, nmat);
-            Mat3 f = gas ? ray_scat_matrix(nmat, cos_sca, t.depol) : mie_scat_matrix(nmat, cos_sca, t.species[size_t(sp - 1)]);
-            Mat3 p = matmul_stokes_rot(nmat, f, rot);
-            double ns[3];
-            apply(nmat, p, s, ns);
+            Mat4 f = gas ? ray_scat_matrix(nmat, cos_sca, t.depol) : mie_scat_matrix(nmat, cos_sca, t.species[size_t(sp - 1)]);
+            Mat4 p = matmul_stokes_rot(nmat, f, rot);
+            double ns[4];
+            if (backward) {
+                // M = M P^T; the sampling vector is (M11, M12, -M13, M14).
+                double next[4][4] = {};
+                for (int r = 0; r < nmat; ++r)
+                    for (int col = 0; col < nmat; ++col) {
+                        double acc = 0.0;
+                        for (int q = 0; q < nmat; ++q) acc += M[r][q] * p.m[col][q];
+                        next[r][col] = acc;
+                    }
+                std::memcpy(M, next, sizeof(M));
+                ns[0] = M[0][0];
+                if (nmat > 1) { ns[1] = M[0][1]; ns[2] = -M[0][2]; }
+                if (nmat > 3) ns[3] = M[0][3];
+            } else {
+                apply(nmat, p, s, ns);
+            }
             double s0 = ns[0];
             for (int m = 0; m < nmat; ++m) s[m] = ns[m] / s0;
             if (s[0] < 1.0e-100) for (int m = 0; m < nmat; ++m) s[m] = 0.0;
             for (int m = 0; m < nmat; ++m) if (!std::isfinite(s[m])) return 8;
             if (nmat == 3 && std::sqrt(s[1] * s[1] + s[2] * s[2]) > s[0] + kStokesCriterium) return 8;
+            if (nmat == 4 && std::sqrt(s[1] * s[1] + s[2] * s[2] + s[3] * s[3]) > s[0] + kStokesCriterium) return 8;
+            if (backward) {
+                const double m11 = M[0][0];
+                for (int r = 0; r < nmat; ++r) for (int col = 0; col < nmat; ++col) M[r][col] /= m11;
+            }
             double a_bak = a, b_bak = b, c_bak = c;
             a = std::cos(phi_out) * std::sqrt(std::max(0.0, 1.0 - cos_out * cos_out));
             b = std::sin(phi_out) * std::sqrt(std::max(0.0, 1.0 - cos_out * cos_out));
@@ -917,9 +1012,9 @@ void monki_oracle_uniforms(uint32_t photon, uint32_t round, uint32_t seed, uint3
 void monki_oracle_scatter_stokes(double depol, double uo, double u1, double phio, double phi1,
                                  const double stokes[3], double out[3]) {
     double cs = uo * u1 + std::sqrt(1 - uo * uo) * std::sqrt(1 - u1 * u1) * std::cos(phio - phi1);
-    Mat3 f = ray_scat_matrix(3, cs, depol);
+    Mat4 f = ray_scat_matrix(3, cs, depol);
     Rotation r = stokes_rot_mat(cs, uo, u1, phio, phi1, 3);
-    Mat3 p = matmul_stokes_rot(3, f, r);
+    Mat4 p = matmul_stokes_rot(3, f, r);
     apply(3, p, stokes, out);
 }
 
@@ -974,6 +1069,10 @@ int monki_oracle_run_guided(const double* tables, size_t table_count, const uint
         const uint32_t rounds = controls[7];
         if (!per_round || !rounds || uint64_t(first) + count > uint64_t(per_round) * rounds) {
             write_error(err, errlen, "Invalid round group");
+            return 1;
+        }
+        if (t.backward && (guide[0] > 0.0 || guide[1] > 0.0 || importance || pixel_weight)) {
+            write_error(err, errlen, "Guided transport and importance tallies need forward transport");
             return 1;
         }
         Transport tr(t, max_steps);
@@ -1037,8 +1136,8 @@ int monki_oracle_run_guided(const double* tables, size_t table_count, const uint
                 for (size_t v = 0; v < 2 * cells; ++v) importance[v] += imp_partial[size_t(q)][v];
             }
         }
-        // mu0/mu geometry factor on Stokes only (mc.f90:1456-1474).
-        for (uint32_t r = 0; r < rounds; ++r)
+        // mu0/mu geometry factor on Stokes only, forward transport only (mc.f90:1456-1474).
+        for (uint32_t r = 0; r < (t.backward ? 0u : rounds); ++r)
             for (int ia = 0; ia < t.angles; ++ia) {
                 double f = std::fabs(std::cos(tr.vartheta0_rad)) / std::fabs(std::cos(kDegToRad * t.vartheta[ia]));
                 for (int j = 1; j <= t.ny; ++j)

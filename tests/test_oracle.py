@@ -44,7 +44,9 @@ def test_polarization_probe_matches_golden(oracle):
 
 @pytest.mark.parametrize(
     "field,value",
-    [(0, 3), (4, 4), (7, 1), (8, 0), (11, 1)],
+    # version 4; nmat 2; nmat 4 with particles but no F34 / F44 tables (a v1 stream);
+    # version 3 without its F34 / F44 tables (truncated); source and detector off the top
+    [(0, 4), (4, 2), (4, 4), (0, 3), (7, 1), (8, 0)],
 )
 def test_unsupported_tables_are_rejected(oracle, field, value):
     import monki.scenes as scenes
