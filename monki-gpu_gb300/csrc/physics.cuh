@@ -74,7 +74,7 @@ template <typename T> __device__ __forceinline__ T fsign(T a, T b) { return sign
 // reference (radiance normalized for incident E0 = pi).
 // ---------------------------------------------------------------------------------
 template <typename T>
-struct Phase { T f11, f22, f33, f12; };
+struct Phase { T f11, f22, f33, f12, f34, f44; };  // f34, f44 only for nmat 4
 
 template <typename T>
 __device__ __forceinline__ Phase<T> rayleigh(T cs, T depol, int nmat) {
@@ -87,6 +87,9 @@ __device__ __forceinline__ Phase<T> rayleigh(T cs, T depol, int nmat) {
     f.f22 = diag / T(4);
     f.f33 = delta * (T(1.5) * cs) / T(4);
     f.f12 = nmat > 1 ? delta * (T(-0.75) * sin2) / T(4) : T(0);
+    // F44 = Delta' F33 with Delta' = (1 - 2 depol) / (1 - depol); Rayleigh has no F34.
+    f.f34 = T(0);
+    f.f44 = nmat > 3 ? (T(1) - T(2) * depol) / (T(1) - depol) * f.f33 : T(0);
     return f;
 }
 
@@ -127,6 +130,24 @@ __device__ __forceinline__ Phase<T> particle(const SceneView<T>& s, int sp, T cs
     }
     r.f11 /= T(4); r.f22 /= T(4); r.f33 /= T(4);
     r.f12 = nmat > 1 ? r.f12 / T(4) : T(0);
+    r.f34 = T(0); r.f44 = T(0);
+    if (nmat > 3) {
+        // {F34, F44} per node (version 3 tables), interpolated like the other elements.
+        const T* __restrict__ v = s.lut_v[sp];
+        if (lo == n - 1) {
+            r.f34 = __ldg(v + 2 * lo); r.f44 = __ldg(v + 2 * lo + 1);
+        } else {
+            const T x0 = __ldg(cosv + lo), x1 = __ldg(cosv + lo + 1);
+            auto lerp = [&](int e) {
+                T y0 = __ldg(v + 2 * lo + e), y1 = __ldg(v + 2 * lo + 2 + e);
+                if (cs == x1) return y1;
+                if (cs == x0) return y0;
+                return (y1 - y0) / (x1 - x0) * (cs - x0) + y0;
+            };
+            r.f34 = lerp(0); r.f44 = lerp(1);
+        }
+        r.f34 /= T(4); r.f44 /= T(4);
+    }
     return r;
 }
 
@@ -198,7 +219,9 @@ __device__ __forceinline__ Rot<T> rotation(T cs, T uo, T u1, T phio, T phi1) {
     return rotation_pre<T>(cs, uo, u1, phio, phi1, cpo, spo, cp1, sp1);
 }
 
-// S_out = L2 * F * L1 * S (matmul_stokes_rot followed by the forward-mode product).
+// S_out = L2 * F * L1 * S (matmul_stokes_rot followed by the forward-mode product). The
+// scattering matrix has F(3,4) = F34 and F(4,3) = -F34, so the rotated phase matrix has
+// P(2,4) = -S2 F34, P(3,4) = C2 F34, P(4,2) = -S1 F34, P(4,3) = -C1 F34, P(4,4) = F44.
 template <typename T>
 __device__ __forceinline__ void scatter_stokes(const Phase<T>& f, const Rot<T>& r, int nmat,
                                                const T* s, T* out) {
@@ -209,6 +232,38 @@ __device__ __forceinline__ void scatter_stokes(const Phase<T>& f, const Rot<T>& 
              (-C2 * S1 * f.f22 - C1 * S2 * f.f33) * s[2];
     out[2] = S2 * f.f12 * s[0] + (C1 * S2 * f.f22 + C2 * S1 * f.f33) * s[1] +
              (C1 * C2 * f.f33 - S1 * S2 * f.f22) * s[2];
+    if (nmat > 3) {
+        out[1] += -S2 * f.f34 * s[3];
+        out[2] += C2 * f.f34 * s[3];
+        out[3] = -S1 * f.f34 * s[1] - C1 * f.f34 * s[2] + f.f44 * s[3];
+    }
+}
+
+// The rotated phase matrix P = L2 F L1 of matmul_stokes_rot, row-major nmat x nmat.
+template <typename T>
+__device__ __forceinline__ void phase_matrix(const Phase<T>& f, const Rot<T>& r, int nmat, T P[4][4]) {
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) P[a][b] = T(0);
+    P[0][0] = f.f11;
+    if (nmat == 1) return;
+    const T C1 = r.c1, S1 = r.s1, C2 = r.c2, S2 = r.s2;
+    P[0][1] = f.f12 * C1;
+    P[0][2] = -f.f12 * S1;
+    P[1][0] = C2 * f.f12;
+    P[1][1] = C1 * C2 * f.f22 - S1 * S2 * f.f33;
+    P[1][2] = -C2 * S1 * f.f22 - C1 * S2 * f.f33;
+    P[2][0] = S2 * f.f12;
+    P[2][1] = C1 * S2 * f.f22 + C2 * S1 * f.f33;
+    P[2][2] = C1 * C2 * f.f33 - S1 * S2 * f.f22;
+    if (nmat > 3) {
+        P[1][3] = -S2 * f.f34;
+        P[2][3] = C2 * f.f34;
+        P[3][1] = -S1 * f.f34;
+        P[3][2] = -C1 * f.f34;
+        P[3][3] = f.f44;
+    }
 }
 
 // Spherical trigonometry after an accepted (cos_sca, sigma) sample.
@@ -245,12 +300,13 @@ __device__ __forceinline__ T sample_cdf(const SceneView<T>& s, int sp, T u) {
     return (y1 - y0) / (x1 - x0) * (u - x0) + y0;
 }
 
-// Polarized rejection sampling (forward sign -1). Rayleigh: uniform cosine with the
-// F11(0 deg) bound; particles: bound F11 + |F12| drawn from its CDF. Capped at 4096.
+// Polarized rejection sampling: pdf F11 + F12 (Q cos 2 sigma + sign U sin 2 sigma) with
+// sign -1 forward and +1 backward. Rayleigh: uniform cosine with the F11(0 deg) bound;
+// particles: bound F11 + |F12| drawn from its CDF. Capped at 4096.
 template <typename T, typename Stream>
 __device__ __forceinline__ bool sample_direction(const SceneView<T>& s, int sp, int nmat, const T* st,
                                                  T cos_in, Stream& rng, T& cos_out, T& dphi,
-                                                 T& cos_sca) {
+                                                 T& cos_sca, T sign = T(-1)) {
     const T pi = pi_v<T>();
     const T bound_gas = rayleigh<T>(T(1), s.depol, 1).f11;
     for (int attempt = 0; attempt < 4096; ++attempt) {
@@ -262,7 +318,7 @@ __device__ __forceinline__ bool sample_direction(const SceneView<T>& s, int sp, 
         if (nmat > 1) {
             T s2, c2;
             sincos(T(2) * sigma, &s2, &c2);
-            pdf = f.f11 + f.f12 * (st[1] * c2 - st[2] * s2);
+            pdf = f.f11 + f.f12 * (st[1] * c2 + sign * st[2] * s2);
         }
         T bound = sp < 0 ? bound_gas : f.f11 + fabs(f.f12);
         if (T(rng.next()) * bound > pdf) continue;

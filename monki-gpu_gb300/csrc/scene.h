@@ -16,6 +16,7 @@
 //   run_lo[nz], run_hi[nz]   first / last layer of the uniform run containing k (ints)
 //   lut_f[4 * n]             {F11, F22, F33, F12} per scattering angle, per species
 //   lut_cos[n], lut_cdf[n]   ascending cosine grid and the bound-function CDF
+//   lut_v[2 * n]             {F34, F44} per scattering angle, per species (nmat 4 only)
 //   guide[kGuide + 1]        CDF guide table: largest i with cdf[i] <= g / kGuide
 //   band[nx * ny * uniform_top]  extinction of every cell below the horizontally uniform
 //                            top (the only cells a cell walk visits), 16-byte aligned and
@@ -51,6 +52,7 @@ enum Failure : uint32_t {
 template <typename T>
 struct SceneView {
     int nx, ny, nz, nmat, angles, ntypes, paths, uniform_top;
+    int backward;       // backward transport: weight matrices, registration at the injection column
     int lut_n[kMaxSpecies];
     T xunit, yunit, depol;
     T xinv, yinv;        // 1 / xunit, 1 / yunit
@@ -74,6 +76,7 @@ struct SceneView {
     const T* lut_cos[kMaxSpecies];
     const T* lut_cdf[kMaxSpecies];
     const int* guide[kMaxSpecies];
+    const T* lut_v[kMaxSpecies];  // {F34, F44} per node (nmat 4), else null
     const T* band;          // extinction below the uniform top, i + nx * (j + ny * k)
     uint32_t band_bytes;    // padded size when staged in shared memory, else 0
     const uint32_t* extent; // equal-extinction rectangles of the band cells, or null

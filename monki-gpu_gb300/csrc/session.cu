@@ -108,10 +108,10 @@ Config parse_config(const char* text) {
 // version 2 adds one view azimuth per view after the view zeniths).
 struct Prepared {
     int nx, ny, nz, nmat, angles, ntypes;
-    bool paths;
+    bool paths, backward;
     double xunit, yunit, depol, vartheta0, phi0;
     std::vector<double> zunit, vartheta, vphi, albedo, beta, fractions, ssalb_gas;
-    struct Lut { int n; double ssalb; std::vector<double> cos, cdf, f11, f22, f33, f12; };
+    struct Lut { int n; double ssalb; std::vector<double> cos, cdf, f11, f22, f33, f12, f34, f44; };
     std::vector<Lut> luts;
 };
 
@@ -134,25 +134,27 @@ Prepared parse(const double* raw, size_t count) {
         if (!std::isfinite(raw[q])) throw std::runtime_error("Invalid/nonfinite prepared transport export");
     const double* h = take(12);
     int version = integer(h[0]);
-    if (version != 1 && version != 2) throw std::runtime_error("Unsupported transport export version");
+    if (version < 1 || version > 3) throw std::runtime_error("Unsupported transport export version");
     p.nx = integer(h[1]); p.ny = integer(h[2]); p.nz = integer(h[3]);
     p.nmat = integer(h[4]); p.angles = integer(h[5]); p.ntypes = integer(h[6]);
     int ks = integer(h[7]), kd = integer(h[8]), kr = integer(h[9]);
     p.paths = integer(h[10]) != 0;
-    bool backward = integer(h[11]) != 0;
+    p.backward = integer(h[11]) != 0;
     if (p.nx < 1 || p.ny < 1 || p.nz < 2 || p.nz > kMaxLayers || p.angles < 1 || p.angles > kMaxViews)
         throw std::runtime_error("Scene exceeds the supported grid limits");
     if (uint64_t(p.nx) * p.ny * p.nz > (1ull << 28)) throw std::runtime_error("Scene exceeds the supported grid limits");
-    if ((p.nmat != 1 && p.nmat != 3) || p.ntypes < 0 || p.ntypes > kMaxSpecies || backward ||
+    if ((p.nmat != 1 && p.nmat != 3 && p.nmat != 4) || p.ntypes < 0 || p.ntypes > kMaxSpecies ||
         ks != p.nz || kd != p.nz || kr != p.nz)
-        throw std::runtime_error("CUDA supports forward I/IQU, up to 3 particle species, TOA source/detector/grid");
+        throw std::runtime_error("CUDA supports I, IQU or IQUV, up to 3 particle species, TOA source/detector/grid");
+    if (p.nmat == 4 && version < 3 && p.ntypes > 0)
+        throw std::runtime_error("nmat 4 with particles needs the version 3 table stream (F34, F44)");
     const double* g = take(6);
     p.xunit = g[0]; p.yunit = g[1]; p.depol = g[2]; p.vartheta0 = g[3]; p.phi0 = g[4];
     const double phi = g[5];
     const size_t cols = size_t(p.nx) * p.ny, cells = cols * p.nz;
     const double* q = take(p.nz); p.zunit.assign(q, q + p.nz);
     q = take(p.angles); p.vartheta.assign(q, q + p.angles);
-    if (version == 2) { q = take(p.angles); p.vphi.assign(q, q + p.angles); }
+    if (version >= 2) { q = take(p.angles); p.vphi.assign(q, q + p.angles); }
     else p.vphi.assign(p.angles, phi);
     const double* surface = take(cols);
     q = take(cols); p.albedo.assign(q, q + cols);
@@ -169,6 +171,10 @@ Prepared parse(const double* raw, size_t count) {
         l.cos.assign(t, t + l.n); l.cdf.assign(t + l.n, t + 2 * l.n);
         l.f11.assign(t + 2 * l.n, t + 3 * l.n); l.f22.assign(t + 3 * l.n, t + 4 * l.n);
         l.f33.assign(t + 4 * l.n, t + 5 * l.n); l.f12.assign(t + 5 * l.n, t + 6 * l.n);
+        if (version >= 3) {
+            const double* v = take(size_t(l.n) * 2);
+            l.f34.assign(v, v + l.n); l.f44.assign(v + l.n, v + 2 * l.n);
+        }
         p.luts.push_back(std::move(l));
     }
     if (off != count) throw std::runtime_error("Trailing data in transport export");
@@ -229,6 +235,7 @@ struct Packed {
     std::vector<int> guides;
     size_t cells, zunit, zsum, ssalb_gas, albedo, tau_above, layer_beta, vprefix, run_lo, run_hi;
     size_t lut_f[kMaxSpecies], lut_cos[kMaxSpecies], lut_cdf[kMaxSpecies], guide[kMaxSpecies];
+    size_t lut_v[kMaxSpecies];
     size_t band, band_count, extent;
     int uniform_top;
 };
@@ -364,6 +371,14 @@ Packed<T> pack(const Prepared& p, bool uniform_prefix, bool rectangles = true) {
         for (int i = 0; i < l.n; ++i) v[k.lut_cos[s] + i] = T(l.cos[i]);
         k.lut_cdf[s] = reserve(l.n);
         for (int i = 0; i < l.n; ++i) v[k.lut_cdf[s] + i] = T(l.cdf[i]);
+        k.lut_v[s] = SIZE_MAX;
+        if (p.nmat == 4) {
+            k.lut_v[s] = reserve(2 * size_t(l.n));
+            for (int i = 0; i < l.n; ++i) {
+                v[k.lut_v[s] + 2 * i] = T(l.f34[i]);
+                v[k.lut_v[s] + 2 * i + 1] = T(l.f44[i]);
+            }
+        }
         // Guide: largest i <= n - 2 with cdf[i] <= g / kGuide (at transport precision).
         k.guide[s] = k.guides.size();
         int i = 0;
@@ -431,6 +446,7 @@ SceneView<T> make_view(const Prepared& p, const Packed<T>& k, void* base) {
     const int* gv = reinterpret_cast<const int*>(static_cast<const char*>(base) + k.values.size() * sizeof(T));
     s.nx = p.nx; s.ny = p.ny; s.nz = p.nz; s.nmat = p.nmat; s.angles = p.angles; s.ntypes = p.ntypes;
     s.paths = p.paths; s.uniform_top = k.uniform_top;
+    s.backward = p.backward ? 1 : 0;
     s.xunit = T(p.xunit); s.yunit = T(p.yunit); s.depol = T(p.depol);
     s.xinv = T(1) / s.xunit; s.yinv = T(1) / s.yunit;
     const double th0 = kDegToRad * p.vartheta0, ph0 = kDegToRad * p.phi0;
@@ -456,6 +472,7 @@ SceneView<T> make_view(const Prepared& p, const Packed<T>& k, void* base) {
         s.znorm[sp] = T(analog_norm(p.luts[sp], p.nmat));
         s.lut_f[sp] = tv + k.lut_f[sp]; s.lut_cos[sp] = tv + k.lut_cos[sp]; s.lut_cdf[sp] = tv + k.lut_cdf[sp];
         s.guide[sp] = gv + k.guide[sp];
+        s.lut_v[sp] = k.lut_v[sp] == SIZE_MAX ? nullptr : tv + k.lut_v[sp];
     }
     return s;
 }
@@ -483,7 +500,10 @@ Pool<T> allocate_pool(Session& s) {
                             n * nz * sizeof(T), n * sizeof(uint32_t), 2 * n * sizeof(T),
                             3 * n * sizeof(uint32_t), 16 * sizeof(uint32_t),
                             ring * sizeof(uint32_t), ring * sizeof(T), s.cfg.importance ? n * sizeof(uint32_t) : 0,
-                            s.cfg.orders ? n * sizeof(uint32_t) : 0};
+                            s.cfg.orders ? n * sizeof(uint32_t) : 0,
+                            (s.prep.nmat == 4 && !s.prep.backward) ? n * sizeof(T) : 0,
+                            s.prep.backward ? size_t(s.prep.nmat) * s.prep.nmat * n * sizeof(T) : 0,
+                            (s.prep.backward && s.cfg.orders) ? n * sizeof(uint32_t) : 0};
     size_t bytes = 0;
     for (size_t part : parts) bytes += align_up(part, 256);
     check(cudaMalloc(&s.pool_memory, bytes), "cudaMalloc(pool)");
@@ -510,6 +530,9 @@ Pool<T> allocate_pool(Session& s) {
         P.importance = s.importance;
     }
     if (s.cfg.orders) P.order = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
+    if (s.prep.nmat == 4 && !s.prep.backward) P.vee = reinterpret_cast<T*>(take(n * sizeof(T)));
+    if (s.prep.backward) P.matrix = reinterpret_cast<T*>(take(size_t(s.prep.nmat) * s.prep.nmat * n * sizeof(T)));
+    if (s.prep.backward && s.cfg.orders) P.first = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
     return P;
 }
 
@@ -543,11 +566,15 @@ void wave_iteration(Session& s, const SceneView<T>& v, Pool<T>& P, const Control
     wf_transit<T, PATHS><<<slots_grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, s.cfg.walk, s.failure,
                                                                               s.counters);
     if (ev) cudaEventRecord(ev[1], s.stream);
-    wf_peel<T, T, NMAT, PATHS><<<grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, banks, s.wave, s.failure, s.counters);
+    if (v.backward)
+        wf_peel<T, T, NMAT, PATHS, true><<<grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, banks, s.wave, s.failure, s.counters);
+    else
+        wf_peel<T, T, NMAT, PATHS, false><<<grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, banks, s.wave, s.failure, s.counters);
     if (ev) cudaEventRecord(ev[2], s.stream);
     Guide<T> g{T(s.cfg.epsilon), T(s.cfg.roulette), s.cfg.cap > 0.0 ? T(s.cfg.cap) : T(INFINITY),
                static_cast<const T*>(s.scale)};
-    wf_scatter<T, NMAT><<<slots_grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, g, s.failure);
+    if (v.backward) wf_scatter<T, NMAT, true><<<slots_grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, g, s.failure);
+    else wf_scatter<T, NMAT, false><<<slots_grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, g, s.failure);
     if (ev) cudaEventRecord(ev[3], s.stream);
 }
 
@@ -583,6 +610,8 @@ void run_wavefront(Session& s, const Controls& c) {
             cudaEvent_t* ev = profile ? s.stage_events.data() + 4 * b : nullptr;
             if (nm == 1 && !paths) wave_iteration<T, 1, false>(s, v, P, c, dv, grid, ev);
             else if (nm == 1) wave_iteration<T, 1, true>(s, v, P, c, dv, grid, ev);
+            else if (nm == 4 && !paths) wave_iteration<T, 4, false>(s, v, P, c, dv, grid, ev);
+            else if (nm == 4) wave_iteration<T, 4, true>(s, v, P, c, dv, grid, ev);
             else if (!paths) wave_iteration<T, 3, false>(s, v, P, c, dv, grid, ev);
             else wave_iteration<T, 3, true>(s, v, P, c, dv, grid, ev);
         }
@@ -803,6 +832,10 @@ void* monki_cuda_create(uint32_t device, const double* tables, size_t table_coun
     try {
         Config cfg = parse_config(config);
         Prepared prep = parse(tables, table_count);
+        if ((prep.backward || prep.nmat == 4) && !cfg.wavefront)
+            throw std::runtime_error("backward transport and nmat 4 need engine=wavefront");
+        if (prep.backward && (cfg.epsilon > 0.0 || cfg.roulette > 0.0 || cfg.importance))
+            throw std::runtime_error("guided transport and importance tallies need forward transport");
         if (round_capacity < 1 || round_capacity > 4096) throw std::runtime_error("round_capacity must be in [1, 4096]");
         int n = 0;
         cudaError_t e = cudaGetDeviceCount(&n);
@@ -838,6 +871,8 @@ void* monki_cuda_create(uint32_t device, const double* tables, size_t table_coun
         W.locations = uint32_t(p.nx * p.ny * p.nz * p.angles);
         W.orders = cfg.orders ? W.count : 0u;
         if (cfg.orders) W.count += 4u * (pixels + 2u * W.locations);
+        W.vee = p.nmat == 4 ? W.count : 0u;
+        if (p.nmat == 4) W.count += pixels;
         W.shards = cfg.shards;
         const size_t elem = cfg.fp64 ? sizeof(double) : sizeof(float);
         const size_t per_round = cfg.wavefront ? W.count : L.count;
@@ -846,8 +881,10 @@ void* monki_cuda_create(uint32_t device, const double* tables, size_t table_coun
         check(cudaMemset(s->banks, 0, bank_bytes), "cudaMemset(banks)");
         check(cudaMalloc(&s->out, size_t(round_capacity) * L.count * sizeof(double)), "cudaMalloc(out)");
         std::vector<double> mu(size_t(p.angles));
+        // mu0/mu on forward Stokes tallies only (mc.f90:1456-1474).
         for (int ia = 0; ia < p.angles; ++ia)
-            mu[size_t(ia)] = std::fabs(std::cos(kDegToRad * p.vartheta0)) / std::fabs(std::cos(kDegToRad * p.vartheta[ia]));
+            mu[size_t(ia)] = p.backward ? 1.0
+                                        : std::fabs(std::cos(kDegToRad * p.vartheta0)) / std::fabs(std::cos(kDegToRad * p.vartheta[ia]));
         check(cudaMalloc(&s->mu0mu, mu.size() * sizeof(double)), "cudaMalloc(mu0mu)");
         check(cudaMemcpy(s->mu0mu, mu.data(), mu.size() * sizeof(double), cudaMemcpyHostToDevice), "upload(mu0mu)");
         check(cudaMalloc(&s->failure, sizeof(uint32_t)), "cudaMalloc(failure)");
@@ -878,8 +915,8 @@ void* monki_cuda_create(uint32_t device, const double* tables, size_t table_coun
         if (!per_sm) {
             if (cfg.wavefront) {
                 int blocks = 0;
-                const void* fn = cfg.fp64 ? reinterpret_cast<const void*>(&wf_peel<double, double, 3, true>)
-                                          : reinterpret_cast<const void*>(&wf_peel<float, float, 3, true>);
+                const void* fn = cfg.fp64 ? reinterpret_cast<const void*>(&wf_peel<double, double, 3, true, false>)
+                                          : reinterpret_cast<const void*>(&wf_peel<float, float, 3, true, false>);
                 check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, cfg.block, 0), "occupancy");
                 per_sm = std::max(blocks, 1);
             } else {
@@ -1187,6 +1224,8 @@ extern "C" int monki_cuda_run_static(uint32_t device, const double* tables, size
         }
 
         const Prepared p = parse(tables, table_count);
+        if (p.backward || p.nmat == 4)
+            throw std::runtime_error("backward transport and nmat 4 need the session API (engine=wavefront)");
         const Controls c{controls[0], controls[1], controls[2], controls[3], controls[4], controls[5], controls[6], controls[7]};
         if (!c.per_round || !c.rounds || !c.max_steps || uint64_t(c.first) + c.count > uint64_t(c.per_round) * c.rounds)
             throw std::runtime_error("Invalid CUDA round group");

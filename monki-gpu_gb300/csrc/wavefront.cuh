@@ -79,6 +79,9 @@ struct WaveTally {
     // surface, then their single-scattering part.
     uint32_t orders;
     uint32_t locations;  // nx * ny * nz * angles
+    // Circular polarization (nmat 4): element offset of one V record per pixel (the pixel
+    // records hold {I, Q, U, path weight}); order records carry V in their fourth element.
+    uint32_t vee;
 };
 
 template <typename T>
@@ -105,6 +108,11 @@ struct Pool {
     double* importance;   // 2 * nx * ny * nz
     const T* pixel_weight;  // nx * ny * angles weights of the contributions, or null (all 1)
     uint32_t* order;      // events so far of each slot's history (scattering-order tallies), or null
+    T* vee;               // V of the normalized Stokes vector (forward nmat 4), or null
+    // Backward transport: the weight matrix of each history, nmat * nmat elements
+    // (row-major, M11 = 1 after normalization), element e of slot s at matrix[e * capacity + s].
+    T* matrix;
+    uint32_t* first;      // backward with order tallies: the first event's cell (i | j << 12 | layer << 24)
 };
 
 __device__ __forceinline__ uint32_t pack_layers(int k, int k1, int wmin, int wmax) {
@@ -584,6 +592,11 @@ wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, 
         if (fresh) {
             P.dir[slot] = dir;
             if (P.ring_n) P.ring_n[slot] = 0u;
+            if (P.vee) P.vee[slot] = T(0);
+            if (P.matrix) {
+                const int nm = s.nmat;
+                for (int e = 0; e < nm * nm; ++e) P.matrix[size_t(e) * P.capacity + slot] = (e % (nm + 1) == 0) ? T(1) : T(0);
+            }
         }
     }
 
@@ -624,7 +637,7 @@ __device__ __forceinline__ uint32_t queue_entry(uint32_t* const* queue, uint32_t
 // ----------------------------------------------------------------------------------
 // peel: one event per thread, every view.
 // ----------------------------------------------------------------------------------
-template <typename T, typename TA, int NMAT, bool PATHS>
+template <typename T, typename TA, int NMAT, bool PATHS, bool BACKWARD>
 __global__ void __launch_bounds__(256, 3)
 wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ banks, WaveTally L,
         uint32_t* __restrict__ failure, unsigned long long* __restrict__ counters) {
@@ -653,7 +666,15 @@ wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ b
         const int sp = surface ? -1 : int(P.kind[slot]) - 1;
         const T x = pos.x, y = pos.y, z = pos.z, weight = pos.w;
         const T a = dir.x, b = dir.y, c = dir.z, phi = dir.w;
-        const T st[3] = {T(1), pol.x, pol.y};
+        const T st[4] = {T(1), pol.x, pol.y, (NMAT > 3 && P.vee) ? P.vee[slot] : T(0)};
+        // Backward transport: the history's weight matrix (M11 = 1).
+        T M[NMAT][NMAT];
+        if (BACKWARD) {
+#pragma unroll
+            for (int r = 0; r < NMAT; ++r)
+#pragma unroll
+                for (int q = 0; q < NMAT; ++q) M[r][q] = P.matrix[size_t(r * NMAT + q) * P.capacity + slot];
+        }
         const uint32_t round_offset = dv.per_round.div(pid);
         TA* bank = banks + (size_t(round_offset) * L.shards + shard) * L.count;
         Quad<TA>* pixrec = reinterpret_cast<Quad<TA>*>(bank);
@@ -667,12 +688,34 @@ wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ b
         // Scattering-order diagnostics: the event's history order and its location record
         // (layer 0 = an event on the surface).
         const uint32_t order = P.order ? P.order[slot] : 0u;
-        const uint32_t location_layer = (k == 0 && z < eps) ? 0u : uint32_t(k + 1);
+        uint32_t location_i = uint32_t(i), location_j = uint32_t(j);
+        uint32_t location_layer = (k == 0 && z < eps) ? 0u : uint32_t(k + 1);
+        if (BACKWARD && L.orders && P.first) {
+            // The sensor of backward transport looks at the history's first event.
+            if (order <= 1u) {
+                P.first[slot] = location_i | (location_j << 12) | (location_layer << 24);
+            } else {
+                const uint32_t w = P.first[slot];
+                location_i = w & 0xFFFu; location_j = (w >> 12) & 0xFFFu; location_layer = w >> 24;
+            }
+        }
+        // Backward transport registers every view at the injection column.
+        uint32_t inject_i = 0, inject_j = 0;
+        if (BACKWARD) {
+            const uint32_t column = dv.ncol.mod(pid - round_offset * ctl.per_round);
+            inject_j = dv.nx.div(column);
+            inject_i = column - inject_j * uint32_t(s.nx);
+            inject_j = min(inject_j, uint32_t(s.ny - 1));
+        }
         for (int ia = 0; ia < s.angles; ++ia) {
             const T vc = s.vc[ia];
-            T prob[3] = {T(0), T(0), T(0)};
+            T prob[4] = {T(0), T(0), T(0), T(0)};
             if (surface) {
-                prob[0] = vc > T(0) ? vc * weight : T(0);
+                if (vc > T(0)) {
+                    // Forward As S keeps I (= 1); backward M As S0 is the first column of M.
+                    if (BACKWARD) for (int m = 0; m < NMAT; ++m) prob[m] = M[m][0] * vc * weight;
+                    else prob[0] = vc * weight;
+                }
             } else {
                 // cos(phi - phi_view) from the sines and cosines of both azimuths.
                 const T cdphi = cphi * s.vcos_phi[ia] + sphi * s.vsin_phi[ia];
@@ -680,8 +723,20 @@ wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ b
                 const Rot<T> r = NMAT > 1 ? rotation_pre<T>(cs, c, vc, phi, s.vphi[ia], cphi, sphi, s.vcos_phi[ia], s.vsin_phi[ia])
                                           : Rot<T>{T(1), T(0), T(1), T(0)};
                 const Phase<T> f = phase<T>(s, sp, cs, NMAT);
-                T back[3];
-                scatter_stokes<T>(f, r, NMAT, st, back);
+                T back[4];
+                if (BACKWARD) {
+                    // M P^T S0: M times the first row of P, (F11, F12 C1, -F12 S1, 0).
+                    const T row[4] = {f.f11, f.f12 * r.c1, -f.f12 * r.s1, T(0)};
+#pragma unroll
+                    for (int m = 0; m < NMAT; ++m) {
+                        T acc = T(0);
+#pragma unroll
+                        for (int q = 0; q < NMAT; ++q) acc += M[m][q] * row[q];
+                        back[m] = acc;
+                    }
+                } else {
+                    scatter_stokes<T>(f, r, NMAT, st, back);
+                }
                 for (int m = 0; m < NMAT; ++m) prob[m] = back[m] * weight;
                 if (prob[0] < Tol<T>::negligible) for (int m = 0; m < NMAT; ++m) prob[m] = T(0);
             }
@@ -729,23 +784,26 @@ wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ b
             pi_ = pi_ < 0 ? pi_ + s.nx : (pi_ >= s.nx ? pi_ - s.nx : pi_);
             int pj_ = j + js * int(dv.ny.mod(dj));
             pj_ = pj_ < 0 ? pj_ + s.ny : (pj_ >= s.ny ? pj_ - s.ny : pj_);
-            const uint32_t pixel = uint32_t(pi_ + s.nx * (pj_ + s.ny * ia));
+            const uint32_t pixel = BACKWARD ? inject_i + uint32_t(s.nx) * (inject_j + uint32_t(s.ny) * uint32_t(ia))
+                                              : uint32_t(pi_ + s.nx * (pj_ + s.ny * ia));
             const T att = exp(-tau);
             const T w = prob[0] * att;
             contributed += P.pixel_weight ? w * __ldg(P.pixel_weight + pixel) : w;
+            const T q3 = NMAT > 3 ? prob[3] * att : T(0);
             if (L.orders) {
                 const T q1 = NMAT > 1 ? prob[1] * att : T(0), q2 = NMAT > 2 ? prob[2] * att : T(0);
                 Quad<TA>* single = reinterpret_cast<Quad<TA>*>(bank + L.orders);
                 Quad<TA>* located = single + L.pixels;
-                const uint32_t cell = uint32_t(i) + uint32_t(s.nx) * (uint32_t(j) + uint32_t(s.ny) * (location_layer + uint32_t(s.nz) * uint32_t(ia)));
-                quad_add(located + cell, TA(w), TA(q1), TA(q2), TA(0));
+                const uint32_t cell = location_i + uint32_t(s.nx) * (location_j + uint32_t(s.ny) * (location_layer + uint32_t(s.nz) * uint32_t(ia)));
+                quad_add(located + cell, TA(w), TA(q1), TA(q2), TA(q3));
                 if (order == 1u) {
-                    quad_add(single + pixel, TA(w), TA(q1), TA(q2), TA(0));
-                    quad_add(located + L.locations + cell, TA(w), TA(q1), TA(q2), TA(0));
+                    quad_add(single + pixel, TA(w), TA(q1), TA(q2), TA(q3));
+                    quad_add(located + L.locations + cell, TA(w), TA(q1), TA(q2), TA(q3));
                 }
             }
             quad_add(pixrec + pixel, TA(w), TA(NMAT > 1 ? prob[1] * att : T(0)), TA(NMAT > 2 ? prob[2] * att : T(0)),
                      TA(PATHS ? w : T(0)));
+            if (NMAT > 3 && q3 != T(0)) atomicAdd(bank + L.vee + pixel, TA(q3));
             ++updates;
             if (PATHS) {
                 Quad<TA>* rec = layrec + size_t(pixel) * (s.nz + 1);
@@ -855,7 +913,7 @@ __device__ __forceinline__ T ddis_factor(const SceneView<T>& s, const Guide<T>& 
     return q > T(0) ? p_an / q : T(0);
 }
 
-template <typename T, int NMAT>
+template <typename T, int NMAT, bool BACKWARD>
 __global__ void __launch_bounds__(256, 4)
 wf_scatter(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, Guide<T> g, uint32_t* __restrict__ failure) {
     const T eps = Tol<T>::eps;
@@ -876,7 +934,16 @@ wf_scatter(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, Guide<T> g, uin
         const Quad<T> dir0 = P.dir[slot];
         Quad<T> pol = P.pol[slot];
         const T a0 = dir0.x, b0 = dir0.y, c0 = dir0.z;
-        T a, b, c, phi_out, q = T(0), u = T(0);
+        T a, b, c, phi_out, q = T(0), u = T(0), v = T(0);
+        // Backward transport: the weight matrix (M11 = 1), updated by M P^T (M As at the
+        // surface) and renormalized by its M11.
+        T M[NMAT][NMAT];
+        if (BACKWARD) {
+#pragma unroll
+            for (int r = 0; r < NMAT; ++r)
+#pragma unroll
+                for (int col = 0; col < NMAT; ++col) M[r][col] = P.matrix[size_t(r * NMAT + col) * P.capacity + slot];
+        }
         const int ci = int(meta.z & 0xFFFF), cj = int(meta.z >> 16), ck = int(meta.w & 0xFF) - 1;
         T roulette = g.roulette;
         if (g.scale) roulette *= __ldg(g.scale + ci + s.nx * (cj + s.ny * ck));
@@ -892,10 +959,20 @@ wf_scatter(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, Guide<T> g, uin
             T sp, cp;
             sincos(phi_out, &sp, &cp);
             a = sine * cp; b = sine * sp; c = fabs(mu);
+            if (BACKWARD) {
+                // M As keeps the first column of M; then M / M11.
+                const T m11 = M[0][0];
+#pragma unroll
+                for (int r = 0; r < NMAT; ++r) {
+#pragma unroll
+                    for (int col = 1; col < NMAT; ++col) M[r][col] = T(0);
+                    M[r][0] = M[r][0] / m11;
+                }
+            }
         } else {
             const int sp = int(P.kind[slot]) - 1;
             const T phi = dir0.w;
-            T st[3] = {T(1), pol.x, pol.y};
+            T st[4] = {T(1), pol.x, pol.y, (NMAT > 3 && P.vee) ? P.vee[slot] : T(0)};
             T cos_out, dphi, cos_sca;
             const bool guided = sp >= 0 && g.epsilon > T(0) && pos.w < g.cap;
             if (guided && T(rng.next()) < g.epsilon) {
@@ -921,7 +998,7 @@ wf_scatter(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, Guide<T> g, uin
                 sincos(phi_out, &sp_, &cp_);
                 cos_sca = fmin(T(1), fmax(T(-1), a0 * (cp_ * so) + b0 * (sp_ * so) + c0 * cos_out));
             } else {
-                if (!sample_direction<T>(s, sp, NMAT, st, c0, rng, cos_out, dphi, cos_sca)) {
+                if (!sample_direction<T>(s, sp, NMAT, st, c0, rng, cos_out, dphi, cos_sca, BACKWARD ? T(1) : T(-1))) {
                     atomicOr(failure, kSamplingCap);
                     P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u);
                     continue;
@@ -930,15 +1007,40 @@ wf_scatter(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, Guide<T> g, uin
             }
             const Rot<T> r = NMAT > 1 ? rotation<T>(cos_sca, c0, cos_out, phi, phi_out) : Rot<T>{T(1), T(0), T(1), T(0)};
             const Phase<T> f = phase<T>(s, sp, cos_sca, NMAT);
-            T out[3];
-            scatter_stokes<T>(f, r, NMAT, st, out);
+            T out[4] = {T(0), T(0), T(0), T(0)};
+            if (BACKWARD) {
+                // M = M P^T; the sampling vector is (M11, M12, -M13, M14).
+                T Pm[4][4];
+                phase_matrix<T>(f, r, NMAT, Pm);
+                T next[NMAT][NMAT];
+#pragma unroll
+                for (int row = 0; row < NMAT; ++row)
+#pragma unroll
+                    for (int col = 0; col < NMAT; ++col) {
+                        T acc = T(0);
+#pragma unroll
+                        for (int k2 = 0; k2 < NMAT; ++k2) acc += M[row][k2] * Pm[col][k2];
+                        next[row][col] = acc;
+                    }
+                const T m11 = next[0][0];
+#pragma unroll
+                for (int row = 0; row < NMAT; ++row)
+#pragma unroll
+                    for (int col = 0; col < NMAT; ++col) M[row][col] = next[row][col] / m11;
+                out[0] = next[0][0];
+                if (NMAT > 1) { out[1] = next[0][1]; out[2] = -next[0][2]; }
+                if (NMAT > 3) out[3] = next[0][3];
+            } else {
+                scatter_stokes<T>(f, r, NMAT, st, out);
+            }
             // S / S(1): I becomes 1 (NaN when S(1) is 0 or not finite).
             const T s0 = out[0];
             const T one = s0 / s0;
             bool ok = isfinite(one);
             if (NMAT > 1) {
                 q = out[1] / s0; u = out[2] / s0;
-                ok = ok && isfinite(q) && isfinite(u) && sqrt(q * q + u * u) <= one + T(1e-2);
+                if (NMAT > 3) v = out[3] / s0;
+                ok = ok && isfinite(q) && isfinite(u) && isfinite(v) && sqrt(q * q + u * u + v * v) <= one + T(1e-2);
             }
             if (!ok) { atomicOr(failure, kInvalidStokes); P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u); continue; }
             const T so = sqrt(fmax(T(0), T(1) - cos_out * cos_out));
@@ -958,6 +1060,13 @@ wf_scatter(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, Guide<T> g, uin
             pos.z = fmax(T(0), __ldg(s.zunit + k) - pos.z);
         }
         pol.x = q; pol.y = u;
+        if (NMAT > 3 && P.vee) P.vee[slot] = v;
+        if (BACKWARD) {
+#pragma unroll
+            for (int r = 0; r < NMAT; ++r)
+#pragma unroll
+                for (int col = 0; col < NMAT; ++col) P.matrix[size_t(r * NMAT + col) * P.capacity + slot] = M[r][col];
+        }
         if (!surface) pol.z = -log(fmax(T(rng.next()), eps));
         meta.y = rng.draw;
         P.pos[slot] = pos;
@@ -997,7 +1106,7 @@ __global__ void wf_flush(const TA* __restrict__ banks, WaveTally L, int nmat, in
             const uint32_t m = o % uint32_t(nmat);
             const uint32_t pixel = o / uint32_t(nmat);
             const uint32_t ia = pixel / uint32_t(nx * ny);
-            value = sum(size_t(pixel) * 4 + m) * mu0mu[ia];
+            value = (m < 3 ? sum(size_t(pixel) * 4 + m) : sum(size_t(L.vee) + pixel)) * mu0mu[ia];
         } else if (paths && o < stokes_out + pixels * uint32_t(nz)) {
             const uint32_t q = o - stokes_out;  // i + nx * (j + ny * (k + nz * ia))
             const uint32_t i = q % nx;

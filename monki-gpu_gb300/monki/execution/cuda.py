@@ -175,13 +175,16 @@ class CUDA(Backend):
         if not isinstance(scene, TransportScene):
             raise TypeError("CUDA.prepare expects a TransportScene or a ReferenceCase")
 
-        if scene.backward:
-            raise NotImplementedError("CUDA backward transport is not implemented")
-
         tables = np.array(scene.tables, dtype=np.float64, copy=True)
 
         if tables.ndim != 1 or tables.size < 18 or not np.all(np.isfinite(tables)):
             raise ValueError("Invalid/nonfinite prepared transport export")
+
+        if bool(scene.backward) != bool(tables[11]):
+            raise ValueError("scene.backward disagrees with the backward flag of its table stream")
+
+        if scene.backward and (self.guided is not None or self.importance_tally):
+            raise ValueError("guided transport and importance tallies need forward transport")
 
         if self.save_path is not None:
             tables[10] = float(self.save_path)

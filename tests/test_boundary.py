@@ -112,7 +112,9 @@ def test_equal_extinction_rectangles_tile_each_band_layer(native, name, fp64):
         assert layers == 0
 
 
-@pytest.mark.parametrize("field,value", [(0, 3), (4, 4), (7, 1), (11, 1), (6, 4)])
+# version 4; nmat 2; nmat 4 with particles but no F34 / F44 tables; version 3 without
+# them (truncated); source off the top; four particle species
+@pytest.mark.parametrize("field,value", [(0, 4), (4, 2), (4, 4), (0, 3), (7, 1), (6, 4)])
 def test_packer_rejects_unsupported_tables(native, field, value):
     import monki.scenes as scenes
     from monki.execution.native import F64P
