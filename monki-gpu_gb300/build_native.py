@@ -19,7 +19,7 @@ from pathlib import Path
 PACKAGE_ROOT = Path(__file__).resolve().parent
 SOURCES = PACKAGE_ROOT / "csrc"
 OUTPUT = PACKAGE_ROOT / "monki" / "_native" / "libmonki_cuda.so"
-UNITS = ("session.cu", "probes.cu", "mlp.cu")
+UNITS = ("session.cu", "tail.cu", "probes.cu", "mlp.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

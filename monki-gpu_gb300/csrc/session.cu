@@ -17,6 +17,7 @@
 #include <mutex>
 #include <vector>
 
+#include "tail.h"
 #include "statistics.cuh"
 #include "wavefront.cuh"
 
@@ -42,6 +43,7 @@ struct Config {
     bool graphs = true;          // replay each batch of wavefront iterations as a CUDA graph
     bool orders = false;         // scattering-order diagnostics (single scattering, locations)
     bool rectangles = true;      // cross equal-extinction rectangles of the band in one step
+    uint32_t tail = 1u << 16;    // run a group's last photons to their end in one launch below this many (0 = off)
 };
 
 Config parse_config(const char* text) {
@@ -96,6 +98,7 @@ Config parse_config(const char* text) {
         else if (key == "graphs") c.graphs = as_int(0, 1) != 0;
         else if (key == "orders") c.orders = as_int(0, 1) != 0;
         else if (key == "rectangles") c.rectangles = as_int(0, 1) != 0;
+        else if (key == "tail") c.tail = uint32_t(as_int(0, 1l << 26));
         else throw std::runtime_error("Unknown config key: " + key);
     }
     if (c.block % 32) throw std::runtime_error("block must be a multiple of 32");
@@ -403,6 +406,8 @@ struct Session {
     double* mu0mu = nullptr;
     uint32_t* failure = nullptr;
     unsigned long long* counters = nullptr;
+    uint32_t* tail_next = nullptr;   // slot counter of the tail launch
+    uint64_t tails = 0;              // tail launches so far
     uint32_t round_capacity = 1;
     TallyLayout layout{};       // output layout (and the megakernel's device layout)
     WaveTally wave{};           // wavefront device layout
@@ -597,7 +602,7 @@ void run_wavefront(Session& s, const Controls& c) {
     const int nm = s.prep.nmat;
     const bool paths = s.prep.paths;
     const uint64_t limit = uint64_t(c.max_steps) + 16;  // events per photon are bounded by its steps
-    uint64_t it = 0;
+    uint64_t it = 0, launches = 0;
     const bool profile = c.profile != 0;
     if (profile && s.stage_events.size() < 4 * size_t(s.cfg.check_every)) {
         for (cudaEvent_t e : s.stage_events) cudaEventDestroy(e);
@@ -648,6 +653,7 @@ void run_wavefront(Session& s, const Controls& c) {
         if (exec) check(cudaGraphLaunch(exec, s.stream), "graph launch");
         else batch();
         it += s.cfg.check_every;
+        launches += 3 * uint64_t(s.cfg.check_every);
         check(cudaGetLastError(), "wavefront launch");
         check(cudaStreamSynchronize(s.stream), "wavefront");
         if (profile) {
@@ -664,10 +670,24 @@ void run_wavefront(Session& s, const Controls& c) {
         // Done when every photon was claimed and none is queued for an event or paused
         // mid-walk by the per-launch step budget.
         if (h[4] >= c.count && h[0] == 0 && h[1] == 0 && h[2] == 0 && h[3] == 0) break;
+        // Few photons left and none to claim: run each to its end in one launch (not while
+        // timing stages, which keeps the three kernels apart).
+        const uint64_t live = uint64_t(h[0]) + h[1] + h[2] + h[3];
+        if (!profile && s.cfg.tail && h[4] >= c.count && live <= s.cfg.tail) {
+            Guide<T> g{T(s.cfg.epsilon), T(s.cfg.roulette), s.cfg.cap > 0.0 ? T(s.cfg.cap) : T(INFINITY),
+                       static_cast<const T*>(s.scale)};
+            check(launch_tail<T>(v, c, dv, P, static_cast<T*>(s.banks), s.wave, g, s.failure, s.counters, s.tail_next,
+                                 s.stream), "tail launch");
+            check(cudaMemsetAsync(P.counts, 0, 4 * sizeof(uint32_t), s.stream), "memset(queues)");
+            check(cudaStreamSynchronize(s.stream), "tail");
+            s.tails += 1;
+            launches += 1;
+            break;  // every photon of the group has ended
+        }
         if (it > limit * 4 + 1024 && it > 1000000) throw std::runtime_error("wavefront did not drain");
     }
     s.iterations += it;
-    s.totals[5] += 3 * it;
+    s.totals[5] += launches;
 }
 
 template <typename T>
@@ -685,7 +705,7 @@ void destroy(Session* s) {
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
     cudaFree(s->scene); cudaFree(s->banks); cudaFree(s->out); cudaFree(s->mu0mu);
-    cudaFree(s->failure); cudaFree(s->counters);
+    cudaFree(s->failure); cudaFree(s->counters); cudaFree(s->tail_next);
     cudaFree(s->pool_memory); cudaFree(s->flush_info); cudaFree(s->scale); cudaFree(s->importance); cudaFree(s->pixel_weight);
     cudaFree(s->stats); cudaFree(s->history);
     if (s->host_counts) cudaFreeHost(s->host_counts);
@@ -888,6 +908,7 @@ void* monki_cuda_create(uint32_t device, const double* tables, size_t table_coun
         check(cudaMalloc(&s->mu0mu, mu.size() * sizeof(double)), "cudaMalloc(mu0mu)");
         check(cudaMemcpy(s->mu0mu, mu.data(), mu.size() * sizeof(double), cudaMemcpyHostToDevice), "upload(mu0mu)");
         check(cudaMalloc(&s->failure, sizeof(uint32_t)), "cudaMalloc(failure)");
+        check(cudaMalloc(&s->tail_next, sizeof(uint32_t)), "cudaMalloc(tail)");
         check(cudaMalloc(&s->counters, 4 * sizeof(unsigned long long)), "cudaMalloc(counters)");
         if (cfg.fp64) upload<double>(*s); else upload<float>(*s);
         if (cfg.importance) {

@@ -1,0 +1,23 @@
+// Host entry of the tail launch (tail.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "scene.h"
+
+namespace monki {
+
+struct Controls;
+struct Divisors;
+struct WaveTally;
+template <typename T> struct Pool;
+
+// Runs every photon left in the pool to its end in one launch on `stream` (each thread
+// takes live slots through the counter *next, which the launch clears first). Call it only
+// once every photon of the round group is claimed.
+template <typename T>
+cudaError_t launch_tail(const SceneView<T>& v, const Controls& c, const Divisors& dv, const Pool<T>& P, T* banks,
+                        const WaveTally& W, const Guide<T>& g, uint32_t* failure, unsigned long long* counters,
+                        uint32_t* next, cudaStream_t stream);
+
+}  // namespace monki

@@ -196,6 +196,33 @@ __device__ __forceinline__ uint32_t warp_reserve(uint32_t* counters, int key = 0
     return base + uint32_t(__popc(group & ((1u << lane) - 1u)));
 }
 
+// Sum N per-thread counters over the block and add each nonzero total to its target from
+// one thread. Per-warp atomics on a few shared addresses serialize in L2: tens of
+// thousands of them cost a launch over ten microseconds even when it has no work.
+template <int N, typename U>
+__device__ __forceinline__ void block_add(const unsigned long long (&v)[N], U* const (&target)[N]) {
+    __shared__ unsigned long long part[N][32];
+    const int warp = int(threadIdx.x >> 5), lane = int(threadIdx.x & 31);
+    const int warps = int((blockDim.x + 31) >> 5);
+#pragma unroll
+    for (int q = 0; q < N; ++q) {
+        unsigned long long x = v[q];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+        if (lane == 0) part[q][warp] = x;
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int q = 0; q < N; ++q) {
+            unsigned long long x = lane < warps ? part[q][lane] : 0ull;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+            if (lane == 0 && x) atomicAdd(target[q], U(x));
+        }
+    }
+}
+
 // Add v to the wander entry of layer kk, keeping [wmin, wmax] the only valid range:
 // entries newly covered by the range are zeroed first, so a new photon needs no clearing.
 template <typename T>
@@ -413,206 +440,231 @@ __device__ __forceinline__ int uniform_jump(const SceneView<T>& s, int& k, T& z,
 // ----------------------------------------------------------------------------------
 // transit: free path to the next interaction for every pooled photon.
 // ----------------------------------------------------------------------------------
+// One slot's walk to its next event: claims a photon into an empty slot (when claims are
+// open), walks it, selects the interaction and stores the state. Returns the event's queue
+// (surface, gas, particle) or -1 when the slot holds no event (empty, finished, or paused
+// by the step budget). QUEUE enqueues the event for the peel and scatter launches; without
+// it the caller handles the event (the tail kernel).
+template <typename T, bool PATHS, bool QUEUE>
+__device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s, const T* band, const Controls& ctl,
+                                            const Divisors& dv, const Pool<T>& P, uint32_t walk, bool may_claim,
+                                            uint32_t* __restrict__ failure, uint64_t& scatters, uint64_t& visits,
+                                            uint32_t& paused) {
+    const T eps = Tol<T>::eps;
+    const int top = s.nz - 1;
+    int event = -1;
+    const uint4 meta = P.meta[slot];
+    uint32_t pid = meta.x;
+    DrawStream rng;
+    int i = 0, j = 0, k = 0, k1 = -2, wmin = 255, wmax = 0;
+    Quad<T> pos{}, dir{}, pol{};
+    uint32_t steps = 0, budget = walk, order = 0;
+    bool fresh = false;
+    PathRecord<T> path{PATHS ? P.wander + size_t(slot) * s.nz : nullptr, 255, 0, kNoRuns, T(0), T(0)};
+
+    if (pid != kNone) {
+        const uint32_t ro = dv.per_round.div(pid);
+        rng.init(pid - ro * ctl.per_round, ctl.first_round + ro, ctl.seed, meta.y);
+        i = int(meta.z & 0xFFFF); j = int(meta.z >> 16);
+        unpack_layers(meta.w, k, k1, wmin, wmax);
+        pos = P.pos[slot];
+        dir = P.dir[slot];
+        pol = P.pol[slot];
+        steps = P.steps[slot];
+        if (P.order) order = P.order[slot];
+        if (PATHS) {
+            path.runs = P.runs[slot];
+            path.ci0 = P.run_ci[2 * size_t(slot)];
+            path.ci1 = P.run_ci[2 * size_t(slot) + 1];
+        }
+    }
+    path.wmin = wmin; path.wmax = wmax;
+    T& x = pos.x; T& y = pos.y; T& z = pos.z; T& weight = pos.w;
+    T& remains = pol.z; T& init_part = pol.w;
+
+    for (;;) {
+        if (pid == kNone) {
+            // Read first so a drained group stops reserving (the counter never wraps).
+            if (!may_claim || *reinterpret_cast<volatile uint32_t*>(P.counts + 4) >= ctl.count) break;
+            const uint32_t n = warp_reserve(P.counts + 4);
+            if (n >= ctl.count) break;
+            pid = ctl.first + n;
+            const uint32_t ro = dv.per_round.div(pid);
+            const uint32_t photon = pid - ro * ctl.per_round;
+            rng.init(photon, ctl.first_round + ro, ctl.seed, 0u);
+            const uint32_t column = dv.ncol.mod(photon);
+            const uint32_t row = dv.nx.div(column);
+            i = int(column - row * uint32_t(s.nx));
+            j = min(int(row), s.ny - 1);
+            k = top;
+            x = s.xunit * T(rng.next());
+            y = s.yunit * T(rng.next());
+            z = __ldg(s.zunit + k);
+            weight = T(1);
+            order = 0;
+            dir = Quad<T>{s.a0, s.b0, s.c0, s.phi0};
+            pol.x = T(0); pol.y = T(0);
+            steps = 0;
+            k1 = -2; init_part = T(0);
+            path.wmin = 255; path.wmax = 0; path.runs = kNoRuns;
+            remains = -log(fmax(T(rng.next()), eps));
+            fresh = true;
+        }
+        const T a = dir.x, b = dir.y, c = dir.z;
+        const int is = signbit(a) ? -1 : 1, js = signbit(b) ? -1 : 1, ks = signbit(c) ? -1 : 1;
+        const T aa = fabs(a), ba = fabs(b), ca = fabs(c);
+        const T ai = T(1) / fmax(aa, eps), bi = T(1) / fmax(ba, eps), ci = T(1) / fmax(ca, eps);
+        // Path length of the current layer, added to the wander array on layer change.
+        const bool record = PATHS && k1 > -2;
+        int acc_k = -1;
+        T acc = T(0);
+        int outcome = -1;  // 0 atmosphere, 1 surface, 2 escaped, 3 step limit, 4 paused
+        for (;;) {
+            if (budget == 0) { outcome = 4; break; }
+            --budget;
+            if (++steps > ctl.max_steps) { outcome = 3; break; }
+            ++visits;
+            if (__ldg(s.layer_beta + k) >= T(0)) {
+                outcome = uniform_jump<T>(s, k, z, remains, ks, ca, ci, record, path, i, x, is, aa, j, y, js, ba);
+                if (outcome >= 0) break;
+                continue;
+            }
+            const T bv = k < top ? band_beta<T>(s, band, i, j, k) : T(0);
+            int ex = 0, ey = 0;
+            if (k < top) rectangle_reach(s, i, j, k, is, js, ex, ey);
+            if (bv > eps) {
+                const T de = remains / bv;
+                if (de < (ex ? x + T(ex) * s.xunit : x) * ai && de < (ey ? y + T(ey) * s.yunit : y) * bi &&
+                    de < z * ci) {
+                    move_within(i, x, is, aa * de, s.xunit, s.xinv, s.nx, ex);
+                    move_within(j, y, js, ba * de, s.yunit, s.yinv, s.ny, ey);
+                    z = fmax(T(0), z - ca * de);
+                    if (record) {
+                        if (acc_k != k) {
+                            if (acc_k >= 0) path.add(acc_k, acc);
+                            acc_k = k; acc = T(0);
+                        }
+                        acc += de;
+                    }
+                    outcome = 0;
+                    break;
+                }
+            }
+            const int k_old = k;
+            const T dist = advance_rectangle(s, i, j, k, x, y, z, is, js, ks, aa, ba, ca, ai, bi, ci, ex, ey);
+            if (record) {
+                if (acc_k != k_old) {
+                    if (acc_k >= 0) path.add(acc_k, acc);
+                    acc_k = k_old; acc = T(0);
+                }
+                acc += dist;
+            }
+            remains -= dist * bv;
+            if (k >= 0 && k <= top) continue;
+            outcome = k > top ? 2 : 1;
+            break;
+        }
+        if (PATHS && acc_k >= 0) path.add(acc_k, acc);
+        if (outcome == 4) { ++paused; break; }  // budget spent: the walk resumes next iteration
+        // A finished history leaves its slot empty until the next launch, where it is
+        // refilled before the walks start: claiming and walking a second photon here
+        // would make the whole warp wait on the few lanes whose photon escaped.
+        if (outcome == 3) { atomicOr(failure, kHistoryCap); pid = kNone; break; }
+        if (outcome == 2) { pid = kNone; break; }
+        int kind;
+        if (outcome == 1) {
+            if (PATHS && k1 == -2) { k1 = -1; init_part = T(0); }
+            k = 0;
+            z = T(0);
+            weight *= __ldg(s.albedo + i + s.nx * j);
+            if (weight < eps) { pid = kNone; break; }
+            kind = 255;
+        } else {
+            if (PATHS && k1 == -2) {
+                k1 = k;
+                init_part = (__ldg(s.zunit + k) - z) * ci;
+            }
+            const T rtemp = T(rng.next());
+            int sp = -1;
+            const T* cellp = s.cells + 4 * (i + s.nx * (j + s.ny * k));
+            for (int q = 0; q < s.ntypes; ++q)
+                if (__ldg(cellp + 1 + q) > rtemp) { sp = q; break; }
+            weight *= sp < 0 ? __ldg(s.ssalb_gas + k) : s.ssalb_aer[sp];
+            if (weight < eps) { pid = kNone; break; }
+            kind = sp + 1;
+        }
+        ++scatters;
+        ++order;
+        const int queue = kind == 255 ? kQueueSurface : (kind == 0 ? kQueueGas : kQueueParticle);
+        if (QUEUE) {
+            const uint32_t at = warp_reserve(P.counts, queue);
+            P.queue[queue][at] = slot;
+        }
+        P.kind[slot] = uint8_t(kind);
+        event = queue;
+        break;
+    }
+
+    if (pid == kNone) {
+        if (meta.x != kNone) P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u);
+        return -1;
+    }
+    P.meta[slot] = make_uint4(pid, rng.draw, uint32_t(i) | (uint32_t(j) << 16), pack_layers(k, k1, path.wmin, path.wmax));
+    P.steps[slot] = steps;
+    if (P.order) P.order[slot] = order;
+    if (PATHS) {
+        P.runs[slot] = path.runs;
+        P.run_ci[2 * size_t(slot)] = path.ci0;
+        P.run_ci[2 * size_t(slot) + 1] = path.ci1;
+    }
+    P.pos[slot] = pos;
+    P.pol[slot] = pol;
+    if (fresh) {
+        P.dir[slot] = dir;
+        if (P.ring_n) P.ring_n[slot] = 0u;
+        if (P.vee) P.vee[slot] = T(0);
+        if (P.matrix) {
+            const int nm = s.nmat;
+            for (int e = 0; e < nm * nm; ++e) P.matrix[size_t(e) * P.capacity + slot] = (e % (nm + 1) == 0) ? T(1) : T(0);
+        }
+    }
+    return event;
+}
+
+template <typename T, bool PATHS>
+__device__ __forceinline__ void transit_phase(const SceneView<T>& s, const T* band, const Controls& ctl,
+                                              const Divisors& dv, const Pool<T>& P, uint32_t walk,
+                                              uint32_t* __restrict__ failure,
+                                              unsigned long long* __restrict__ counters) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    uint64_t scatters = 0, visits = 0;
+    uint32_t paused = 0;
+    // Once every photon of the group is claimed (the counter only grows), empty slots stop
+    // at once: one read per block instead of one per empty lane on a single address.
+    __shared__ uint32_t claims_open;
+    if (threadIdx.x == 0) claims_open = *reinterpret_cast<volatile uint32_t*>(P.counts + 4) < ctl.count;
+    __syncthreads();
+    const bool may_claim = claims_open != 0u;
+
+    for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < P.capacity; slot += stride) {
+        transit_slot<T, PATHS, true>(slot, s, band, ctl, dv, P, walk, may_claim, failure, scatters, visits, paused);
+    }
+
+    const unsigned long long totals[2] = {scatters, visits};
+    unsigned long long* const targets[2] = {counters + 0, counters + 1};
+    block_add<2>(totals, targets);
+    const unsigned long long held[1] = {paused};
+    uint32_t* const held_target[1] = {P.counts + 3};
+    block_add<1>(held, held_target);
+}
+
 template <typename T, bool PATHS>
 __global__ void __launch_bounds__(256, 4)
 wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, uint32_t* __restrict__ failure,
            unsigned long long* __restrict__ counters) {
     extern __shared__ __align__(16) unsigned char staged[];
     const T* band = stage_band<T>(s, staged, failure);
-    const T eps = Tol<T>::eps;
-    const int top = s.nz - 1;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    uint64_t scatters = 0, visits = 0;
-    uint32_t paused = 0;
-
-    for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < P.capacity; slot += stride) {
-        const uint4 meta = P.meta[slot];
-        uint32_t pid = meta.x;
-        DrawStream rng;
-        int i = 0, j = 0, k = 0, k1 = -2, wmin = 255, wmax = 0;
-        Quad<T> pos{}, dir{}, pol{};
-        uint32_t steps = 0, budget = walk, order = 0;
-        bool fresh = false;
-        PathRecord<T> path{PATHS ? P.wander + size_t(slot) * s.nz : nullptr, 255, 0, kNoRuns, T(0), T(0)};
-
-        if (pid != kNone) {
-            const uint32_t ro = dv.per_round.div(pid);
-            rng.init(pid - ro * ctl.per_round, ctl.first_round + ro, ctl.seed, meta.y);
-            i = int(meta.z & 0xFFFF); j = int(meta.z >> 16);
-            unpack_layers(meta.w, k, k1, wmin, wmax);
-            pos = P.pos[slot];
-            dir = P.dir[slot];
-            pol = P.pol[slot];
-            steps = P.steps[slot];
-            if (P.order) order = P.order[slot];
-            if (PATHS) {
-                path.runs = P.runs[slot];
-                path.ci0 = P.run_ci[2 * size_t(slot)];
-                path.ci1 = P.run_ci[2 * size_t(slot) + 1];
-            }
-        }
-        path.wmin = wmin; path.wmax = wmax;
-        T& x = pos.x; T& y = pos.y; T& z = pos.z; T& weight = pos.w;
-        T& remains = pol.z; T& init_part = pol.w;
-
-        for (;;) {
-            if (pid == kNone) {
-                // Read first so a drained group stops reserving (the counter never wraps).
-                if (*reinterpret_cast<volatile uint32_t*>(P.counts + 4) >= ctl.count) break;
-                const uint32_t n = warp_reserve(P.counts + 4);
-                if (n >= ctl.count) break;
-                pid = ctl.first + n;
-                const uint32_t ro = dv.per_round.div(pid);
-                const uint32_t photon = pid - ro * ctl.per_round;
-                rng.init(photon, ctl.first_round + ro, ctl.seed, 0u);
-                const uint32_t column = dv.ncol.mod(photon);
-                const uint32_t row = dv.nx.div(column);
-                i = int(column - row * uint32_t(s.nx));
-                j = min(int(row), s.ny - 1);
-                k = top;
-                x = s.xunit * T(rng.next());
-                y = s.yunit * T(rng.next());
-                z = __ldg(s.zunit + k);
-                weight = T(1);
-                order = 0;
-                dir = Quad<T>{s.a0, s.b0, s.c0, s.phi0};
-                pol.x = T(0); pol.y = T(0);
-                steps = 0;
-                k1 = -2; init_part = T(0);
-                path.wmin = 255; path.wmax = 0; path.runs = kNoRuns;
-                remains = -log(fmax(T(rng.next()), eps));
-                fresh = true;
-            }
-            const T a = dir.x, b = dir.y, c = dir.z;
-            const int is = signbit(a) ? -1 : 1, js = signbit(b) ? -1 : 1, ks = signbit(c) ? -1 : 1;
-            const T aa = fabs(a), ba = fabs(b), ca = fabs(c);
-            const T ai = T(1) / fmax(aa, eps), bi = T(1) / fmax(ba, eps), ci = T(1) / fmax(ca, eps);
-            // Path length of the current layer, added to the wander array on layer change.
-            const bool record = PATHS && k1 > -2;
-            int acc_k = -1;
-            T acc = T(0);
-            int outcome = -1;  // 0 atmosphere, 1 surface, 2 escaped, 3 step limit, 4 paused
-            for (;;) {
-                if (budget == 0) { outcome = 4; break; }
-                --budget;
-                if (++steps > ctl.max_steps) { outcome = 3; break; }
-                ++visits;
-                if (__ldg(s.layer_beta + k) >= T(0)) {
-                    outcome = uniform_jump<T>(s, k, z, remains, ks, ca, ci, record, path, i, x, is, aa, j, y, js, ba);
-                    if (outcome >= 0) break;
-                    continue;
-                }
-                const T bv = k < top ? band_beta<T>(s, band, i, j, k) : T(0);
-                int ex = 0, ey = 0;
-                if (k < top) rectangle_reach(s, i, j, k, is, js, ex, ey);
-                if (bv > eps) {
-                    const T de = remains / bv;
-                    if (de < (ex ? x + T(ex) * s.xunit : x) * ai && de < (ey ? y + T(ey) * s.yunit : y) * bi &&
-                        de < z * ci) {
-                        move_within(i, x, is, aa * de, s.xunit, s.xinv, s.nx, ex);
-                        move_within(j, y, js, ba * de, s.yunit, s.yinv, s.ny, ey);
-                        z = fmax(T(0), z - ca * de);
-                        if (record) {
-                            if (acc_k != k) {
-                                if (acc_k >= 0) path.add(acc_k, acc);
-                                acc_k = k; acc = T(0);
-                            }
-                            acc += de;
-                        }
-                        outcome = 0;
-                        break;
-                    }
-                }
-                const int k_old = k;
-                const T dist = advance_rectangle(s, i, j, k, x, y, z, is, js, ks, aa, ba, ca, ai, bi, ci, ex, ey);
-                if (record) {
-                    if (acc_k != k_old) {
-                        if (acc_k >= 0) path.add(acc_k, acc);
-                        acc_k = k_old; acc = T(0);
-                    }
-                    acc += dist;
-                }
-                remains -= dist * bv;
-                if (k >= 0 && k <= top) continue;
-                outcome = k > top ? 2 : 1;
-                break;
-            }
-            if (PATHS && acc_k >= 0) path.add(acc_k, acc);
-            if (outcome == 4) { ++paused; break; }  // budget spent: the walk resumes next iteration
-            // A finished history leaves its slot empty until the next launch, where it is
-            // refilled before the walks start: claiming and walking a second photon here
-            // would make the whole warp wait on the few lanes whose photon escaped.
-            if (outcome == 3) { atomicOr(failure, kHistoryCap); pid = kNone; break; }
-            if (outcome == 2) { pid = kNone; break; }
-            int kind;
-            if (outcome == 1) {
-                if (PATHS && k1 == -2) { k1 = -1; init_part = T(0); }
-                k = 0;
-                z = T(0);
-                weight *= __ldg(s.albedo + i + s.nx * j);
-                if (weight < eps) { pid = kNone; break; }
-                kind = 255;
-            } else {
-                if (PATHS && k1 == -2) {
-                    k1 = k;
-                    init_part = (__ldg(s.zunit + k) - z) * ci;
-                }
-                const T rtemp = T(rng.next());
-                int sp = -1;
-                const T* cellp = s.cells + 4 * (i + s.nx * (j + s.ny * k));
-                for (int q = 0; q < s.ntypes; ++q)
-                    if (__ldg(cellp + 1 + q) > rtemp) { sp = q; break; }
-                weight *= sp < 0 ? __ldg(s.ssalb_gas + k) : s.ssalb_aer[sp];
-                if (weight < eps) { pid = kNone; break; }
-                kind = sp + 1;
-            }
-            ++scatters;
-            ++order;
-            const int queue = kind == 255 ? kQueueSurface : (kind == 0 ? kQueueGas : kQueueParticle);
-            const uint32_t at = warp_reserve(P.counts, queue);
-            P.queue[queue][at] = slot;
-            P.kind[slot] = uint8_t(kind);
-            break;
-        }
-
-        if (pid == kNone) {
-            if (meta.x != kNone) P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u);
-            continue;
-        }
-        P.meta[slot] = make_uint4(pid, rng.draw, uint32_t(i) | (uint32_t(j) << 16), pack_layers(k, k1, path.wmin, path.wmax));
-        P.steps[slot] = steps;
-        if (P.order) P.order[slot] = order;
-        if (PATHS) {
-            P.runs[slot] = path.runs;
-            P.run_ci[2 * size_t(slot)] = path.ci0;
-            P.run_ci[2 * size_t(slot) + 1] = path.ci1;
-        }
-        P.pos[slot] = pos;
-        P.pol[slot] = pol;
-        if (fresh) {
-            P.dir[slot] = dir;
-            if (P.ring_n) P.ring_n[slot] = 0u;
-            if (P.vee) P.vee[slot] = T(0);
-            if (P.matrix) {
-                const int nm = s.nmat;
-                for (int e = 0; e < nm * nm; ++e) P.matrix[size_t(e) * P.capacity + slot] = (e % (nm + 1) == 0) ? T(1) : T(0);
-            }
-        }
-    }
-
-    unsigned long long v0 = scatters, v1 = visits;
-    uint32_t v2 = paused;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        v0 += __shfl_down_sync(0xffffffffu, v0, off);
-        v1 += __shfl_down_sync(0xffffffffu, v1, off);
-        v2 += __shfl_down_sync(0xffffffffu, v2, off);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(counters + 0, v0);
-        atomicAdd(counters + 1, v1);
-        if (v2) atomicAdd(P.counts + 3, v2);
-    }
+    transit_phase<T, PATHS>(s, band, ctl, dv, P, walk, failure, counters);
 }
 
 // 128-bit tally update (FP32: one vector atomic; FP64: per nonzero element).
@@ -637,14 +689,224 @@ __device__ __forceinline__ uint32_t queue_entry(uint32_t* const* queue, uint32_t
 // ----------------------------------------------------------------------------------
 // peel: one event per thread, every view.
 // ----------------------------------------------------------------------------------
+// Peel-off of one event (slot) to every view: the phase matrix, the optical depth along
+// each view ray, the register pixel and the tallies (Stokes, layer paths, order records,
+// importance ring).
 template <typename T, typename TA, int NMAT, bool PATHS, bool BACKWARD>
-__global__ void __launch_bounds__(256, 3)
-wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ banks, WaveTally L,
-        uint32_t* __restrict__ failure, unsigned long long* __restrict__ counters) {
-    extern __shared__ __align__(16) unsigned char staged[];
-    const T* band = stage_band<T>(s, staged, failure);
+__device__ __forceinline__ void peel_event(uint32_t slot, bool surface, const uint4& meta, const SceneView<T>& s,
+                                           const T* band, const Controls& ctl, const Divisors& dv, const Pool<T>& P,
+                                           TA* __restrict__ banks, const WaveTally& L, uint32_t shard,
+                                           uint32_t* __restrict__ failure, uint64_t& visits, uint64_t& updates) {
     const T eps = Tol<T>::eps;
     const int top = s.nz - 1;
+    const uint32_t pid = meta.x;
+    const int i = int(meta.z & 0xFFFF), j = int(meta.z >> 16);
+    int k, k1, wmin, wmax;
+    unpack_layers(meta.w, k, k1, wmin, wmax);
+    const Quad<T> pos = P.pos[slot];
+    const Quad<T> dir = P.dir[slot];
+    const Quad<T> pol = P.pol[slot];
+    const int sp = surface ? -1 : int(P.kind[slot]) - 1;
+    const T x = pos.x, y = pos.y, z = pos.z, weight = pos.w;
+    const T a = dir.x, b = dir.y, c = dir.z, phi = dir.w;
+    const T st[4] = {T(1), pol.x, pol.y, (NMAT > 3 && P.vee) ? P.vee[slot] : T(0)};
+    // Backward transport: the history's weight matrix (M11 = 1).
+    T M[NMAT][NMAT];
+    if (BACKWARD) {
+#pragma unroll
+        for (int r = 0; r < NMAT; ++r)
+#pragma unroll
+            for (int q = 0; q < NMAT; ++q) M[r][q] = P.matrix[size_t(r * NMAT + q) * P.capacity + slot];
+    }
+    const uint32_t round_offset = dv.per_round.div(pid);
+    TA* bank = banks + (size_t(round_offset) * L.shards + shard) * L.count;
+    Quad<TA>* pixrec = reinterpret_cast<Quad<TA>*>(bank);
+    Quad<TA>* layrec = reinterpret_cast<Quad<TA>*>(bank + 4 * size_t(L.pixels));
+    const T* wander = PATHS ? P.wander + size_t(slot) * s.nz : nullptr;
+    const T sin_c = sqrt(fmax(eps, T(1) - c * c));
+    T sphi, cphi;
+    sincos(phi, &sphi, &cphi);
+    T contributed = T(0);  // Stokes-I peel-off of this event, all views
+    bool failed = false;
+    // Scattering-order diagnostics: the event's history order and its location record
+    // (layer 0 = an event on the surface).
+    const uint32_t order = P.order ? P.order[slot] : 0u;
+    uint32_t location_i = uint32_t(i), location_j = uint32_t(j);
+    uint32_t location_layer = (k == 0 && z < eps) ? 0u : uint32_t(k + 1);
+    if (BACKWARD && L.orders && P.first) {
+        // The sensor of backward transport looks at the history's first event.
+        if (order <= 1u) {
+            P.first[slot] = location_i | (location_j << 12) | (location_layer << 24);
+        } else {
+            const uint32_t w = P.first[slot];
+            location_i = w & 0xFFFu; location_j = (w >> 12) & 0xFFFu; location_layer = w >> 24;
+        }
+    }
+    // Backward transport registers every view at the injection column.
+    uint32_t inject_i = 0, inject_j = 0;
+    if (BACKWARD) {
+        const uint32_t column = dv.ncol.mod(pid - round_offset * ctl.per_round);
+        inject_j = dv.nx.div(column);
+        inject_i = column - inject_j * uint32_t(s.nx);
+        inject_j = min(inject_j, uint32_t(s.ny - 1));
+    }
+    for (int ia = 0; ia < s.angles; ++ia) {
+        const T vc = s.vc[ia];
+        T prob[4] = {T(0), T(0), T(0), T(0)};
+        if (surface) {
+            if (vc > T(0)) {
+                // Forward As S keeps I (= 1); backward M As S0 is the first column of M.
+                if (BACKWARD) for (int m = 0; m < NMAT; ++m) prob[m] = M[m][0] * vc * weight;
+                else prob[0] = vc * weight;
+            }
+        } else {
+            // cos(phi - phi_view) from the sines and cosines of both azimuths.
+            const T cdphi = cphi * s.vcos_phi[ia] + sphi * s.vsin_phi[ia];
+            const T cs = c * vc + sin_c * s.vsin[ia] * cdphi;
+            const Rot<T> r = NMAT > 1 ? rotation_pre<T>(cs, c, vc, phi, s.vphi[ia], cphi, sphi, s.vcos_phi[ia], s.vsin_phi[ia])
+                                      : Rot<T>{T(1), T(0), T(1), T(0)};
+            const Phase<T> f = phase<T>(s, sp, cs, NMAT);
+            T back[4];
+            if (BACKWARD) {
+                // M P^T S0: M times the first row of P, (F11, F12 C1, -F12 S1, 0).
+                const T row[4] = {f.f11, f.f12 * r.c1, -f.f12 * r.s1, T(0)};
+#pragma unroll
+                for (int m = 0; m < NMAT; ++m) {
+                    T acc = T(0);
+#pragma unroll
+                    for (int q = 0; q < NMAT; ++q) acc += M[m][q] * row[q];
+                    back[m] = acc;
+                }
+            } else {
+                scatter_stokes<T>(f, r, NMAT, st, back);
+            }
+            for (int m = 0; m < NMAT; ++m) prob[m] = back[m] * weight;
+            if (prob[0] < Tol<T>::negligible) for (int m = 0; m < NMAT; ++m) prob[m] = T(0);
+        }
+        bool finite = true;
+        for (int m = 0; m < NMAT; ++m) finite = finite && isfinite(prob[m]);
+        if (!finite) { atomicOr(failure, kNonfinite); failed = true; break; }
+        if (!(prob[0] > eps)) continue;
+
+        // Detector ray: explicit cell walk below the uniform top, then the prefix.
+        const T va = s.va[ia], vb = s.vb[ia];
+        T rx = x, ry = y, rz = z;
+        if (va * a < T(0)) rx = fmax(T(0), s.xunit - rx);
+        if (vb * b < T(0)) ry = fmax(T(0), s.yunit - ry);
+        if (vc * c < T(0)) rz = fmax(T(0), __ldg(s.zunit + k) - rz);
+        const int is = signbit(va) ? -1 : 1, js = signbit(vb) ? -1 : 1, ks = signbit(vc) ? -1 : 1;
+        const T aa = fabs(va), ba = fabs(vb), ca = fabs(vc);
+        const T ai = T(1) / fmax(aa, eps), bi = T(1) / fmax(ba, eps), ci = T(1) / fmax(ca, eps);
+        const T x_old = rx, y_old = ry, z_old = rz;
+        T tau = T(0);
+        int ri = i, rj = j, rk = k;
+        uint32_t rsteps = 0;
+        bool capped = false;
+        while (rk >= 0 && rk < top) {
+            if (rk >= s.uniform_top) {
+                // Uniform layers: one extinction per layer, the same in every cell.
+                tau += (rz * __ldg(s.layer_beta + rk) + __ldg(s.tau_above + rk)) * ci;
+                ++visits;
+                break;
+            }
+            if (++rsteps > ctl.max_steps) { capped = true; break; }
+            // Face by face: view rays cross few band cells, and the rectangle
+            // lookup costs more than it skips here (measured on the box cloud).
+            const T bv = band_beta<T>(s, band, ri, rj, rk);
+            const T dist = advance(s, ri, rj, rk, rx, ry, rz, is, js, ks, aa, ba, ca, ai, bi, ci);
+            tau += dist * bv;
+            ++visits;
+        }
+        if (capped) { atomicOr(failure, kDetectorCap); failed = true; break; }
+        T height = __ldg(s.zsum + k) + (ks > 0 ? __ldg(s.zunit + k) - z_old : z_old);
+        height = __ldg(s.zsum + top) - height;
+        const T dxp = aa * height / ca, dyp = ba * height / ca;
+        const uint32_t di = uint32_t(((s.xunit - x_old) + dxp) / s.xunit);
+        const uint32_t dj = uint32_t(((s.yunit - y_old) + dyp) / s.yunit);
+        int pi_ = i + is * int(dv.nx.mod(di));
+        pi_ = pi_ < 0 ? pi_ + s.nx : (pi_ >= s.nx ? pi_ - s.nx : pi_);
+        int pj_ = j + js * int(dv.ny.mod(dj));
+        pj_ = pj_ < 0 ? pj_ + s.ny : (pj_ >= s.ny ? pj_ - s.ny : pj_);
+        const uint32_t pixel = BACKWARD ? inject_i + uint32_t(s.nx) * (inject_j + uint32_t(s.ny) * uint32_t(ia))
+                                          : uint32_t(pi_ + s.nx * (pj_ + s.ny * ia));
+        const T att = exp(-tau);
+        const T w = prob[0] * att;
+        contributed += P.pixel_weight ? w * __ldg(P.pixel_weight + pixel) : w;
+        const T q3 = NMAT > 3 ? prob[3] * att : T(0);
+        if (L.orders) {
+            const T q1 = NMAT > 1 ? prob[1] * att : T(0), q2 = NMAT > 2 ? prob[2] * att : T(0);
+            Quad<TA>* single = reinterpret_cast<Quad<TA>*>(bank + L.orders);
+            Quad<TA>* located = single + L.pixels;
+            const uint32_t cell = location_i + uint32_t(s.nx) * (location_j + uint32_t(s.ny) * (location_layer + uint32_t(s.nz) * uint32_t(ia)));
+            quad_add(located + cell, TA(w), TA(q1), TA(q2), TA(q3));
+            if (order == 1u) {
+                quad_add(single + pixel, TA(w), TA(q1), TA(q2), TA(q3));
+                quad_add(located + L.locations + cell, TA(w), TA(q1), TA(q2), TA(q3));
+            }
+        }
+        quad_add(pixrec + pixel, TA(w), TA(NMAT > 1 ? prob[1] * att : T(0)), TA(NMAT > 2 ? prob[2] * att : T(0)),
+                 TA(PATHS ? w : T(0)));
+        if (NMAT > 3 && q3 != T(0)) atomicAdd(bank + L.vee + pixel, TA(q3));
+        ++updates;
+        if (PATHS) {
+            Quad<TA>* rec = layrec + size_t(pixel) * (s.nz + 1);
+            // Layers touched: the wander range, the event layer k (partial view ray and
+            // the view prefix weight), and the first-event layer k1 (partial descent and
+            // the descent prefix weight; record nz when the surface came first).
+            int lo = k, hi = k;
+            if (wmin <= wmax) { lo = min(lo, wmin); hi = max(hi, wmax); }
+            if (k1 >= 0) { lo = min(lo, k1); hi = max(hi, k1); }
+            const T init_piece = k1 >= 0 ? w * pol.w : T(0);
+            for (int kk = lo; kk <= hi; ++kk) {
+                T px = (kk >= wmin && kk <= wmax) ? w * wander[kk] : T(0);
+                T py = T(0), pz = T(0);
+                if (kk == k) { px += w * z_old * ci; py = w; }
+                if (kk == k1) { px += init_piece; pz = w; }
+                if (px != T(0) || py != T(0) || pz != T(0)) {
+                    quad_add(rec + kk, TA(px), TA(py), TA(pz), TA(0));
+                    ++updates;
+                }
+            }
+            if (k1 < 0) {
+                quad_add(rec + s.nz, TA(0), TA(0), TA(w), TA(0));
+                ++updates;
+            }
+            // Straight runs of whole layers: +w/|cos| from the first layer, -w/|cos| past the last.
+            const uint32_t runs = P.runs[slot];
+            for (int r = 0; r < 2; ++r) {
+                const uint32_t lh = (runs >> (16 * r)) & 0xFFFFu;
+                if ((lh & 0xFFu) == 0xFFu) continue;
+                const T v = w * P.run_ci[2 * size_t(slot) + r];
+                quad_add(rec + (lh & 0xFFu), TA(0), TA(0), TA(0), TA(v));
+                quad_add(rec + (lh >> 8) + 1, TA(0), TA(0), TA(0), TA(-v));
+                updates += 2;
+            }
+        }
+    }
+    if (P.ring_n && !failed) {
+        // Importance tally: this event enters the ring, and its contribution is credited,
+        // per unit weight, to every event of the ring (itself included).
+        const uint32_t cells = uint32_t(s.nx) * uint32_t(s.ny) * uint32_t(s.nz);
+        const uint32_t cell = uint32_t(i) + uint32_t(s.nx) * (uint32_t(j) + uint32_t(s.ny) * uint32_t(k));
+        const uint32_t n = P.ring_n[slot];
+        uint32_t* rc = P.ring_cell + size_t(slot) * kRing;
+        T* ri = P.ring_inv + size_t(slot) * kRing;
+        rc[n % kRing] = cell;
+        ri[n % kRing] = T(1) / weight;
+        P.ring_n[slot] = n + 1;
+        atomicAdd(P.importance + cells + cell, 1.0);
+        if (contributed != T(0)) {
+            const uint32_t live = min(n + 1, uint32_t(kRing));
+            for (uint32_t q = 0; q < live; ++q) atomicAdd(P.importance + rc[q], double(contributed * ri[q]));
+        }
+    }
+}
+
+template <typename T, typename TA, int NMAT, bool PATHS, bool BACKWARD>
+__device__ __forceinline__ void peel_phase(const SceneView<T>& s, const T* band, const Controls& ctl,
+                                           const Divisors& dv, const Pool<T>& P, TA* __restrict__ banks,
+                                           const WaveTally& L, uint32_t* __restrict__ failure,
+                                           unsigned long long* __restrict__ counters) {
     const uint32_t ns = P.counts[0], ng = P.counts[1], np = P.counts[2];
     const uint32_t total = ns + ng + np;
     const uint32_t shard = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) % L.shards;
@@ -657,217 +919,21 @@ wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ b
         const uint4 meta = P.meta[slot];
         const uint32_t pid = meta.x;
         if (pid == kNone) { atomicOr(failure, kQueueCorrupt); continue; }
-        const int i = int(meta.z & 0xFFFF), j = int(meta.z >> 16);
-        int k, k1, wmin, wmax;
-        unpack_layers(meta.w, k, k1, wmin, wmax);
-        const Quad<T> pos = P.pos[slot];
-        const Quad<T> dir = P.dir[slot];
-        const Quad<T> pol = P.pol[slot];
-        const int sp = surface ? -1 : int(P.kind[slot]) - 1;
-        const T x = pos.x, y = pos.y, z = pos.z, weight = pos.w;
-        const T a = dir.x, b = dir.y, c = dir.z, phi = dir.w;
-        const T st[4] = {T(1), pol.x, pol.y, (NMAT > 3 && P.vee) ? P.vee[slot] : T(0)};
-        // Backward transport: the history's weight matrix (M11 = 1).
-        T M[NMAT][NMAT];
-        if (BACKWARD) {
-#pragma unroll
-            for (int r = 0; r < NMAT; ++r)
-#pragma unroll
-                for (int q = 0; q < NMAT; ++q) M[r][q] = P.matrix[size_t(r * NMAT + q) * P.capacity + slot];
-        }
-        const uint32_t round_offset = dv.per_round.div(pid);
-        TA* bank = banks + (size_t(round_offset) * L.shards + shard) * L.count;
-        Quad<TA>* pixrec = reinterpret_cast<Quad<TA>*>(bank);
-        Quad<TA>* layrec = reinterpret_cast<Quad<TA>*>(bank + 4 * size_t(L.pixels));
-        const T* wander = PATHS ? P.wander + size_t(slot) * s.nz : nullptr;
-        const T sin_c = sqrt(fmax(eps, T(1) - c * c));
-        T sphi, cphi;
-        sincos(phi, &sphi, &cphi);
-        T contributed = T(0);  // Stokes-I peel-off of this event, all views
-        bool failed = false;
-        // Scattering-order diagnostics: the event's history order and its location record
-        // (layer 0 = an event on the surface).
-        const uint32_t order = P.order ? P.order[slot] : 0u;
-        uint32_t location_i = uint32_t(i), location_j = uint32_t(j);
-        uint32_t location_layer = (k == 0 && z < eps) ? 0u : uint32_t(k + 1);
-        if (BACKWARD && L.orders && P.first) {
-            // The sensor of backward transport looks at the history's first event.
-            if (order <= 1u) {
-                P.first[slot] = location_i | (location_j << 12) | (location_layer << 24);
-            } else {
-                const uint32_t w = P.first[slot];
-                location_i = w & 0xFFFu; location_j = (w >> 12) & 0xFFFu; location_layer = w >> 24;
-            }
-        }
-        // Backward transport registers every view at the injection column.
-        uint32_t inject_i = 0, inject_j = 0;
-        if (BACKWARD) {
-            const uint32_t column = dv.ncol.mod(pid - round_offset * ctl.per_round);
-            inject_j = dv.nx.div(column);
-            inject_i = column - inject_j * uint32_t(s.nx);
-            inject_j = min(inject_j, uint32_t(s.ny - 1));
-        }
-        for (int ia = 0; ia < s.angles; ++ia) {
-            const T vc = s.vc[ia];
-            T prob[4] = {T(0), T(0), T(0), T(0)};
-            if (surface) {
-                if (vc > T(0)) {
-                    // Forward As S keeps I (= 1); backward M As S0 is the first column of M.
-                    if (BACKWARD) for (int m = 0; m < NMAT; ++m) prob[m] = M[m][0] * vc * weight;
-                    else prob[0] = vc * weight;
-                }
-            } else {
-                // cos(phi - phi_view) from the sines and cosines of both azimuths.
-                const T cdphi = cphi * s.vcos_phi[ia] + sphi * s.vsin_phi[ia];
-                const T cs = c * vc + sin_c * s.vsin[ia] * cdphi;
-                const Rot<T> r = NMAT > 1 ? rotation_pre<T>(cs, c, vc, phi, s.vphi[ia], cphi, sphi, s.vcos_phi[ia], s.vsin_phi[ia])
-                                          : Rot<T>{T(1), T(0), T(1), T(0)};
-                const Phase<T> f = phase<T>(s, sp, cs, NMAT);
-                T back[4];
-                if (BACKWARD) {
-                    // M P^T S0: M times the first row of P, (F11, F12 C1, -F12 S1, 0).
-                    const T row[4] = {f.f11, f.f12 * r.c1, -f.f12 * r.s1, T(0)};
-#pragma unroll
-                    for (int m = 0; m < NMAT; ++m) {
-                        T acc = T(0);
-#pragma unroll
-                        for (int q = 0; q < NMAT; ++q) acc += M[m][q] * row[q];
-                        back[m] = acc;
-                    }
-                } else {
-                    scatter_stokes<T>(f, r, NMAT, st, back);
-                }
-                for (int m = 0; m < NMAT; ++m) prob[m] = back[m] * weight;
-                if (prob[0] < Tol<T>::negligible) for (int m = 0; m < NMAT; ++m) prob[m] = T(0);
-            }
-            bool finite = true;
-            for (int m = 0; m < NMAT; ++m) finite = finite && isfinite(prob[m]);
-            if (!finite) { atomicOr(failure, kNonfinite); failed = true; break; }
-            if (!(prob[0] > eps)) continue;
+        peel_event<T, TA, NMAT, PATHS, BACKWARD>(slot, surface, meta, s, band, ctl, dv, P, banks, L, shard, failure,
+                                                 visits, updates);
+    }
+    const unsigned long long totals[2] = {visits, updates};
+    unsigned long long* const targets[2] = {counters + 2, counters + 3};
+    block_add<2>(totals, targets);
+}
 
-            // Detector ray: explicit cell walk below the uniform top, then the prefix.
-            const T va = s.va[ia], vb = s.vb[ia];
-            T rx = x, ry = y, rz = z;
-            if (va * a < T(0)) rx = fmax(T(0), s.xunit - rx);
-            if (vb * b < T(0)) ry = fmax(T(0), s.yunit - ry);
-            if (vc * c < T(0)) rz = fmax(T(0), __ldg(s.zunit + k) - rz);
-            const int is = signbit(va) ? -1 : 1, js = signbit(vb) ? -1 : 1, ks = signbit(vc) ? -1 : 1;
-            const T aa = fabs(va), ba = fabs(vb), ca = fabs(vc);
-            const T ai = T(1) / fmax(aa, eps), bi = T(1) / fmax(ba, eps), ci = T(1) / fmax(ca, eps);
-            const T x_old = rx, y_old = ry, z_old = rz;
-            T tau = T(0);
-            int ri = i, rj = j, rk = k;
-            uint32_t rsteps = 0;
-            bool capped = false;
-            while (rk >= 0 && rk < top) {
-                if (rk >= s.uniform_top) {
-                    // Uniform layers: one extinction per layer, the same in every cell.
-                    tau += (rz * __ldg(s.layer_beta + rk) + __ldg(s.tau_above + rk)) * ci;
-                    ++visits;
-                    break;
-                }
-                if (++rsteps > ctl.max_steps) { capped = true; break; }
-                // Face by face: view rays cross few band cells, and the rectangle
-                // lookup costs more than it skips here (measured on the box cloud).
-                const T bv = band_beta<T>(s, band, ri, rj, rk);
-                const T dist = advance(s, ri, rj, rk, rx, ry, rz, is, js, ks, aa, ba, ca, ai, bi, ci);
-                tau += dist * bv;
-                ++visits;
-            }
-            if (capped) { atomicOr(failure, kDetectorCap); failed = true; break; }
-            T height = __ldg(s.zsum + k) + (ks > 0 ? __ldg(s.zunit + k) - z_old : z_old);
-            height = __ldg(s.zsum + top) - height;
-            const T dxp = aa * height / ca, dyp = ba * height / ca;
-            const uint32_t di = uint32_t(((s.xunit - x_old) + dxp) / s.xunit);
-            const uint32_t dj = uint32_t(((s.yunit - y_old) + dyp) / s.yunit);
-            int pi_ = i + is * int(dv.nx.mod(di));
-            pi_ = pi_ < 0 ? pi_ + s.nx : (pi_ >= s.nx ? pi_ - s.nx : pi_);
-            int pj_ = j + js * int(dv.ny.mod(dj));
-            pj_ = pj_ < 0 ? pj_ + s.ny : (pj_ >= s.ny ? pj_ - s.ny : pj_);
-            const uint32_t pixel = BACKWARD ? inject_i + uint32_t(s.nx) * (inject_j + uint32_t(s.ny) * uint32_t(ia))
-                                              : uint32_t(pi_ + s.nx * (pj_ + s.ny * ia));
-            const T att = exp(-tau);
-            const T w = prob[0] * att;
-            contributed += P.pixel_weight ? w * __ldg(P.pixel_weight + pixel) : w;
-            const T q3 = NMAT > 3 ? prob[3] * att : T(0);
-            if (L.orders) {
-                const T q1 = NMAT > 1 ? prob[1] * att : T(0), q2 = NMAT > 2 ? prob[2] * att : T(0);
-                Quad<TA>* single = reinterpret_cast<Quad<TA>*>(bank + L.orders);
-                Quad<TA>* located = single + L.pixels;
-                const uint32_t cell = location_i + uint32_t(s.nx) * (location_j + uint32_t(s.ny) * (location_layer + uint32_t(s.nz) * uint32_t(ia)));
-                quad_add(located + cell, TA(w), TA(q1), TA(q2), TA(q3));
-                if (order == 1u) {
-                    quad_add(single + pixel, TA(w), TA(q1), TA(q2), TA(q3));
-                    quad_add(located + L.locations + cell, TA(w), TA(q1), TA(q2), TA(q3));
-                }
-            }
-            quad_add(pixrec + pixel, TA(w), TA(NMAT > 1 ? prob[1] * att : T(0)), TA(NMAT > 2 ? prob[2] * att : T(0)),
-                     TA(PATHS ? w : T(0)));
-            if (NMAT > 3 && q3 != T(0)) atomicAdd(bank + L.vee + pixel, TA(q3));
-            ++updates;
-            if (PATHS) {
-                Quad<TA>* rec = layrec + size_t(pixel) * (s.nz + 1);
-                // Layers touched: the wander range, the event layer k (partial view ray and
-                // the view prefix weight), and the first-event layer k1 (partial descent and
-                // the descent prefix weight; record nz when the surface came first).
-                int lo = k, hi = k;
-                if (wmin <= wmax) { lo = min(lo, wmin); hi = max(hi, wmax); }
-                if (k1 >= 0) { lo = min(lo, k1); hi = max(hi, k1); }
-                const T init_piece = k1 >= 0 ? w * pol.w : T(0);
-                for (int kk = lo; kk <= hi; ++kk) {
-                    T px = (kk >= wmin && kk <= wmax) ? w * wander[kk] : T(0);
-                    T py = T(0), pz = T(0);
-                    if (kk == k) { px += w * z_old * ci; py = w; }
-                    if (kk == k1) { px += init_piece; pz = w; }
-                    if (px != T(0) || py != T(0) || pz != T(0)) {
-                        quad_add(rec + kk, TA(px), TA(py), TA(pz), TA(0));
-                        ++updates;
-                    }
-                }
-                if (k1 < 0) {
-                    quad_add(rec + s.nz, TA(0), TA(0), TA(w), TA(0));
-                    ++updates;
-                }
-                // Straight runs of whole layers: +w/|cos| from the first layer, -w/|cos| past the last.
-                const uint32_t runs = P.runs[slot];
-                for (int r = 0; r < 2; ++r) {
-                    const uint32_t lh = (runs >> (16 * r)) & 0xFFFFu;
-                    if ((lh & 0xFFu) == 0xFFu) continue;
-                    const T v = w * P.run_ci[2 * size_t(slot) + r];
-                    quad_add(rec + (lh & 0xFFu), TA(0), TA(0), TA(0), TA(v));
-                    quad_add(rec + (lh >> 8) + 1, TA(0), TA(0), TA(0), TA(-v));
-                    updates += 2;
-                }
-            }
-        }
-        if (P.ring_n && !failed) {
-            // Importance tally: this event enters the ring, and its contribution is credited,
-            // per unit weight, to every event of the ring (itself included).
-            const uint32_t cells = uint32_t(s.nx) * uint32_t(s.ny) * uint32_t(s.nz);
-            const uint32_t cell = uint32_t(i) + uint32_t(s.nx) * (uint32_t(j) + uint32_t(s.ny) * uint32_t(k));
-            const uint32_t n = P.ring_n[slot];
-            uint32_t* rc = P.ring_cell + size_t(slot) * kRing;
-            T* ri = P.ring_inv + size_t(slot) * kRing;
-            rc[n % kRing] = cell;
-            ri[n % kRing] = T(1) / weight;
-            P.ring_n[slot] = n + 1;
-            atomicAdd(P.importance + cells + cell, 1.0);
-            if (contributed != T(0)) {
-                const uint32_t live = min(n + 1, uint32_t(kRing));
-                for (uint32_t q = 0; q < live; ++q) atomicAdd(P.importance + rc[q], double(contributed * ri[q]));
-            }
-        }
-    }
-    unsigned long long v2 = visits, v3 = updates;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        v2 += __shfl_down_sync(0xffffffffu, v2, off);
-        v3 += __shfl_down_sync(0xffffffffu, v3, off);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(counters + 2, v2);
-        atomicAdd(counters + 3, v3);
-    }
+template <typename T, typename TA, int NMAT, bool PATHS, bool BACKWARD>
+__global__ void __launch_bounds__(256, 3)
+wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ banks, WaveTally L,
+        uint32_t* __restrict__ failure, unsigned long long* __restrict__ counters) {
+    extern __shared__ __align__(16) unsigned char staged[];
+    const T* band = stage_band<T>(s, staged, failure);
+    peel_phase<T, TA, NMAT, PATHS, BACKWARD>(s, band, ctl, dv, P, banks, L, failure, counters);
 }
 
 // ----------------------------------------------------------------------------------
@@ -913,167 +979,223 @@ __device__ __forceinline__ T ddis_factor(const SceneView<T>& s, const Guide<T>& 
     return q > T(0) ? p_an / q : T(0);
 }
 
+// Scattering of one event (slot): the new direction (Lambert, polarized sampling or the
+// guided detector branch), the Stokes or weight-matrix update, roulette and the next free
+// path. Returns false when the photon ends here.
 template <typename T, int NMAT, bool BACKWARD>
-__global__ void __launch_bounds__(256, 4)
-wf_scatter(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, Guide<T> g, uint32_t* __restrict__ failure) {
+__device__ __forceinline__ bool scatter_event(uint32_t slot, bool surface, uint4 meta, const SceneView<T>& s,
+                                              const Controls& ctl, const Divisors& dv, const Pool<T>& P,
+                                              const Guide<T>& g, uint32_t* __restrict__ failure) {
     const T eps = Tol<T>::eps;
     const T pi = pi_v<T>();
+    const uint32_t pid = meta.x;
+    const uint32_t ro = dv.per_round.div(pid);
+    DrawStream rng;
+    rng.init(pid - ro * ctl.per_round, ctl.first_round + ro, ctl.seed, meta.y);
+    Quad<T> pos = P.pos[slot];
+    const Quad<T> dir0 = P.dir[slot];
+    Quad<T> pol = P.pol[slot];
+    const T a0 = dir0.x, b0 = dir0.y, c0 = dir0.z;
+    T a, b, c, phi_out, q = T(0), u = T(0), v = T(0);
+    // Backward transport: the weight matrix (M11 = 1), updated by M P^T (M As at the
+    // surface) and renormalized by its M11.
+    T M[NMAT][NMAT];
+    if (BACKWARD) {
+#pragma unroll
+        for (int r = 0; r < NMAT; ++r)
+#pragma unroll
+            for (int col = 0; col < NMAT; ++col) M[r][col] = P.matrix[size_t(r * NMAT + col) * P.capacity + slot];
+    }
+    const int ci = int(meta.z & 0xFFFF), cj = int(meta.z >> 16), ck = int(meta.w & 0xFF) - 1;
+    T roulette = g.roulette;
+    if (g.scale) roulette *= __ldg(g.scale + ci + s.nx * (cj + s.ny * ck));
+    if (surface) {
+        const T Pd = T(rng.next()), U = T(rng.next());
+        if (roulette > T(0) && pos.w < roulette) {
+            if (T(rng.next()) * roulette < pos.w) pos.w = roulette;
+            else { P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u); return false; }
+        }
+        const T mu = sqrt(Pd);
+        phi_out = T(2) * pi * U;
+        const T sine = sqrt(fmax(T(0), T(1) - mu * mu));
+        T sp, cp;
+        sincos(phi_out, &sp, &cp);
+        a = sine * cp; b = sine * sp; c = fabs(mu);
+        if (BACKWARD) {
+            // M As keeps the first column of M; then M / M11.
+            const T m11 = M[0][0];
+#pragma unroll
+            for (int r = 0; r < NMAT; ++r) {
+#pragma unroll
+                for (int col = 1; col < NMAT; ++col) M[r][col] = T(0);
+                M[r][0] = M[r][0] / m11;
+            }
+        }
+    } else {
+        const int sp = int(P.kind[slot]) - 1;
+        const T phi = dir0.w;
+        T st[4] = {T(1), pol.x, pol.y, (NMAT > 3 && P.vee) ? P.vee[slot] : T(0)};
+        T cos_out, dphi, cos_sca;
+        const bool guided = sp >= 0 && g.epsilon > T(0) && pos.w < g.cap;
+        if (guided && T(rng.next()) < g.epsilon) {
+            // Detector branch: a view, a cosine about it from the proposal, an azimuth.
+            const int v = min(int(T(rng.next()) * T(s.angles)), s.angles - 1);
+            const T cd = sample_cdf<T>(s, sp, T(rng.next()));
+            const T psi = T(2) * pi * T(rng.next());
+            const T dx = s.va[v], dy = s.vb[v], dz = s.vc[v];
+            const T h = sqrt(dx * dx + dy * dy);
+            const bool tilted = h > T(1e-12);
+            const T e1x = tilted ? -dy / h : T(1), e1y = tilted ? dx / h : T(0);
+            const T e2x = -dz * e1y, e2y = dz * e1x, e2z = dx * e1y - dy * e1x;
+            const T sd = sqrt(fmax(T(0), T(1) - cd * cd));
+            T spsi, cpsi;
+            sincos(psi, &spsi, &cpsi);
+            const T wx = cd * dx + sd * (cpsi * e1x + spsi * e2x);
+            const T wy = cd * dy + sd * (cpsi * e1y + spsi * e2y);
+            const T wz = cd * dz + sd * spsi * e2z;
+            cos_out = fmin(T(1), fmax(T(-1), wz));
+            phi_out = atan2(wy, wx);
+            const T so = sqrt(fmax(T(0), T(1) - cos_out * cos_out));
+            T sp_, cp_;
+            sincos(phi_out, &sp_, &cp_);
+            cos_sca = fmin(T(1), fmax(T(-1), a0 * (cp_ * so) + b0 * (sp_ * so) + c0 * cos_out));
+        } else {
+            if (!sample_direction<T>(s, sp, NMAT, st, c0, rng, cos_out, dphi, cos_sca, BACKWARD ? T(1) : T(-1))) {
+                atomicOr(failure, kSamplingCap);
+                P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u);
+                return false;
+            }
+            phi_out = phi + dphi;
+        }
+        const Rot<T> r = NMAT > 1 ? rotation<T>(cos_sca, c0, cos_out, phi, phi_out) : Rot<T>{T(1), T(0), T(1), T(0)};
+        const Phase<T> f = phase<T>(s, sp, cos_sca, NMAT);
+        T out[4] = {T(0), T(0), T(0), T(0)};
+        if (BACKWARD) {
+            // M = M P^T; the sampling vector is (M11, M12, -M13, M14).
+            T Pm[4][4];
+            phase_matrix<T>(f, r, NMAT, Pm);
+            T next[NMAT][NMAT];
+#pragma unroll
+            for (int row = 0; row < NMAT; ++row)
+#pragma unroll
+                for (int col = 0; col < NMAT; ++col) {
+                    T acc = T(0);
+#pragma unroll
+                    for (int k2 = 0; k2 < NMAT; ++k2) acc += M[row][k2] * Pm[col][k2];
+                    next[row][col] = acc;
+                }
+            const T m11 = next[0][0];
+#pragma unroll
+            for (int row = 0; row < NMAT; ++row)
+#pragma unroll
+                for (int col = 0; col < NMAT; ++col) M[row][col] = next[row][col] / m11;
+            out[0] = next[0][0];
+            if (NMAT > 1) { out[1] = next[0][1]; out[2] = -next[0][2]; }
+            if (NMAT > 3) out[3] = next[0][3];
+        } else {
+            scatter_stokes<T>(f, r, NMAT, st, out);
+        }
+        // S / S(1): I becomes 1 (NaN when S(1) is 0 or not finite).
+        const T s0 = out[0];
+        const T one = s0 / s0;
+        bool ok = isfinite(one);
+        if (NMAT > 1) {
+            q = out[1] / s0; u = out[2] / s0;
+            if (NMAT > 3) v = out[3] / s0;
+            ok = ok && isfinite(q) && isfinite(u) && isfinite(v) && sqrt(q * q + u * u + v * v) <= one + T(1e-2);
+        }
+        if (!ok) { atomicOr(failure, kInvalidStokes); P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u); return false; }
+        const T so = sqrt(fmax(T(0), T(1) - cos_out * cos_out));
+        T spo, cpo;
+        sincos(phi_out, &spo, &cpo);
+        a = cpo * so; b = spo * so; c = cos_out;
+        if (guided) pos.w *= ddis_factor<T, NMAT>(s, g, sp, cos_sca, s0, a, b, c);
+        if (roulette > T(0) && pos.w < roulette) {
+            if (T(rng.next()) * roulette < pos.w) pos.w = roulette;
+            else { P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u); return false; }
+        }
+    }
+    if (a * a0 < T(0)) pos.x = fmax(T(0), s.xunit - pos.x);
+    if (b * b0 < T(0)) pos.y = fmax(T(0), s.yunit - pos.y);
+    if (c * c0 < T(0)) {
+        const int k = int(meta.w & 0xFF) - 1;
+        pos.z = fmax(T(0), __ldg(s.zunit + k) - pos.z);
+    }
+    pol.x = q; pol.y = u;
+    if (NMAT > 3 && P.vee) P.vee[slot] = v;
+    if (BACKWARD) {
+#pragma unroll
+        for (int r = 0; r < NMAT; ++r)
+#pragma unroll
+            for (int col = 0; col < NMAT; ++col) P.matrix[size_t(r * NMAT + col) * P.capacity + slot] = M[r][col];
+    }
+    if (!surface) pol.z = -log(fmax(T(rng.next()), eps));
+    meta.y = rng.draw;
+    P.pos[slot] = pos;
+    P.dir[slot] = Quad<T>{a, b, c, phi_out};
+    P.pol[slot] = pol;
+    P.meta[slot] = meta;
+    return true;
+}
+
+template <typename T, int NMAT, bool BACKWARD>
+__device__ __forceinline__ void scatter_phase(const SceneView<T>& s, const Controls& ctl, const Divisors& dv,
+                                              const Pool<T>& P, const Guide<T>& g, uint32_t* __restrict__ failure) {
     const uint32_t ns = P.counts[0], ng = P.counts[1], np = P.counts[2];
     const uint32_t total = ns + ng + np;
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
         bool surface;
         const uint32_t slot = queue_entry(P.queue, e, ns, ng, surface);
         if (slot >= P.capacity) { atomicOr(failure, kQueueCorrupt); continue; }
-        uint4 meta = P.meta[slot];
+        const uint4 meta = P.meta[slot];
         const uint32_t pid = meta.x;
         if (pid == kNone) { atomicOr(failure, kQueueCorrupt); continue; }
-        const uint32_t ro = dv.per_round.div(pid);
-        DrawStream rng;
-        rng.init(pid - ro * ctl.per_round, ctl.first_round + ro, ctl.seed, meta.y);
-        Quad<T> pos = P.pos[slot];
-        const Quad<T> dir0 = P.dir[slot];
-        Quad<T> pol = P.pol[slot];
-        const T a0 = dir0.x, b0 = dir0.y, c0 = dir0.z;
-        T a, b, c, phi_out, q = T(0), u = T(0), v = T(0);
-        // Backward transport: the weight matrix (M11 = 1), updated by M P^T (M As at the
-        // surface) and renormalized by its M11.
-        T M[NMAT][NMAT];
-        if (BACKWARD) {
-#pragma unroll
-            for (int r = 0; r < NMAT; ++r)
-#pragma unroll
-                for (int col = 0; col < NMAT; ++col) M[r][col] = P.matrix[size_t(r * NMAT + col) * P.capacity + slot];
-        }
-        const int ci = int(meta.z & 0xFFFF), cj = int(meta.z >> 16), ck = int(meta.w & 0xFF) - 1;
-        T roulette = g.roulette;
-        if (g.scale) roulette *= __ldg(g.scale + ci + s.nx * (cj + s.ny * ck));
-        if (surface) {
-            const T Pd = T(rng.next()), U = T(rng.next());
-            if (roulette > T(0) && pos.w < roulette) {
-                if (T(rng.next()) * roulette < pos.w) pos.w = roulette;
-                else { P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u); continue; }
-            }
-            const T mu = sqrt(Pd);
-            phi_out = T(2) * pi * U;
-            const T sine = sqrt(fmax(T(0), T(1) - mu * mu));
-            T sp, cp;
-            sincos(phi_out, &sp, &cp);
-            a = sine * cp; b = sine * sp; c = fabs(mu);
-            if (BACKWARD) {
-                // M As keeps the first column of M; then M / M11.
-                const T m11 = M[0][0];
-#pragma unroll
-                for (int r = 0; r < NMAT; ++r) {
-#pragma unroll
-                    for (int col = 1; col < NMAT; ++col) M[r][col] = T(0);
-                    M[r][0] = M[r][0] / m11;
-                }
-            }
-        } else {
-            const int sp = int(P.kind[slot]) - 1;
-            const T phi = dir0.w;
-            T st[4] = {T(1), pol.x, pol.y, (NMAT > 3 && P.vee) ? P.vee[slot] : T(0)};
-            T cos_out, dphi, cos_sca;
-            const bool guided = sp >= 0 && g.epsilon > T(0) && pos.w < g.cap;
-            if (guided && T(rng.next()) < g.epsilon) {
-                // Detector branch: a view, a cosine about it from the proposal, an azimuth.
-                const int v = min(int(T(rng.next()) * T(s.angles)), s.angles - 1);
-                const T cd = sample_cdf<T>(s, sp, T(rng.next()));
-                const T psi = T(2) * pi * T(rng.next());
-                const T dx = s.va[v], dy = s.vb[v], dz = s.vc[v];
-                const T h = sqrt(dx * dx + dy * dy);
-                const bool tilted = h > T(1e-12);
-                const T e1x = tilted ? -dy / h : T(1), e1y = tilted ? dx / h : T(0);
-                const T e2x = -dz * e1y, e2y = dz * e1x, e2z = dx * e1y - dy * e1x;
-                const T sd = sqrt(fmax(T(0), T(1) - cd * cd));
-                T spsi, cpsi;
-                sincos(psi, &spsi, &cpsi);
-                const T wx = cd * dx + sd * (cpsi * e1x + spsi * e2x);
-                const T wy = cd * dy + sd * (cpsi * e1y + spsi * e2y);
-                const T wz = cd * dz + sd * spsi * e2z;
-                cos_out = fmin(T(1), fmax(T(-1), wz));
-                phi_out = atan2(wy, wx);
-                const T so = sqrt(fmax(T(0), T(1) - cos_out * cos_out));
-                T sp_, cp_;
-                sincos(phi_out, &sp_, &cp_);
-                cos_sca = fmin(T(1), fmax(T(-1), a0 * (cp_ * so) + b0 * (sp_ * so) + c0 * cos_out));
-            } else {
-                if (!sample_direction<T>(s, sp, NMAT, st, c0, rng, cos_out, dphi, cos_sca, BACKWARD ? T(1) : T(-1))) {
-                    atomicOr(failure, kSamplingCap);
-                    P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u);
-                    continue;
-                }
-                phi_out = phi + dphi;
-            }
-            const Rot<T> r = NMAT > 1 ? rotation<T>(cos_sca, c0, cos_out, phi, phi_out) : Rot<T>{T(1), T(0), T(1), T(0)};
-            const Phase<T> f = phase<T>(s, sp, cos_sca, NMAT);
-            T out[4] = {T(0), T(0), T(0), T(0)};
-            if (BACKWARD) {
-                // M = M P^T; the sampling vector is (M11, M12, -M13, M14).
-                T Pm[4][4];
-                phase_matrix<T>(f, r, NMAT, Pm);
-                T next[NMAT][NMAT];
-#pragma unroll
-                for (int row = 0; row < NMAT; ++row)
-#pragma unroll
-                    for (int col = 0; col < NMAT; ++col) {
-                        T acc = T(0);
-#pragma unroll
-                        for (int k2 = 0; k2 < NMAT; ++k2) acc += M[row][k2] * Pm[col][k2];
-                        next[row][col] = acc;
-                    }
-                const T m11 = next[0][0];
-#pragma unroll
-                for (int row = 0; row < NMAT; ++row)
-#pragma unroll
-                    for (int col = 0; col < NMAT; ++col) M[row][col] = next[row][col] / m11;
-                out[0] = next[0][0];
-                if (NMAT > 1) { out[1] = next[0][1]; out[2] = -next[0][2]; }
-                if (NMAT > 3) out[3] = next[0][3];
-            } else {
-                scatter_stokes<T>(f, r, NMAT, st, out);
-            }
-            // S / S(1): I becomes 1 (NaN when S(1) is 0 or not finite).
-            const T s0 = out[0];
-            const T one = s0 / s0;
-            bool ok = isfinite(one);
-            if (NMAT > 1) {
-                q = out[1] / s0; u = out[2] / s0;
-                if (NMAT > 3) v = out[3] / s0;
-                ok = ok && isfinite(q) && isfinite(u) && isfinite(v) && sqrt(q * q + u * u + v * v) <= one + T(1e-2);
-            }
-            if (!ok) { atomicOr(failure, kInvalidStokes); P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u); continue; }
-            const T so = sqrt(fmax(T(0), T(1) - cos_out * cos_out));
-            T spo, cpo;
-            sincos(phi_out, &spo, &cpo);
-            a = cpo * so; b = spo * so; c = cos_out;
-            if (guided) pos.w *= ddis_factor<T, NMAT>(s, g, sp, cos_sca, s0, a, b, c);
-            if (roulette > T(0) && pos.w < roulette) {
-                if (T(rng.next()) * roulette < pos.w) pos.w = roulette;
-                else { P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u); continue; }
-            }
-        }
-        if (a * a0 < T(0)) pos.x = fmax(T(0), s.xunit - pos.x);
-        if (b * b0 < T(0)) pos.y = fmax(T(0), s.yunit - pos.y);
-        if (c * c0 < T(0)) {
-            const int k = int(meta.w & 0xFF) - 1;
-            pos.z = fmax(T(0), __ldg(s.zunit + k) - pos.z);
-        }
-        pol.x = q; pol.y = u;
-        if (NMAT > 3 && P.vee) P.vee[slot] = v;
-        if (BACKWARD) {
-#pragma unroll
-            for (int r = 0; r < NMAT; ++r)
-#pragma unroll
-                for (int col = 0; col < NMAT; ++col) P.matrix[size_t(r * NMAT + col) * P.capacity + slot] = M[r][col];
-        }
-        if (!surface) pol.z = -log(fmax(T(rng.next()), eps));
-        meta.y = rng.draw;
-        P.pos[slot] = pos;
-        P.dir[slot] = Quad<T>{a, b, c, phi_out};
-        P.pol[slot] = pol;
-        P.meta[slot] = meta;
+        scatter_event<T, NMAT, BACKWARD>(slot, surface, meta, s, ctl, dv, P, g, failure);
     }
+}
+
+template <typename T, int NMAT, bool BACKWARD>
+__global__ void __launch_bounds__(256, 4)
+wf_scatter(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, Guide<T> g, uint32_t* __restrict__ failure) {
+    scatter_phase<T, NMAT, BACKWARD>(s, ctl, dv, P, g, failure);
+}
+
+// ----------------------------------------------------------------------------------
+// tail: the end of a round group in one launch. Once every photon is claimed and few
+// remain, a wavefront iteration has little work and its three launches cost more than
+// the work; the longest cloud histories need a hundred or more such iterations. Here each
+// thread takes live slots one at a time (reserved together with the other idle lanes of
+// its warp) and runs each photon to its end: walk, peel-off and scattering, event after
+// event, through the same slot functions as the wavefront kernels.
+// ----------------------------------------------------------------------------------
+template <typename T, int NMAT, bool PATHS, bool BACKWARD>
+__global__ void __launch_bounds__(256, 2)
+wf_tail(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, T* __restrict__ banks, WaveTally L, Guide<T> g,
+        uint32_t* __restrict__ failure, unsigned long long* __restrict__ counters, uint32_t* __restrict__ next) {
+    extern __shared__ __align__(16) unsigned char staged[];
+    const T* band = stage_band<T>(s, staged, failure);
+    const uint32_t shard = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) % L.shards;
+    uint64_t scatters = 0, visits = 0, detector = 0, updates = 0;
+    uint32_t paused = 0;
+    for (;;) {
+        const uint32_t slot = warp_reserve(next);
+        if (slot >= P.capacity) break;
+        if (P.meta[slot].x == kNone) continue;
+        // No step budget: the walk pauses only at the history step cap, which ends it.
+        for (;;) {
+            const int queue = transit_slot<T, PATHS, false>(slot, s, band, ctl, dv, P, 0xFFFFFFFFu, false, failure,
+                                                             scatters, visits, paused);
+            if (queue < 0) break;
+            const uint4 meta = P.meta[slot];
+            const bool surface = queue == kQueueSurface;
+            peel_event<T, T, NMAT, PATHS, BACKWARD>(slot, surface, meta, s, band, ctl, dv, P, banks, L, shard, failure,
+                                                    detector, updates);
+            if (!scatter_event<T, NMAT, BACKWARD>(slot, surface, meta, s, ctl, dv, P, g, failure)) break;
+        }
+    }
+    const unsigned long long totals[4] = {scatters, visits, detector, updates};
+    unsigned long long* const targets[4] = {counters + 0, counters + 1, counters + 2, counters + 3};
+    block_add<4>(totals, targets);
 }
 
 // ----------------------------------------------------------------------------------

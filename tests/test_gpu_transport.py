@@ -288,6 +288,44 @@ def test_rectangle_steps_match_face_by_face_walks(native, device, name):
     np.testing.assert_allclose(results[0], results[1], rtol=1e-9, atol=1e-14)
 
 
+@pytest.mark.parametrize("name", ["layered_cloud", "box_cloud"])
+def test_tail_launch_matches_launch_per_iteration(native, device, name):
+    """Running a group's last photons to their ends in one launch (the tail kernel) is the
+    same transport as three launches per iteration: equal event counts, and FP64 tallies
+    within the oracle-parity tolerance (the kernels inline the same slot functions, but the
+    compiler may contract their arithmetic differently, and rounding differences grow along
+    a history that crosses a cloud edge)."""
+    import monki.scenes as scenes
+    from monki.execution.native import F64P, U64P
+
+    scene = scenes.layered_cloud(6, 2, nx=10, ny=8) if name == "layered_cloud" else \
+        scenes.box_cloud(6, 2, nx=12, ny=10, box_x=(3, 8), box_y=(2, 6))
+    tables = np.ascontiguousarray(scene.tables)
+    results = []
+
+    for tail in (0, 1 << 20, 256):
+        err = _err()
+        config = f"precision=fp64,pool=4096,tail={tail}".encode()
+        handle = native.monki_cuda_create(0, tables.ctypes.data_as(F64P), tables.size, 2, config, err, len(err))
+        assert handle, err.value
+        try:
+            count = int(native.monki_cuda_tally_count(handle))
+            out = np.zeros(2 * count)
+            controls = (ctypes.c_uint32 * 8)(*_controls(scene, 2, 4))
+            assert native.monki_cuda_run(handle, controls, out.ctypes.data_as(F64P), err, len(err)) == 0, err.value
+            counters = np.zeros(6, dtype=np.uint64)
+            native.monki_cuda_counters(handle, counters.ctypes.data_as(U64P))
+            results.append((out, int(counters[0]), int(counters[4]), int(counters[5])))
+        finally:
+            native.monki_cuda_close(handle)
+
+    (base, scatters, photons, launches), *others = results
+    for out, s, p, n in others:
+        assert (s, p) == (scatters, photons)
+        assert n < launches  # the tail replaced launches
+        np.testing.assert_allclose(out, base, rtol=1e-6, atol=1e-12)
+
+
 def test_off_plane_polarization_is_nonzero_and_bounded(device):
     import monki.scenes as scenes
 
