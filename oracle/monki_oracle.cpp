@@ -86,13 +86,16 @@ void philox(uint32_t ctr[4], const uint32_t key_in[2]) {
     }
 }
 
+// The stream of one history: counter (photon, round, block, lineage), where lineage 0 is
+// the photon itself and a copy made by splitting has its own nonzero lineage.
 struct Stream {
-    uint32_t photon, round, seed, block = 0, lane = 4;
+    uint32_t photon, round, seed, lineage = 0, block = 0, lane = 4, draws = 0;
     uint32_t words[4] = {0, 0, 0, 0};
     // One uniform on the open float32 grid; returned widened to double exactly.
     double uniform() {
+        ++draws;
         if (lane == 4) {
-            uint32_t ctr[4] = {photon, round, block++, 0};
+            uint32_t ctr[4] = {photon, round, block++, lineage};
             uint32_t key[2] = {seed, 0};
             philox(ctr, key);
             std::memcpy(words, ctr, sizeof(words));
@@ -489,7 +492,22 @@ struct Guide {
     double roulette = 0.0;
     double cap = 1.0e300;         // DDIS only while the weight is below this
     const double* scale = nullptr;  // per-cell roulette threshold scale (nx * ny * nz), or none
+    double split = 0.0;           // split above split x the cell's roulette weight (0 = off)
 };
+
+// Splitting (the upper bound of a weight window): after an atmospheric scatter, a photon
+// heavier than split x W (W = the roulette weight of its cell) continues as n = min(weight /
+// W, kSplitMax) copies of weight / n; the copies wait on a stack of kSplitStack per history,
+// which also bounds n, and each runs with its own stream (lineage = split_lineage of the
+// parent's lineage, its draws so far and the copy's index) once the history before it ends.
+constexpr int kSplitMax = 8;
+constexpr int kSplitStack = 8;
+
+uint32_t split_lineage(uint32_t lineage, uint32_t draws, uint32_t copy) {
+    uint32_t h = lineage * 0x9E3779B1u ^ draws * 0x85EBCA77u ^ copy * 0xC2B2AE3Du;
+    h ^= h >> 16; h *= 0x85EBCA6Bu; h ^= h >> 13; h *= 0xC2B2AE35u; h ^= h >> 16;
+    return h ? h : 1u;
+}
 
 // Importance tally: for every event, the Stokes-I peel-off contributions of that event and
 // of the next kRing - 1 events of the same history, per unit weight at the event, summed
@@ -789,6 +807,15 @@ struct Transport {
         double remains = 0;
         bool new_path = true;  // label 1000 (draw a new optical path) vs 1010
         uint32_t steps = 0;
+        // Copies made by splitting, run after the history before them ends (last first).
+        struct Copy {
+            int i, j, k;
+            double x, y, z, a, b, c, phi, s[4], weight;
+            uint32_t steps, nscat, lineage;
+        };
+        Copy pending[kSplitStack];
+        int waiting = 0;
+    history:
         for (;;) {
             if (new_path) remains = -std::log(std::max(rng.uniform(), kEps));
             new_path = false;
@@ -819,7 +846,7 @@ struct Transport {
                 if (t.paths) path_layers[size_t(k_old - 1)] += dist;
                 remains -= dist * bv;
                 if (k <= nz && k >= 1) continue;
-                if (k > nz) return 0;  // escaped through TOA
+                if (k > nz) goto ended;  // escaped through TOA
                 surface = true;
                 break;
             }
@@ -828,7 +855,7 @@ struct Transport {
                 k = std::max(k, 1);
                 z = 0.0;
                 weight *= t.albedo[size_t(i - 1) + size_t(nx) * size_t(j - 1)];
-                if (weight < kEps) return 0;
+                if (weight < kEps) goto ended;
                 ++cnt.scatters;
                 ++nscat;
                 locate(i, j, k, z);
@@ -848,7 +875,7 @@ struct Transport {
                 record(i, j, k, weight, contributed);
                 // GROUND_LAMB2: theta = acos(sqrt(P)), phi = 2 pi U.
                 double P = rng.uniform(), U = rng.uniform();
-                if (!roulette(weight, rng, i, j, k)) return 0;
+                if (!roulette(weight, rng, i, j, k)) goto ended;
                 double theta = std::acos(std::sqrt(P));
                 double phi_out = 2.0 * kPi * U;
                 a = std::sin(theta) * std::cos(phi_out);
@@ -882,7 +909,7 @@ struct Transport {
             }
             bool gas = sp == t.ntypes + 1;
             weight *= gas ? t.ssalb_gas[size_t(k - 1)] : t.species[size_t(sp - 1)].ssalb;
-            if (weight < kEps) return 0;
+            if (weight < kEps) goto ended;
             ++cnt.scatters;
             ++nscat;
             locate(i, j, k, z);
@@ -974,13 +1001,40 @@ struct Transport {
             b = std::sin(phi_out) * std::sqrt(std::max(0.0, 1.0 - cos_out * cos_out));
             c = cos_out;
             if (guided) weight *= ddis_factor(sp - 1, cos_sca, s0, a, b, c);
-            if (!roulette(weight, rng, i, j, k)) return 0;
+            if (!roulette(weight, rng, i, j, k)) goto ended;
             if (a * a_bak < 0.0) x = std::max(0.0, t.xunit - x);
             if (b * b_bak < 0.0) y = std::max(0.0, t.yunit - y);
             if (c * c_bak < 0.0) z = std::max(0.0, t.zu(k) - z);
             phi_in = phi_out;
+            if (guide.split > 0.0) {
+                double w_cell = guide.roulette;
+                if (guide.scale) w_cell *= guide.scale[size_t(i - 1) + size_t(nx) * (size_t(j - 1) + size_t(ny) * size_t(k - 1))];
+                if (w_cell > 0.0 && weight > guide.split * w_cell) {
+                    const int n = std::min({int(weight / w_cell), kSplitMax, 1 + kSplitStack - waiting});
+                    if (n >= 2) {
+                        weight /= double(n);
+                        for (int copy = 1; copy < n; ++copy) {
+                            Copy& p = pending[waiting++];
+                            p = Copy{i, j, k, x, y, z, a, b, c, phi_in, {s[0], s[1], s[2], s[3]}, weight, steps, nscat,
+                                     split_lineage(rng.lineage, rng.draws, uint32_t(copy))};
+                        }
+                    }
+                }
+            }
             new_path = true;  // GOTO 1000
         }
+    ended:
+        // The history ended (GOTO 4000); a copy left by splitting continues the photon.
+        if (waiting > 0) {
+            const Copy& p = pending[--waiting];
+            i = p.i; j = p.j; k = p.k; x = p.x; y = p.y; z = p.z; a = p.a; b = p.b; c = p.c; phi_in = p.phi;
+            for (int m = 0; m < 4; ++m) s[m] = p.s[m];
+            weight = p.weight; steps = p.steps; nscat = p.nscat;
+            rng = Stream{photon_id, round, seed, p.lineage};
+            new_path = true;
+            goto history;
+        }
+        return 0;
     }
 };
 
@@ -1036,26 +1090,27 @@ int monki_oracle_validate(const double* tables, size_t count, char* err, size_t 
 // counters (5 x u64): scatters, photons, free-path cell visits, detector cell visits,
 // tally updates. Returns the failure flag (0 on success); a nonzero flag rejects the run.
 int monki_oracle_run_guided(const double* tables, size_t table_count, const uint32_t controls[8],
-                            const double guide[3], const double* scale, int threads, double* out,
+                            const double guide[4], const double* scale, int threads, double* out,
                             uint64_t* counters, double* importance, const double* pixel_weight,
                             uint32_t options, char* err, size_t errlen);
 
 int monki_oracle_run(const double* tables, size_t table_count, const uint32_t controls[8], int threads,
                      double* out, uint64_t* counters, char* err, size_t errlen) {
-    const double plain[3] = {0.0, 0.0, 0.0};
+    const double plain[4] = {0.0, 0.0, 0.0, 0.0};
     return monki_oracle_run_guided(tables, table_count, controls, plain, nullptr, threads, out, counters, nullptr,
                                    nullptr, 0u, err, errlen);
 }
 
 // The same round group with guided transport: guide = {epsilon (DDIS probability at
-// particle scatters, [0, 1)), roulette weight (0 = off), DDIS weight cap (0 = none)};
+// particle scatters, [0, 1)), roulette weight (0 = off), DDIS weight cap (0 = none),
+// splitting factor (0 = off, else >= 1: split above that many roulette weights)};
 // scale (nx * ny * nz, or NULL) multiplies the roulette weight per cell. importance
 // (2 * nx * ny * nz, or NULL) receives the importance tally: per cell the summed future
 // contribution per unit weight, then the event count; pixel_weight (nx * ny * angles, or
 // NULL) weights each contribution by its output pixel. options bit 0 adds the
 // scattering-order diagnostics to each round's tallies.
 int monki_oracle_run_guided(const double* tables, size_t table_count, const uint32_t controls[8],
-                            const double guide[3], const double* scale, int threads, double* out,
+                            const double guide[4], const double* scale, int threads, double* out,
                             uint64_t* counters, double* importance, const double* pixel_weight,
                             uint32_t options, char* err, size_t errlen) {
     try {
@@ -1071,6 +1126,14 @@ int monki_oracle_run_guided(const double* tables, size_t table_count, const uint
             write_error(err, errlen, "Invalid round group");
             return 1;
         }
+        if (!(guide[3] == 0.0 || (guide[3] >= 1.0 && std::isfinite(guide[3])))) {
+            write_error(err, errlen, "Invalid guide: split must be 0 or at least 1");
+            return 1;
+        }
+        if (guide[3] > 0.0 && (t.paths || importance || guide[1] <= 0.0)) {
+            write_error(err, errlen, "Splitting needs a roulette weight and no layer paths or importance tallies");
+            return 1;
+        }
         if (t.backward && (guide[0] > 0.0 || guide[1] > 0.0 || importance || pixel_weight)) {
             write_error(err, errlen, "Guided transport and importance tallies need forward transport");
             return 1;
@@ -1079,6 +1142,7 @@ int monki_oracle_run_guided(const double* tables, size_t table_count, const uint
         tr.guide.epsilon = guide[0];
         tr.guide.roulette = guide[1];
         if (guide[2] > 0.0) tr.guide.cap = guide[2];
+        tr.guide.split = guide[3];
         tr.guide.scale = scale;
         tr.pixel_weight = pixel_weight;
         if (options & 1u) tr.enable_orders();

@@ -108,8 +108,9 @@ def run(tables, controls, threads: int | None = None, guide=None, scale=None, im
     """Run one round group; returns (tallies[rounds, tally_count], counters dict[, importance]).
 
     ``controls`` are the eight words of the CUDA run call. ``guide`` = (epsilon, roulette
-    [, DDIS weight cap]) selects guided transport (detector-directed sampling at particle
-    scatters and Russian roulette); None is the analog method. ``scale`` (nx, ny, nz),
+    [, DDIS weight cap[, splitting factor]]) selects guided transport (detector-directed
+    sampling at particle scatters, Russian roulette and splitting); None is the analog
+    method. ``scale`` (nx, ny, nz),
     Fortran order, multiplies the roulette weight per cell. With ``importance`` the third
     result is the importance tally, shape (2, nx, ny, nz): summed future contribution per
     unit weight and event count per cell, each contribution weighted by ``pixel_weights``
@@ -125,7 +126,7 @@ def run(tables, controls, threads: int | None = None, guide=None, scale=None, im
     counters = np.zeros(5, dtype=np.uint64)
     err = ctypes.create_string_buffer(4096)
     threads = threads or os.cpu_count() or 1
-    g = np.zeros(3)
+    g = np.zeros(4)
     g[: len(guide or ())] = guide or ()
     scale_arr = None if scale is None else np.ascontiguousarray(np.asarray(scale, dtype=np.float64).ravel(order="F"))
     if scale_arr is not None and scale_arr.size != nx * ny * nz:

@@ -107,11 +107,15 @@ def test_guide_settings_are_validated(oracle):
     for bad in ((1.0, 0.0, 0.0), (-0.1, 0.0, 0.0), (0.0, 1.5, 0.0)):
         with pytest.raises(RuntimeError, match="Invalid guide"):
             oracle.run(scene.tables, _controls(scene, 1, 1), 2, guide=bad)
-    for kwargs in ({"epsilon": 1.0}, {"roulette": -1.0}, {"roulette": 2.0}, {"cap": -1.0}, {"epsilon": float("nan")}):
+    with pytest.raises(RuntimeError, match="split"):
+        oracle.run(scene.tables, _controls(scene, 1, 1), 2, guide=(0.0, 0.5, 0.0, 0.5))
+    for kwargs in ({"epsilon": 1.0}, {"roulette": -1.0}, {"roulette": 2.0}, {"cap": -1.0}, {"epsilon": float("nan")},
+                   {"split": 0.5}, {"split": 2.0, "roulette": 0.0}):
         with pytest.raises(ValueError):
             Guided(**kwargs)
-    assert Guided(0.25, 0.5, 1.5).oracle() == (0.25, 0.5, 1.5)
+    assert Guided(0.25, 0.5, 1.5).oracle() == (0.25, 0.5, 1.5, 0.0)
     assert "epsilon=0.25" in Guided(0.25, 0.5, 1.5).config()
+    assert "split" not in Guided(0.25, 0.5, 1.5).config() and "split=2.0" in Guided(0.0, 0.5, 0.0, 2.0).config()
 
 
 def test_scattering_order_tallies_add_up(oracle):
@@ -129,3 +133,63 @@ def test_scattering_order_tallies_add_up(oracle):
     np.testing.assert_allclose(located_single.sum(axis=(1, 2, 3)), single.sum(axis=(1, 2)), rtol=1e-12)
     assert located[0][:, :, 0, :].sum() > 0  # surface reflections
     assert located.shape[3] == nz  # the surface and the nz - 1 physical layers
+
+
+def _splitting_map(scene):
+    """Roulette scale 4 outside the box cloud's columns and 0.25 inside them: photons
+    gather weight outside and split when they scatter in the cloud."""
+
+    nmat, nx, ny, nz, angles = scene.shape
+    scale = np.full((nx, ny, nz), 4.0)
+    scale[3:8, 2:6, :] = 0.25
+    return scale
+
+
+def test_splitting_keeps_the_analog_expectation(oracle):
+    scene = _small_box()
+    scale = _splitting_map(scene)
+    plain, _ = oracle.run(scene.tables, _controls(scene, 32, 21), 8)
+    split, counters = oracle.run(scene.tables, _controls(scene, 32, 22), 8, guide=(0.0, 0.5, 0.0, 2.0), scale=scale)
+    z = _z(_stokes_rounds(oracle, scene, split), _stokes_rounds(oracle, scene, plain))
+    assert np.mean(np.abs(z) < 3) >= 0.98, np.sort(np.abs(z))[-8:]
+    assert abs(z.mean()) < 0.3
+    gi = _stokes_rounds(oracle, scene, split)[:, 0].sum(axis=(1, 2, 3))
+    pi = _stokes_rounds(oracle, scene, plain)[:, 0].sum(axis=(1, 2, 3))
+    assert abs((gi.mean() - pi.mean()) / np.hypot(gi.std(ddof=1), pi.std(ddof=1)) * np.sqrt(32)) < 4
+
+
+def test_splitting_spends_more_events_where_the_map_is_important(oracle):
+    scene = _small_box(ppc=20, rounds=4)
+    scale = _splitting_map(scene)
+    controls = _controls(scene, 4, 5)
+    _, without = oracle.run(scene.tables, controls, 8, guide=(0.0, 0.5, 0.0, 0.0), scale=scale)
+    _, with_split = oracle.run(scene.tables, controls, 8, guide=(0.0, 0.5, 0.0, 2.0), scale=scale)
+    assert with_split["photons"] == without["photons"]
+    assert with_split["scatters"] > 1.2 * without["scatters"]
+
+
+def test_splitting_is_deterministic_and_off_below_the_window(oracle):
+    scene = _small_box(ppc=10, rounds=2)
+    nmat, nx, ny, nz, angles = scene.shape
+    controls = _controls(scene, 2, 9)
+    scale = _splitting_map(scene)
+    first, c0 = oracle.run(scene.tables, controls, 1, guide=(0.0, 0.5, 0.0, 2.0), scale=scale)
+    again, c1 = oracle.run(scene.tables, controls, 1, guide=(0.0, 0.5, 0.0, 2.0), scale=scale)
+    np.testing.assert_array_equal(first, again)
+    assert c0 == c1
+    # A uniform map keeps every weight at or below the roulette weight: nothing splits.
+    flat, f0 = oracle.run(scene.tables, controls, 1, guide=(0.0, 0.5, 0.0, 2.0))
+    plain_roulette, f1 = oracle.run(scene.tables, controls, 1, guide=(0.0, 0.5, 0.0, 0.0))
+    np.testing.assert_array_equal(flat, plain_roulette)
+    assert f0 == f1
+
+
+def test_splitting_rejects_paths_and_missing_roulette(oracle):
+    import monki.scenes as scenes
+
+    layered = scenes.layered_cloud(2, 1, nx=3, ny=2)
+    with pytest.raises(RuntimeError, match="Splitting"):
+        oracle.run(layered.tables, _controls(layered, 1, 1), 1, guide=(0.0, 0.5, 0.0, 2.0))
+    box = _small_box(ppc=2, rounds=1)
+    with pytest.raises(RuntimeError, match="Splitting"):
+        oracle.run(box.tables, _controls(box, 1, 1), 1, guide=(0.0, 0.0, 0.0, 2.0))
