@@ -90,7 +90,20 @@ struct Guide {
     T roulette;        // roulette weight (0 = off), times scale[cell] when a map is set
     T cap;             // detector branch only while the weight is below cap
     const T* scale;    // per-cell roulette scale (nx * ny * nz), or null
+    T split;           // split above split x the cell's roulette weight (0 = off)
 };
+
+// Splitting: at most kSplitMax copies per split, at most kSplitStack waiting per slot.
+constexpr int kSplitMax = 8;
+constexpr int kSplitStack = 8;
+
+// Stream of a copy made by splitting: a 32-bit mix of its parent's lineage, the parent's
+// draws so far and the copy's index (never 0, the lineage of the photon itself).
+__host__ __device__ inline uint32_t split_lineage(uint32_t lineage, uint32_t draws, uint32_t copy) {
+    uint32_t h = lineage * 0x9E3779B1u ^ draws * 0x85EBCA77u ^ copy * 0xC2B2AE3Du;
+    h ^= h >> 16; h *= 0x85EBCA6Bu; h ^= h >> 13; h *= 0xC2B2AE35u; h ^= h >> 16;
+    return h ? h : 1u;
+}
 
 // Importance tally of a pilot run: per cell the summed Stokes-I contribution, per unit
 // weight at the event, of the event and the next kRing - 1 events of its history, then

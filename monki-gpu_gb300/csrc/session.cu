@@ -39,6 +39,7 @@ struct Config {
     double epsilon = 0.0;        // guided: detector-branch probability at particle scatters
     double roulette = 0.0;       // guided: roulette weight (0 = off)
     double cap = 0.0;            // guided: detector branch only below this weight (0 = always)
+    double split = 0.0;          // guided: split above split x the roulette weight (0 = off)
     bool importance = false;     // tally per-cell importance (pilot runs)
     bool graphs = true;          // replay each batch of wavefront iterations as a CUDA graph
     bool orders = false;         // scattering-order diagnostics (single scattering, locations)
@@ -81,7 +82,7 @@ Config parse_config(const char* text) {
         } else if (key == "pool") c.pool = uint32_t(as_int(1024, 1l << 26));
         else if (key == "check_every") c.check_every = uint32_t(as_int(1, 1024));
         else if (key == "walk") c.walk = uint32_t(as_int(1, 1 << 20));
-        else if (key == "epsilon" || key == "roulette" || key == "cap") {
+        else if (key == "epsilon" || key == "roulette" || key == "cap" || key == "split") {
             char* e = nullptr;
             const double v = std::strtod(value.c_str(), &e);
             if (!e || *e || !std::isfinite(v) || v < 0.0) throw std::runtime_error("Invalid config value: " + item);
@@ -91,6 +92,9 @@ Config parse_config(const char* text) {
             } else if (key == "roulette") {
                 if (v > 1.0) throw std::runtime_error("roulette must be in [0, 1]");
                 c.roulette = v;
+            } else if (key == "split") {
+                if (v != 0.0 && v < 1.0) throw std::runtime_error("split must be 0 or at least 1");
+                c.split = v;
             } else {
                 c.cap = v;
             }
@@ -102,6 +106,8 @@ Config parse_config(const char* text) {
         else throw std::runtime_error("Unknown config key: " + key);
     }
     if (c.block % 32) throw std::runtime_error("block must be a multiple of 32");
+    if (c.split > 0.0 && (c.roulette <= 0.0 || c.importance))
+        throw std::runtime_error("splitting needs a roulette weight and no importance tally");
     if (!c.wavefront && (c.epsilon > 0.0 || c.roulette > 0.0 || c.importance || c.orders))
         throw std::runtime_error("guided transport, importance and scattering-order tallies need engine=wavefront");
     return c;
@@ -508,7 +514,10 @@ Pool<T> allocate_pool(Session& s) {
                             s.cfg.orders ? n * sizeof(uint32_t) : 0,
                             (s.prep.nmat == 4 && !s.prep.backward) ? n * sizeof(T) : 0,
                             s.prep.backward ? size_t(s.prep.nmat) * s.prep.nmat * n * sizeof(T) : 0,
-                            (s.prep.backward && s.cfg.orders) ? n * sizeof(uint32_t) : 0};
+                            (s.prep.backward && s.cfg.orders) ? n * sizeof(uint32_t) : 0,
+                            s.cfg.split > 0.0 ? n * sizeof(uint32_t) : 0,
+                            s.cfg.split > 0.0 ? n * kSplitStack * sizeof(SplitCopy<T>) : 0,
+                            s.cfg.split > 0.0 ? n * sizeof(uint32_t) : 0};
     size_t bytes = 0;
     for (size_t part : parts) bytes += align_up(part, 256);
     check(cudaMalloc(&s.pool_memory, bytes), "cudaMalloc(pool)");
@@ -538,6 +547,11 @@ Pool<T> allocate_pool(Session& s) {
     if (s.prep.nmat == 4 && !s.prep.backward) P.vee = reinterpret_cast<T*>(take(n * sizeof(T)));
     if (s.prep.backward) P.matrix = reinterpret_cast<T*>(take(size_t(s.prep.nmat) * s.prep.nmat * n * sizeof(T)));
     if (s.prep.backward && s.cfg.orders) P.first = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
+    if (s.cfg.split > 0.0) {
+        P.lineage = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
+        P.copies = reinterpret_cast<SplitCopy<T>*>(take(n * kSplitStack * sizeof(SplitCopy<T>)));
+        P.waiting = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
+    }
     return P;
 }
 
@@ -577,7 +591,7 @@ void wave_iteration(Session& s, const SceneView<T>& v, Pool<T>& P, const Control
         wf_peel<T, T, NMAT, PATHS, false><<<grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, banks, s.wave, s.failure, s.counters);
     if (ev) cudaEventRecord(ev[2], s.stream);
     Guide<T> g{T(s.cfg.epsilon), T(s.cfg.roulette), s.cfg.cap > 0.0 ? T(s.cfg.cap) : T(INFINITY),
-               static_cast<const T*>(s.scale)};
+               static_cast<const T*>(s.scale), T(s.cfg.split)};
     if (v.backward) wf_scatter<T, NMAT, true><<<slots_grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, g, s.failure);
     else wf_scatter<T, NMAT, false><<<slots_grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, g, s.failure);
     if (ev) cudaEventRecord(ev[3], s.stream);
@@ -596,6 +610,7 @@ void run_wavefront(Session& s, const Controls& c) {
     P.capacity = uint32_t(std::min<uint64_t>(P.capacity, (uint64_t(c.count) + 255) / 256 * 256));
     check(cudaMemsetAsync(P.counts, 0, 16 * sizeof(uint32_t), s.stream), "memset(counts)");
     check(cudaMemsetAsync(P.meta, 0xFF, size_t(P.capacity) * sizeof(uint4), s.stream), "memset(pool)");
+    if (P.waiting) check(cudaMemsetAsync(P.waiting, 0, size_t(P.capacity) * sizeof(uint32_t), s.stream), "memset(copies)");
     Divisors dv{FastDiv::make(c.per_round), FastDiv::make(uint32_t(s.prep.nx)), FastDiv::make(uint32_t(s.prep.ny)),
                 FastDiv::make(uint32_t(s.prep.nx * s.prep.ny))};
     const int grid = s.grid;
@@ -675,7 +690,7 @@ void run_wavefront(Session& s, const Controls& c) {
         const uint64_t live = uint64_t(h[0]) + h[1] + h[2] + h[3];
         if (!profile && s.cfg.tail && h[4] >= c.count && live <= s.cfg.tail) {
             Guide<T> g{T(s.cfg.epsilon), T(s.cfg.roulette), s.cfg.cap > 0.0 ? T(s.cfg.cap) : T(INFINITY),
-                       static_cast<const T*>(s.scale)};
+                       static_cast<const T*>(s.scale), T(s.cfg.split)};
             check(launch_tail<T>(v, c, dv, P, static_cast<T*>(s.banks), s.wave, g, s.failure, s.counters, s.tail_next,
                                  s.stream), "tail launch");
             check(cudaMemsetAsync(P.counts, 0, 4 * sizeof(uint32_t), s.stream), "memset(queues)");
@@ -856,6 +871,7 @@ void* monki_cuda_create(uint32_t device, const double* tables, size_t table_coun
             throw std::runtime_error("backward transport and nmat 4 need engine=wavefront");
         if (prep.backward && (cfg.epsilon > 0.0 || cfg.roulette > 0.0 || cfg.importance))
             throw std::runtime_error("guided transport and importance tallies need forward transport");
+        if (cfg.split > 0.0 && prep.paths) throw std::runtime_error("splitting needs a scene without layer paths");
         if (round_capacity < 1 || round_capacity > 4096) throw std::runtime_error("round_capacity must be in [1, 4096]");
         int n = 0;
         cudaError_t e = cudaGetDeviceCount(&n);

@@ -84,6 +84,15 @@ struct WaveTally {
     uint32_t vee;
 };
 
+// A photon copy made by splitting, waiting in its slot: the records of the pool (with V in
+// place of the free path, which the copy draws anew) and {steps, lineage, order, 0}.
+template <typename T>
+struct SplitCopy {
+    uint4 meta;
+    Quad<T> pos, dir, pol;
+    uint4 extra;
+};
+
 template <typename T>
 struct Pool {
     uint32_t capacity;
@@ -113,6 +122,11 @@ struct Pool {
     // (row-major, M11 = 1 after normalization), element e of slot s at matrix[e * capacity + s].
     T* matrix;
     uint32_t* first;      // backward with order tallies: the first event's cell (i | j << 12 | layer << 24)
+    // Splitting (null when off): each slot's stream lineage, its waiting copies (copy c of
+    // slot s at copies[s * kSplitStack + c]) and their count.
+    uint32_t* lineage;
+    SplitCopy<T>* copies;
+    uint32_t* waiting;
 };
 
 __device__ __forceinline__ uint32_t pack_layers(int k, int k1, int wmin, int wmax) {
@@ -165,15 +179,17 @@ __device__ __forceinline__ T band_beta(const SceneView<T>& s, const T* band, int
 
 // A photon's Philox stream addressed by draw index: draw d is word d % 4 of block d / 4.
 struct DrawStream {
-    uint32_t photon, round, seed, draw, loaded;
+    uint32_t photon, round, seed, draw, loaded, lineage;
     uint4 words;
-    __device__ __forceinline__ void init(uint32_t p, uint32_t r, uint32_t s, uint32_t d) {
-        photon = p; round = r; seed = s; draw = d; loaded = kNone;
+    // lineage: 0 for the photon itself, a split copy's own value otherwise (the fourth
+    // counter word).
+    __device__ __forceinline__ void init(uint32_t p, uint32_t r, uint32_t s, uint32_t d, uint32_t l = 0u) {
+        photon = p; round = r; seed = s; draw = d; loaded = kNone; lineage = l;
     }
     __device__ __forceinline__ float next() {
         const uint32_t blk = draw >> 2;
         if (blk != loaded) {
-            words = philox4x32_10(make_uint4(photon, round, blk, 0u), make_uint2(seed, 0u));
+            words = philox4x32_10(make_uint4(photon, round, blk, lineage), make_uint2(seed, 0u));
             loaded = blk;
         }
         const uint32_t lane = draw & 3u;
@@ -465,9 +481,11 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
     bool fresh = false;
     PathRecord<T> path{PATHS ? P.wander + size_t(slot) * s.nz : nullptr, 255, 0, kNoRuns, T(0), T(0)};
 
+    uint32_t lineage = 0u;
     if (pid != kNone) {
         const uint32_t ro = dv.per_round.div(pid);
-        rng.init(pid - ro * ctl.per_round, ctl.first_round + ro, ctl.seed, meta.y);
+        if (P.lineage) lineage = P.lineage[slot];
+        rng.init(pid - ro * ctl.per_round, ctl.first_round + ro, ctl.seed, meta.y, lineage);
         i = int(meta.z & 0xFFFF); j = int(meta.z >> 16);
         unpack_layers(meta.w, k, k1, wmin, wmax);
         pos = pos_in;
@@ -485,7 +503,26 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
     T& x = pos.x; T& y = pos.y; T& z = pos.z; T& weight = pos.w;
     T& remains = pol.z; T& init_part = pol.w;
 
+    T vee = T(0);
     for (;;) {
+        if (pid == kNone && P.waiting && P.waiting[slot] > 0u) {
+            // A copy left by splitting continues in this slot, with its own stream and a
+            // new free path drawn from it.
+            const uint32_t n = P.waiting[slot] - 1u;
+            const SplitCopy<T> cp = P.copies[size_t(slot) * kSplitStack + n];
+            P.waiting[slot] = n;
+            pid = cp.meta.x;
+            i = int(cp.meta.z & 0xFFFF); j = int(cp.meta.z >> 16);
+            unpack_layers(cp.meta.w, k, k1, wmin, wmax);
+            path.wmin = wmin; path.wmax = wmax;
+            pos = cp.pos; dir = cp.dir; pol = cp.pol;
+            steps = cp.extra.x; lineage = cp.extra.y; order = cp.extra.z;
+            vee = cp.pol.z;
+            const uint32_t ro = dv.per_round.div(pid);
+            rng.init(pid - ro * ctl.per_round, ctl.first_round + ro, ctl.seed, 0u, lineage);
+            remains = -log(fmax(T(rng.next()), eps));
+            fresh = true;
+        }
         if (pid == kNone) {
             // Read first so a drained group stops reserving (the counter never wraps).
             if (!may_claim || *reinterpret_cast<volatile uint32_t*>(P.counts + 4) >= ctl.count) break;
@@ -511,6 +548,7 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
             k1 = -2; init_part = T(0);
             path.wmin = 255; path.wmax = 0; path.runs = kNoRuns;
             remains = -log(fmax(T(rng.next()), eps));
+            lineage = 0u; vee = T(0);
             fresh = true;
         }
         const T a = dir.x, b = dir.y, c = dir.z;
@@ -609,7 +647,9 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
     }
 
     if (pid == kNone) {
-        if (meta.x != kNone) P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u);
+        if (meta.x != kNone || fresh) P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u);
+        // Copies still waiting keep the slot live: the round group is not over.
+        if (P.waiting && P.waiting[slot] > 0u) ++paused;
         return -1;
     }
     P.meta[slot] = make_uint4(pid, rng.draw, uint32_t(i) | (uint32_t(j) << 16), pack_layers(k, k1, path.wmin, path.wmax));
@@ -625,7 +665,8 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
     if (fresh) {
         P.dir[slot] = dir;
         if (P.ring_n) P.ring_n[slot] = 0u;
-        if (P.vee) P.vee[slot] = T(0);
+        if (P.vee) P.vee[slot] = vee;
+        if (P.lineage) P.lineage[slot] = lineage;
         if (P.matrix) {
             const int nm = s.nmat;
             for (int e = 0; e < nm * nm; ++e) P.matrix[size_t(e) * P.capacity + slot] = (e % (nm + 1) == 0) ? T(1) : T(0);
@@ -1000,7 +1041,7 @@ __device__ __forceinline__ bool scatter_event(uint32_t slot, bool surface, const
     if (pid == kNone) { atomicOr(failure, kQueueCorrupt); return false; }
     const uint32_t ro = dv.per_round.div(pid);
     DrawStream rng;
-    rng.init(pid - ro * ctl.per_round, ctl.first_round + ro, ctl.seed, meta.y);
+    rng.init(pid - ro * ctl.per_round, ctl.first_round + ro, ctl.seed, meta.y, P.lineage ? P.lineage[slot] : 0u);
     const T a0 = dir0.x, b0 = dir0.y, c0 = dir0.z;
     T a, b, c, phi_out, q = T(0), u = T(0), v = T(0);
     // Backward transport: the weight matrix (M11 = 1), updated by M P^T (M As at the
@@ -1128,6 +1169,29 @@ __device__ __forceinline__ bool scatter_event(uint32_t slot, bool surface, const
         pos.z = fmax(T(0), __ldg(s.zunit + k) - pos.z);
     }
     pol.x = q; pol.y = u;
+    if (!surface && g.split > T(0) && P.waiting && roulette > T(0) && pos.w > g.split * roulette) {
+        // Splitting: n copies of weight / n, n - 1 of them left waiting in this slot, each
+        // with its own stream (drawn before this history's next free path).
+        const uint32_t held = P.waiting[slot];
+        const int n = min(min(int(pos.w / roulette), kSplitMax), 1 + kSplitStack - int(held));
+        if (n >= 2) {
+            pos.w = pos.w / T(n);
+            const uint32_t lineage = P.lineage[slot];
+            const uint32_t steps = P.steps[slot];
+            const uint32_t order = P.order ? P.order[slot] : 0u;
+            const Quad<T> dir_out{a, b, c, phi_out};
+            const Quad<T> pol_out{q, u, v, pol.w};
+            for (int copy = 1; copy < n; ++copy) {
+                SplitCopy<T>& cp = P.copies[size_t(slot) * kSplitStack + held + uint32_t(copy) - 1u];
+                cp.meta = make_uint4(pid, 0u, meta.z, meta.w);
+                cp.pos = pos;
+                cp.dir = dir_out;
+                cp.pol = pol_out;
+                cp.extra = make_uint4(steps, split_lineage(lineage, rng.draw, uint32_t(copy)), order, 0u);
+            }
+            P.waiting[slot] = held + uint32_t(n) - 1u;
+        }
+    }
     if (NMAT > 3 && P.vee) P.vee[slot] = v;
     if (BACKWARD) {
 #pragma unroll
@@ -1183,16 +1247,21 @@ wf_tail(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, T* __restrict__ ba
     for (;;) {
         const uint32_t slot = warp_reserve(next);
         if (slot >= P.capacity) break;
-        if (P.meta[slot].x == kNone) continue;
+        if (P.meta[slot].x == kNone && !(P.waiting && P.waiting[slot] > 0u)) continue;
         // No step budget: the walk pauses only at the history step cap, which ends it.
         for (;;) {
             const int queue = transit_slot<T, PATHS, false>(slot, s, band, ctl, dv, P, 0xFFFFFFFFu, false, failure,
                                                              scatters, visits, paused);
-            if (queue < 0) break;
+            if (queue < 0) {
+                if (P.waiting && P.waiting[slot] > 0u) continue;  // its split copies next
+                break;
+            }
             const bool surface = queue == kQueueSurface;
             peel_event<T, T, NMAT, PATHS, BACKWARD>(slot, surface, s, band, ctl, dv, P, banks, L, shard, failure,
                                                     detector, updates);
-            if (!scatter_event<T, NMAT, BACKWARD>(slot, surface, s, ctl, dv, P, g, failure)) break;
+            if (!scatter_event<T, NMAT, BACKWARD>(slot, surface, s, ctl, dv, P, g, failure) &&
+                !(P.waiting && P.waiting[slot] > 0u))
+                break;
         }
     }
     const unsigned long long totals[4] = {scatters, visits, detector, updates};

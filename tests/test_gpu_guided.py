@@ -81,6 +81,52 @@ def test_fp64_guided_roulette_map_reproduces_oracle(oracle, device):
     assert close.mean() == 1.0, f"{(~close).sum()} of {close.size} tallies differ"
 
 
+def _splitting_map(scene):
+    nmat, nx, ny, nz, angles = scene.shape
+    scale = np.full((nx, ny, nz), 4.0)
+    scale[3:8, 2:6, :] = 0.25
+    return scale
+
+
+@pytest.mark.parametrize("pool", [1 << 20, 1024])
+def test_fp64_splitting_reproduces_oracle(oracle, device, pool):
+    """Split copies wait in their slot and run with their own streams; the histories are the
+    oracle's (FP64 tallies within 1e-6, equal scatter counts), whether the copies run in
+    wavefront launches (small pool) or in the tail kernel."""
+    from monki import Guided
+
+    scene = _box(8, 2)
+    scale = _splitting_map(scene)
+    guide = Guided(0.0, 0.5, 0.0, 2.0)
+    batches, provenance, _ = _run(scene, 2, 31, "fp64", scale=scale, guided=guide, pool=pool)
+    expected, counters = oracle.run(scene.tables, _controls(scene, 2, 31), 8, guide=guide.oracle(), scale=scale)
+    _, plain = oracle.run(scene.tables, _controls(scene, 2, 31), 8, guide=(0.0, 0.5, 0.0), scale=scale)
+    assert counters["scatters"] > 1.2 * plain["scatters"]  # copies were made and run
+    actual = np.stack([_flat(b) for b in batches])
+    assert provenance["scatters"] == counters["scatters"]
+    close = np.isclose(actual, expected, rtol=1e-6, atol=1e-12)
+    assert close.mean() == 1.0, f"{(~close).sum()} of {close.size} tallies differ"
+
+
+def test_fp32_splitting_agrees_with_analog_oracle(oracle, device):
+    import monki.scenes as scenes
+    from monki import Guided
+
+    rounds = 32
+    scene = scenes.box_cloud(12, rounds)
+    nmat, nx, ny, nz, angles = scene.shape
+    scale = np.full((nx, ny, nz), 4.0)
+    scale[10:20, 7:13, :] = 0.25
+    batches, _, _ = _run(scene, rounds, 883, "fp32", scale=scale, guided=Guided(0.0, 0.5, 0.0, 2.0))
+    gpu = np.stack([_flat(b) for b in batches])
+    cpu, _ = oracle.run(scene.tables, _controls(scene, rounds, 23274), 16)
+    se = np.hypot(gpu.std(0, ddof=1), cpu.std(0, ddof=1)) / np.sqrt(rounds)
+    mask = se > 0
+    z = (gpu.mean(0) - cpu.mean(0))[mask] / se[mask]
+    assert np.mean(np.abs(z) < 3) >= 0.99
+    assert abs(z.mean()) < 0.1
+
+
 def test_fp64_importance_tally_matches_oracle(oracle, device):
     scene = _box(8, 2)
     batches, provenance, importance = _run(scene, 2, 23274, "fp64", importance=True)

@@ -42,15 +42,17 @@ def test_learned_importance_generalises_and_keeps_estimates_unbiased(device):
         assert np.all(np.isfinite(losses)) and losses[-50:].mean() < 0.5 * losses[:20].mean()
         gains = []
         for seed in (1000, 1001):
-            scene = scenes.box_cloud_variant(seed, 2000, 32)
+            # 64 rounds: roulette makes the estimates skewed, and with few rounds a low sample
+            # mean comes with a low sample variance, which pulls the mean z below zero.
+            scene = scenes.box_cloud_variant(seed, 2000, 64)
             tally, _ = pilot(scene, rounds=2, photons_per_column=300, seed=3)
             target, weight = importance_targets(tally)
             prediction = model.predict(cell_features(scene.tables))
             assert r_squared(prediction[weight > 0], target[weight > 0], weight[weight > 0]) > 0.8
             scale = learned_scale(model, scene)
-            plain, t_plain = _rounds(scene, None, None, 2000, 32, seed)
-            constant, t_constant = _rounds(scene, Guided(0.0, 1.0, 0.0), None, 2000, 32, seed + 1)
-            learned, t_learned = _rounds(scene, Guided(0.0, 1.0, 0.0), scale, 2000, 32, seed + 2)
+            plain, t_plain = _rounds(scene, None, None, 2000, 64, seed)
+            constant, t_constant = _rounds(scene, Guided(0.0, 1.0, 0.0), None, 2000, 64, seed + 1)
+            learned, t_learned = _rounds(scene, Guided(0.0, 1.0, 0.0), scale, 2000, 64, seed + 2)
             n = plain.shape[0]
             se = lambda a: a.std(0, ddof=1) / np.sqrt(n)  # noqa: E731
             z = (learned.mean(0) - plain.mean(0)) / np.hypot(se(learned), se(plain))
