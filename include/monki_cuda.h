@@ -60,8 +60,10 @@ int monki_cuda_last_timing(void *session, float out[2]);
 int monki_cuda_counters(void *session, uint64_t out[6]);
 
 /* Wavefront stage timing of the last run with the profiling flag set, from CUDA events
- * around each launch: summed milliseconds and launch counts of the transit, peel and
- * scatter kernels. No reference counterpart. */
+ * around each launch: summed milliseconds and launch counts of (0) the walks — the fused
+ * step kernel, which also scatters the previous iteration's events, or the transit kernel
+ * of scenes with layer paths —, (1) the peel-off and (2) the separate scattering kernel of
+ * scenes with layer paths (0 when fused). No reference counterpart. */
 int monki_cuda_stage_timing(void *session, double ms[3], uint64_t launches[3]);
 
 /* Number of float64 values per round in a run's output; no reference counterpart. */

@@ -45,6 +45,7 @@ struct Config {
     bool orders = false;         // scattering-order diagnostics (single scattering, locations)
     bool rectangles = true;      // cross equal-extinction rectangles of the band in one step
     uint32_t tail = 1u << 16;    // run a group's last photons to their end in one launch below this many (0 = off)
+    int fused = -1;              // 1: scatter and walk in one step kernel; 0: separate kernels; -1: by scene
 };
 
 Config parse_config(const char* text) {
@@ -80,7 +81,7 @@ Config parse_config(const char* text) {
             else if (value == "megakernel") c.wavefront = false;
             else throw std::runtime_error("engine must be wavefront or megakernel");
         } else if (key == "pool") c.pool = uint32_t(as_int(1024, 1l << 26));
-        else if (key == "check_every") c.check_every = uint32_t(as_int(1, 1024));
+        else if (key == "check_every") c.check_every = uint32_t(as_int(1, 1024) + 1) & ~1u;  // even: see run_wavefront
         else if (key == "walk") c.walk = uint32_t(as_int(1, 1 << 20));
         else if (key == "epsilon" || key == "roulette" || key == "cap" || key == "split") {
             char* e = nullptr;
@@ -103,6 +104,7 @@ Config parse_config(const char* text) {
         else if (key == "orders") c.orders = as_int(0, 1) != 0;
         else if (key == "rectangles") c.rectangles = as_int(0, 1) != 0;
         else if (key == "tail") c.tail = uint32_t(as_int(0, 1l << 26));
+        else if (key == "fused") c.fused = int(as_int(-1, 1));
         else throw std::runtime_error("Unknown config key: " + key);
     }
     if (c.block % 32) throw std::runtime_error("block must be a multiple of 32");
@@ -509,7 +511,7 @@ Pool<T> allocate_pool(Session& s) {
     const size_t ring = s.cfg.importance ? n * kRing : 0;
     const size_t parts[] = {quad, quad, quad, n * sizeof(uint4), n * sizeof(uint32_t), n,
                             n * nz * sizeof(T), n * sizeof(uint32_t), 2 * n * sizeof(T),
-                            3 * n * sizeof(uint32_t), 16 * sizeof(uint32_t),
+                            10 * n * sizeof(uint32_t), kCountWords * sizeof(uint32_t),
                             ring * sizeof(uint32_t), ring * sizeof(T), s.cfg.importance ? n * sizeof(uint32_t) : 0,
                             s.cfg.orders ? n * sizeof(uint32_t) : 0,
                             (s.prep.nmat == 4 && !s.prep.backward) ? n * sizeof(T) : 0,
@@ -534,9 +536,13 @@ Pool<T> allocate_pool(Session& s) {
     P.wander = reinterpret_cast<T*>(take(n * nz * sizeof(T)));
     P.runs = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
     P.run_ci = reinterpret_cast<T*>(take(2 * n * sizeof(T)));
-    uint32_t* queues = reinterpret_cast<uint32_t*>(take(3 * n * sizeof(uint32_t)));
-    for (int q = 0; q < 3; ++q) P.queue[q] = queues + size_t(q) * n;
-    P.counts = reinterpret_cast<uint32_t*>(take(16 * sizeof(uint32_t)));
+    uint32_t* lists = reinterpret_cast<uint32_t*>(take(10 * n * sizeof(uint32_t)));
+    for (int b = 0; b < 2; ++b) {
+        for (int q = 0; q < 3; ++q) P.queue[b][q] = lists + size_t(5 * b + q) * n;
+        P.paused[b] = lists + size_t(5 * b + 3) * n;
+        P.vacant[b] = lists + size_t(5 * b + 4) * n;
+    }
+    P.counts = reinterpret_cast<uint32_t*>(take(kCountWords * sizeof(uint32_t)));
     if (s.cfg.importance) {
         P.ring_cell = reinterpret_cast<uint32_t*>(take(ring * sizeof(uint32_t)));
         P.ring_inv = reinterpret_cast<T*>(take(ring * sizeof(T)));
@@ -574,26 +580,44 @@ void launch_transport(Session& s, const Controls& c, int grid) {
 
 template <typename T, int NMAT, bool PATHS>
 void wave_iteration(Session& s, const SceneView<T>& v, Pool<T>& P, const Controls& c, const Divisors& dv, int grid,
-                    cudaEvent_t* ev) {
+                    uint32_t cur, cudaEvent_t* ev) {
     T* banks = static_cast<T*>(s.banks);
-    check(cudaMemsetAsync(P.counts, 0, 4 * sizeof(uint32_t), s.stream), "memset(queues)");
+    const uint32_t out = cur ^ 1u;
+    check(cudaMemsetAsync(P.counts + kListCounts * out, 0, kListCounts * sizeof(uint32_t), s.stream), "memset(lists)");
     if (ev) cudaEventRecord(ev[0], s.stream);
-    // One thread per pool slot (transit) or per possible event (scatter): a thread that
-    // looped over several slots drifted away from its warp's other lanes (each slot's walk
-    // has its own length). The peel keeps the persistent grid, which measured faster.
+    // One thread per work-list entry (at most one per slot): a thread that looped over
+    // several entries drifted away from its warp's other lanes (each walk has its own
+    // length). The peel keeps the persistent grid, which measured faster.
     const int slots_grid = int((P.capacity + uint32_t(s.cfg.block) - 1) / uint32_t(s.cfg.block));
-    wf_transit<T, PATHS><<<slots_grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, s.cfg.walk, s.failure,
-                                                                              s.counters);
-    if (ev) cudaEventRecord(ev[1], s.stream);
-    if (v.backward)
-        wf_peel<T, T, NMAT, PATHS, true><<<grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, banks, s.wave, s.failure, s.counters);
-    else
-        wf_peel<T, T, NMAT, PATHS, false><<<grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, banks, s.wave, s.failure, s.counters);
-    if (ev) cudaEventRecord(ev[2], s.stream);
     Guide<T> g{T(s.cfg.epsilon), T(s.cfg.roulette), s.cfg.cap > 0.0 ? T(s.cfg.cap) : T(INFINITY),
                static_cast<const T*>(s.scale), T(s.cfg.split)};
-    if (v.backward) wf_scatter<T, NMAT, true><<<slots_grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, g, s.failure);
-    else wf_scatter<T, NMAT, false><<<slots_grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, g, s.failure);
+    // Fused: each event's scattering and its photon's next walk in one kernel (the events of
+    // the previous iteration, peeled there). Unfused (scenes with layer paths by default):
+    // the walks in slot order, the peel-off, then the scatterings.
+    const bool fused = s.cfg.fused == 1 || (s.cfg.fused < 0 && !PATHS);
+    if (fused) {
+        if (v.backward)
+            wf_step<T, NMAT, PATHS, true><<<slots_grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, g, s.cfg.walk,
+                                                                                               cur, s.failure, s.counters);
+        else
+            wf_step<T, NMAT, PATHS, false><<<slots_grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, g, s.cfg.walk,
+                                                                                                cur, s.failure, s.counters);
+    } else {
+        wf_transit<T, PATHS><<<slots_grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, s.cfg.walk, out, s.failure,
+                                                                                  s.counters);
+    }
+    if (ev) cudaEventRecord(ev[1], s.stream);
+    if (v.backward)
+        wf_peel<T, T, NMAT, PATHS, true><<<grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, banks, s.wave, out,
+                                                                                       s.failure, s.counters);
+    else
+        wf_peel<T, T, NMAT, PATHS, false><<<grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, banks, s.wave, out,
+                                                                                        s.failure, s.counters);
+    if (ev) cudaEventRecord(ev[2], s.stream);
+    if (!fused) {
+        if (v.backward) wf_scatter<T, NMAT, true><<<slots_grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, g, out, s.failure);
+        else wf_scatter<T, NMAT, false><<<slots_grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, g, out, s.failure);
+    }
     if (ev) cudaEventRecord(ev[3], s.stream);
 }
 
@@ -608,9 +632,8 @@ void run_wavefront(Session& s, const Controls& c) {
     P.pixel_weight = static_cast<const T*>(s.pixel_weight);
     // Small groups scan only as many slots as they have photons.
     P.capacity = uint32_t(std::min<uint64_t>(P.capacity, (uint64_t(c.count) + 255) / 256 * 256));
-    check(cudaMemsetAsync(P.counts, 0, 16 * sizeof(uint32_t), s.stream), "memset(counts)");
-    check(cudaMemsetAsync(P.meta, 0xFF, size_t(P.capacity) * sizeof(uint4), s.stream), "memset(pool)");
-    if (P.waiting) check(cudaMemsetAsync(P.waiting, 0, size_t(P.capacity) * sizeof(uint32_t), s.stream), "memset(copies)");
+    wf_reset<T><<<int((P.capacity + 255) / 256), 256, 0, s.stream>>>(P);
+    check(cudaGetLastError(), "reset launch");
     Divisors dv{FastDiv::make(c.per_round), FastDiv::make(uint32_t(s.prep.nx)), FastDiv::make(uint32_t(s.prep.ny)),
                 FastDiv::make(uint32_t(s.prep.nx * s.prep.ny))};
     const int grid = s.grid;
@@ -625,22 +648,25 @@ void run_wavefront(Session& s, const Controls& c) {
         for (cudaEvent_t& e : s.stage_events) check(cudaEventCreate(&e), "cudaEventCreate");
     }
     if (profile) for (int q = 0; q < 3; ++q) { s.stage_ms[q] = 0; s.stage_launches[q] = 0; }
+    // A batch is an even number of iterations, so each starts reading the work lists of
+    // buffer 0 and leaves its last lists there.
     auto batch = [&]() {
         for (uint32_t b = 0; b < s.cfg.check_every; ++b) {
             cudaEvent_t* ev = profile ? s.stage_events.data() + 4 * b : nullptr;
-            if (nm == 1 && !paths) wave_iteration<T, 1, false>(s, v, P, c, dv, grid, ev);
-            else if (nm == 1) wave_iteration<T, 1, true>(s, v, P, c, dv, grid, ev);
-            else if (nm == 4 && !paths) wave_iteration<T, 4, false>(s, v, P, c, dv, grid, ev);
-            else if (nm == 4) wave_iteration<T, 4, true>(s, v, P, c, dv, grid, ev);
-            else if (!paths) wave_iteration<T, 3, false>(s, v, P, c, dv, grid, ev);
-            else wave_iteration<T, 3, true>(s, v, P, c, dv, grid, ev);
+            const uint32_t cur = b & 1u;
+            if (nm == 1 && !paths) wave_iteration<T, 1, false>(s, v, P, c, dv, grid, cur, ev);
+            else if (nm == 1) wave_iteration<T, 1, true>(s, v, P, c, dv, grid, cur, ev);
+            else if (nm == 4 && !paths) wave_iteration<T, 4, false>(s, v, P, c, dv, grid, cur, ev);
+            else if (nm == 4) wave_iteration<T, 4, true>(s, v, P, c, dv, grid, cur, ev);
+            else if (!paths) wave_iteration<T, 3, false>(s, v, P, c, dv, grid, cur, ev);
+            else wave_iteration<T, 3, true>(s, v, P, c, dv, grid, cur, ev);
         }
-        check(cudaMemcpyAsync(s.host_counts, P.counts, 5 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s.stream),
-              "copy(counts)");
+        check(cudaMemcpyAsync(s.host_counts, P.counts, kCountWords * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                              s.stream), "copy(counts)");
     };
-    // Without per-stage timing, the batch of check_every iterations (3 launches and a queue
+    // Without per-stage timing, the batch of check_every iterations (2 launches and a list
     // reset each, then the counts read-back) is captured once per run and replayed as one
-    // CUDA graph: the host submits one launch per batch instead of 4 * check_every.
+    // CUDA graph: the host submits one launch per batch instead of 3 * check_every.
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     if (s.cfg.graphs && !profile) {
@@ -668,7 +694,8 @@ void run_wavefront(Session& s, const Controls& c) {
         if (exec) check(cudaGraphLaunch(exec, s.stream), "graph launch");
         else batch();
         it += s.cfg.check_every;
-        launches += 3 * uint64_t(s.cfg.check_every);
+        const bool fused = s.cfg.fused == 1 || (s.cfg.fused < 0 && !paths);
+        launches += (fused ? 2 : 3) * uint64_t(s.cfg.check_every);
         check(cudaGetLastError(), "wavefront launch");
         check(cudaStreamSynchronize(s.stream), "wavefront");
         if (profile) {
@@ -682,18 +709,19 @@ void run_wavefront(Session& s, const Controls& c) {
             }
         }
         const uint32_t* h = s.host_counts;
-        // Done when every photon was claimed and none is queued for an event or paused
-        // mid-walk by the per-launch step budget.
-        if (h[4] >= c.count && h[0] == 0 && h[1] == 0 && h[2] == 0 && h[3] == 0) break;
+        // Done when every photon was claimed and no slot is listed: no event waits for its
+        // scattering, no walk is paused by the per-launch step budget, no vacant slot holds
+        // split copies.
+        const bool claimed = h[kClaimCount] >= c.count;
+        const uint64_t live = uint64_t(h[0]) + h[1] + h[2] + h[3] + h[4];
+        if (claimed && live == 0) break;
         // Few photons left and none to claim: run each to its end in one launch (not while
-        // timing stages, which keeps the three kernels apart).
-        const uint64_t live = uint64_t(h[0]) + h[1] + h[2] + h[3];
-        if (!profile && s.cfg.tail && h[4] >= c.count && live <= s.cfg.tail) {
+        // timing stages, which keeps the kernels apart).
+        if (!profile && s.cfg.tail && claimed && live <= s.cfg.tail) {
             Guide<T> g{T(s.cfg.epsilon), T(s.cfg.roulette), s.cfg.cap > 0.0 ? T(s.cfg.cap) : T(INFINITY),
                        static_cast<const T*>(s.scale), T(s.cfg.split)};
-            check(launch_tail<T>(v, c, dv, P, static_cast<T*>(s.banks), s.wave, g, s.failure, s.counters, s.tail_next,
-                                 s.stream), "tail launch");
-            check(cudaMemsetAsync(P.counts, 0, 4 * sizeof(uint32_t), s.stream), "memset(queues)");
+            check(launch_tail<T>(v, c, dv, P, static_cast<T*>(s.banks), s.wave, g, 0u, fused, s.failure, s.counters,
+                                 s.tail_next, s.stream), "tail launch");
             check(cudaStreamSynchronize(s.stream), "tail");
             s.tails += 1;
             launches += 1;
@@ -946,7 +974,7 @@ void* monki_cuda_create(uint32_t device, const double* tables, size_t table_coun
             }
             check(cudaMalloc(&s->flush_info, info.size() * sizeof(double)), "cudaMalloc(flush info)");
             check(cudaMemcpy(s->flush_info, info.data(), info.size() * sizeof(double), cudaMemcpyHostToDevice), "upload(flush info)");
-            check(cudaMallocHost(&s->host_counts, 16 * sizeof(uint32_t)), "cudaMallocHost(counts)");
+            check(cudaMallocHost(&s->host_counts, kCountWords * sizeof(uint32_t)), "cudaMallocHost(counts)");
         }
         int per_sm = cfg.blocks_per_sm;
         if (!per_sm) {

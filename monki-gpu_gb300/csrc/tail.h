@@ -12,12 +12,13 @@ struct Divisors;
 struct WaveTally;
 template <typename T> struct Pool;
 
-// Runs every photon left in the pool to its end in one launch on `stream` (each thread
-// takes live slots through the counter *next, which the launch clears first). Call it only
-// once every photon of the round group is claimed.
+// Runs every photon left in the pool to its end on `stream`: with `pending`, first the
+// events queued in work-list buffer b (peeled, not yet scattered: the fused step's last
+// iteration), then every other live slot; each launch is a resident wave whose threads take
+// entries through the counter *next. Call it only once every photon of the group is claimed.
 template <typename T>
 cudaError_t launch_tail(const SceneView<T>& v, const Controls& c, const Divisors& dv, const Pool<T>& P, T* banks,
-                        const WaveTally& W, const Guide<T>& g, uint32_t* failure, unsigned long long* counters,
-                        uint32_t* next, cudaStream_t stream);
+                        const WaveTally& W, const Guide<T>& g, uint32_t b, bool pending, uint32_t* failure,
+                        unsigned long long* counters, uint32_t* next, cudaStream_t stream);
 
 }  // namespace monki

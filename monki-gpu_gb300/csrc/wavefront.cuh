@@ -93,6 +93,10 @@ struct SplitCopy {
     uint4 extra;
 };
 
+constexpr uint32_t kListCounts = 8;   // counts per work-list buffer
+constexpr uint32_t kClaimCount = 16;  // index of the claim counter
+constexpr uint32_t kCountWords = 20;  // words of the counts array
+
 template <typename T>
 struct Pool {
     uint32_t capacity;
@@ -105,9 +109,16 @@ struct Pool {
     T* wander;       // capacity * nz path lengths after the first event
     uint32_t* runs;  // two straight runs of whole layers: lo0 | hi0 << 8 | lo1 << 16 | hi1 << 24
     T* run_ci;       // capacity * 2: 1 / |cos| of each run
-    uint32_t* queue[3];
-    // [0..2] queue sizes and [3] photons paused mid-walk, of the last transit launch
-    // (a photon is live exactly when it is queued or paused); [4] next photon to claim.
+    // Work lists of a wavefront iteration, double buffered (b = 0, 1): the event queues
+    // (surface, gas, particle), the photons paused mid-walk and the empty slots to fill.
+    // A step launch reads buffer b and writes buffer 1 - b; the peel-off reads the events
+    // the step wrote.
+    uint32_t* queue[2][3];
+    uint32_t* paused[2];
+    uint32_t* vacant[2];
+    // counts[kListCounts * b + ...]: [0..2] queue sizes, [3] paused, [4] vacant slots of
+    // buffer b; counts[kClaimCount]: the next photon to claim. A photon is live exactly
+    // when its slot is queued or paused, or holds waiting split copies.
     uint32_t* counts;
     // Importance tally (pilot runs only; null otherwise): the cells and 1 / weight of the
     // last kRing events of each history, and the per-cell FP64 sums.
@@ -456,16 +467,17 @@ __device__ __forceinline__ int uniform_jump(const SceneView<T>& s, int& k, T& z,
 // ----------------------------------------------------------------------------------
 // transit: free path to the next interaction for every pooled photon.
 // ----------------------------------------------------------------------------------
-// One slot's walk to its next event: claims a photon into an empty slot (when claims are
-// open), walks it, selects the interaction and stores the state. Returns the event's queue
-// (surface, gas, particle) or -1 when the slot holds no event (empty, finished, or paused
-// by the step budget). QUEUE enqueues the event for the peel and scatter launches; without
-// it the caller handles the event (the tail kernel).
+// One slot's walk to its next event: continues a split copy or claims a photon into an
+// empty slot (when claims are open), walks it, selects the interaction and stores the
+// state. Returns the event's queue (surface, gas, particle) or -1 when the slot holds no
+// event (empty, finished, or paused by the step budget). QUEUE files the slot in the work
+// lists of buffer `out` (its event queue, the paused list, or the vacant list while it can
+// still be filled); without it the caller handles the event (the tail kernel).
 template <typename T, bool PATHS, bool QUEUE>
 __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s, const T* band, const Controls& ctl,
                                             const Divisors& dv, const Pool<T>& P, uint32_t walk, bool may_claim,
-                                            uint32_t* __restrict__ failure, uint64_t& scatters, uint64_t& visits,
-                                            uint32_t& paused) {
+                                            uint32_t out, uint32_t* __restrict__ failure, uint64_t& scatters,
+                                            uint64_t& visits) {
     const T eps = Tol<T>::eps;
     const int top = s.nz - 1;
     int event = -1;
@@ -525,8 +537,8 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
         }
         if (pid == kNone) {
             // Read first so a drained group stops reserving (the counter never wraps).
-            if (!may_claim || *reinterpret_cast<volatile uint32_t*>(P.counts + 4) >= ctl.count) break;
-            const uint32_t n = warp_reserve(P.counts + 4);
+            if (!may_claim || *reinterpret_cast<volatile uint32_t*>(P.counts + kClaimCount) >= ctl.count) break;
+            const uint32_t n = warp_reserve(P.counts + kClaimCount);
             if (n >= ctl.count) break;
             pid = ctl.first + n;
             const uint32_t ro = dv.per_round.div(pid);
@@ -606,7 +618,10 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
             break;
         }
         if (PATHS && acc_k >= 0) path.add(acc_k, acc);
-        if (outcome == 4) { ++paused; break; }  // budget spent: the walk resumes next iteration
+        if (outcome == 4) {  // budget spent: the walk resumes next iteration
+            if (QUEUE) P.paused[out][warp_reserve(P.counts + kListCounts * out, 3)] = slot;
+            break;
+        }
         // A finished history leaves its slot empty until the next launch, where it is
         // refilled before the walks start: claiming and walking a second photon here
         // would make the whole warp wait on the few lanes whose photon escaped.
@@ -637,10 +652,7 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
         ++scatters;
         ++order;
         const int queue = kind == 255 ? kQueueSurface : (kind == 0 ? kQueueGas : kQueueParticle);
-        if (QUEUE) {
-            const uint32_t at = warp_reserve(P.counts, queue);
-            P.queue[queue][at] = slot;
-        }
+        if (QUEUE) P.queue[out][queue][warp_reserve(P.counts + kListCounts * out, queue)] = slot;
         P.kind[slot] = uint8_t(kind);
         event = queue;
         break;
@@ -648,8 +660,10 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
 
     if (pid == kNone) {
         if (meta.x != kNone || fresh) P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u);
-        // Copies still waiting keep the slot live: the round group is not over.
-        if (P.waiting && P.waiting[slot] > 0u) ++paused;
+        // An empty slot waits for the next launch: copies still waiting keep it live; while
+        // photons remain to claim it is refilled there.
+        if (QUEUE && ((P.waiting && P.waiting[slot] > 0u) || may_claim))
+            P.vacant[out][warp_reserve(P.counts + kListCounts * out, 4)] = slot;
         return -1;
     }
     P.meta[slot] = make_uint4(pid, rng.draw, uint32_t(i) | (uint32_t(j) << 16), pack_layers(k, k1, path.wmin, path.wmax));
@@ -673,42 +687,6 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
         }
     }
     return event;
-}
-
-template <typename T, bool PATHS>
-__device__ __forceinline__ void transit_phase(const SceneView<T>& s, const T* band, const Controls& ctl,
-                                              const Divisors& dv, const Pool<T>& P, uint32_t walk,
-                                              uint32_t* __restrict__ failure,
-                                              unsigned long long* __restrict__ counters) {
-    const uint32_t stride = gridDim.x * blockDim.x;
-    uint64_t scatters = 0, visits = 0;
-    uint32_t paused = 0;
-    // Once every photon of the group is claimed (the counter only grows), empty slots stop
-    // at once: one read per block instead of one per empty lane on a single address.
-    __shared__ uint32_t claims_open;
-    if (threadIdx.x == 0) claims_open = *reinterpret_cast<volatile uint32_t*>(P.counts + 4) < ctl.count;
-    __syncthreads();
-    const bool may_claim = claims_open != 0u;
-
-    for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < P.capacity; slot += stride) {
-        transit_slot<T, PATHS, true>(slot, s, band, ctl, dv, P, walk, may_claim, failure, scatters, visits, paused);
-    }
-
-    const unsigned long long totals[2] = {scatters, visits};
-    unsigned long long* const targets[2] = {counters + 0, counters + 1};
-    block_add<2>(totals, targets);
-    const unsigned long long held[1] = {paused};
-    uint32_t* const held_target[1] = {P.counts + 3};
-    block_add<1>(held, held_target);
-}
-
-template <typename T, bool PATHS>
-__global__ void __launch_bounds__(256, 4)
-wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, uint32_t* __restrict__ failure,
-           unsigned long long* __restrict__ counters) {
-    extern __shared__ __align__(16) unsigned char staged[];
-    const T* band = stage_band<T>(s, staged, failure);
-    transit_phase<T, PATHS>(s, band, ctl, dv, P, walk, failure, counters);
 }
 
 // 128-bit tally update (FP32: one vector atomic; FP64: per nonzero element).
@@ -952,16 +930,17 @@ __device__ __forceinline__ void peel_event(uint32_t slot, bool surface, const Sc
 template <typename T, typename TA, int NMAT, bool PATHS, bool BACKWARD>
 __device__ __forceinline__ void peel_phase(const SceneView<T>& s, const T* band, const Controls& ctl,
                                            const Divisors& dv, const Pool<T>& P, TA* __restrict__ banks,
-                                           const WaveTally& L, uint32_t* __restrict__ failure,
+                                           const WaveTally& L, uint32_t b, uint32_t* __restrict__ failure,
                                            unsigned long long* __restrict__ counters) {
-    const uint32_t ns = P.counts[0], ng = P.counts[1], np = P.counts[2];
+    const uint32_t* c = P.counts + kListCounts * b;
+    const uint32_t ns = c[0], ng = c[1], np = c[2];
     const uint32_t total = ns + ng + np;
     const uint32_t shard = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) % L.shards;
     uint64_t visits = 0, updates = 0;
 
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
         bool surface;
-        const uint32_t slot = queue_entry(P.queue, e, ns, ng, surface);
+        const uint32_t slot = queue_entry(P.queue[b], e, ns, ng, surface);
         if (slot >= P.capacity) { atomicOr(failure, kQueueCorrupt); continue; }
         peel_event<T, TA, NMAT, PATHS, BACKWARD>(slot, surface, s, band, ctl, dv, P, banks, L, shard, failure, visits,
                                                  updates);
@@ -973,11 +952,11 @@ __device__ __forceinline__ void peel_phase(const SceneView<T>& s, const T* band,
 
 template <typename T, typename TA, int NMAT, bool PATHS, bool BACKWARD>
 __global__ void __launch_bounds__(256, 3)
-wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ banks, WaveTally L,
+wf_peel(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, TA* __restrict__ banks, WaveTally L, uint32_t b,
         uint32_t* __restrict__ failure, unsigned long long* __restrict__ counters) {
     extern __shared__ __align__(16) unsigned char staged[];
     const T* band = stage_band<T>(s, staged, failure);
-    peel_phase<T, TA, NMAT, PATHS, BACKWARD>(s, band, ctl, dv, P, banks, L, failure, counters);
+    peel_phase<T, TA, NMAT, PATHS, BACKWARD>(s, band, ctl, dv, P, banks, L, b, failure, counters);
 }
 
 // ----------------------------------------------------------------------------------
@@ -1208,23 +1187,105 @@ __device__ __forceinline__ bool scatter_event(uint32_t slot, bool surface, const
     return true;
 }
 
+// ----------------------------------------------------------------------------------
+// step: one wavefront iteration's scattering and walks, reading the work lists of buffer
+// `cur` and filing every slot in those of buffer 1 - cur. Each queued event is scattered
+// and its photon walks on to its next event in the same thread (no reload of its state,
+// no launch in between); paused photons resume their walks; vacant slots take a waiting
+// split copy or the next photon of the round group and walk it. One thread per list
+// entry: the lists hold at most one entry per slot.
+// ----------------------------------------------------------------------------------
+template <typename T, int NMAT, bool PATHS, bool BACKWARD>
+__device__ __forceinline__ void step_phase(const SceneView<T>& s, const T* band, const Controls& ctl,
+                                           const Divisors& dv, const Pool<T>& P, const Guide<T>& g, uint32_t walk,
+                                           uint32_t cur, uint32_t* __restrict__ failure,
+                                           unsigned long long* __restrict__ counters) {
+    const uint32_t* c = P.counts + kListCounts * cur;
+    const uint32_t ns = c[0], ng = c[1], np = c[2], held = c[3], vacant = c[4];
+    const uint32_t events = ns + ng + np, total = events + held + vacant;
+    const uint32_t out = cur ^ 1u;
+    uint64_t scatters = 0, visits = 0;
+    // Once every photon of the group is claimed (the counter only grows), vacant slots stop
+    // at once: one read per block instead of one per lane on a single address.
+    __shared__ uint32_t claims_open;
+    if (threadIdx.x == 0) claims_open = *reinterpret_cast<volatile uint32_t*>(P.counts + kClaimCount) < ctl.count;
+    __syncthreads();
+    const bool may_claim = claims_open != 0u;
+
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        uint32_t slot;
+        if (e < events) {
+            bool surface;
+            slot = queue_entry(P.queue[cur], e, ns, ng, surface);
+            if (slot >= P.capacity) { atomicOr(failure, kQueueCorrupt); continue; }
+            scatter_event<T, NMAT, BACKWARD>(slot, surface, s, ctl, dv, P, g, failure);  // may leave it vacant
+        } else {
+            slot = e < events + held ? P.paused[cur][e - events] : P.vacant[cur][e - events - held];
+            if (slot >= P.capacity) { atomicOr(failure, kQueueCorrupt); continue; }
+        }
+        transit_slot<T, PATHS, true>(slot, s, band, ctl, dv, P, walk, may_claim, out, failure, scatters, visits);
+    }
+    const unsigned long long totals[2] = {scatters, visits};
+    unsigned long long* const targets[2] = {counters + 0, counters + 1};
+    block_add<2>(totals, targets);
+}
+
+template <typename T, int NMAT, bool PATHS, bool BACKWARD>
+__global__ void __launch_bounds__(256, 4)
+wf_step(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, Guide<T> g, uint32_t walk, uint32_t cur,
+        uint32_t* __restrict__ failure, unsigned long long* __restrict__ counters) {
+    extern __shared__ __align__(16) unsigned char staged[];
+    const T* band = stage_band<T>(s, staged, failure);
+    step_phase<T, NMAT, PATHS, BACKWARD>(s, band, ctl, dv, P, g, walk, cur, failure, counters);
+}
+
+// The same iteration in two launches, for scenes with layer paths, whose walks and
+// scatterings together need more registers than one kernel has without spilling: the walks
+// of every slot in slot order (transit), then, after the peel-off, the scatterings of the
+// queued events (scatter). Both file slots in the work lists of buffer `out` like the step.
+template <typename T, bool PATHS>
+__global__ void __launch_bounds__(256, 4)
+wf_transit(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, uint32_t walk, uint32_t out,
+           uint32_t* __restrict__ failure, unsigned long long* __restrict__ counters) {
+    extern __shared__ __align__(16) unsigned char staged[];
+    const T* band = stage_band<T>(s, staged, failure);
+    uint64_t scatters = 0, visits = 0;
+    __shared__ uint32_t claims_open;
+    if (threadIdx.x == 0) claims_open = *reinterpret_cast<volatile uint32_t*>(P.counts + kClaimCount) < ctl.count;
+    __syncthreads();
+    const bool may_claim = claims_open != 0u;
+    for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < P.capacity; slot += gridDim.x * blockDim.x)
+        transit_slot<T, PATHS, true>(slot, s, band, ctl, dv, P, walk, may_claim, out, failure, scatters, visits);
+    const unsigned long long totals[2] = {scatters, visits};
+    unsigned long long* const targets[2] = {counters + 0, counters + 1};
+    block_add<2>(totals, targets);
+}
+
 template <typename T, int NMAT, bool BACKWARD>
-__device__ __forceinline__ void scatter_phase(const SceneView<T>& s, const Controls& ctl, const Divisors& dv,
-                                              const Pool<T>& P, const Guide<T>& g, uint32_t* __restrict__ failure) {
-    const uint32_t ns = P.counts[0], ng = P.counts[1], np = P.counts[2];
-    const uint32_t total = ns + ng + np;
+__global__ void __launch_bounds__(256, 4)
+wf_scatter(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, Guide<T> g, uint32_t b,
+           uint32_t* __restrict__ failure) {
+    const uint32_t* c = P.counts + kListCounts * b;
+    const uint32_t ns = c[0], ng = c[1], total = c[0] + c[1] + c[2];
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
         bool surface;
-        const uint32_t slot = queue_entry(P.queue, e, ns, ng, surface);
+        const uint32_t slot = queue_entry(P.queue[b], e, ns, ng, surface);
         if (slot >= P.capacity) { atomicOr(failure, kQueueCorrupt); continue; }
         scatter_event<T, NMAT, BACKWARD>(slot, surface, s, ctl, dv, P, g, failure);
     }
 }
 
-template <typename T, int NMAT, bool BACKWARD>
-__global__ void __launch_bounds__(256, 4)
-wf_scatter(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, Guide<T> g, uint32_t* __restrict__ failure) {
-    scatter_phase<T, NMAT, BACKWARD>(s, ctl, dv, P, g, failure);
+// Start of a round group: every slot empty and listed vacant in buffer 0, no claims yet.
+template <typename T>
+__global__ void wf_reset(Pool<T> P) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < P.capacity; slot += stride) {
+        P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u);
+        P.vacant[0][slot] = slot;
+        if (P.waiting) P.waiting[slot] = 0u;
+    }
+    if (blockIdx.x == 0 && threadIdx.x < kCountWords)
+        P.counts[threadIdx.x] = threadIdx.x == 4 ? P.capacity : 0u;
 }
 
 // ----------------------------------------------------------------------------------
@@ -1235,23 +1296,39 @@ wf_scatter(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, Guide<T> g, uin
 // its warp) and runs each photon to its end: walk, peel-off and scattering, event after
 // event, through the same slot functions as the wavefront kernels.
 // ----------------------------------------------------------------------------------
+// pending = true: the events queued in buffer b, peeled but not yet scattered (the fused
+// step scatters them in the next iteration), are scattered first; pending = false: every
+// other live slot (paused walks, waiting split copies).
 template <typename T, int NMAT, bool PATHS, bool BACKWARD>
 __global__ void __launch_bounds__(256, 2)
 wf_tail(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, T* __restrict__ banks, WaveTally L, Guide<T> g,
-        uint32_t* __restrict__ failure, unsigned long long* __restrict__ counters, uint32_t* __restrict__ next) {
+        uint32_t b, bool pending, uint32_t* __restrict__ failure, unsigned long long* __restrict__ counters,
+        uint32_t* __restrict__ next) {
     extern __shared__ __align__(16) unsigned char staged[];
     const T* band = stage_band<T>(s, staged, failure);
     const uint32_t shard = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) % L.shards;
+    const uint32_t* c = P.counts + kListCounts * b;
+    const uint32_t ns = c[0], ng = c[1], events = c[0] + c[1] + c[2];
     uint64_t scatters = 0, visits = 0, detector = 0, updates = 0;
-    uint32_t paused = 0;
     for (;;) {
-        const uint32_t slot = warp_reserve(next);
-        if (slot >= P.capacity) break;
-        if (P.meta[slot].x == kNone && !(P.waiting && P.waiting[slot] > 0u)) continue;
+        const uint32_t n = warp_reserve(next);
+        uint32_t slot = n;
+        if (pending) {
+            if (n >= events) break;
+            bool surface;
+            slot = queue_entry(P.queue[b], n, ns, ng, surface);
+            if (slot >= P.capacity) { atomicOr(failure, kQueueCorrupt); continue; }
+            if (!scatter_event<T, NMAT, BACKWARD>(slot, surface, s, ctl, dv, P, g, failure) &&
+                !(P.waiting && P.waiting[slot] > 0u))
+                continue;
+        } else {
+            if (slot >= P.capacity) break;
+            if (P.meta[slot].x == kNone && !(P.waiting && P.waiting[slot] > 0u)) continue;
+        }
         // No step budget: the walk pauses only at the history step cap, which ends it.
         for (;;) {
-            const int queue = transit_slot<T, PATHS, false>(slot, s, band, ctl, dv, P, 0xFFFFFFFFu, false, failure,
-                                                             scatters, visits, paused);
+            const int queue = transit_slot<T, PATHS, false>(slot, s, band, ctl, dv, P, 0xFFFFFFFFu, false, 0u, failure,
+                                                             scatters, visits);
             if (queue < 0) {
                 if (P.waiting && P.waiting[slot] > 0u) continue;  // its split copies next
                 break;

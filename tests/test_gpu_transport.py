@@ -326,6 +326,37 @@ def test_tail_launch_matches_launch_per_iteration(native, device, name):
         np.testing.assert_allclose(out, base, rtol=1e-6, atol=1e-12)
 
 
+@pytest.mark.parametrize("name", ["layered_cloud", "box_cloud"])
+def test_fused_step_matches_separate_kernels(native, device, name):
+    """Scattering each event and walking its photon on in one step kernel is the same
+    transport as separate walk and scatter kernels: equal counts, FP64 tallies within the
+    oracle-parity tolerance."""
+    import monki.scenes as scenes
+    from monki.execution.native import F64P, U64P
+
+    scene = scenes.layered_cloud(6, 2, nx=10, ny=8) if name == "layered_cloud" else \
+        scenes.box_cloud(6, 2, nx=12, ny=10, box_x=(3, 8), box_y=(2, 6))
+    tables = np.ascontiguousarray(scene.tables)
+    results = []
+    for fused in (0, 1):
+        err = _err()
+        config = f"precision=fp64,pool=4096,tail=0,fused={fused}".encode()
+        handle = native.monki_cuda_create(0, tables.ctypes.data_as(F64P), tables.size, 2, config, err, len(err))
+        assert handle, err.value
+        try:
+            out = np.zeros(2 * int(native.monki_cuda_tally_count(handle)))
+            controls = (ctypes.c_uint32 * 8)(*_controls(scene, 2, 8))
+            assert native.monki_cuda_run(handle, controls, out.ctypes.data_as(F64P), err, len(err)) == 0, err.value
+            counters = np.zeros(6, dtype=np.uint64)
+            native.monki_cuda_counters(handle, counters.ctypes.data_as(U64P))
+            results.append((out, int(counters[0]), int(counters[4])))
+        finally:
+            native.monki_cuda_close(handle)
+    (a, sa, pa), (b, sb, pb) = results
+    assert (sa, pa) == (sb, pb)
+    np.testing.assert_allclose(a, b, rtol=1e-6, atol=1e-12)
+
+
 def test_off_plane_polarization_is_nonzero_and_bounded(device):
     import monki.scenes as scenes
 
