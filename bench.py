@@ -60,6 +60,9 @@ TALLY_BYTES = 32  # one 128-bit tally atomic: 16 B read + 16 B written in L2
 SLOT_SCAN_BYTES = 16  # transit reads every slot's bookkeeping record
 TRANSIT_EVENT_BYTES = 109  # per event: state read (52 B) and written (52 B), queue entry and kind (5 B)
 SCATTER_EVENT_BYTES = 116  # per event: queue entry (4 B), state read (64 B) and written (48 B)
+# Fused step (scenes without layer paths): per event its list entry (4 B), its state read once
+# (64 B) and written once after the walk (52 B), its new queue entry and kind (5 B).
+STEP_EVENT_BYTES = 125
 
 
 def peaks():
@@ -508,16 +511,20 @@ def main():
     value = total_scatters / device_seconds
     # Roofline per wavefront kernel: algorithmic bytes per launch over the event-timed
     # launch duration; the line reports the kernel with the largest share of device time.
+    #   step     (scenes without layer paths) each event's list entry, its state read once
+    #            and written once, its new queue entry, 16 B per free-path cell visit
     #   transit  every slot's bookkeeping record, each event's state read and written and
     #            its queue entry, 16 B per free-path cell visit
     #   peel     each event's state, 16 B per detector-ray cell visit, 32 B per tally atomic
     #   scatter  each event's queue entry and state read and written
     peak, peak_kind = peaks()
     stage_total = max(sum(stage_ms), 1e-9)
-    names = ("transit", "peel", "scatter")
+    fused = not scene.save_path  # the session's default: fused step unless the scene has layer paths
+    names = ("step", "peel") if fused else ("transit", "peel", "scatter")
     stage_share = {name: stage_ms[q] / stage_total for q, name in enumerate(names)}
     pool = 1 << 20
     algorithmic = {
+        "step": STEP_EVENT_BYTES * p_scatters + CELL_BYTES * p_visits_fp,
         "transit": SLOT_SCAN_BYTES * pool * int(stage_launches[0]) + TRANSIT_EVENT_BYTES * p_scatters + CELL_BYTES * p_visits_fp,
         "peel": STATE_BYTES * p_scatters + CELL_BYTES * p_visits_det + TALLY_BYTES * p_updates,
         "scatter": SCATTER_EVENT_BYTES * p_scatters,
