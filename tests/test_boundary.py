@@ -179,6 +179,39 @@ def test_invalid_settings_fail_before_any_device_work(settings):
         CUDA(**settings)
 
 
+@pytest.mark.parametrize(
+    "scene,config,message",
+    [
+        ("box", "split=0.5", "split must be 0 or at least 1"),
+        ("box", "roulette=0,split=2", "splitting needs a roulette weight"),
+        ("layered", "roulette=0.5,split=2", "splitting needs a scene without layer paths"),
+        ("box", "fused=2", "Invalid config value"),
+        ("box", "tail=-1", "Invalid config value"),
+        ("backward", "roulette=0.5", "guided transport and importance tallies need forward transport"),
+        ("backward", "engine=megakernel", "backward transport and nmat 4 need engine=wavefront"),
+        ("box", "engine=megakernel,orders=1", "need engine=wavefront"),
+    ],
+)
+def test_session_settings_are_validated_before_any_device_work(native, scene, config, message):
+    """The packer and the configuration parser reject unsupported combinations with the
+    message the host reports, before looking for a device (so this runs on any machine)."""
+    import monki.scenes as scenes
+    from monki.execution.native import F64P
+
+    if scene == "backward":
+        tables = scenes.box_cloud(2, 1, nx=6, ny=4, box_x=(1, 3), box_y=(1, 2)).tables.copy()
+        tables[11] = 1
+    elif scene == "layered":
+        tables = scenes.layered_cloud(2, 1, nx=3, ny=2).tables
+    else:
+        tables = scenes.box_cloud(2, 1, nx=6, ny=4, box_x=(1, 3), box_y=(1, 2)).tables
+    tables = np.ascontiguousarray(tables)
+    err = ctypes.create_string_buffer(512)
+    handle = native.monki_cuda_create(0, tables.ctypes.data_as(F64P), tables.size, 1, config.encode(), err, len(err))
+    assert not handle
+    assert message in err.value.decode()
+
+
 def test_cuda_rejects_cloud_and_unprepared_use():
     from monki.execution import CUDA, BatchControls
 
