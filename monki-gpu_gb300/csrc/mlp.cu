@@ -146,11 +146,29 @@ __global__ void transpose(const bf16* __restrict__ in, int rows, int cols, int R
     }
 }
 
-// out[n] += sum over m < rows of GT[n * R + m] (bias gradients from a transposed matrix).
+// Bias gradients: out[n] += sum over m < rows of GT[n R + m]. Grid (height, segments): a
+// block sums one segment of row n with 16-byte loads of eight values (R is a multiple of
+// 128, so every row starts 256-byte aligned), the last segment adds the rows past the last
+// whole group of eight, and each block adds its sum with one atomic. One block per row
+// with 2-byte loads was latency bound (116 us per launch at 65,536 rows).
 __global__ void row_sums(const bf16* __restrict__ GT, int rows, int R, float* __restrict__ out) {
     const int n = blockIdx.x;
+    const bf16* row = GT + size_t(n) * R;
+    const int groups = rows >> 3;
+    const int per = (groups + int(gridDim.y) - 1) / int(gridDim.y);
+    const int g0 = int(blockIdx.y) * per, g1 = min(groups, g0 + per);
     float acc = 0.f;
-    for (int m = threadIdx.x; m < rows; m += blockDim.x) acc += __bfloat162float(GT[size_t(n) * R + m]);
+    for (int g = g0 + int(threadIdx.x); g < g1; g += int(blockDim.x)) {
+        const uint4 v = reinterpret_cast<const uint4*>(row)[g];
+        const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&v);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float2 f = __bfloat1622float2(h[q]);
+            acc += f.x + f.y;
+        }
+    }
+    if (blockIdx.y == gridDim.y - 1)
+        for (int m = (groups << 3) + int(threadIdx.x); m < rows; m += int(blockDim.x)) acc += __bfloat162float(row[m]);
     __shared__ float part[32];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
@@ -159,8 +177,13 @@ __global__ void row_sums(const bf16* __restrict__ GT, int rows, int R, float* __
     if (threadIdx.x == 0) {
         float s = 0.f;
         for (int q = 0; q < int(blockDim.x >> 5); ++q) s += part[q];
-        out[n] += s;
+        atomicAdd(out + n, s);
     }
+}
+
+// Segments per row for row_sums: about 1,024 groups of eight per block, at most 32.
+inline unsigned row_segments(int rows) {
+    return unsigned(std::min(32, std::max(1, ((rows >> 3) + 1023) / 1024)));
 }
 
 __global__ void adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1, float* __restrict__ m2,
@@ -287,7 +310,7 @@ void backward(Net& n, int rows, float inv_weight, float* loss) {
     check(cudaMemsetAsync(n.G3, 0, size_t(R) * kHidden * sizeof(bf16), n.stream), "memset");
     head_backward<<<(rows + 63) / 64, kHidden, 0, n.stream>>>(n.dy, n.H3, n.params + ow4, n.Z3, rows, n.grads, n.G3);
     transpose<<<dim3(kHidden / 32, (R + 31) / 32), dim3(32, 8), 0, n.stream>>>(n.G3, R, kHidden, R, n.G3T);
-    row_sums<<<kHidden, 256, 0, n.stream>>>(n.G3T, rows, R, n.grads + ob3);
+    row_sums<<<dim3(kHidden, row_segments(rows)), 256, 0, n.stream>>>(n.G3T, rows, R, n.grads + ob3);
     check(cudaGetLastError(), "head backward launch");
     // Split-K over the rows for the weight gradients: 64-row multiples, 512 rows per slice.
     const int chunk = 512, K = (rows + 63) / 64 * 64, splits = (K + chunk - 1) / chunk;
@@ -298,7 +321,7 @@ void backward(Net& n, int rows, float inv_weight, float* loss) {
     p.zprev = n.Z2; p.H = n.G2; p.HT = n.G2T; p.rows_ht = R;
     gemm<umma::kBackward>(p, 1, n.stream);
     clear_tail(n.G2T, rows, R, kHidden, n.stream);
-    row_sums<<<kHidden, 256, 0, n.stream>>>(n.G2T, rows, R, n.grads + ob2);
+    row_sums<<<dim3(kHidden, row_segments(rows)), 256, 0, n.stream>>>(n.G2T, rows, R, n.grads + ob2);
     p = params_for(n.G2T, n.H1T, kHidden, kHidden, K, n.failure);
     p.lda = R; p.ldb = R; p.k_chunk = chunk; p.C = n.grads + oW2;
     gemm<umma::kAccumulate>(p, splits, n.stream);
@@ -306,7 +329,7 @@ void backward(Net& n, int rows, float inv_weight, float* loss) {
     p.zprev = n.Z1; p.H = n.G1; p.HT = n.G1T; p.rows_ht = R;
     gemm<umma::kBackward>(p, 1, n.stream);
     clear_tail(n.G1T, rows, R, kHidden, n.stream);
-    row_sums<<<kHidden, 256, 0, n.stream>>>(n.G1T, rows, R, n.grads + ob1);
+    row_sums<<<dim3(kHidden, row_segments(rows)), 256, 0, n.stream>>>(n.G1T, rows, R, n.grads + ob1);
     p = params_for(n.G1T, n.XT, kHidden, kIn, K, n.failure);
     p.lda = R; p.ldb = R; p.k_chunk = chunk; p.C = n.grads + oW1;
     gemm<umma::kAccumulate>(p, splits, n.stream);
