@@ -21,6 +21,14 @@ What each fixture pins, and where it comes from:
   driver_statistics.npz  The reference's own simulate() (python/monki/simulation.py)
                          driven by a fixed synthetic backend: radiance, standard error,
                          DOP, convergence history, layer AMF and its standard error.
+  comparator_verdicts.json
+                         The reference's own check_result / compare / select_views
+                         (python/monki/validation.py) on the seeded products and cases of
+                         comparator_cases.py: each verdict, its counts and largest errors,
+                         and its reasons.
+
+``python tests/golden/make_golden.py [name ...]`` writes only the named fixtures (the stem
+of each file name); with no names, all of them.
 """
 
 from __future__ import annotations
@@ -377,18 +385,67 @@ def benchmark_scenes():
     return out
 
 
-def main():
+def comparator_verdicts(ref):
+    """The reference comparator's verdicts on the cases of comparator_cases.py."""
+
+    import monki.output
+    import monki.validation
+
+    sys.path.insert(0, str(HERE))
+    import comparator_cases as cases
+
+    def result(p):
+        return monki.output.SimulationResult(Path("synthetic.nc"), *p)
+
+    def verdict(c):
+        out = c.to_dict()
+        out["details"] = sorted(out["details"])
+        return out
+
+    compare = [
+        {"label": label, **verdict(monki.validation.compare(result(a), result(b), **kwargs))}
+        for label, a, b, kwargs in cases.compare_cases()
+    ]
+    check = [
+        {"label": label, "failures": sorted(monki.validation.check_result(result(p), require_uncertainty=req))}
+        for label, p, req in cases.check_cases()
+    ]
+    views = []
+    for label, p, angles in cases.view_cases():
+        try:
+            chosen = monki.validation.select_views(result(p), angles)
+            views.append({"label": label, "theta": chosen.values["theta"].tolist(),
+                          "radiance_sum": [float(chosen.values["radiance"][i].sum()) for i in range(len(angles))]})
+        except ValueError as error:
+            views.append({"label": label, "error": str(error)})
+    return {"compare": compare, "check": check, "views": views}
+
+
+def main(names=()):
     ref, Dataset = reference_package()
-    np.savez_compressed(HERE / "prepared_2boxclouds.npz", **prepared_fixture())
-    for name, arrays in benchmark_scenes().items():
+    wanted = set(names)
+
+    def want(name):
+        return not wanted or name in wanted
+
+    if want("prepared_2boxclouds"):
+        np.savez_compressed(HERE / "prepared_2boxclouds.npz", **prepared_fixture())
+    for name, arrays in benchmark_scenes().items() if want("prepared_benchmark") else ():
         np.savez_compressed(HERE / f"prepared_{name.replace('-', '_')}.npz", **arrays)
-    (HERE / "philox_kat.json").write_text(json.dumps(philox_kat(), indent=1) + "\n")
-    (HERE / "polarization_probe.json").write_text(json.dumps(polarization_probe(), indent=1) + "\n")
-    np.savez_compressed(HERE / "amf_moments.npz", **amf_moments(ref))
-    (HERE / "uniform_top.json").write_text(json.dumps(uniform_top(ref)) + "\n")
-    np.savez_compressed(HERE / "driver_statistics.npz", **driver_statistics(ref, Dataset))
+    if want("philox_kat"):
+        (HERE / "philox_kat.json").write_text(json.dumps(philox_kat(), indent=1) + "\n")
+    if want("polarization_probe"):
+        (HERE / "polarization_probe.json").write_text(json.dumps(polarization_probe(), indent=1) + "\n")
+    if want("amf_moments"):
+        np.savez_compressed(HERE / "amf_moments.npz", **amf_moments(ref))
+    if want("uniform_top"):
+        (HERE / "uniform_top.json").write_text(json.dumps(uniform_top(ref)) + "\n")
+    if want("driver_statistics"):
+        np.savez_compressed(HERE / "driver_statistics.npz", **driver_statistics(ref, Dataset))
+    if want("comparator_verdicts"):
+        (HERE / "comparator_verdicts.json").write_text(json.dumps(comparator_verdicts(ref), indent=1) + "\n")
     print("golden fixtures written to", HERE)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])
