@@ -154,7 +154,6 @@ def simulate(case, backend: Backend, output, *, convergence: AMFConvergence | No
 
         completed = len(history)
         _, nx, ny, angles = total.shape
-        completed = len(history)
         radiance = total / completed / case.photons_per_column
         uncertainty = np.full_like(radiance, 999.0)
 
