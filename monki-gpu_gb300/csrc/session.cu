@@ -4,8 +4,10 @@
 // create :30-84, run :88-133, gpu_seconds :135, device_name :140, close :145) with the
 // CUDA names declared in include/monki_cuda.h. A session owns: the packed scene, the FP32
 // (or FP64) tally banks of one round group, the FP64 per-round output, a failure word and
-// the work counters, all allocated once at create time. A run launches the transport
-// kernel and the FP64 flush on the session stream, copies the finished rounds to the
+// the work counters, all allocated once at create time (with the wavefront engine also the
+// photon pool and its work lists). A run launches the transport kernels (wavefront
+// iterations, captured as CUDA graphs, then the tail kernel; or the one-thread-per-history
+// megakernel) and the FP64 flush on the session stream, copies the finished rounds to the
 // caller's buffer and reports any failure flag as an error; it never falls back to the CPU.
 #include <cuda_runtime.h>
 #include <algorithm>

@@ -13,7 +13,16 @@
 //            the top along each view (calc_radiances_and_paths_pol,
 //            mc_routines_cartesian_mod.f90:849-1222) and the tallies, as 128-bit atomics.
 //   scatter  Lambertian reflection (GROUND_LAMB2) or polarized rejection sampling of the
-//            new direction with the Stokes update (mc.f90:1266-1431).
+//            new direction with the Stokes update (mc.f90:1266-1431), then roulette and
+//            splitting of guided transport.
+//   step     (scenes without layer paths; the default there) scatter and transit fused:
+//            from double-buffered work lists (the three event queues, the walks paused by
+//            the step budget, the vacant slots), each queued event is scattered and its
+//            photon walks on to its next event in the same thread, filing the slot in the
+//            other buffer's lists. One iteration is then step + peel.
+//   tail     the end of a round group: once every photon is claimed and few remain, one
+//            resident wave runs each remaining photon to its end with the same per-slot
+//            walk, peel-off and scattering functions.
 //
 // Photon state is stored as 16-byte records per slot (position, direction, polarization,
 // bookkeeping), one load or store per record.
