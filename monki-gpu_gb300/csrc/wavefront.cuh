@@ -1202,8 +1202,9 @@ __device__ __forceinline__ bool scatter_event(uint32_t slot, bool surface, const
 // ----------------------------------------------------------------------------------
 // step: one wavefront iteration's scattering and walks, reading the work lists of buffer
 // `cur` and filing every slot in those of buffer 1 - cur. Each queued event is scattered
-// and its photon walks on to its next event in the same thread (no reload of its state,
-// no launch in between); paused photons resume their walks; vacant slots take a waiting
+// and its photon walks on to its next event in the same thread, with no launch in between
+// (the scattering stores the photon's records and the walk reads them back, as the two
+// separate kernels do); paused photons resume their walks; vacant slots take a waiting
 // split copy or the next photon of the round group and walk it. One thread per list
 // entry: the lists hold at most one entry per slot.
 // ----------------------------------------------------------------------------------
