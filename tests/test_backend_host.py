@@ -242,3 +242,24 @@ def test_controls_words_carry_the_session_settings(fake):
         assert backend.provenance["gpu_seconds"] == 0.25
         config = fake["fake"].calls[0][2].decode()
         assert "precision=fp32" in config and "engine=wavefront" in config
+
+
+def test_missing_library_raises_and_nothing_falls_back(tmp_path):
+    """The product has no CPU path: without the CUDA library prepare raises, and no module of
+    the package imports the oracle (test infrastructure only)."""
+
+    import re
+    from pathlib import Path
+
+    from monki.execution import CUDA
+
+    backend = CUDA(library=str(tmp_path / "libmonki_cuda.so"))
+    with pytest.raises(FileNotFoundError):
+        backend.prepare(_scene())
+    assert backend.metadata is None
+
+    package = Path(__file__).resolve().parents[1] / "monki-gpu_gb300"
+    pattern = re.compile(r"^\s*(from|import)\s+oracle\b|monki_oracle", re.MULTILINE)
+    offenders = [str(p) for p in package.rglob("*") if p.suffix in (".py", ".cu", ".cuh", ".h", ".cpp")
+                 and pattern.search(p.read_text(errors="ignore"))]
+    assert offenders == []
