@@ -421,17 +421,29 @@ def comparator_verdicts(ref):
     return {"compare": compare, "check": check, "views": views}
 
 
+def _forget_package():
+    """Drop this repository's ``monki`` (and its path) so the reference's package, which has
+    the same name, can be imported next."""
+
+    for name in [m for m in sys.modules if m == "monki" or m.startswith("monki.")]:
+        del sys.modules[name]
+    ours = str(REPO / "monki-gpu_gb300")
+    sys.path[:] = [p for p in sys.path if p != ours]
+
+
 def main(names=()):
-    ref, Dataset = reference_package()
     wanted = set(names)
 
     def want(name):
         return not wanted or name in wanted
 
+    # Fixtures prepared by this repository's package first, then the reference's package.
     if want("prepared_2boxclouds"):
         np.savez_compressed(HERE / "prepared_2boxclouds.npz", **prepared_fixture())
     for name, arrays in benchmark_scenes().items() if want("prepared_benchmark") else ():
         np.savez_compressed(HERE / f"prepared_{name.replace('-', '_')}.npz", **arrays)
+    _forget_package()
+    ref, Dataset = reference_package()
     if want("philox_kat"):
         (HERE / "philox_kat.json").write_text(json.dumps(philox_kat(), indent=1) + "\n")
     if want("polarization_probe"):
