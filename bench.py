@@ -323,6 +323,32 @@ def time_to_target(workload, ppc, device, seed, guided, scale=None):
     }
 
 
+def learned_leg(workload, ppc, device, rank):
+    """The learned roulette map: train the importance network on the device from analog
+    importance tallies of the training family, apply it, and time the guided run."""
+
+    from monki.importance import learned_scale, train_model, training_scenes
+
+    start = time.perf_counter()
+    model, losses, rows = train_model(training_scenes(24), device=device)
+    trained = time.perf_counter() - start
+    fit_seconds = model.fit_seconds
+    with model:
+        scale = learned_scale(model, build_scene(workload, ppc, 1))
+    learned = time_to_target(workload, ppc, device, 23274 + rank, GUIDED, scale)
+    # Dense-contraction roofline of the network's training: FLOPs of the tcgen05 GEMMs per
+    # step (forward 3 layers, backward weight and input gradients).
+    flops = len(losses) * model.rows * 2 * (3 * (64 * 256 + 2 * 256 * 256) - 64 * 256)
+    peaks_path = ROOT / "MEASURED_PEAKS.json"
+    tensor_peak = json.loads(peaks_path.read_text()).get("bf16_tflops") if peaks_path.is_file() else 1900.0
+    learned["training"] = {"seconds_with_pilots": trained, "fit_seconds": fit_seconds, "rows": rows,
+                           "steps": len(losses), "batch": model.rows,
+                           "loss_first": float(losses[:20].mean()), "loss_last": float(losses[-50:].mean()),
+                           "gemm_tflops": flops / fit_seconds / 1e12,
+                           "frac_of_bf16_peak": flops / fit_seconds / 1e12 / tensor_peak}
+    return learned
+
+
 # The reference's published time to AMF SE < 1 % (validation/README.md:230-233; Apple M4,
 # end to end, median of three seeds, 8,000 photons per column, AMFConvergence defaults).
 PUBLISHED_AMF = {
@@ -547,38 +573,24 @@ def main():
         }
     dominant = max(names, key=lambda name: stage_share[name])
 
+    # Everything after the timed region is reported, never fatal: a leg that raises is
+    # recorded as {"error": ...} in the line, so no extra can erase the measurement.
+    def attempt(leg):
+        try:
+            return leg()
+        except Exception as exc:  # noqa: BLE001 - reported in the JSON line
+            return {"error": f"{type(exc).__name__}: {exc}"[:800]}
+
     # Time to the precision target through the public API, analog then guided, on every
     # rank (independent seeds); the analog run is also the end-to-end throughput.
     target = None
     if not args.no_target:
         barrier()
-        plain = time_to_target(args.workload, ppc, local, 23274 + rank, None)
-        guided = time_to_target(args.workload, ppc, local, 23274 + rank, GUIDED)
-        target = {"analog": plain, "guided": guided}
+        target = {"analog": attempt(lambda: time_to_target(args.workload, ppc, local, 23274 + rank, None)),
+                  "guided": attempt(lambda: time_to_target(args.workload, ppc, local, 23274 + rank, GUIDED))}
 
         if not args.no_learned:
-            # The learned roulette map: train the importance network on the device from
-            # analog importance tallies of the training family, then apply it.
-            from monki.importance import learned_scale, train_model, training_scenes
-
-            start = time.perf_counter()
-            model, losses, rows = train_model(training_scenes(24), device=local)
-            trained = time.perf_counter() - start
-            fit_seconds = model.fit_seconds
-            with model:
-                scale = learned_scale(model, build_scene(args.workload, ppc, 1))
-            learned = time_to_target(args.workload, ppc, local, 23274 + rank, GUIDED, scale)
-            # Dense-contraction roofline of the network's training: FLOPs of the tcgen05
-            # GEMMs per step (forward 3 layers, backward weight and input gradients).
-            flops = len(losses) * model.rows * 2 * (3 * (64 * 256 + 2 * 256 * 256) - 64 * 256)
-            tensor_peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("bf16_tflops") \
-                if (ROOT / "MEASURED_PEAKS.json").is_file() else 1900.0
-            learned["training"] = {"seconds_with_pilots": trained, "fit_seconds": fit_seconds, "rows": rows,
-                                   "steps": len(losses), "batch": model.rows,
-                                   "loss_first": float(losses[:20].mean()), "loss_last": float(losses[-50:].mean()),
-                                   "gemm_tflops": flops / fit_seconds / 1e12,
-                                   "frac_of_bf16_peak": flops / fit_seconds / 1e12 / tensor_peak}
-            target["guided_learned"] = learned
+            target["guided_learned"] = attempt(lambda: learned_leg(args.workload, ppc, local, rank))
 
     if rank != 0:
         if world > 1:
@@ -629,44 +641,46 @@ def main():
 
     if target is not None:
         plain, guided = target["analog"], target["guided"]
-        line["time_to_target"] = {
-            "target": f"SE/|I| < {TARGET:g} in every pixel and view, first checked at round 32",
-            "analog_s": plain["seconds"],
-            "guided_s": guided["seconds"],
-            "guided_speedup": plain["seconds"] / guided["seconds"],
-            "guided_method": {"epsilon": GUIDED[0], "roulette": GUIDED[1], "cap": GUIDED[2]},
-            "analog": plain,
-            "guided": guided,
-        }
+        summary = {"target": f"SE/|I| < {TARGET:g} in every pixel and view, first checked at round 32",
+                   "guided_method": {"epsilon": GUIDED[0], "roulette": GUIDED[1], "cap": GUIDED[2]},
+                   "analog": plain, "guided": guided}
+        if "seconds" in plain and "seconds" in guided:
+            summary.update(analog_s=plain["seconds"], guided_s=guided["seconds"],
+                           guided_speedup=plain["seconds"] / guided["seconds"])
         if "guided_learned" in target:
-            line["time_to_target"]["guided_learned_s"] = target["guided_learned"]["seconds"]
-            line["time_to_target"]["guided_learned"] = target["guided_learned"]
-        line["e2e"] = {
-            "value": plain["scatters_per_s"] * world,
-            "unit": UNIT,
-            "h2d_bytes_per_step": plain["h2d_bytes"] / plain["rounds"],
-            "d2h_bytes_per_step": plain["d2h_bytes"] / plain["rounds"],
-            "wall_s": plain["seconds"],
-            "note": "the analog time-to-target run: simulate() with CUDA(), table upload, FP64 round "
-            "statistics on the device, per-round pixel sums and the statistics at each check copied "
-            "to the host, NetCDF output",
-        }
+            summary["guided_learned"] = target["guided_learned"]
+            if "seconds" in target["guided_learned"]:
+                summary["guided_learned_s"] = target["guided_learned"]["seconds"]
+        line["time_to_target"] = summary
+        if "scatters_per_s" in plain:
+            line["e2e"] = {
+                "value": plain["scatters_per_s"] * world,
+                "unit": UNIT,
+                "h2d_bytes_per_step": plain["h2d_bytes"] / plain["rounds"],
+                "d2h_bytes_per_step": plain["d2h_bytes"] / plain["rounds"],
+                "wall_s": plain["seconds"],
+                "note": "the analog time-to-target run: simulate() with CUDA(), table upload, FP64 round "
+                "statistics on the device, per-round pixel sums and the statistics at each check copied "
+                "to the host, NetCDF output",
+            }
+        else:
+            line["e2e"] = {"error": plain.get("error", "analog time-to-target run failed")}
+
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = attempt(lambda: cpu_baseline(build_scene(args.workload, ppc, 1)))
 
     if not args.no_batched:
-        line["batched"] = batched_scenes(local, args.batched_scale)
+        line["batched"] = attempt(lambda: batched_scenes(local, args.batched_scale))
 
     if not args.no_reference_benchmark:
-        line["reference_benchmark"] = reference_benchmark(local)
+        line["reference_benchmark"] = attempt(lambda: reference_benchmark(local))
 
     if not args.no_target:
         # FP32 bias of the product transport against the FP64 build, per Stokes component.
         from monki.precision import fp32_bias
 
-        line["fp32_bias"] = fp32_bias(build_scene(args.workload, 2000, 8), rounds=8, photons_per_column=2000,
-                                      device=local)
-
-    if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(build_scene(args.workload, ppc, 1))
+        line["fp32_bias"] = attempt(lambda: fp32_bias(build_scene(args.workload, 2000, 8), rounds=8,
+                                                      photons_per_column=2000, device=local))
 
     print(json.dumps(line))
 

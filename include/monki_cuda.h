@@ -145,7 +145,9 @@ int monki_cuda_inspect_rectangles(const double *tables, size_t table_count, int 
  * caller's host arrays, as for create + run. Scenes whose scratch exceeds 16 MiB are
  * rejected with an error. All calls share the array: calls that overlap on the GPU race,
  * and each call clears what must start at zero. The first call on a device looks up the
- * array's device address; make it before any stream capture. */
+ * array's device address and keeps it for the process's lifetime; make it before any
+ * stream capture, and do not reset the device between calls. A call that returns nonzero
+ * leaves `out` untouched. */
 int monki_cuda_run_static(uint32_t device, const double *tables, size_t table_count,
                           const uint32_t controls[8], double *out, char *err, size_t errlen);
 

@@ -17,6 +17,8 @@
 #include <stdexcept>
 #include <string>
 #include <mutex>
+#include <tuple>
+#include <utility>
 #include <vector>
 
 #include "tail.h"
@@ -497,10 +499,13 @@ void upload(Session& s) {
     Packed<T> k = pack<T>(s.prep, s.cfg.uniform_prefix, s.cfg.rectangles);
     size_t bytes = k.values.size() * sizeof(T) + k.guides.size() * sizeof(int);
     check(cudaMalloc(&s.scene, std::max<size_t>(bytes, 16)), "cudaMalloc(scene)");
-    check(cudaMemcpy(s.scene, k.values.data(), k.values.size() * sizeof(T), cudaMemcpyHostToDevice), "upload(scene)");
+    // Stream-ordered copies, complete before the host image goes out of scope.
+    check(cudaMemcpyAsync(s.scene, k.values.data(), k.values.size() * sizeof(T), cudaMemcpyHostToDevice, s.stream),
+          "upload(scene)");
     if (!k.guides.empty())
-        check(cudaMemcpy(static_cast<char*>(s.scene) + k.values.size() * sizeof(T), k.guides.data(),
-                         k.guides.size() * sizeof(int), cudaMemcpyHostToDevice), "upload(guides)");
+        check(cudaMemcpyAsync(static_cast<char*>(s.scene) + k.values.size() * sizeof(T), k.guides.data(),
+                              k.guides.size() * sizeof(int), cudaMemcpyHostToDevice, s.stream), "upload(guides)");
+    check(cudaStreamSynchronize(s.stream), "upload");
     SceneView<T> v = make_view<T>(s.prep, k, s.scene);
     if constexpr (sizeof(T) == 4) s.view32 = v; else s.view64 = v;
 }
@@ -580,17 +585,90 @@ void launch_transport(Session& s, const Controls& c, int grid) {
     else transport_kernel<T, T, 3, true><<<grid, s.cfg.block, 0, s.stream>>>(v, c, banks, s.layout, s.failure, s.counters);
 }
 
+// Stream work of a wavefront batch, either launched on the session stream at once or, with
+// a graph, appended as a chain of graph nodes (kernel, memset and copy nodes built through
+// the graph API). Building the graph node by node rather than by stream capture keeps it
+// independent of what other host threads do meanwhile: a capture is invalidated by any
+// device-wide synchronization (cudaFree, cudaDeviceSynchronize, a synchronous copy) that
+// another session's thread makes while it is open.
+struct Recorder {
+    cudaStream_t stream = nullptr;
+    cudaGraph_t graph = nullptr;     // null: launch on the stream
+    cudaGraphNode_t last = nullptr;  // the chain's last node
+
+    template <typename... P, typename... A>
+    void kernel(void (*fn)(P...), unsigned grid, unsigned block, size_t smem, const A&... args) {
+        static_assert(sizeof...(P) == sizeof...(A), "one argument per kernel parameter");
+        std::tuple<P...> values(static_cast<P>(args)...);
+        launch(reinterpret_cast<const void*>(fn), grid, block, smem, values, std::index_sequence_for<P...>{});
+    }
+
+    // count 32-bit words at dst set to zero.
+    void clear(uint32_t* dst, size_t count) {
+        if (!graph) {
+            check(cudaMemsetAsync(dst, 0, count * sizeof(uint32_t), stream), "memset(lists)");
+            return;
+        }
+        cudaMemsetParams m{};
+        m.dst = dst;
+        m.value = 0u;
+        m.elementSize = sizeof(uint32_t);
+        m.width = count;
+        m.height = 1;
+        cudaGraphNode_t node = nullptr;
+        check(cudaGraphAddMemsetNode(&node, graph, last ? &last : nullptr, last ? 1 : 0, &m), "graph memset node");
+        last = node;
+    }
+
+    void copy_to_host(void* dst, const void* src, size_t bytes) {
+        if (!graph) {
+            check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream), "copy(counts)");
+            return;
+        }
+        cudaGraphNode_t node = nullptr;
+        check(cudaGraphAddMemcpyNode1D(&node, graph, last ? &last : nullptr, last ? 1 : 0, dst, src, bytes,
+                                       cudaMemcpyDeviceToHost), "graph copy node");
+        last = node;
+    }
+
+    // Per-stage timing events: stream launches only.
+    void event(cudaEvent_t e) {
+        if (e && !graph) check(cudaEventRecord(e, stream), "event");
+    }
+
+  private:
+    template <typename Tuple, size_t... I>
+    void launch(const void* fn, unsigned grid, unsigned block, size_t smem, Tuple& values, std::index_sequence<I...>) {
+        void* params[] = {static_cast<void*>(&std::get<I>(values))...};
+        if (!graph) {
+            check(cudaLaunchKernel(fn, dim3(grid), dim3(block), params, smem, stream), "wavefront launch");
+            return;
+        }
+        cudaKernelNodeParams p{};
+        p.func = const_cast<void*>(fn);
+        p.gridDim = dim3(grid);
+        p.blockDim = dim3(block);
+        p.sharedMemBytes = unsigned(smem);
+        p.kernelParams = params;
+        p.extra = nullptr;
+        cudaGraphNode_t node = nullptr;
+        check(cudaGraphAddKernelNode(&node, graph, last ? &last : nullptr, last ? 1 : 0, &p), "graph kernel node");
+        last = node;
+    }
+};
+
 template <typename T, int NMAT, bool PATHS>
-void wave_iteration(Session& s, const SceneView<T>& v, Pool<T>& P, const Controls& c, const Divisors& dv, int grid,
-                    uint32_t cur, cudaEvent_t* ev) {
+void wave_iteration(Session& s, Recorder& rec, const SceneView<T>& v, Pool<T>& P, const Controls& c,
+                    const Divisors& dv, int grid, uint32_t cur, cudaEvent_t* ev) {
     T* banks = static_cast<T*>(s.banks);
     const uint32_t out = cur ^ 1u;
-    check(cudaMemsetAsync(P.counts + kListCounts * out, 0, kListCounts * sizeof(uint32_t), s.stream), "memset(lists)");
-    if (ev) cudaEventRecord(ev[0], s.stream);
+    rec.clear(P.counts + kListCounts * out, kListCounts);
+    if (ev) rec.event(ev[0]);
     // One thread per work-list entry (at most one per slot): a thread that looped over
     // several entries drifted away from its warp's other lanes (each walk has its own
     // length). The peel keeps the persistent grid, which measured faster.
-    const int slots_grid = int((P.capacity + uint32_t(s.cfg.block) - 1) / uint32_t(s.cfg.block));
+    const unsigned slots_grid = (P.capacity + uint32_t(s.cfg.block) - 1) / uint32_t(s.cfg.block);
+    const unsigned block = unsigned(s.cfg.block);
     Guide<T> g{T(s.cfg.epsilon), T(s.cfg.roulette), s.cfg.cap > 0.0 ? T(s.cfg.cap) : T(INFINITY),
                static_cast<const T*>(s.scale), T(s.cfg.split)};
     // Fused: each event's scattering and its photon's next walk in one kernel (the events of
@@ -599,28 +677,28 @@ void wave_iteration(Session& s, const SceneView<T>& v, Pool<T>& P, const Control
     const bool fused = s.cfg.fused == 1 || (s.cfg.fused < 0 && !PATHS);
     if (fused) {
         if (v.backward)
-            wf_step<T, NMAT, PATHS, true><<<slots_grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, g, s.cfg.walk,
-                                                                                               cur, s.failure, s.counters);
+            rec.kernel(&wf_step<T, NMAT, PATHS, true>, slots_grid, block, v.band_bytes, v, c, dv, P, g, s.cfg.walk, cur,
+                       s.failure, s.counters);
         else
-            wf_step<T, NMAT, PATHS, false><<<slots_grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, g, s.cfg.walk,
-                                                                                                cur, s.failure, s.counters);
+            rec.kernel(&wf_step<T, NMAT, PATHS, false>, slots_grid, block, v.band_bytes, v, c, dv, P, g, s.cfg.walk, cur,
+                       s.failure, s.counters);
     } else {
-        wf_transit<T, PATHS><<<slots_grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, s.cfg.walk, out, s.failure,
-                                                                                  s.counters);
+        rec.kernel(&wf_transit<T, PATHS>, slots_grid, block, v.band_bytes, v, c, dv, P, s.cfg.walk, out, s.failure,
+                   s.counters);
     }
-    if (ev) cudaEventRecord(ev[1], s.stream);
+    if (ev) rec.event(ev[1]);
     if (v.backward)
-        wf_peel<T, T, NMAT, PATHS, true><<<grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, banks, s.wave, out,
-                                                                                       s.failure, s.counters);
+        rec.kernel(&wf_peel<T, T, NMAT, PATHS, true>, unsigned(grid), block, v.band_bytes, v, c, dv, P, banks, s.wave,
+                   out, s.failure, s.counters);
     else
-        wf_peel<T, T, NMAT, PATHS, false><<<grid, s.cfg.block, v.band_bytes, s.stream>>>(v, c, dv, P, banks, s.wave, out,
-                                                                                        s.failure, s.counters);
-    if (ev) cudaEventRecord(ev[2], s.stream);
+        rec.kernel(&wf_peel<T, T, NMAT, PATHS, false>, unsigned(grid), block, v.band_bytes, v, c, dv, P, banks, s.wave,
+                   out, s.failure, s.counters);
+    if (ev) rec.event(ev[2]);
     if (!fused) {
-        if (v.backward) wf_scatter<T, NMAT, true><<<slots_grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, g, out, s.failure);
-        else wf_scatter<T, NMAT, false><<<slots_grid, s.cfg.block, 0, s.stream>>>(v, c, dv, P, g, out, s.failure);
+        if (v.backward) rec.kernel(&wf_scatter<T, NMAT, true>, slots_grid, block, 0, v, c, dv, P, g, out, s.failure);
+        else rec.kernel(&wf_scatter<T, NMAT, false>, slots_grid, block, 0, v, c, dv, P, g, out, s.failure);
     }
-    if (ev) cudaEventRecord(ev[3], s.stream);
+    if (ev) rec.event(ev[3]);
 }
 
 template <typename T>
@@ -652,49 +730,37 @@ void run_wavefront(Session& s, const Controls& c) {
     if (profile) for (int q = 0; q < 3; ++q) { s.stage_ms[q] = 0; s.stage_launches[q] = 0; }
     // A batch is an even number of iterations, so each starts reading the work lists of
     // buffer 0 and leaves its last lists there.
-    auto batch = [&]() {
+    auto batch = [&](Recorder& rec) {
         for (uint32_t b = 0; b < s.cfg.check_every; ++b) {
             cudaEvent_t* ev = profile ? s.stage_events.data() + 4 * b : nullptr;
             const uint32_t cur = b & 1u;
-            if (nm == 1 && !paths) wave_iteration<T, 1, false>(s, v, P, c, dv, grid, cur, ev);
-            else if (nm == 1) wave_iteration<T, 1, true>(s, v, P, c, dv, grid, cur, ev);
-            else if (nm == 4 && !paths) wave_iteration<T, 4, false>(s, v, P, c, dv, grid, cur, ev);
-            else if (nm == 4) wave_iteration<T, 4, true>(s, v, P, c, dv, grid, cur, ev);
-            else if (!paths) wave_iteration<T, 3, false>(s, v, P, c, dv, grid, cur, ev);
-            else wave_iteration<T, 3, true>(s, v, P, c, dv, grid, cur, ev);
+            if (nm == 1 && !paths) wave_iteration<T, 1, false>(s, rec, v, P, c, dv, grid, cur, ev);
+            else if (nm == 1) wave_iteration<T, 1, true>(s, rec, v, P, c, dv, grid, cur, ev);
+            else if (nm == 4 && !paths) wave_iteration<T, 4, false>(s, rec, v, P, c, dv, grid, cur, ev);
+            else if (nm == 4) wave_iteration<T, 4, true>(s, rec, v, P, c, dv, grid, cur, ev);
+            else if (!paths) wave_iteration<T, 3, false>(s, rec, v, P, c, dv, grid, cur, ev);
+            else wave_iteration<T, 3, true>(s, rec, v, P, c, dv, grid, cur, ev);
         }
-        check(cudaMemcpyAsync(s.host_counts, P.counts, kCountWords * sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                              s.stream), "copy(counts)");
+        rec.copy_to_host(s.host_counts, P.counts, kCountWords * sizeof(uint32_t));
     };
     // Without per-stage timing, the batch of check_every iterations (2 launches and a list
-    // reset each, then the counts read-back) is captured once per run and replayed as one
-    // CUDA graph: the host submits one launch per batch instead of 3 * check_every.
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    if (s.cfg.graphs && !profile) {
-        check(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-        try {
-            batch();
-        } catch (...) {
-            cudaGraph_t partial = nullptr;
-            cudaStreamEndCapture(s.stream, &partial);  // leave capture mode before reporting
-            if (partial) cudaGraphDestroy(partial);
-            throw;
-        }
-        check(cudaStreamEndCapture(s.stream, &graph), "end capture");
-        const cudaError_t inst = cudaGraphInstantiate(&exec, graph, 0);
-        if (inst != cudaSuccess) {
-            cudaGraphDestroy(graph);
-            check(inst, "graph instantiate");
-        }
-    }
+    // reset each, then the counts read-back) is built once per run as a CUDA graph and
+    // replayed: the host submits one launch per batch instead of 3 * check_every.
     struct GraphGuard {
-        cudaGraph_t g; cudaGraphExec_t e;
+        cudaGraph_t g = nullptr; cudaGraphExec_t e = nullptr;
         ~GraphGuard() { if (e) cudaGraphExecDestroy(e); if (g) cudaGraphDestroy(g); }
-    } guard{graph, exec};
+    } guard;
+    Recorder direct{s.stream};
+    if (s.cfg.graphs && !profile) {
+        check(cudaGraphCreate(&guard.g, 0), "graph create");
+        Recorder chain{s.stream, guard.g};
+        batch(chain);
+        check(cudaGraphInstantiate(&guard.e, guard.g, 0), "graph instantiate");
+    }
+    const cudaGraphExec_t exec = guard.e;
     for (;;) {
         if (exec) check(cudaGraphLaunch(exec, s.stream), "graph launch");
-        else batch();
+        else batch(direct);
         it += s.cfg.check_every;
         const bool fused = s.cfg.fused == 1 || (s.cfg.fused < 0 && !paths);
         launches += (fused ? 2 : 3) * uint64_t(s.cfg.check_every);
@@ -944,7 +1010,7 @@ void* monki_cuda_create(uint32_t device, const double* tables, size_t table_coun
         const size_t per_round = cfg.wavefront ? W.count : L.count;
         const size_t bank_bytes = size_t(round_capacity) * L.shards * per_round * elem;
         check(cudaMalloc(&s->banks, bank_bytes), "cudaMalloc(banks)");
-        check(cudaMemset(s->banks, 0, bank_bytes), "cudaMemset(banks)");
+        check(cudaMemsetAsync(s->banks, 0, bank_bytes, s->stream), "cudaMemset(banks)");
         check(cudaMalloc(&s->out, size_t(round_capacity) * L.count * sizeof(double)), "cudaMalloc(out)");
         std::vector<double> mu(size_t(p.angles));
         // mu0/mu on forward Stokes tallies only (mc.f90:1456-1474).
@@ -952,7 +1018,9 @@ void* monki_cuda_create(uint32_t device, const double* tables, size_t table_coun
             mu[size_t(ia)] = p.backward ? 1.0
                                         : std::fabs(std::cos(kDegToRad * p.vartheta0)) / std::fabs(std::cos(kDegToRad * p.vartheta[ia]));
         check(cudaMalloc(&s->mu0mu, mu.size() * sizeof(double)), "cudaMalloc(mu0mu)");
-        check(cudaMemcpy(s->mu0mu, mu.data(), mu.size() * sizeof(double), cudaMemcpyHostToDevice), "upload(mu0mu)");
+        check(cudaMemcpyAsync(s->mu0mu, mu.data(), mu.size() * sizeof(double), cudaMemcpyHostToDevice, s->stream),
+              "upload(mu0mu)");
+        check(cudaStreamSynchronize(s->stream), "upload(mu0mu)");
         check(cudaMalloc(&s->failure, sizeof(uint32_t)), "cudaMalloc(failure)");
         check(cudaMalloc(&s->tail_next, sizeof(uint32_t)), "cudaMalloc(tail)");
         check(cudaMalloc(&s->counters, 4 * sizeof(unsigned long long)), "cudaMalloc(counters)");
@@ -960,7 +1028,7 @@ void* monki_cuda_create(uint32_t device, const double* tables, size_t table_coun
         if (cfg.importance) {
             const size_t cells = size_t(p.nx) * p.ny * p.nz;
             check(cudaMalloc(&s->importance, 2 * cells * sizeof(double)), "cudaMalloc(importance)");
-            check(cudaMemset(s->importance, 0, 2 * cells * sizeof(double)), "cudaMemset(importance)");
+            check(cudaMemsetAsync(s->importance, 0, 2 * cells * sizeof(double), s->stream), "cudaMemset(importance)");
         }
         if (cfg.wavefront) {
             if (cfg.fp64) s->pool64 = allocate_pool<double>(*s); else s->pool32 = allocate_pool<float>(*s);
@@ -975,7 +1043,9 @@ void* monki_cuda_create(uint32_t device, const double* tables, size_t table_coun
                 info[size_t(p.nz) + 1 + p.angles + ia] = mu[size_t(ia)];
             }
             check(cudaMalloc(&s->flush_info, info.size() * sizeof(double)), "cudaMalloc(flush info)");
-            check(cudaMemcpy(s->flush_info, info.data(), info.size() * sizeof(double), cudaMemcpyHostToDevice), "upload(flush info)");
+            check(cudaMemcpyAsync(s->flush_info, info.data(), info.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                  s->stream), "upload(flush info)");
+            check(cudaStreamSynchronize(s->stream), "upload(flush info)");
             check(cudaMallocHost(&s->host_counts, kCountWords * sizeof(uint32_t)), "cudaMallocHost(counts)");
         }
         int per_sm = cfg.blocks_per_sm;
@@ -991,7 +1061,9 @@ void* monki_cuda_create(uint32_t device, const double* tables, size_t table_coun
             }
         }
         s->grid = prop.multiProcessorCount * per_sm;
-        check(cudaDeviceSynchronize(), "create");
+        // This session's stream only: a device-wide synchronization would also wait for
+        // (and stall) the sessions other host threads are running.
+        check(cudaStreamSynchronize(s->stream), "create");
         return s;
     } catch (const std::exception& e) {
         write_error(err, errlen, e.what());
@@ -1125,10 +1197,12 @@ int monki_cuda_set_roulette_scale(void* handle, const double* scale, size_t cell
         const size_t elem = s->cfg.fp64 ? sizeof(double) : sizeof(float);
         if (!s->scale) check(cudaMalloc(&s->scale, n * elem), "cudaMalloc(scale)");
         if (s->cfg.fp64) {
-            check(cudaMemcpy(s->scale, scale, n * elem, cudaMemcpyHostToDevice), "upload(scale)");
+            check(cudaMemcpyAsync(s->scale, scale, n * elem, cudaMemcpyHostToDevice, s->stream), "upload(scale)");
+            check(cudaStreamSynchronize(s->stream), "upload(scale)");
         } else {
             std::vector<float> f(scale, scale + n);
-            check(cudaMemcpy(s->scale, f.data(), n * elem, cudaMemcpyHostToDevice), "upload(scale)");
+            check(cudaMemcpyAsync(s->scale, f.data(), n * elem, cudaMemcpyHostToDevice, s->stream), "upload(scale)");
+            check(cudaStreamSynchronize(s->stream), "upload(scale)");
         }
         return 0;
     } catch (const std::exception& e) {
@@ -1156,10 +1230,14 @@ int monki_cuda_set_importance_weights(void* handle, const double* weights, size_
         const size_t elem = s->cfg.fp64 ? sizeof(double) : sizeof(float);
         if (!s->pixel_weight) check(cudaMalloc(&s->pixel_weight, n * elem), "cudaMalloc(weights)");
         if (s->cfg.fp64) {
-            check(cudaMemcpy(s->pixel_weight, weights, n * elem, cudaMemcpyHostToDevice), "upload(weights)");
+            check(cudaMemcpyAsync(s->pixel_weight, weights, n * elem, cudaMemcpyHostToDevice, s->stream),
+                  "upload(weights)");
+            check(cudaStreamSynchronize(s->stream), "upload(weights)");
         } else {
             std::vector<float> f(weights, weights + n);
-            check(cudaMemcpy(s->pixel_weight, f.data(), n * elem, cudaMemcpyHostToDevice), "upload(weights)");
+            check(cudaMemcpyAsync(s->pixel_weight, f.data(), n * elem, cudaMemcpyHostToDevice, s->stream),
+                  "upload(weights)");
+            check(cudaStreamSynchronize(s->stream), "upload(weights)");
         }
         return 0;
     } catch (const std::exception& e) {
@@ -1177,8 +1255,10 @@ int monki_cuda_importance(void* handle, double* out, size_t count, int reset, ch
         if (!out || count != n) throw std::runtime_error("importance needs 2 * nx * ny * nz values");
         check(cudaSetDevice(s->device), "cudaSetDevice");
         check(cudaStreamSynchronize(s->stream), "sync");
-        check(cudaMemcpy(out, s->importance, n * sizeof(double), cudaMemcpyDeviceToHost), "copy(importance)");
-        if (reset) check(cudaMemset(s->importance, 0, n * sizeof(double)), "memset(importance)");
+        check(cudaMemcpyAsync(out, s->importance, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream),
+              "copy(importance)");
+        if (reset) check(cudaMemsetAsync(s->importance, 0, n * sizeof(double), s->stream), "memset(importance)");
+        check(cudaStreamSynchronize(s->stream), "copy(importance)");
         return 0;
     } catch (const std::exception& e) {
         write_error(err, errlen, e.what());
@@ -1243,8 +1323,9 @@ int monki_cuda_inspect_rectangles(const double* tables, size_t table_count, int 
 // exits. All calls share it and it keeps the last call's contents: each call clears the
 // parts that must start at zero, and two calls that overlap on the GPU (from several host
 // threads or on several streams) race on it. The first call on a device looks up the
-// array's device address for that device, so make that first call before any stream
-// capture.
+// array's device address for that device and keeps it for the life of the process, so
+// make that first call before any stream capture, and do not reset the device
+// (cudaDeviceReset) between calls: the kept address would no longer be valid.
 // ---------------------------------------------------------------------------------------
 namespace monki {
 namespace {
@@ -1354,12 +1435,13 @@ extern "C" int monki_cuda_run_static(uint32_t device, const double* tables, size
         check(cudaGetLastError(), "flush launch");
         uint32_t flag = 0;
         check(cudaMemcpy(&flag, failure, sizeof(flag), cudaMemcpyDeviceToHost), "copy(failure)");
-        check(cudaMemcpy(out, staged, total * sizeof(double), cudaMemcpyDeviceToHost), "copy(tallies)");
+        // A rejected group leaves the caller's buffer untouched.
         if (flag) {
             char msg[128];
             std::snprintf(msg, sizeof msg, "CUDA transport failed (flag %u); round rejected", flag);
             throw std::runtime_error(msg);
         }
+        check(cudaMemcpy(out, staged, total * sizeof(double), cudaMemcpyDeviceToHost), "copy(tallies)");
         return 0;
     } catch (const std::exception& e) {
         monki::write_error(err, errlen, e.what());

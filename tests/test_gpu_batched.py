@@ -55,6 +55,35 @@ def test_batched_scenes_equal_scenes_run_alone(device):
         np.testing.assert_allclose(_flat(batches), _flat(alone), rtol=1e-9, atol=1e-15)
 
 
+def test_sessions_open_and_close_while_others_replay_graphs(device):
+    """Sixteen uneven scenes on four host threads, CUDA graphs on and launch shapes from the
+    autotuner: sessions are created and destroyed (device allocations and frees) while the
+    other threads build and replay their graphs. Every scene still gives exactly what it
+    gives run alone."""
+
+    import monki.scenes as scenes
+    from monki.batched import run_batched, run_scene
+    from monki.tuning import autotune
+
+    batch = [scenes.batched_scene(seed, photons_scale=0.003) for seed in range(16)]
+    shapes = {}
+
+    def tune(scene):
+        _, nx, ny, _, _ = scene.shape
+        key = nx * ny * scene.photons_per_column >= 1 << 16
+        if key not in shapes:
+            shapes[key] = autotune(scene, device=0, photons_per_round=1 << 16).options()
+        return {**shapes[key], "precision": "fp64"}
+
+    for attempt in range(2):
+        results, summary = run_batched(batch, concurrency=4, tune=tune)
+        assert summary["scenes"] == 16 and summary["scatters"] > 0
+        for scene, (batches, provenance) in zip(batch, results, strict=True):
+            alone, alone_provenance = run_scene(scene, options=tune(scene))
+            assert provenance["scatters"] == alone_provenance["scatters"], (attempt, scene.description)
+            np.testing.assert_allclose(_flat(batches), _flat(alone), rtol=1e-9, atol=1e-15)
+
+
 def test_autotuner_returns_the_fastest_candidate(device):
     import monki.scenes as scenes
     from monki.tuning import autotune
