@@ -56,7 +56,7 @@ MOLAR_MASS = {"N2": 28.0134, "O2": 32.00, "Ar": 39.948, "CO2": 44.01}
 class FixtureInput:
     nx: int
     ny: int
-    levels: int  # number of level rows (= layers including the vacuum layer)
+    levels: int  # number of level rows, nz + 1 (= physical layers plus the vacuum layer)
     x_dim: float
     y_dim: float
     k_source: int
@@ -104,7 +104,10 @@ def parse_input(path) -> FixtureInput:
                 return _value(line)
         raise ValueError(f"{path}: unexpected end of the input file")
 
-    nx, ny, levels = int(next_value()), int(next_value()), int(next_value())
+    # rdsize reads nz and adds the vacuum layer (nz + 1, main_routines_cartesian_mod.f90:75-82);
+    # rdinput then reads that many level rows (all nz + 1 of the file) and puts the vacuum
+    # level 1e-6 m above the last (:392-459).
+    nx, ny, levels = int(next_value()), int(next_value()), int(next_value()) + 1
     x_dim, y_dim = float(next_value()), float(next_value())
     k_source, k_detector, k_register = int(next_value()), int(next_value()), int(next_value())
     photons, rounds = int(next_value()), int(next_value())
@@ -148,10 +151,11 @@ def parse_input(path) -> FixtureInput:
         parts = line.split()
         if parts and parts[0].isdigit() and len(parts) >= 5 + 6 * nclouds:
             rows.append(parts)
-    # rdinput reads the first nz rows; the layer above the last one is the vacuum layer.
+    # Every level row is read; the layer above the last level is the vacuum layer.
     if len(rows) < levels:
         raise ValueError(f"{path}: expected {levels} level rows, found {len(rows)}")
-    rows = rows[:levels]
+    if len(rows) > levels:
+        raise ValueError(f"{path}: more level rows than nz + 1 = {levels}")
     alt = np.array([float(r[1]) for r in rows])
     pres = np.array([float(r[2]) for r in rows])
     temp = np.array([float(r[3]) for r in rows])

@@ -21,6 +21,11 @@ What each fixture pins, and where it comes from:
   driver_statistics.npz  The reference's own simulate() (python/monki/simulation.py)
                          driven by a fixed synthetic backend: radiance, standard error,
                          DOP, convergence history, layer AMF and its standard error.
+  archived_*.npz         The reference's archived Fortran outputs of its three test runs
+                         (fortran/monki/upstream/OUTPUT/testrun/*.nc, read by
+                         hdf5_reader.py): radiance, standard error and settings, the
+                         Fortran preparer's optical depths, and the tables that
+                         monki.preparation builds for the same run.
   comparator_verdicts.json
                          The reference's own check_result / compare / select_views
                          (python/monki/validation.py) on the seeded products and cases of
@@ -385,6 +390,51 @@ def benchmark_scenes():
     return out
 
 
+ARCHIVED = {
+    "cloudfree": "MONKI_MLS_cloudfree_340_340_test.in",
+    "1layercloud": "MONKI_MLS_1layercloud_340_340_test.in",
+    "2boxclouds": "MONKI_MLS_2boxclouds_340_340_test.in",
+}
+ARCHIVED_VIEWS = 15  # view zeniths per prepared scene (the device scene holds up to 16)
+ARCHIVED_ARRAYS = ("radiance", "std_radiance", "DOP", "AMF_layer", "theta", "theta0", "phi0", "phi", "asurf",
+                   "n_photons_per_column", "n_rounds", "bmsca", "bmabs", "baer", "alt", "z_unit", "x_unit", "y_unit")
+
+
+def archived_runs():
+    """The reference's archived Fortran outputs (fortran/monki/upstream/OUTPUT/testrun/*.nc,
+    NetCDF-4 read by hdf5_reader.py) with the scene this repository prepares for each: the
+    radiance, its standard error and the run's settings, the Fortran preparer's optical
+    depths, and the prepared table stream of the run's first view_group (later groups
+    differ only in their view zeniths)."""
+
+    sys.path.insert(0, str(REPO / "monki-gpu_gb300"))
+    sys.path.insert(0, str(HERE))
+    from hdf5_reader import HDF5File
+    from monki import ReferenceCase
+    from monki.preparation import prepare_reference_case
+
+    home = REFERENCE / "fortran" / "monki" / "upstream"
+    out = {}
+    for name, input_file in ARCHIVED.items():
+        path = next((home / "OUTPUT" / "testrun").glob(f"MONKI_MLS_{name}_340_340_*.nc"))
+        with HDF5File(path) as f:
+            arrays = {key: f.read(key) for key in ARCHIVED_ARRAYS if key in f.links()}
+        theta = np.asarray(arrays["theta"], dtype=float)
+        groups = [np.arange(g, min(g + ARCHIVED_VIEWS, theta.size)) for g in range(0, theta.size, ARCHIVED_VIEWS)]
+        case = ReferenceCase(name, f"testrun/{input_file}",
+                             photons_per_column=int(arrays["n_photons_per_column"][0]),
+                             rounds=int(arrays["n_rounds"][0]), surface_albedo=float(arrays["asurf"][0]),
+                             solar_zenith=float(arrays["theta0"][0]), solar_azimuth=float(arrays["phi0"][0]),
+                             view_azimuth=float(arrays["phi"][0]), view_zeniths=tuple(theta[groups[0]]))
+        scene = prepare_reference_case(case, home)
+        arrays = {key: np.asarray(value) for key, value in arrays.items()}
+        arrays["tables"] = scene.tables
+        arrays["view_groups"] = np.array([[g[0], g[-1] + 1] for g in groups])
+        arrays["source"] = np.array(f"fortran/monki/upstream/OUTPUT/testrun/{path.name}")
+        out[name] = arrays
+    return out
+
+
 def comparator_verdicts(ref):
     """The reference comparator's verdicts on the cases of comparator_cases.py."""
 
@@ -442,6 +492,8 @@ def main(names=()):
         np.savez_compressed(HERE / "prepared_2boxclouds.npz", **prepared_fixture())
     for name, arrays in benchmark_scenes().items() if want("prepared_benchmark") else ():
         np.savez_compressed(HERE / f"prepared_{name.replace('-', '_')}.npz", **arrays)
+    for name, arrays in archived_runs().items() if want("archived") else ():
+        np.savez_compressed(HERE / f"archived_{name}.npz", **arrays)
     _forget_package()
     ref, Dataset = reference_package()
     if want("philox_kat"):

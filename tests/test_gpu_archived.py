@@ -1,0 +1,78 @@
+"""The FP32 CUDA transport against the reference's archived Fortran runs, at the archived
+runs' own budgets (10,000 / 20,000 / 5,000 photons per column, 100 rounds), on the tables
+monki.preparation builds for them (the Fortran preparer's optical depths exactly).
+
+Per run, every view's I, Q, U (every pixel of the box clouds): the reference's criterion
+|z| < 3 in at least 99 % of entries, and no |z| beyond the Bonferroni bound at family
+error 1e-6; the mean z where the entries are many and weakly correlated (box clouds). The
+layered-cloud run also archived its layer AMFs (without their standard error): those are
+compared with twice our own error (the same budget), layer by layer.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import archived_runs as ar
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(tables, photons_per_column, rounds, seed):
+    from monki.execution import CUDA, BatchControls
+    from monki.scenes import TransportScene
+
+    scene = TransportScene("archived", tables, None, photons_per_column, rounds)
+    with CUDA(seed=seed) as backend:
+        backend.prepare(scene)
+        batches = backend.run_batches([BatchControls(i, photons_per_column) for i in range(1, rounds + 1)])
+    stokes = np.stack([b.stokes for b in batches])
+    paths = None if batches[0].weighted_paths is None else np.stack([b.weighted_paths for b in batches])
+    weights = None if batches[0].weights is None else np.stack([b.weights for b in batches])
+    return stokes, paths, weights
+
+
+def _estimate(fixture, seed):
+    ppc, rounds = int(fixture["n_photons_per_column"][0]), int(fixture["n_rounds"][0])
+    radiance = np.zeros(fixture["radiance"].shape[:-1])
+    error = np.zeros_like(radiance)
+    amf = amf_error = None
+    if "AMF_layer" in fixture:
+        amf = np.zeros(fixture["AMF_layer"].shape[:-1])
+        amf_error = np.zeros_like(amf)
+    dz = fixture["z_unit"]
+    for lo, hi in ar.view_groups(fixture):
+        tables = ar.with_views(fixture["tables"], fixture["theta"][lo:hi])
+        stokes, paths, weights = _run(tables, ppc, rounds, seed)
+        radiance[lo:hi], error[lo:hi] = ar.round_statistics(stokes, ppc)
+        if amf is not None:
+            # Layer AMF (main.f90:1238-1241): summed paths over summed weights per layer
+            # thickness; its error is that of a ratio of sums over independent rounds,
+            # sqrt(n / (n - 1) * sum_r (p_r - A w_r)^2) / W.
+            p = paths[:, :, :, : dz.size]  # (round, x, y, layer, view)
+            w = weights[:, :, :, None, :]
+            ratio = p.sum(0) / w.sum(0)
+            spread = np.sqrt(rounds / (rounds - 1) * ((p - ratio[None] * w) ** 2).sum(0)) / w.sum(0)
+            scale = dz[None, None, :, None]
+            amf[lo:hi] = (ratio / scale).transpose(3, 2, 1, 0)
+            amf_error[lo:hi] = (spread / scale).transpose(3, 2, 1, 0)
+    return radiance, error, amf, amf_error
+
+
+@pytest.mark.parametrize("name", ar.NAMES)
+def test_fp32_transport_agrees_with_the_archived_fortran_run(device, name):
+    fixture = ar.load(name)
+    radiance, error, amf, amf_error = _estimate(fixture, seed=20260)
+    z = ar.z_scores(radiance, error, fixture)
+    assert z.size == fixture["radiance"].size
+    assert np.mean(np.abs(z) < 3) >= 0.99, np.sort(np.abs(z))[-5:]
+    assert np.abs(z).max() < ar.bonferroni_bound(z.size), np.abs(z).max()
+    if name == "2boxclouds":
+        assert abs(z.mean()) < 0.1, z.mean()
+    if amf is not None:
+        archived = fixture["AMF_layer"][..., 0]
+        combined = np.sqrt(2.0) * amf_error
+        mask = combined > 0
+        za = (amf - archived)[mask] / combined[mask]
+        assert np.mean(np.abs(za) < 3) >= 0.99, np.sort(np.abs(za))[-5:]

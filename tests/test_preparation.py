@@ -23,14 +23,15 @@ def test_fixture_input_is_parsed_like_rdinput():
     from monki.preparation import parse_input
 
     fx = parse_input(HOME / "INPUT" / "testrun" / "MONKI_MLS_2boxclouds_340_340_test.in")
-    assert (fx.nx, fx.ny, fx.levels, fx.nmat) == (30, 20, 33, 3)
+    # nz = 33 in the file; rdsize adds the vacuum layer and rdinput reads all 34 level rows.
+    assert (fx.nx, fx.ny, fx.levels, fx.nmat) == (30, 20, 34, 3)
     assert fx.x_dim / fx.nx == 4.0 and fx.y_dim / fx.ny == 4.0
     assert fx.wavelength_nm == 340.0 and fx.cloud_input == "baer"
     # Level 13 (11 km) carries two clouds: optical depth 10 over columns 4-11 x 8-12 and
     # 20 over 14-17 x 9-11 (1-based, inclusive), species 1.
     assert fx.clouds.sum() == pytest.approx(10 * 8 * 5 + 20 * 4 * 3)
     assert fx.clouds[0, 3, 7, 12] == 10 and fx.clouds[0, 13, 8, 12] == 20 and fx.clouds[0, 2, 7, 12] == 0
-    assert fx.altitude_km[-1] == 70.0  # only the first nz rows are read
+    assert fx.altitude_km[-1] == 100.0 and fx.altitude_km.size == 34
 
 
 @needs_fixtures
