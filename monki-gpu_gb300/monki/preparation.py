@@ -323,6 +323,7 @@ def prepare_reference_case(case: ReferenceCase, home) -> TransportScene:
         view_zeniths=list(case.view_zeniths), view_azimuths=[case.view_azimuth] * len(case.view_zeniths),
         albedo=case.surface_albedo, gas_scattering=bmsca, gas_absorption=bmabs, particle_optical_depth=clouds,
         save_path=fixture.save_path, pixel_km=(x_unit, y_unit), wavelength_nm=fixture.wavelength_nm,
+        pressure_pa=fixture.pressure_bar * 1e5, temperature_k=fixture.temperature_k, vmr_ppm=fixture.o3_ppm,
     )
     return TransportScene(case.name, tables, metadata, case.photons_per_column, case.rounds, case.backward,
                           {"fixture": case.input_file, "depolarization": depol,
@@ -337,14 +338,15 @@ def scene_arrays(scene: TransportScene, fixture_description: dict) -> dict:
     return {
         "tables": scene.tables,
         "levels_km": v["alt"] / 1000.0,
-        "bmsca": v["bmsca"][0],
-        "bmabs": v["bmabs"][0],
+        "bmsca": v["bmsca"][:, 0],
+        "bmabs": v["bmabs"][:, 0],
         "baer": v["baer"][..., 0].transpose(3, 2, 1, 0),
         "geometry": np.array([v["theta0"][0], v["phi0"][0], v["asurf"][0], v["x_unit"][0], v["y_unit"][0], v["wav"][0]]),
         "view_zeniths": v["theta"],
-        "view_azimuths": v["phi"],
+        "view_azimuths": np.broadcast_to(v["phi"], v["theta"].shape).copy(),
         "sizes": np.array([scene.photons_per_column, scene.rounds]),
         "name": np.array(scene.name),
+        **({"pres": v["pres"], "temp": v["temp"], "vmrgas": v["vmrgas"]} if "pres" in v else {}),
     }
 
 
@@ -360,6 +362,8 @@ def scene_from_arrays(arrays) -> TransportScene:
         albedo=albedo, gas_scattering=np.asarray(arrays["bmsca"]), gas_absorption=np.asarray(arrays["bmabs"]),
         particle_optical_depth=np.asarray(arrays["baer"]), save_path=bool(tables[10]), pixel_km=(x_unit, y_unit),
         wavelength_nm=wavelength,
+        **({"pressure_pa": arrays["pres"], "temperature_k": arrays["temp"], "vmr_ppm": arrays["vmrgas"]}
+           if "pres" in arrays else {}),
     )
     ppc, rounds = (int(v) for v in arrays["sizes"])
     return TransportScene(str(arrays["name"]), tables, metadata, ppc, rounds, False, {})

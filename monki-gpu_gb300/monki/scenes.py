@@ -268,12 +268,21 @@ def scene_metadata(
     save_path: bool,
     pixel_km=1.0,
     wavelength_nm: float = 340.0,
+    pressure_pa=None,
+    temperature_k=None,
+    vmr_ppm=None,
 ) -> SimulationResult:
-    """Labels and optical fields with the reference product's names (worker.f90:1272-1600)."""
+    """Labels and optical fields with the reference product's names, dimensions and
+    attributes (long_name, units, plot_title; kernels/cpu/worker.f90:1272-1600). A fixture
+    scene also carries its level profiles (pressure in Pa, temperature in K, absorbing-gas
+    volume mixing ratios in ppm at every level). One view azimuth for all views is stored
+    on the "single" dimension like the reference's; scenes that pair each view zenith with
+    its own azimuth store one per view."""
 
     layers = len(levels_km) - 1
     alt = np.append(np.asarray(levels_km) * 1000.0, levels_km[-1] * 1000.0 + 1e-6)
     angles = len(view_zeniths)
+    single_azimuth = np.all(np.asarray(view_azimuths, dtype=float) == float(view_azimuths[0]))
     tau_p = np.asarray(particle_optical_depth, dtype=float)
     species = tau_p.shape[0]
     values = {
@@ -283,13 +292,13 @@ def scene_metadata(
         "theta0": np.array([float(solar_zenith)]),
         "theta": np.asarray(view_zeniths, dtype=float),
         "phi0": np.array([float(solar_azimuth)]),
-        "phi": np.asarray(view_azimuths, dtype=float),
+        "phi": np.asarray(view_azimuths, dtype=float)[:1] if single_azimuth else np.asarray(view_azimuths, dtype=float),
         "x_unit": np.array([pixel_km if np.isscalar(pixel_km) else pixel_km[0]]),
         "y_unit": np.array([pixel_km if np.isscalar(pixel_km) else pixel_km[1]]),
         "z_unit": np.diff(alt) / 1000.0,
         "alt": alt,
-        "bmabs": np.append(gas_absorption, 0.0)[None, :],
-        "bmsca": np.append(gas_scattering, 0.0)[None, :],
+        "bmabs": np.append(gas_absorption, 0.0)[:, None],
+        "bmsca": np.append(gas_scattering, 0.0)[:, None],
         "baer": np.concatenate([tau_p, np.zeros(tau_p.shape[:3] + (1,))], axis=3).transpose(3, 2, 1, 0)[..., None],
         "wav": np.array([wavelength_nm]),
     }
@@ -300,13 +309,13 @@ def scene_metadata(
         "theta0": ("single",),
         "theta": ("nvza",),
         "phi0": ("single",),
-        "phi": ("nvza",),
+        "phi": ("single",) if single_azimuth else ("nvza",),
         "x_unit": ("single",),
         "y_unit": ("single",),
         "z_unit": ("nz",),
         "alt": ("nlev",),
-        "bmabs": ("nwavs", "nz"),
-        "bmsca": ("nwavs", "nz"),
+        "bmabs": ("nz", "nwavs"),
+        "bmsca": ("nz", "nwavs"),
         "baer": ("nz", "ny", "nx", "nscatt_types", "nwavs"),
         "wav": ("nwavs",),
         "radiance": ("nvza", "ny", "nx", "nmat", "nwavs"),
@@ -314,38 +323,54 @@ def scene_metadata(
         "DOP": ("nvza", "ny", "nx", "nwavs"),
         "radiance_convergence": ("nrounds", "nmat", "nwavs"),
     }
-    attributes = {
-        "asurf": {"long_name": "Surface albedo", "units": "-"},
-        "n_photons_per_column": {"long_name": "Number of photons per column", "units": "-"},
-        "n_rounds": {"long_name": "Number of rounds used", "units": "-"},
-        "theta0": {"long_name": "Solar zenith angle", "units": "deg"},
-        "theta": {"long_name": "Viewing zenith angle", "units": "deg"},
-        "phi0": {"long_name": "Solar azimuth angle", "units": "deg"},
-        "phi": {"long_name": "Viewing azimuth angle", "units": "deg"},
-        "x_unit": {"long_name": "Spatial resolution in the x-direction", "units": "km"},
-        "y_unit": {"long_name": "Spatial resolution in the y-direction", "units": "km"},
-        "z_unit": {"long_name": "Spatial resolution in the z-direction (layer dependent)", "units": "km"},
-        "alt": {"long_name": "Altitude", "units": "m"},
-        "bmabs": {"long_name": "Molecular absorption optical thickness", "units": "-"},
-        "bmsca": {"long_name": "Molecular scattering optical thickness", "units": "-"},
-        "baer": {"long_name": "Aerosol total optical thickness (baerabs+baersca)", "units": "-"},
-        "wav": {"long_name": "Wavelength of the light", "units": "nm"},
-        "radiance": {"long_name": "TOA radiance", "units": "-, assuming E0=pi"},
-        "std_radiance": {"long_name": "Standard deviation of TOA radiance", "units": "-"},
-        "DOP": {"long_name": "Degree of polarization", "units": "-"},
-        "radiance_convergence": {"long_name": "radiance_convergence", "units": "-"},
+    # (long_name, units, plot_title) of worker.f90:1512-1596.
+    labels = {
+        "asurf": ("Surface albedo", "-", "asurf"),
+        "n_photons_per_column": ("Number of photons used per column and per round", "-", "n_photons_per_column"),
+        "n_rounds": ("Number of rounds used", "-", "n_rounds"),
+        "theta0": ("Solar zenith angle", "deg", "solar_zenith_angle"),
+        "theta": ("Viewing zenith angle", "deg", "viewing_zenith_angle"),
+        "phi0": ("Solar azimuth angle", "deg", "solar_azimuth_angle"),
+        "phi": ("Viewing azimuth angle", "deg", "viewing_azimuth_angle"),
+        "x_unit": ("Spatial resolution in the x-direction", "km", "x_unit"),
+        "y_unit": ("Spatial resolution in the y-direction", "km", "y_unit"),
+        "z_unit": ("Spatial resolution in the z-direction (layer dependent)", "km", "z_unit"),
+        "alt": ("Altitude", "m", "alt"),
+        "bmabs": ("Molecular absorption optical thickness", "-", "bmabs"),
+        "bmsca": ("Molecular scattering optical thickness", "-", "bmsca"),
+        "baer": ("Aerosol total optical thickness (baerabs+baersca)", "-", "baer"),
+        "wav": ("Wavelength of the light", "nm", "wav"),
+        "radiance": ("TOA radiance", "-, assuming E0=pi", "radiance"),
+        "std_radiance": ("Standard deviation of TOA radiance", "-", "std"),
+        "DOP": ("Degree of polarization", "-", "DOP"),
+        "radiance_convergence": ("radiance_convergence", "-", "radiance convergence history"),
+        "AMF_layer": ("Layer AMF", "-", "AMF_layer"),
+        "pres": ("Pressure", "Pa", "pres"),
+        "temp": ("Temperature", "K", "temp"),
+        "vmrgas": ("Volume mixing ratio of the absorbing gases", "ppm", "vmrgas"),
     }
+    attributes = {name: {"long_name": long, "units": units, "plot_title": title}
+                  for name, (long, units, title) in labels.items() if name in dimensions}
+    if pressure_pa is not None:
+        # Level profiles of a fixture (rdinput): every level row, without the vacuum level.
+        values["pres"] = np.asarray(pressure_pa, dtype=float)[: layers + 1]
+        values["temp"] = np.asarray(temperature_k, dtype=float)[: layers + 1]
+        values["vmrgas"] = np.asarray(vmr_ppm, dtype=float).reshape(layers + 1, -1)
+        dimensions.update({"pres": ("nlev",), "temp": ("nlev",), "vmrgas": ("nlev", "ngases")})
+        for name in ("pres", "temp", "vmrgas"):
+            long, units, title = labels[name]
+            attributes[name] = {"long_name": long, "units": units, "plot_title": title}
 
     if save_path:
         dimensions["AMF_layer"] = ("nvza", "nz", "ny", "nx", "nwavs")
-        attributes["AMF_layer"] = {"long_name": "Layer AMF", "units": "-"}
+        attributes["AMF_layer"] = dict(zip(("long_name", "units", "plot_title"), labels["AMF_layer"], strict=True))
         values["AMF_layer"] = np.zeros((angles, layers, ny, nx, 1))
 
     # z_unit and the AMF layer axis exclude the vacuum layer in the public product.
     values["z_unit"] = values["z_unit"][:layers]
     values["alt"] = alt[: layers + 1]
-    values["bmabs"] = values["bmabs"][:, :layers]
-    values["bmsca"] = values["bmsca"][:, :layers]
+    values["bmabs"] = values["bmabs"][:layers]
+    values["bmsca"] = values["bmsca"][:layers]
     values["baer"] = values["baer"][:layers]
     _ = (name, nmat, species)
     return SimulationResult(None, values, dimensions, attributes)

@@ -13,6 +13,7 @@ chunked (version 1 B-tree, deflate and shuffle filters) layout. Anything else ra
     with HDF5File(path) as f:
         f.names()                 # the root group's link names
         f.read("std_radiance")    # numpy array in the file's (C) dimension order
+        f.attributes("radiance")  # {"long_name": ..., "units": ..., ...}
 """
 
 from __future__ import annotations
@@ -27,7 +28,7 @@ SIGNATURE = b"\x89HDF\r\n\x1a\n"
 UNDEFINED = 0xFFFFFFFFFFFFFFFF
 
 # Object header message types used here (specification section IV.A.2).
-DATASPACE, LINK_INFO, DATATYPE, LINK, LAYOUT, FILTERS, CONTINUATION = 0x01, 0x02, 0x03, 0x06, 0x08, 0x0B, 0x10
+DATASPACE, LINK_INFO, DATATYPE, LINK, LAYOUT, FILTERS, ATTRIBUTE, CONTINUATION = 0x01, 0x02, 0x03, 0x06, 0x08, 0x0B, 0x0C, 0x10
 
 
 class HDF5File:
@@ -206,6 +207,47 @@ class HDF5File:
             elif kind == FILTERS:
                 info["filters"] = self._filters(body)
         return info
+
+    def attributes(self, name: str) -> dict:
+        """Attributes stored in a dataset's object header (compact storage): fixed-length
+        strings as str, numbers as arrays. Attributes in dense storage are not read."""
+
+        address = self.links().get(name)
+        if address is None:
+            raise KeyError(name)
+        out = {}
+        for kind, body, _ in self.messages(address):
+            if kind != ATTRIBUTE:
+                continue
+            version = self.data[body]
+            name_size, type_size, space_size = self._u(body + 2, 2), self._u(body + 4, 2), self._u(body + 6, 2)
+            if version == 1:
+                pad = lambda n: (n + 7) // 8 * 8  # noqa: E731
+                p = body + 8
+                key = self.data[p : p + name_size].split(b"\0")[0].decode()
+                p += pad(name_size)
+                dtype_at, p = p, p + pad(type_size)
+                space_at, p = p, p + pad(space_size)
+            elif version in (2, 3):
+                p = body + 8 + (1 if version == 3 else 0)
+                key = self.data[p : p + name_size].split(b"\0")[0].decode()
+                p += name_size
+                dtype_at, p = p, p + type_size
+                space_at, p = p, p + space_size
+            else:
+                raise NotImplementedError(f"attribute message version {version}")
+            cls = self.data[dtype_at] & 0x0F
+            if cls not in (0, 1, 3):
+                continue  # references and variable-length data (netCDF-4 bookkeeping)
+            dtype = self._datatype(dtype_at)
+            shape = self._dataspace(space_at)
+            count = int(np.prod(shape)) if shape else 1
+            raw = self.data[p : p + count * dtype.itemsize]
+            if cls == 3:
+                out[key] = b"".join(np.frombuffer(raw, dtype=dtype)).split(b"\0")[0].decode("utf-8", "replace")
+            else:
+                out[key] = np.frombuffer(raw, dtype=dtype).copy()
+        return out
 
     def read(self, name: str) -> np.ndarray:
         info = self.dataset(name)

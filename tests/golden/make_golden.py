@@ -397,7 +397,29 @@ ARCHIVED = {
 }
 ARCHIVED_VIEWS = 15  # view zeniths per prepared scene (the device scene holds up to 16)
 ARCHIVED_ARRAYS = ("radiance", "std_radiance", "DOP", "AMF_layer", "theta", "theta0", "phi0", "phi", "asurf",
-                   "n_photons_per_column", "n_rounds", "bmsca", "bmabs", "baer", "alt", "z_unit", "x_unit", "y_unit")
+                   "n_photons_per_column", "n_rounds", "bmsca", "bmabs", "baer", "alt", "z_unit", "x_unit", "y_unit",
+                   "pres", "temp", "vmrgas", "wav")
+
+
+def archived_schema(f) -> dict:
+    """Dimensions (name: size) and, per variable, its dimension names and its long_name,
+    units and plot_title, from the netCDF-4 bookkeeping of an archived file: dimensions are
+    the datasets marked as dimension scales (_Netcdf4Dimid), a variable's dimensions its
+    _Netcdf4Coordinates ids."""
+
+    scales, variables = {}, {}
+    for name in f.names():
+        attributes = f.attributes(name)
+        if attributes.get("CLASS") == "DIMENSION_SCALE":
+            scales[int(attributes["_Netcdf4Dimid"][0])] = (name, int(f.dataset(name)["shape"][0]))
+    for name in f.names():
+        attributes = f.attributes(name)
+        if "_Netcdf4Coordinates" in attributes:
+            variables[name] = {
+                "dimensions": [scales[int(i)][0] for i in attributes["_Netcdf4Coordinates"]],
+                "attributes": {key: attributes[key] for key in ("long_name", "units", "plot_title") if key in attributes},
+            }
+    return {"dimensions": {name: size for name, size in scales.values()}, "variables": variables}
 
 
 def archived_runs():
@@ -419,6 +441,7 @@ def archived_runs():
         path = next((home / "OUTPUT" / "testrun").glob(f"MONKI_MLS_{name}_340_340_*.nc"))
         with HDF5File(path) as f:
             arrays = {key: f.read(key) for key in ARCHIVED_ARRAYS if key in f.links()}
+            schema = archived_schema(f)
         theta = np.asarray(arrays["theta"], dtype=float)
         groups = [np.arange(g, min(g + ARCHIVED_VIEWS, theta.size)) for g in range(0, theta.size, ARCHIVED_VIEWS)]
         case = ReferenceCase(name, f"testrun/{input_file}",
@@ -431,6 +454,7 @@ def archived_runs():
         arrays["tables"] = scene.tables
         arrays["view_groups"] = np.array([[g[0], g[-1] + 1] for g in groups])
         arrays["source"] = np.array(f"fortran/monki/upstream/OUTPUT/testrun/{path.name}")
+        arrays["schema"] = np.array(json.dumps(schema, sort_keys=True))
         out[name] = arrays
     return out
 

@@ -156,3 +156,52 @@ def test_oracle_agrees_with_the_archived_fortran_run(oracle, name):
         assert abs(z.mean()) < 0.1, z.mean()
     else:
         assert np.abs(z).max() < ar.bonferroni_bound(z.size), np.abs(z).max()
+
+
+def _fixture_scene(fixture, photons_per_column, rounds):
+    """The archived run's first view group as a TransportScene with the product metadata of
+    a fixture scene (level profiles included)."""
+
+    from monki.scenes import TransportScene, scene_metadata
+
+    lo, hi = ar.view_groups(fixture)[0]
+    tables = ar.with_views(fixture["tables"], fixture["theta"][lo:hi])
+    nx, ny, nmat = int(tables[1]), int(tables[2]), int(tables[4])
+    metadata = scene_metadata(
+        "archived", fixture["alt"] / 1000.0, nx=nx, ny=ny, nmat=nmat, solar_zenith=float(fixture["theta0"][0]),
+        solar_azimuth=float(fixture["phi0"][0]), view_zeniths=list(fixture["theta"][lo:hi]),
+        view_azimuths=[float(fixture["phi"][0])] * (hi - lo), albedo=float(fixture["asurf"][0]),
+        gas_scattering=fixture["bmsca"][:, 0], gas_absorption=fixture["bmabs"][:, 0],
+        particle_optical_depth=fixture["baer"][..., 0].transpose(3, 2, 1, 0), save_path=bool(tables[10]),
+        pixel_km=(float(fixture["x_unit"][0]), float(fixture["y_unit"][0])), wavelength_nm=float(fixture["wav"][0]),
+        pressure_pa=fixture["pres"], temperature_k=fixture["temp"], vmr_ppm=fixture["vmrgas"])
+    return TransportScene("archived", tables, metadata, photons_per_column, rounds)
+
+
+@pytest.mark.parametrize("name", ar.NAMES)
+def test_product_schema_is_the_fortran_outputs(oracle, tmp_path, name):
+    """The NetCDF product written by simulate() for a fixture scene has the variables,
+    dimension names and sizes, and long_name / units / plot_title attributes of the
+    reference's own output (worker.f90 / main.f90 report), read from the archived file. The
+    view and round counts are the run's own."""
+
+    import json
+
+    from monki import simulate
+    from monki.output import SimulationResult
+    from oracle_backend import oracle_backend
+
+    fixture = ar.load(name)
+    schema = json.loads(str(fixture["schema"]))
+    scene = _fixture_scene(fixture, 2, 3)
+    simulate(scene, oracle_backend(oracle, seed=3), tmp_path / "product.nc")
+    product = SimulationResult.load(tmp_path / "product.nc")
+    assert set(product.values) == set(schema["variables"])
+    for variable, spec in schema["variables"].items():
+        assert product.dimensions[variable] == tuple(spec["dimensions"]), variable
+        assert product.attributes[variable] == spec["attributes"], variable
+        for dimension, size in zip(spec["dimensions"], product.values[variable].shape, strict=True):
+            if dimension not in ("nvza", "nrounds"):
+                assert size == schema["dimensions"][dimension], (variable, dimension)
+    for key in ("pres", "temp", "vmrgas", "alt", "bmsca", "bmabs", "baer", "z_unit", "theta0", "phi", "asurf"):
+        np.testing.assert_array_equal(product.values[key], fixture[key], err_msg=key)
