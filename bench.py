@@ -393,14 +393,18 @@ def reference_benchmark(device):
 def batched_scenes(device, scale):
     """The batched workload: 64 seeded scenes of uneven size (grids 8-128 columns a side,
     20-60 layers, log-uniform photon budgets scaled by ``scale``, lognormal cloud fields),
-    one round each, with launch shapes from the autotuner (tuned once per size class),
-    concurrent sessions on one GPU."""
+    one round each. Persistent: every scene in one multi-scene launch sequence (one shared
+    photon pool; graph-replayed batches), after one warm-up run. Beside it, the scenes as
+    concurrent sessions from four host threads with launch shapes from the autotuner
+    (tuned once per size class)."""
 
     import monki.scenes as scenes
-    from monki.batched import run_batched
+    from monki.batched import run_batched, run_persistent
     from monki.tuning import autotune
 
     batch = [scenes.batched_scene(seed, photons_scale=scale) for seed in range(64)]
+    run_persistent(batch[:8], device=device)  # warm-up: module load, graph instantiation
+    _, persistent = run_persistent(batch, device=device)
 
     def size_class(scene):
         _, nx, ny, _, _ = scene.shape
@@ -410,10 +414,10 @@ def batched_scenes(device, scale):
     tuned = {}
     for scene in batch:
         tuned.setdefault(size_class(scene), autotune(scene, device=device))
-    _, summary = run_batched(batch, device=device, concurrency=4, tune=lambda s: tuned[size_class(s)].options())
-    summary["photons_scale"] = scale
-    summary["tuned"] = {str(k): v.options() for k, v in tuned.items()}
-    return summary
+    _, sessions = run_batched(batch, device=device, concurrency=4, tune=lambda s: tuned[size_class(s)].options(),
+                              persistent=False)
+    sessions["tuned"] = {str(k): v.options() for k, v in tuned.items()}
+    return {"photons_scale": scale, "persistent": persistent, "concurrent_sessions": sessions}
 
 
 def main():

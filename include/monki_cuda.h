@@ -151,6 +151,28 @@ int monki_cuda_inspect_rectangles(const double *tables, size_t table_count, int 
 int monki_cuda_run_static(uint32_t device, const double *tables, size_t table_count,
                           const uint32_t controls[8], double *out, char *err, size_t errlen);
 
+/* Many scenes in one launch sequence (no counterpart in the reference, which batches the
+ * rounds of one scene: python/monki/execution/metal.py:219-242). Each scene is a prepared
+ * table stream as for monki_cuda_create (forward, no layer paths, nmat 1 or 3); one photon
+ * pool is shared by every scene, each wavefront launch covers all of them, and each scene
+ * keeps its own random streams and tallies. Config keys as for monki_cuda_create (precision,
+ * pool, walk, check_every, graphs, shards, rectangles, uniform_prefix); the analog method
+ * only. Returns NULL on failure with the message in err. */
+void *monki_cuda_multi_create(uint32_t device, uint32_t scenes, const double *const *tables,
+                              const size_t *table_counts, uint32_t round_capacity, const char *config,
+                              char *err, size_t errlen);
+/* Tally values per round of one scene (nmat * nx * ny * angles). */
+size_t monki_cuda_multi_tally_count(void *handle, uint32_t scene);
+/* One round group per scene: controls holds eight words per scene (as monki_cuda_run's),
+ * out[scene] receives rounds x tally count FP64 values in RawTallies order. A scene with a
+ * photon count of 0 sits this run out. Nonzero on failure, with the message in err. */
+int monki_cuda_multi_run(void *handle, const uint32_t *controls, double *const *out, char *err, size_t errlen);
+/* scatters, free-path cell visits, detector cell visits, tally updates, photons, launches. */
+int monki_cuda_multi_counters(void *handle, uint64_t out[6]);
+/* Milliseconds of the last run: transport, and transport plus the FP64 flush. */
+int monki_cuda_multi_last_timing(void *handle, float out[2]);
+void monki_cuda_multi_close(void *handle);
+
 /* Device probes of the production helpers, the counterpart of the reference's probe
  * kernels (tests/integration/test_metal.py:23-103). */
 int monki_cuda_probe_philox(uint32_t device, const uint32_t *counters, const uint32_t *keys,

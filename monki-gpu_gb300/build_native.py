@@ -19,7 +19,7 @@ from pathlib import Path
 PACKAGE_ROOT = Path(__file__).resolve().parent
 SOURCES = PACKAGE_ROOT / "csrc"
 OUTPUT = PACKAGE_ROOT / "monki" / "_native" / "libmonki_cuda.so"
-UNITS = ("session.cu", "tail.cu", "probes.cu", "mlp.cu")
+UNITS = ("session.cu", "tail.cu", "multi.cu", "probes.cu", "mlp.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 # The transport units: single-precision division and square root to within 2 ulp and FP32
@@ -28,7 +28,7 @@ FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxe
 # transcendental functions keep their full-precision library forms. Measured +10 % on the
 # box and layered clouds (the peel-off and scattering kernels are issue bound).
 TRANSPORT_FLAGS = ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"]
-UNIT_FLAGS = {"session.cu": TRANSPORT_FLAGS, "tail.cu": TRANSPORT_FLAGS}
+UNIT_FLAGS = {"session.cu": TRANSPORT_FLAGS, "tail.cu": TRANSPORT_FLAGS, "multi.cu": TRANSPORT_FLAGS}
 
 
 def nvcc() -> str:

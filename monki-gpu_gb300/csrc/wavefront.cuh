@@ -106,15 +106,29 @@ constexpr uint32_t kListCounts = 8;   // counts per work-list buffer
 constexpr uint32_t kClaimCount = 16;  // index of the claim counter
 constexpr uint32_t kCountWords = 20;  // words of the counts array
 
+// Bytes of one slot's state block: three records of four T and the bookkeeping record.
+template <typename T>
+constexpr size_t kRecordBytes = sizeof(T) == 4 ? 64 : 128;
+
+// Bookkeeping word of a slot's cell and pending event: i | j << 12 | kind << 24, with kind
+// 0 gas, 1 + s particle species s, 255 surface (grids up to 4096 columns a side).
+__host__ __device__ __forceinline__ uint32_t pack_cell(int i, int j, int kind) {
+    return uint32_t(i) | (uint32_t(j) << 12) | (uint32_t(kind) << 24);
+}
+__host__ __device__ __forceinline__ int cell_i(uint32_t w) { return int(w & 0xFFFu); }
+__host__ __device__ __forceinline__ int cell_j(uint32_t w) { return int((w >> 12) & 0xFFFu); }
+__host__ __device__ __forceinline__ int cell_kind(uint32_t w) { return int(w >> 24); }
+constexpr int kMaxColumnsPerAxis = 4096;
+
 template <typename T>
 struct Pool {
     uint32_t capacity;
-    Quad<T>* pos;    // x, y, z, weight
-    Quad<T>* dir;    // a, b, c, phi
-    Quad<T>* pol;    // q, u, remains, init_part
-    uint4* meta;     // pid (kNone when empty), next draw, i | j << 16, packed layers
+    // Per slot one block of kRecordBytes<T>: position {x, y, z, weight}, direction {a, b, c,
+    // phi}, polarization {q, u, remains, init_part}, bookkeeping {pid (kNone when empty),
+    // next draw, pack_cell(i, j, pending event kind), packed layers}. The four records of a
+    // slot are read and written together, so its accesses fill whole 32-byte sectors.
+    unsigned char* records;
     uint32_t* steps; // walk steps so far (history step limit)
-    uint8_t* kind;   // pending event: 0 gas, 1 + s particle s, 255 surface
     T* wander;       // capacity * nz path lengths after the first event
     uint32_t* runs;  // two straight runs of whole layers: lo0 | hi0 << 8 | lo1 << 16 | hi1 << 24
     T* run_ci;       // capacity * 2: 1 / |cos| of each run
@@ -147,6 +161,26 @@ struct Pool {
     uint32_t* lineage;
     SplitCopy<T>* copies;
     uint32_t* waiting;
+
+    __device__ __forceinline__ Quad<T>& pos(uint32_t s) const {
+        return *reinterpret_cast<Quad<T>*>(records + size_t(s) * kRecordBytes<T>);
+    }
+    __device__ __forceinline__ Quad<T>& dir(uint32_t s) const {
+        return *reinterpret_cast<Quad<T>*>(records + size_t(s) * kRecordBytes<T> + sizeof(Quad<T>));
+    }
+    __device__ __forceinline__ Quad<T>& pol(uint32_t s) const {
+        return *reinterpret_cast<Quad<T>*>(records + size_t(s) * kRecordBytes<T> + 2 * sizeof(Quad<T>));
+    }
+    __device__ __forceinline__ uint4& meta(uint32_t s) const {
+        return *reinterpret_cast<uint4*>(records + size_t(s) * kRecordBytes<T> + 3 * sizeof(Quad<T>));
+    }
+};
+
+// A slot's four records, handed from the scattering to the walk in registers.
+template <typename T>
+struct SlotState {
+    uint4 meta;
+    Quad<T> pos, dir, pol;
 };
 
 __device__ __forceinline__ uint32_t pack_layers(int k, int k1, int wmin, int wmax) {
@@ -481,18 +515,25 @@ __device__ __forceinline__ int uniform_jump(const SceneView<T>& s, int& k, T& z,
 // state. Returns the event's queue (surface, gas, particle) or -1 when the slot holds no
 // event (empty, finished, or paused by the step budget). QUEUE files the slot in the work
 // lists of buffer `out` (its event queue, the paused list, or the vacant list while it can
-// still be filled); without it the caller handles the event (the tail kernel).
+// still be filled); without it the caller handles the event (the tail kernel). `given`
+// holds the slot's records when the caller has them in registers (a scattering just
+// made them); they are then not read back from memory.
 template <typename T, bool PATHS, bool QUEUE>
 __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s, const T* band, const Controls& ctl,
                                             const Divisors& dv, const Pool<T>& P, uint32_t walk, bool may_claim,
                                             uint32_t out, uint32_t* __restrict__ failure, uint64_t& scatters,
-                                            uint64_t& visits) {
+                                            uint64_t& visits, const SlotState<T>* given = nullptr) {
     const T eps = Tol<T>::eps;
     const int top = s.nz - 1;
     int event = -1;
     // All records at once, before the empty-slot test: one memory latency instead of two.
-    const uint4 meta = P.meta[slot];
-    const Quad<T> pos_in = P.pos[slot], dir_in = P.dir[slot], pol_in = P.pol[slot];
+    uint4 meta;
+    Quad<T> pos_in, dir_in, pol_in;
+    if (given) {
+        meta = given->meta; pos_in = given->pos; dir_in = given->dir; pol_in = given->pol;
+    } else {
+        meta = P.meta(slot); pos_in = P.pos(slot); dir_in = P.dir(slot); pol_in = P.pol(slot);
+    }
     const uint32_t steps_in = P.steps[slot];
     uint32_t pid = meta.x;
     DrawStream rng;
@@ -507,7 +548,7 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
         const uint32_t ro = dv.per_round.div(pid);
         if (P.lineage) lineage = P.lineage[slot];
         rng.init(pid - ro * ctl.per_round, ctl.first_round + ro, ctl.seed, meta.y, lineage);
-        i = int(meta.z & 0xFFFF); j = int(meta.z >> 16);
+        i = cell_i(meta.z); j = cell_j(meta.z);
         unpack_layers(meta.w, k, k1, wmin, wmax);
         pos = pos_in;
         dir = dir_in;
@@ -525,6 +566,7 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
     T& remains = pol.z; T& init_part = pol.w;
 
     T vee = T(0);
+    int pending = 0;  // the event's kind, kept in the bookkeeping record
     for (;;) {
         if (pid == kNone && P.waiting && P.waiting[slot] > 0u) {
             // A copy left by splitting continues in this slot, with its own stream and a
@@ -533,7 +575,7 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
             const SplitCopy<T> cp = P.copies[size_t(slot) * kSplitStack + n];
             P.waiting[slot] = n;
             pid = cp.meta.x;
-            i = int(cp.meta.z & 0xFFFF); j = int(cp.meta.z >> 16);
+            i = cell_i(cp.meta.z); j = cell_j(cp.meta.z);
             unpack_layers(cp.meta.w, k, k1, wmin, wmax);
             path.wmin = wmin; path.wmax = wmax;
             pos = cp.pos; dir = cp.dir; pol = cp.pol;
@@ -662,20 +704,25 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
         ++order;
         const int queue = kind == 255 ? kQueueSurface : (kind == 0 ? kQueueGas : kQueueParticle);
         if (QUEUE) P.queue[out][queue][warp_reserve(P.counts + kListCounts * out, queue)] = slot;
-        P.kind[slot] = uint8_t(kind);
+        pending = kind;
         event = queue;
         break;
     }
 
     if (pid == kNone) {
-        if (meta.x != kNone || fresh) P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u);
+        if (meta.x != kNone || fresh) P.meta(slot) = make_uint4(kNone, 0u, 0u, 0u);
         // An empty slot waits for the next launch: copies still waiting keep it live; while
         // photons remain to claim it is refilled there.
         if (QUEUE && ((P.waiting && P.waiting[slot] > 0u) || may_claim))
             P.vacant[out][warp_reserve(P.counts + kListCounts * out, 4)] = slot;
         return -1;
     }
-    P.meta[slot] = make_uint4(pid, rng.draw, uint32_t(i) | (uint32_t(j) << 16), pack_layers(k, k1, path.wmin, path.wmax));
+    // The whole block, direction included (a scattering or a claim changed it; storing it
+    // always also keeps every sector of the block fully written).
+    P.pos(slot) = pos;
+    P.dir(slot) = dir;
+    P.pol(slot) = pol;
+    P.meta(slot) = make_uint4(pid, rng.draw, pack_cell(i, j, pending), pack_layers(k, k1, path.wmin, path.wmax));
     P.steps[slot] = steps;
     if (P.order) P.order[slot] = order;
     if (PATHS) {
@@ -683,10 +730,7 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
         P.run_ci[2 * size_t(slot)] = path.ci0;
         P.run_ci[2 * size_t(slot) + 1] = path.ci1;
     }
-    P.pos[slot] = pos;
-    P.pol[slot] = pol;
     if (fresh) {
-        P.dir[slot] = dir;
         if (P.ring_n) P.ring_n[slot] = 0u;
         if (P.vee) P.vee[slot] = vee;
         if (P.lineage) P.lineage[slot] = lineage;
@@ -731,16 +775,16 @@ __device__ __forceinline__ void peel_event(uint32_t slot, bool surface, const Sc
     const T eps = Tol<T>::eps;
     const int top = s.nz - 1;
     // All records at once, before the test of the entry: one memory latency.
-    const uint4 meta = P.meta[slot];
-    const Quad<T> pos = P.pos[slot];
-    const Quad<T> dir = P.dir[slot];
-    const Quad<T> pol = P.pol[slot];
+    const uint4 meta = P.meta(slot);
+    const Quad<T> pos = P.pos(slot);
+    const Quad<T> dir = P.dir(slot);
+    const Quad<T> pol = P.pol(slot);
     const uint32_t pid = meta.x;
     if (pid == kNone) { atomicOr(failure, kQueueCorrupt); return; }
-    const int i = int(meta.z & 0xFFFF), j = int(meta.z >> 16);
+    const int i = cell_i(meta.z), j = cell_j(meta.z);
     int k, k1, wmin, wmax;
     unpack_layers(meta.w, k, k1, wmin, wmax);
-    const int sp = surface ? -1 : int(P.kind[slot]) - 1;
+    const int sp = surface ? -1 : cell_kind(meta.z) - 1;
     const T x = pos.x, y = pos.y, z = pos.z, weight = pos.w;
     const T a = dir.x, b = dir.y, c = dir.z, phi = dir.w;
     const T st[4] = {T(1), pol.x, pol.y, (NMAT > 3 && P.vee) ? P.vee[slot] : T(0)};
@@ -940,14 +984,15 @@ template <typename T, typename TA, int NMAT, bool PATHS, bool BACKWARD>
 __device__ __forceinline__ void peel_phase(const SceneView<T>& s, const T* band, const Controls& ctl,
                                            const Divisors& dv, const Pool<T>& P, TA* __restrict__ banks,
                                            const WaveTally& L, uint32_t b, uint32_t* __restrict__ failure,
-                                           unsigned long long* __restrict__ counters) {
+                                           unsigned long long* __restrict__ counters, uint32_t block = blockIdx.x,
+                                           uint32_t blocks = gridDim.x) {
     const uint32_t* c = P.counts + kListCounts * b;
     const uint32_t ns = c[0], ng = c[1], np = c[2];
     const uint32_t total = ns + ng + np;
-    const uint32_t shard = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) % L.shards;
+    const uint32_t shard = ((block * blockDim.x + threadIdx.x) >> 5) % L.shards;
     uint64_t visits = 0, updates = 0;
 
-    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    for (uint32_t e = block * blockDim.x + threadIdx.x; e < total; e += blocks * blockDim.x) {
         bool surface;
         const uint32_t slot = queue_entry(P.queue[b], e, ns, ng, surface);
         if (slot >= P.capacity) { atomicOr(failure, kQueueCorrupt); continue; }
@@ -1016,20 +1061,32 @@ __device__ __forceinline__ T ddis_factor(const SceneView<T>& s, const Guide<T>& 
 
 // Scattering of one event (slot): the new direction (Lambert, polarized sampling or the
 // guided detector branch), the Stokes or weight-matrix update, roulette and the next free
-// path. Returns false when the photon ends here.
+// path. Returns false when the photon ends here. With `handoff` the slot's new records go
+// there (for a walk in the same thread) instead of to memory; a photon that ends is still
+// marked empty in memory.
 template <typename T, int NMAT, bool BACKWARD>
 __device__ __forceinline__ bool scatter_event(uint32_t slot, bool surface, const SceneView<T>& s,
                                               const Controls& ctl, const Divisors& dv, const Pool<T>& P,
-                                              const Guide<T>& g, uint32_t* __restrict__ failure) {
+                                              const Guide<T>& g, uint32_t* __restrict__ failure,
+                                              SlotState<T>* handoff = nullptr) {
     const T eps = Tol<T>::eps;
     const T pi = pi_v<T>();
     // All records at once, before the test of the entry: one memory latency.
-    uint4 meta = P.meta[slot];
-    Quad<T> pos = P.pos[slot];
-    const Quad<T> dir0 = P.dir[slot];
-    Quad<T> pol = P.pol[slot];
+    uint4 meta = P.meta(slot);
+    Quad<T> pos = P.pos(slot);
+    const Quad<T> dir0 = P.dir(slot);
+    Quad<T> pol = P.pol(slot);
     const uint32_t pid = meta.x;
-    if (pid == kNone) { atomicOr(failure, kQueueCorrupt); return false; }
+    auto ended = [&]() {
+        P.meta(slot) = make_uint4(kNone, 0u, 0u, 0u);
+        if (handoff) handoff->meta = make_uint4(kNone, 0u, 0u, 0u);
+        return false;
+    };
+    if (pid == kNone) {
+        atomicOr(failure, kQueueCorrupt);
+        if (handoff) handoff->meta = meta;
+        return false;
+    }
     const uint32_t ro = dv.per_round.div(pid);
     DrawStream rng;
     rng.init(pid - ro * ctl.per_round, ctl.first_round + ro, ctl.seed, meta.y, P.lineage ? P.lineage[slot] : 0u);
@@ -1044,14 +1101,14 @@ __device__ __forceinline__ bool scatter_event(uint32_t slot, bool surface, const
 #pragma unroll
             for (int col = 0; col < NMAT; ++col) M[r][col] = P.matrix[size_t(r * NMAT + col) * P.capacity + slot];
     }
-    const int ci = int(meta.z & 0xFFFF), cj = int(meta.z >> 16), ck = int(meta.w & 0xFF) - 1;
+    const int ci = cell_i(meta.z), cj = cell_j(meta.z), ck = int(meta.w & 0xFF) - 1;
     T roulette = g.roulette;
     if (g.scale) roulette *= __ldg(g.scale + ci + s.nx * (cj + s.ny * ck));
     if (surface) {
         const T Pd = T(rng.next()), U = T(rng.next());
         if (roulette > T(0) && pos.w < roulette) {
             if (T(rng.next()) * roulette < pos.w) pos.w = roulette;
-            else { P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u); return false; }
+            else return ended();
         }
         const T mu = sqrt(Pd);
         phi_out = T(2) * pi * U;
@@ -1070,7 +1127,7 @@ __device__ __forceinline__ bool scatter_event(uint32_t slot, bool surface, const
             }
         }
     } else {
-        const int sp = int(P.kind[slot]) - 1;
+        const int sp = cell_kind(meta.z) - 1;
         const T phi = dir0.w;
         T st[4] = {T(1), pol.x, pol.y, (NMAT > 3 && P.vee) ? P.vee[slot] : T(0)};
         T cos_out, dphi, cos_sca;
@@ -1100,8 +1157,7 @@ __device__ __forceinline__ bool scatter_event(uint32_t slot, bool surface, const
         } else {
             if (!sample_direction<T>(s, sp, NMAT, st, c0, rng, cos_out, dphi, cos_sca, BACKWARD ? T(1) : T(-1))) {
                 atomicOr(failure, kSamplingCap);
-                P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u);
-                return false;
+                return ended();
             }
             phi_out = phi + dphi;
         }
@@ -1142,7 +1198,7 @@ __device__ __forceinline__ bool scatter_event(uint32_t slot, bool surface, const
             if (NMAT > 3) v = out[3] / s0;
             ok = ok && isfinite(q) && isfinite(u) && isfinite(v) && sqrt(q * q + u * u + v * v) <= one + T(1e-2);
         }
-        if (!ok) { atomicOr(failure, kInvalidStokes); P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u); return false; }
+        if (!ok) { atomicOr(failure, kInvalidStokes); return ended(); }
         const T so = sqrt(fmax(T(0), T(1) - cos_out * cos_out));
         T spo, cpo;
         sincos(phi_out, &spo, &cpo);
@@ -1150,7 +1206,7 @@ __device__ __forceinline__ bool scatter_event(uint32_t slot, bool surface, const
         if (guided) pos.w *= ddis_factor<T, NMAT>(s, g, sp, cos_sca, s0, a, b, c);
         if (roulette > T(0) && pos.w < roulette) {
             if (T(rng.next()) * roulette < pos.w) pos.w = roulette;
-            else { P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u); return false; }
+            else return ended();
         }
     }
     if (a * a0 < T(0)) pos.x = fmax(T(0), s.xunit - pos.x);
@@ -1192,10 +1248,15 @@ __device__ __forceinline__ bool scatter_event(uint32_t slot, bool surface, const
     }
     if (!surface) pol.z = -log(fmax(T(rng.next()), eps));
     meta.y = rng.draw;
-    P.pos[slot] = pos;
-    P.dir[slot] = Quad<T>{a, b, c, phi_out};
-    P.pol[slot] = pol;
-    P.meta[slot] = meta;
+    const Quad<T> turned{a, b, c, phi_out};
+    if (handoff) {
+        *handoff = SlotState<T>{meta, pos, turned, pol};
+        return true;
+    }
+    P.pos(slot) = pos;
+    P.dir(slot) = turned;
+    P.pol(slot) = pol;
+    P.meta(slot) = meta;
     return true;
 }
 
@@ -1203,8 +1264,8 @@ __device__ __forceinline__ bool scatter_event(uint32_t slot, bool surface, const
 // step: one wavefront iteration's scattering and walks, reading the work lists of buffer
 // `cur` and filing every slot in those of buffer 1 - cur. Each queued event is scattered
 // and its photon walks on to its next event in the same thread, with no launch in between
-// (the scattering stores the photon's records and the walk reads them back, as the two
-// separate kernels do); paused photons resume their walks; vacant slots take a waiting
+// (the scattered records pass to the walk in registers, and the walk stores the slot's
+// block once); paused photons resume their walks; vacant slots take a waiting
 // split copy or the next photon of the round group and walk it. One thread per list
 // entry: the lists hold at most one entry per slot.
 // ----------------------------------------------------------------------------------
@@ -1212,7 +1273,8 @@ template <typename T, int NMAT, bool PATHS, bool BACKWARD>
 __device__ __forceinline__ void step_phase(const SceneView<T>& s, const T* band, const Controls& ctl,
                                            const Divisors& dv, const Pool<T>& P, const Guide<T>& g, uint32_t walk,
                                            uint32_t cur, uint32_t* __restrict__ failure,
-                                           unsigned long long* __restrict__ counters) {
+                                           unsigned long long* __restrict__ counters, uint32_t block = blockIdx.x,
+                                           uint32_t blocks = gridDim.x) {
     const uint32_t* c = P.counts + kListCounts * cur;
     const uint32_t ns = c[0], ng = c[1], np = c[2], held = c[3], vacant = c[4];
     const uint32_t events = ns + ng + np, total = events + held + vacant;
@@ -1225,18 +1287,22 @@ __device__ __forceinline__ void step_phase(const SceneView<T>& s, const T* band,
     __syncthreads();
     const bool may_claim = claims_open != 0u;
 
-    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    for (uint32_t e = block * blockDim.x + threadIdx.x; e < total; e += blocks * blockDim.x) {
         uint32_t slot;
-        if (e < events) {
+        SlotState<T> state;
+        const bool scattered = e < events;
+        if (scattered) {
             bool surface;
             slot = queue_entry(P.queue[cur], e, ns, ng, surface);
             if (slot >= P.capacity) { atomicOr(failure, kQueueCorrupt); continue; }
-            scatter_event<T, NMAT, BACKWARD>(slot, surface, s, ctl, dv, P, g, failure);  // may leave it vacant
+            // The new records stay in registers for the walk (it may also leave the slot vacant).
+            scatter_event<T, NMAT, BACKWARD>(slot, surface, s, ctl, dv, P, g, failure, &state);
         } else {
             slot = e < events + held ? P.paused[cur][e - events] : P.vacant[cur][e - events - held];
             if (slot >= P.capacity) { atomicOr(failure, kQueueCorrupt); continue; }
         }
-        transit_slot<T, PATHS, true>(slot, s, band, ctl, dv, P, walk, may_claim, out, failure, scatters, visits);
+        transit_slot<T, PATHS, true>(slot, s, band, ctl, dv, P, walk, may_claim, out, failure, scatters, visits,
+                                     scattered ? &state : nullptr);
     }
     const unsigned long long totals[2] = {scatters, visits};
     unsigned long long* const targets[2] = {counters + 0, counters + 1};
@@ -1293,7 +1359,7 @@ template <typename T>
 __global__ void wf_reset(Pool<T> P) {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < P.capacity; slot += stride) {
-        P.meta[slot] = make_uint4(kNone, 0u, 0u, 0u);
+        P.meta(slot) = make_uint4(kNone, 0u, 0u, 0u);
         P.vacant[0][slot] = slot;
         if (P.waiting) P.waiting[slot] = 0u;
     }
@@ -1336,7 +1402,7 @@ wf_tail(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, T* __restrict__ ba
                 continue;
         } else {
             if (slot >= P.capacity) break;
-            if (P.meta[slot].x == kNone && !(P.waiting && P.waiting[slot] > 0u)) continue;
+            if (P.meta(slot).x == kNone && !(P.waiting && P.waiting[slot] > 0u)) continue;
         }
         // No step budget: the walk pauses only at the history step cap, which ends it.
         for (;;) {

@@ -91,6 +91,19 @@ _SIGNATURES = {
         ctypes.c_int,
         [ctypes.c_uint32, _F64P, ctypes.c_size_t, _U32P, _F64P, ctypes.c_char_p, ctypes.c_size_t],
     ),
+    "monki_cuda_multi_create": (
+        ctypes.c_void_p,
+        [ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(_F64P), ctypes.POINTER(ctypes.c_size_t), ctypes.c_uint32,
+         ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t],
+    ),
+    "monki_cuda_multi_tally_count": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_uint32]),
+    "monki_cuda_multi_run": (
+        ctypes.c_int,
+        [ctypes.c_void_p, _U32P, ctypes.POINTER(_F64P), ctypes.c_char_p, ctypes.c_size_t],
+    ),
+    "monki_cuda_multi_counters": (ctypes.c_int, [ctypes.c_void_p, _U64P]),
+    "monki_cuda_multi_last_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]),
+    "monki_cuda_multi_close": (None, [ctypes.c_void_p]),
     "monki_cuda_probe_philox": (
         ctypes.c_int,
         [ctypes.c_uint32, _U32P, _U32P, ctypes.c_uint32, _U32P, ctypes.c_char_p, ctypes.c_size_t],

@@ -544,17 +544,20 @@ def box_cloud_variant(seed: int, photons_per_column: int = 50000, rounds: int = 
     return scene
 
 
-def batched_scene(seed: int, *, photons_scale: float = 1.0) -> TransportScene:
+def batched_scene(seed: int, *, photons_scale: float = 1.0, grid: tuple[int, int] | None = None) -> TransportScene:
     """One scene of the batched workload, drawn from ``numpy.random.default_rng(seed)``.
 
     Grids 8-128 columns a side, 20-60 layers, photons per column log-uniform in 1e3-1e5,
     SZA 0-70, albedo 0.02-0.30, lognormal cloud optical depth (median 5, sigma_ln 1)
-    thresholded to 40 % cover in a 1-3 km layer (g 0.85), I or I/Q/U at random.
+    thresholded to 40 % cover in a 1-3 km layer (g 0.85), I or I/Q/U at random. ``grid``
+    replaces the drawn (nx, ny); every other draw is unchanged.
     """
 
     rng = np.random.default_rng(seed)
     nx = int(rng.integers(8, 129))
     ny = int(rng.integers(8, 129))
+    if grid is not None:
+        nx, ny = (int(v) for v in grid)
     layers = int(rng.integers(20, 61))
     photons = int(round(10 ** rng.uniform(3, 5) * photons_scale))
     sza = float(rng.uniform(0, 70))

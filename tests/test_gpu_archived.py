@@ -6,7 +6,8 @@ Per run, every view's I, Q, U (every pixel of the box clouds): the reference's c
 |z| < 3 in at least 99 % of entries, and no |z| beyond the Bonferroni bound at family
 error 1e-6; the mean z where the entries are many and weakly correlated (box clouds). The
 layered-cloud run also archived its layer AMFs (without their standard error): those are
-compared with twice our own error (the same budget), layer by layer.
+compared with twice our own error (the same budget), layer by layer, below 40 km, and
+within 1 % relative above it (heavy-tailed path tallies; see the test).
 """
 
 from __future__ import annotations
@@ -71,8 +72,20 @@ def test_fp32_transport_agrees_with_the_archived_fortran_run(device, name):
     if name == "2boxclouds":
         assert abs(z.mean()) < 0.1, z.mean()
     if amf is not None:
+        # Layers above 40 km (optical depth below 0.002) have heavy-tailed path tallies: in
+        # the 50,000 km periodic column a photon scattered near the horizontal there crosses
+        # hundreds to thousands of kilometres of one layer (mean free paths of thousands of
+        # km), and every later peel-off of its history carries that path. Neither run's
+        # round-variance error is reliable there (the oracle's 45-50 km AMF drifts up as the
+        # budget grows ten-fold while its error shrinks half as fast as the square root), so
+        # those layers must agree within 1 % relative; the others by the z-criterion.
         archived = fixture["AMF_layer"][..., 0]
-        combined = np.sqrt(2.0) * amf_error
+        optical_depth = fixture["bmsca"][:, 0] + fixture["bmabs"][:, 0] + fixture["baer"][..., 0].sum(axis=(1, 2, 3))
+        thin = optical_depth < 2e-3
+        combined = np.sqrt(2.0) * amf_error[:, ~thin]
         mask = combined > 0
-        za = (amf - archived)[mask] / combined[mask]
+        za = (amf[:, ~thin] - archived[:, ~thin])[mask] / combined[mask]
+        assert za.size >= 0.8 * archived[:, ~thin].size
         assert np.mean(np.abs(za) < 3) >= 0.99, np.sort(np.abs(za))[-5:]
+        relative = np.abs(amf[:, thin] / archived[:, thin] - 1.0)
+        assert relative.max() < 0.01, relative.max()

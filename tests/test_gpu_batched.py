@@ -2,8 +2,10 @@
 
 * a round group replayed as CUDA graphs gives the tallies of the same group launched
   kernel by kernel (FP64 transport; only the device's atomic summation order differs);
-* scenes of uneven size run concurrently from host threads give each scene exactly what
-  running it alone gives;
+* scenes of uneven size in one multi-scene launch sequence (one shared photon pool, every
+  launch covering all scenes) give each scene exactly what running it alone gives, with
+  and without graph replay, I and I/Q/U scenes together;
+* scenes of uneven size run concurrently from host threads in their own sessions do too;
 * the autotuner times its candidates and returns the fastest.
 """
 
@@ -47,12 +49,52 @@ def test_batched_scenes_equal_scenes_run_alone(device):
     from monki.batched import run_batched, run_scene
 
     batch = [scenes.batched_scene(seed, photons_scale=0.002) for seed in range(4)]
-    results, summary = run_batched(batch, concurrency=4, tune=lambda s: {"precision": "fp64"})
+    results, summary = run_batched(batch, concurrency=4, tune=lambda s: {"precision": "fp64"}, persistent=False)
     assert summary["scenes"] == 4 and summary["scatters"] > 0
     for scene, (batches, provenance) in zip(batch, results, strict=True):
         alone, alone_provenance = run_scene(scene, options={"precision": "fp64"})
         assert provenance["scatters"] == alone_provenance["scatters"]
         np.testing.assert_allclose(_flat(batches), _flat(alone), rtol=1e-9, atol=1e-15)
+
+
+@pytest.mark.parametrize("graphs", [True, False])
+def test_persistent_scenes_equal_scenes_run_alone(device, graphs):
+    """Seven uneven scenes (grids 8-128 columns a side, I and I/Q/U, 20-60 layers) in one
+    multi-scene session, FP64, two rounds each: every scene's tallies and scatter count
+    equal the scene run alone in its own session (same seed)."""
+
+    import monki.scenes as scenes
+    from monki.batched import run_persistent, run_scene
+
+    batch = [scenes.batched_scene(seed, photons_scale=0.002) for seed in (0, 1, 2, 5, 11, 17)]
+    batch.append(scenes.batched_scene(93, photons_scale=0.0005, grid=(128, 128)))
+    assert {s.shape[0] for s in batch} == {1, 3}
+    results, summary = run_persistent(batch, rounds=2, precision="fp64", pool=1 << 18, graphs=graphs)
+    assert summary["scenes"] == len(batch) and summary["scatters"] > 0
+    scatters = 0
+    for scene, (batches, _) in zip(batch, results, strict=True):
+        alone, provenance = run_scene(scene, rounds=2, options={"precision": "fp64"})
+        scatters += provenance["scatters"]
+        np.testing.assert_allclose(_flat(batches), _flat(alone), rtol=1e-9, atol=1e-15)
+    assert summary["scatters"] == scatters
+
+
+def test_persistent_fp32_scenes_agree_with_scenes_run_alone(device):
+    """The FP32 product path of the multi-scene session: the same scatters as the scenes run
+    alone (the histories do not depend on the launch layout), tallies equal to FP32
+    summation order."""
+
+    import monki.scenes as scenes
+    from monki.batched import run_persistent, run_scene
+
+    batch = [scenes.batched_scene(seed, photons_scale=0.01) for seed in (3, 4, 6, 7)]
+    results, summary = run_persistent(batch, rounds=1)
+    scatters = 0
+    for scene, (batches, _) in zip(batch, results, strict=True):
+        alone, provenance = run_scene(scene)
+        scatters += provenance["scatters"]
+        np.testing.assert_allclose(_flat(batches), _flat(alone), rtol=2e-4, atol=1e-7 * np.abs(_flat(alone)).max())
+    assert summary["scatters"] == scatters
 
 
 def test_sessions_open_and_close_while_others_replay_graphs(device):
@@ -76,7 +118,7 @@ def test_sessions_open_and_close_while_others_replay_graphs(device):
         return {**shapes[key], "precision": "fp64"}
 
     for attempt in range(2):
-        results, summary = run_batched(batch, concurrency=4, tune=tune)
+        results, summary = run_batched(batch, concurrency=4, tune=tune, persistent=False)
         assert summary["scenes"] == 16 and summary["scatters"] > 0
         for scene, (batches, provenance) in zip(batch, results, strict=True):
             alone, alone_provenance = run_scene(scene, options=tune(scene))
