@@ -20,6 +20,8 @@
 #include <cstring>
 #include <mutex>
 #include <stdexcept>
+
+#include <cuda.h>
 #include <string>
 #include <vector>
 
@@ -259,20 +261,70 @@ void configure(int device) {
     g_attr_done[device] = true;
 }
 
+// cuTensorMapEncodeTiled, from the driver through the runtime (no link against libcuda).
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encoder() {
+    static EncodeTiled fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult found{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &found) == cudaSuccess &&
+            found == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(f);
+    });
+    if (!fn) throw std::runtime_error("cuTensorMapEncodeTiled is unavailable from the driver");
+    return fn;
+}
+
+// Tensor map of a K-major BF16 matrix (rows x k_extent, row stride ld elements) read in
+// tiles of 64 K-elements (128 bytes, the swizzle width) x box_rows rows; reads outside the
+// matrix return zeros.
+CUtensorMap tile_map(const bf16* base, int rows, int k_extent, int ld, int box_rows) {
+    if ((reinterpret_cast<uintptr_t>(base) & 15) || (size_t(ld) * sizeof(bf16)) % 16 || k_extent % umma::kBlockK ||
+        box_rows < 1 || box_rows > 256)
+        throw std::runtime_error("operand outside the tensor-map tiling");
+    CUtensorMap map{};
+    const cuuint64_t dims[2] = {cuuint64_t(k_extent), cuuint64_t(rows)};
+    const cuuint64_t strides[1] = {cuuint64_t(ld) * sizeof(bf16)};
+    const cuuint32_t box[2] = {cuuint32_t(umma::kBlockK), cuuint32_t(box_rows)};
+    const cuuint32_t element[2] = {1, 1};
+    const CUresult r = encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16*>(base), dims, strides, box,
+                                 element, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed (" + std::to_string(int(r)) + ")");
+    return map;
+}
+
+// One GEMM: operands (K-major, row strides lda / ldb) and the epilogue's parameters.
+struct Gemm {
+    const bf16* A;
+    int lda;
+    const bf16* B;
+    int ldb;
+    umma::Params p;
+};
+
 template <int EPI>
-void gemm(const umma::Params& p, int splits, cudaStream_t stream) {
+void gemm(const Gemm& g, int splits, cudaStream_t stream) {
+    const umma::Params& p = g.p;
     if (p.K % umma::kBlockK || p.k_chunk % umma::kBlockK || p.N % 16 || p.N < 16 || p.N > 256 || p.rows_a < 1)
         throw std::runtime_error("GEMM shape outside the kernel's tiling");
+    const CUtensorMap map_a = tile_map(g.A, p.rows_a, p.K, g.lda, umma::kBlockM);
+    const CUtensorMap map_b = tile_map(g.B, p.N, p.K, g.ldb, p.N);
     dim3 grid((p.rows_a + umma::kBlockM - 1) / umma::kBlockM, splits);
-    umma::gemm<EPI><<<grid, umma::kThreads, umma::kSmemBytes, stream>>>(p);
+    umma::gemm<EPI><<<grid, umma::kThreads, umma::kSmemBytes, stream>>>(map_a, map_b, p);
     check(cudaGetLastError(), "gemm launch");
 }
 
-umma::Params params_for(const bf16* A, const bf16* B, int rows, int N, int K, uint32_t* failure) {
-    umma::Params p{};
-    p.A = A; p.B = B; p.rows_a = rows; p.N = N; p.K = K; p.lda = K; p.ldb = K; p.k_chunk = K;
-    p.failure = failure;
-    return p;
+Gemm params_for(const bf16* A, const bf16* B, int rows, int N, int K, uint32_t* failure) {
+    Gemm g{A, K, B, K, umma::Params{}};
+    g.p.rows_a = rows; g.p.N = N; g.p.K = K; g.p.k_chunk = K;
+    g.p.failure = failure;
+    return g;
 }
 
 // Zero the columns [rows, rows rounded up to 64) of a transposed (height x R) matrix: the
@@ -287,15 +339,15 @@ void clear_tail(bf16* T, int rows, int R, int height, cudaStream_t stream) {
 // Forward pass of the first `rows` rows (<= R) of the packed input.
 void forward(Net& n, int rows) {
     const int R = n.R;
-    umma::Params p = params_for(n.X, n.W1, rows, kHidden, kIn, n.failure);
-    p.C = n.Z1; p.bias = n.params + ob1; p.H = n.H1; p.HT = n.H1T; p.rows_ht = R;
-    gemm<umma::kForward>(p, 1, n.stream);
-    p = params_for(n.H1, n.W2, rows, kHidden, kHidden, n.failure);
-    p.C = n.Z2; p.bias = n.params + ob2; p.H = n.H2; p.HT = n.H2T; p.rows_ht = R;
-    gemm<umma::kForward>(p, 1, n.stream);
-    p = params_for(n.H2, n.W3, rows, kHidden, kHidden, n.failure);
-    p.C = n.Z3; p.bias = n.params + ob3; p.H = n.H3; p.HT = nullptr; p.rows_ht = R;
-    gemm<umma::kForward>(p, 1, n.stream);
+    Gemm g = params_for(n.X, n.W1, rows, kHidden, kIn, n.failure);
+    g.p.C = n.Z1; g.p.bias = n.params + ob1; g.p.H = n.H1; g.p.HT = n.H1T; g.p.rows_ht = R;
+    gemm<umma::kForward>(g, 1, n.stream);
+    g = params_for(n.H1, n.W2, rows, kHidden, kHidden, n.failure);
+    g.p.C = n.Z2; g.p.bias = n.params + ob2; g.p.H = n.H2; g.p.HT = n.H2T; g.p.rows_ht = R;
+    gemm<umma::kForward>(g, 1, n.stream);
+    g = params_for(n.H2, n.W3, rows, kHidden, kHidden, n.failure);
+    g.p.C = n.Z3; g.p.bias = n.params + ob3; g.p.H = n.H3; g.p.HT = nullptr; g.p.rows_ht = R;
+    gemm<umma::kForward>(g, 1, n.stream);
     clear_tail(n.H1T, rows, R, kHidden, n.stream);
     clear_tail(n.H2T, rows, R, kHidden, n.stream);
     head_forward<<<(rows * 32 + 255) / 256, 256, 0, n.stream>>>(n.H3, n.params + ow4, n.params + ob4, rows, n.y);
@@ -312,27 +364,28 @@ void backward(Net& n, int rows, float inv_weight, float* loss) {
     transpose<<<dim3(kHidden / 32, (R + 31) / 32), dim3(32, 8), 0, n.stream>>>(n.G3, R, kHidden, R, n.G3T);
     row_sums<<<dim3(kHidden, row_segments(rows)), 256, 0, n.stream>>>(n.G3T, rows, R, n.grads + ob3);
     check(cudaGetLastError(), "head backward launch");
-    // Split-K over the rows for the weight gradients: 64-row multiples, 512 rows per slice.
-    const int chunk = 512, K = (rows + 63) / 64 * 64, splits = (K + chunk - 1) / chunk;
-    umma::Params p = params_for(n.G3T, n.H2T, kHidden, kHidden, K, n.failure);
-    p.lda = R; p.ldb = R; p.k_chunk = chunk; p.C = n.grads + oW3;
-    gemm<umma::kAccumulate>(p, splits, n.stream);
-    p = params_for(n.G3, n.W3T, rows, kHidden, kHidden, n.failure);
-    p.zprev = n.Z2; p.H = n.G2; p.HT = n.G2T; p.rows_ht = R;
-    gemm<umma::kBackward>(p, 1, n.stream);
+    // Split-K over the rows for the weight gradients: 64-row multiples, slices of 1,024 rows
+    // (at batch 65,536 two row tiles x 64 slices = 128 CTAs, each adding one partial).
+    const int chunk = 1024, K = (rows + 63) / 64 * 64, splits = (K + chunk - 1) / chunk;
+    Gemm g = params_for(n.G3T, n.H2T, kHidden, kHidden, K, n.failure);
+    g.lda = R; g.ldb = R; g.p.k_chunk = chunk; g.p.C = n.grads + oW3;
+    gemm<umma::kAccumulate>(g, splits, n.stream);
+    g = params_for(n.G3, n.W3T, rows, kHidden, kHidden, n.failure);
+    g.p.zprev = n.Z2; g.p.H = n.G2; g.p.HT = n.G2T; g.p.rows_ht = R;
+    gemm<umma::kBackward>(g, 1, n.stream);
     clear_tail(n.G2T, rows, R, kHidden, n.stream);
     row_sums<<<dim3(kHidden, row_segments(rows)), 256, 0, n.stream>>>(n.G2T, rows, R, n.grads + ob2);
-    p = params_for(n.G2T, n.H1T, kHidden, kHidden, K, n.failure);
-    p.lda = R; p.ldb = R; p.k_chunk = chunk; p.C = n.grads + oW2;
-    gemm<umma::kAccumulate>(p, splits, n.stream);
-    p = params_for(n.G2, n.W2T, rows, kHidden, kHidden, n.failure);
-    p.zprev = n.Z1; p.H = n.G1; p.HT = n.G1T; p.rows_ht = R;
-    gemm<umma::kBackward>(p, 1, n.stream);
+    g = params_for(n.G2T, n.H1T, kHidden, kHidden, K, n.failure);
+    g.lda = R; g.ldb = R; g.p.k_chunk = chunk; g.p.C = n.grads + oW2;
+    gemm<umma::kAccumulate>(g, splits, n.stream);
+    g = params_for(n.G2, n.W2T, rows, kHidden, kHidden, n.failure);
+    g.p.zprev = n.Z1; g.p.H = n.G1; g.p.HT = n.G1T; g.p.rows_ht = R;
+    gemm<umma::kBackward>(g, 1, n.stream);
     clear_tail(n.G1T, rows, R, kHidden, n.stream);
     row_sums<<<dim3(kHidden, row_segments(rows)), 256, 0, n.stream>>>(n.G1T, rows, R, n.grads + ob1);
-    p = params_for(n.G1T, n.XT, kHidden, kIn, K, n.failure);
-    p.lda = R; p.ldb = R; p.k_chunk = chunk; p.C = n.grads + oW1;
-    gemm<umma::kAccumulate>(p, splits, n.stream);
+    g = params_for(n.G1T, n.XT, kHidden, kIn, K, n.failure);
+    g.lda = R; g.ldb = R; g.p.k_chunk = chunk; g.p.C = n.grads + oW1;
+    gemm<umma::kAccumulate>(g, splits, n.stream);
     check(cudaGetLastError(), "backward launch");
 }
 
@@ -604,11 +657,11 @@ int monki_mlp_gemm_probe(uint32_t device, const uint16_t* a, const uint16_t* b, 
         check(cudaMemcpy(db, b, size_t(N) * K * 2, cudaMemcpyHostToDevice), "upload");
         check(cudaMemset(dc, 0, size_t(M) * N * 4), "memset");
         check(cudaMemset(flag, 0, 4), "memset");
-        umma::Params p = params_for(da, db, M, N, K, flag);
-        p.C = dc;
-        p.k_chunk = K / splits;
-        if (splits == 1) gemm<umma::kStore>(p, 1, nullptr);
-        else gemm<umma::kAccumulate>(p, splits, nullptr);
+        Gemm g = params_for(da, db, M, N, K, flag);
+        g.p.C = dc;
+        g.p.k_chunk = K / splits;
+        if (splits == 1) gemm<umma::kStore>(g, 1, nullptr);
+        else gemm<umma::kAccumulate>(g, splits, nullptr);
         uint32_t f = 0;
         check(cudaMemcpy(&f, flag, 4, cudaMemcpyDeviceToHost), "download");
         check(cudaMemcpy(c, dc, size_t(M) * N * 4, cudaMemcpyDeviceToHost), "download");

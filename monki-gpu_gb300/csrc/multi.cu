@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "host_tables.h"
+#include "tail.h"
 #include "wavefront.cuh"
 
 namespace monki {
@@ -59,6 +60,25 @@ __device__ __forceinline__ void load_entry(SceneEntry<T>& E, const SceneEntry<T>
     __syncthreads();
 }
 
+// True when this block has no entry of its scene's work lists to serve (lists `first` ..
+// `last` of buffer b: 0-2 the event queues, 3 the paused walks, 4 the vacant slots). Such a
+// block returns before it copies the entry or stages the band: late in a round group most
+// segments are drained and most blocks of a launch are idle.
+template <typename T>
+__device__ __forceinline__ bool idle_block(const SceneEntry<T>* __restrict__ scenes, const uint16_t* __restrict__ block_scene,
+                                           uint32_t b, int first, int last) {
+    __shared__ uint32_t idle;
+    if (threadIdx.x == 0) {
+        const SceneEntry<T>* E = scenes + block_scene[blockIdx.x];
+        const uint32_t* c = E->P.counts + kListCounts * b;
+        uint32_t total = 0;
+        for (int q = first; q <= last; ++q) total += c[q];
+        idle = (blockIdx.x - E->block0) * blockDim.x >= total ? 1u : 0u;
+    }
+    __syncthreads();
+    return idle != 0u;
+}
+
 // Start of a round group: every segment's slots empty and vacant, no claims yet.
 template <typename T>
 __global__ void wf_reset_multi(const SceneEntry<T>* __restrict__ scenes, const uint16_t* __restrict__ block_scene) {
@@ -78,6 +98,7 @@ wf_step_multi(const SceneEntry<T>* __restrict__ scenes, const uint16_t* __restri
               uint32_t walk, uint32_t cur, uint32_t* __restrict__ failure, unsigned long long* __restrict__ counters) {
     extern __shared__ __align__(16) unsigned char staged[];
     __shared__ __align__(16) SceneEntry<T> E;
+    if (idle_block(scenes, block_scene, cur, 0, 4)) return;
     load_entry(E, scenes, block_scene);
     const T* band = stage_band<T>(E.s, staged, failure);
     step_phase<T, NMAT, false, false>(E.s, band, E.ctl, E.dv, E.P, g, walk, cur, failure, counters, blockIdx.x - E.block0,
@@ -90,6 +111,7 @@ wf_peel_multi(const SceneEntry<T>* __restrict__ scenes, const uint16_t* __restri
               uint32_t* __restrict__ failure, unsigned long long* __restrict__ counters) {
     extern __shared__ __align__(16) unsigned char staged[];
     __shared__ __align__(16) SceneEntry<T> E;
+    if (idle_block(scenes, block_scene, b, 0, 2)) return;
     load_entry(E, scenes, block_scene);
     const T* band = stage_band<T>(E.s, staged, failure);
     peel_phase<T, T, NMAT, false, false>(E.s, band, E.ctl, E.dv, E.P, E.banks, E.W, b, failure, counters,
@@ -138,8 +160,11 @@ struct Multi {
     std::vector<Group> groups;
     uint32_t* failure = nullptr;
     unsigned long long* counters = nullptr;
+    uint32_t* tail_next = nullptr;             // one counter per scene for its tail launch
+    std::vector<cudaStream_t> tail_streams;    // the scenes' tails run side by side
     cudaEvent_t t0 = nullptr, t1 = nullptr, t2 = nullptr;
     uint64_t totals[6] = {0, 0, 0, 0, 0, 0};
+    uint64_t tails = 0;
     float last_kernel_ms = 0.f, last_run_ms = 0.f;
     std::string name;
 };
@@ -178,7 +203,8 @@ void destroy(Multi* m) {
         if (g.stream) cudaStreamDestroy(g.stream);
     }
     for (Scene& sc : m->scenes) { cudaFree(sc.tables); cudaFree(sc.banks); cudaFree(sc.out); cudaFree(sc.info); }
-    cudaFree(m->failure); cudaFree(m->counters);
+    for (cudaStream_t t : m->tail_streams) { cudaStreamSynchronize(t); cudaStreamDestroy(t); }
+    cudaFree(m->failure); cudaFree(m->counters); cudaFree(m->tail_next);
     if (m->t0) cudaEventDestroy(m->t0);
     if (m->t1) cudaEventDestroy(m->t1);
     if (m->t2) cudaEventDestroy(m->t2);
@@ -356,13 +382,39 @@ void run(Multi& m, const std::vector<Controls>& ctl) {
         for (Group& g : m.groups) {
             if (!g.active) continue;
             check(cudaStreamSynchronize(g.stream), "multi-scene wavefront");
-            bool done = true;
+            bool done = true, claimed = true;
+            uint64_t live_total = 0;
             for (size_t q = 0; q < g.members.size(); ++q) {
                 const uint32_t* h = g.host_counts + q * kCountWords;
                 const Controls& c = ctl[size_t(g.members[q])];
                 if (!c.count) continue;  // no segment this run: its counts are not in use
                 const uint64_t live = uint64_t(h[0]) + h[1] + h[2] + h[3] + h[4];
                 done = done && h[kClaimCount] >= c.count && live == 0;
+                claimed = claimed && h[kClaimCount] >= c.count;
+                live_total += live;
+            }
+            if (!done && claimed && m.cfg.tail && live_total <= m.cfg.tail) {
+                // Few photons left and none to claim: each scene that still has some runs them
+                // to their ends in its own tail launch, sized to its photons, side by side on
+                // the tail streams (the queued events of the last iteration first).
+                const SceneEntry<T>* host = static_cast<const SceneEntry<T>*>(g.host_entries);
+                const Guide<T> guide{T(0), T(0), T(INFINITY), nullptr, T(0)};
+                size_t used = 0;
+                for (size_t q = 0; q < g.members.size(); ++q) {
+                    const uint32_t* h = g.host_counts + q * kCountWords;
+                    const uint64_t live = uint64_t(h[0]) + h[1] + h[2] + h[3] + h[4];
+                    if (!ctl[size_t(g.members[q])].count || !live) continue;
+                    const SceneEntry<T>& E = host[q];
+                    cudaStream_t t = m.tail_streams[used++ % m.tail_streams.size()];
+                    const unsigned blocks = unsigned(std::max<uint64_t>(1, (live + 255) / 256));
+                    check(launch_tail<T>(E.s, E.ctl, E.dv, E.P, E.banks, E.W, guide, 0u, true, m.failure, m.counters,
+                                         m.tail_next + g.members[q], t, blocks), "tail launch");
+                    launches += 2;
+                    m.tails += 1;
+                }
+                for (size_t k = 0; k < std::min(used, m.tail_streams.size()); ++k)
+                    check(cudaStreamSynchronize(m.tail_streams[k]), "tail");
+                done = true;
             }
             if (done) g.active = false;
         }
@@ -481,6 +533,9 @@ void* monki_cuda_multi_create(uint32_t device, uint32_t scenes, const double* co
         }
         check(cudaMalloc(&m->failure, sizeof(uint32_t)), "cudaMalloc(failure)");
         check(cudaMalloc(&m->counters, 4 * sizeof(unsigned long long)), "cudaMalloc(counters)");
+        check(cudaMalloc(&m->tail_next, m->scenes.size() * sizeof(uint32_t)), "cudaMalloc(tail)");
+        m->tail_streams.resize(8);
+        for (cudaStream_t& t : m->tail_streams) check(cudaStreamCreateWithFlags(&t, cudaStreamNonBlocking), "cudaStreamCreate");
         check(cudaEventCreate(&m->t0), "cudaEventCreate");
         check(cudaEventCreate(&m->t1), "cudaEventCreate");
         check(cudaEventCreate(&m->t2), "cudaEventCreate");

@@ -1,20 +1,32 @@
-// Fifth-generation tensor-core GEMM for sm_103a: C = A * B^T with BF16 operands staged
-// in shared memory (128-byte swizzled, K-major), FP32 accumulation in tensor memory
-// (TMEM), one elected thread issuing tcgen05.mma, completion tracked by mbarriers, and a
-// fused epilogue read back from TMEM with tcgen05.ld.
+// Fifth-generation tensor-core GEMM for sm_103a: C = A * B^T with BF16 operands, FP32
+// accumulation in tensor memory (TMEM) and a fused epilogue read back with tcgen05.ld.
+//
+// Roles inside a CTA of eight warps:
+//   producer  (warp 0, one thread) loads the K-steps' A and B tiles with the Tensor Memory
+//             Accelerator (cp.async.bulk.tensor, 128-byte swizzle) into a ring of shared-
+//             memory stages; each load completes on the stage's "full" mbarrier;
+//   MMA       (warp 1, one thread) waits for a stage, issues four tcgen05.mma of K = 16 and
+//             commits them to the stage's "empty" mbarrier, which frees it for the next
+//             load; the last commit also arrives on the "done" mbarrier;
+//   epilogue  (all eight warps) after "done": TMEM lanes 32 (w % 4) .. + 31, every other
+//             32-column chunk from 32 (w / 4); bias, GELU or GELU', FP32 / BF16 stores, and
+//             transposed BF16 stores staged through shared memory so that each thread
+//             writes 64 contiguous bytes of a transposed row.
 //
 // Tile: 128 rows of C per CTA (the MMA's M), all N <= 256 columns (one MMA covers them),
-// K in steps of 64 (one 128-byte swizzle row of BF16), four MMAs of K = 16 per step.
-// Two shared-memory stages: the 256 threads load step s + 1 while the tensor core runs
-// step s; a stage is refilled only after the MMAs that read it have committed. The K
-// range of a CTA is blockIdx.y's slice (split-K for the weight gradients).
+// K in steps of 64 (one 128-byte swizzle row of BF16). The K range of a CTA is blockIdx.y's
+// slice (split-K for the weight gradients, summed by float4 atomics). Every mbarrier wait is
+// bounded: a wait that gives up sets failure bit 1, the CTA skips its stores and still
+// releases its TMEM.
 //
-// Shared-memory matrix layout (K-major, SWIZZLE_128B): row r of a tile occupies bytes
-// [128 r, 128 r + 128); its 16-byte chunk c sits at chunk c ^ (r % 8). Eight rows form a
-// 1024-byte atom, so the descriptor's stride byte offset is 1024 and the tile base is
-// 1024-byte aligned. Advancing the start address by 32 bytes selects the next K = 16.
+// Shared-memory operand layout (K-major, SWIZZLE_128B, what the TMA writes with
+// CU_TENSOR_MAP_SWIZZLE_128B): row r of a tile occupies bytes [128 r, 128 r + 128); its
+// 16-byte chunk c sits at chunk c ^ (r % 8). Eight rows form a 1024-byte atom, so the
+// descriptor's stride byte offset is 1024 and each tile base is 1024-byte aligned.
+// Advancing the start address by 32 bytes selects the next K = 16.
 #pragma once
 #include <stdint.h>
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 namespace monki {
@@ -22,14 +34,16 @@ namespace umma {
 
 constexpr int kBlockM = 128;
 constexpr int kBlockK = 64;
-constexpr int kThreads = 256;                    // eight warps: loaders, then epilogue
+constexpr int kThreads = 256;                    // eight warps
+constexpr int kStages = 2;
 constexpr uint32_t kSmemA = kBlockM * kBlockK * 2;   // 16 KB
 constexpr uint32_t kSmemB = 256 * kBlockK * 2;       // 32 KB (N <= 256)
 constexpr uint32_t kStage = kSmemA + kSmemB;         // 48 KB, 1024-byte multiple
-// 100 KB of dynamic shared memory: two stages plus alignment, and at most two CTAs per SM
-// so their TMEM allocations (256 columns each of the SM's 512) never wait on each other.
+// 100 KB of dynamic shared memory: the stages plus alignment, so two CTAs share an SM and
+// their TMEM allocations (256 columns each of the SM's 512) never wait on each other.
 constexpr uint32_t kSmemBytes = 100u * 1024u;
 constexpr uint32_t kWaitLimit = 1u << 24;          // mbarrier polls before giving up
+constexpr uint32_t kTransposeStride = 80;          // bytes per staged transposed row (32 BF16 + padding)
 
 enum Epilogue : int {
     kStore = 0,      // C (fp32) = acc
@@ -39,16 +53,14 @@ enum Epilogue : int {
 };
 
 struct Params {
-    const __nv_bfloat16* A;   // rows_a x K, row stride lda (elements)
-    const __nv_bfloat16* B;   // N x K, row stride ldb
-    int rows_a, N, K, lda, ldb;
+    int rows_a, N, K;
     int k_chunk;              // K elements per blockIdx.y slice (multiple of 64)
     float* C;                 // kStore / kAccumulate / kForward (Z): rows_a x N, stride N
     const float* bias;        // kForward: N
     const float* zprev;       // kBackward: rows_a x N pre-activations
     __nv_bfloat16* H;         // kForward / kBackward: rows_a x N
     __nv_bfloat16* HT;        // kForward / kBackward: N x rows_ht (transposed), or null
-    int rows_ht;              // row stride of HT (>= rows_a)
+    int rows_ht;              // row stride of HT (>= rows_a, a multiple of 8)
     uint32_t* failure;        // bit 1: an mbarrier wait gave up
 };
 
@@ -81,20 +93,6 @@ __device__ __forceinline__ float gelu_grad(float z) {
     return cdf + z * pdf;
 }
 
-// Copy rows [row0, row0 + rows) x columns [k0, k0 + 64) of a K-major BF16 matrix into a
-// swizzled tile; rows past `limit` are zero.
-__device__ __forceinline__ void load_tile(unsigned char* tile, const __nv_bfloat16* g, int ld, int row0, int rows,
-                                          int limit, int k0) {
-    const int chunks = rows * 8;
-    for (int q = threadIdx.x; q < chunks; q += kThreads) {
-        const int r = q >> 3, c = q & 7;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (row0 + r < limit)
-            v = *reinterpret_cast<const uint4*>(g + size_t(row0 + r) * ld + k0 + c * 8);
-        *reinterpret_cast<uint4*>(tile + r * 128 + ((c ^ (r & 7)) << 4)) = v;
-    }
-}
-
 __device__ __forceinline__ bool wait_parity(uint32_t bar, uint32_t parity) {
     for (uint32_t attempt = 0; attempt < kWaitLimit; ++attempt) {
         uint32_t done;
@@ -106,10 +104,19 @@ __device__ __forceinline__ bool wait_parity(uint32_t bar, uint32_t parity) {
     return false;
 }
 
+// One 2-D tile (x = K element, y = row) of a tensor map into shared memory, completing
+// `bytes` on the mbarrier.
+__device__ __forceinline__ void tma_load(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar) : "memory");
+}
+
 template <int EPI>
-__global__ void __launch_bounds__(kThreads, 1) gemm(Params p) {
+__global__ void __launch_bounds__(kThreads, 1)
+gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, Params p) {
     extern __shared__ __align__(1024) unsigned char raw[];
-    __shared__ __align__(8) uint64_t mma_bar[2];
+    __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages], done_bar;
     __shared__ uint32_t tmem_base;
     __shared__ int aborted;
     unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(raw) + 1023) & ~uintptr_t(1023));
@@ -117,84 +124,91 @@ __global__ void __launch_bounds__(kThreads, 1) gemm(Params p) {
     const int row0 = blockIdx.x * kBlockM;
     const int k_begin = blockIdx.y * p.k_chunk;
     const int k_end = min(p.K, k_begin + p.k_chunk);
+    const int steps = k_end > k_begin ? (k_end - k_begin) / kBlockK : 0;
     const int N = p.N;
     const uint32_t columns = N <= 32 ? 32u : (N <= 64 ? 64u : (N <= 128 ? 128u : 256u));
-    const uint32_t bar[2] = {smem_u32(&mma_bar[0]), smem_u32(&mma_bar[1])};
+    const uint32_t b_rows = uint32_t(N);  // the B tile's rows (the tensor map's box height)
+    const uint32_t stage_bytes = kSmemA + b_rows * kBlockK * 2;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
                      "r"(columns) : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 32) {
         aborted = 0;
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar[0]) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar[1]) : "memory");
+        for (int s = 0; s < kStages; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full_bar[s])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty_bar[s])) : "memory");
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&done_bar)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base;
-    const uint32_t idesc = instr_desc(kBlockM, N);
 
-    // Commits issued and completions observed per stage barrier (uniform in the CTA).
-    uint32_t issued[2] = {0u, 0u}, seen[2] = {0u, 0u};
-    int step = 0;
-    for (int k0 = k_begin; k0 < k_end; k0 += kBlockK, ++step) {
-        const int b = step & 1;
-        unsigned char* tile_a = base + b * kStage;
-        unsigned char* tile_b = tile_a + kSmemA;
-        if (issued[b] > seen[b]) {
-            // The MMAs of step - 2 read this stage: wait for their commit before refilling.
-            if (!wait_parity(bar[b], seen[b] & 1u)) {
+    if (threadIdx.x == 0 && steps > 0) {
+        // Producer: a stage is reloaded only after the MMAs that read it have committed.
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_a)) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_b)) : "memory");
+        for (int step = 0; step < steps; ++step) {
+            const int s = step % kStages, round = step / kStages;
+            if (round > 0 && !wait_parity(smem_u32(&empty_bar[s]), uint32_t(round - 1) & 1u)) {
+                atomicOr(p.failure, 1u);
                 aborted = 1;
-                if (threadIdx.x == 0) atomicOr(p.failure, 1u);
+                break;
             }
-            ++seen[b];
+            const uint32_t full = smem_u32(&full_bar[s]);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full), "r"(stage_bytes) : "memory");
+            const uint32_t tile_a = smem_u32(base + s * kStage), tile_b = tile_a + kSmemA;
+            const int k0 = k_begin + step * kBlockK;
+            tma_load(tile_a, &map_a, k0, row0, full);
+            tma_load(tile_b, &map_b, k0, 0, full);
         }
-        load_tile(tile_a, p.A, p.lda, row0, kBlockM, p.rows_a, k0);
-        load_tile(tile_b, p.B, p.ldb, 0, N, N, k0);
-        // Make the generic-proxy stores visible to the tensor core (async proxy).
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (aborted) break;
-        if (threadIdx.x == 0) {
+    } else if (threadIdx.x == 32 && steps > 0) {
+        // MMA issuer.
+        const uint32_t idesc = instr_desc(kBlockM, N);
+        for (int step = 0; step < steps; ++step) {
+            const int s = step % kStages, round = step / kStages;
+            if (!wait_parity(smem_u32(&full_bar[s]), uint32_t(round) & 1u)) {
+                atomicOr(p.failure, 1u);
+                aborted = 1;
+                break;
+            }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t a_addr = smem_u32(tile_a), b_addr = smem_u32(tile_b);
+            const uint32_t a_addr = smem_u32(base + s * kStage), b_addr = a_addr + kSmemA;
 #pragma unroll
             for (int kk = 0; kk < kBlockK / 16; ++kk) {
                 const uint64_t da = smem_desc(a_addr + kk * 32), db = smem_desc(b_addr + kk * 32);
-                const uint32_t accumulate = (k0 > k_begin || kk > 0) ? 1u : 0u;
+                const uint32_t accumulate = (step > 0 || kk > 0) ? 1u : 0u;
                 asm volatile(
                     "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
                     " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
                     ::"r"(tmem), "l"(da), "l"(db), "r"(idesc), "r"(accumulate) : "memory");
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar[b])
-                         : "memory");
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                         ::"r"(smem_u32(&empty_bar[s])) : "memory");
         }
-        ++issued[b];
+        // Every MMA issued so far completes before "done" arrives.
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                     ::"r"(smem_u32(&done_bar)) : "memory");
     }
-    // Drain: every commit issued is waited for (bounded) before TMEM is read or released.
-    for (int b = 0; b < 2; ++b) {
-        while (seen[b] < issued[b]) {
-            if (!wait_parity(bar[b], seen[b] & 1u)) {
-                aborted = 1;
-                if (threadIdx.x == 0) atomicOr(p.failure, 1u);
-            }
-            ++seen[b];
-        }
+    __syncwarp();
+    if (steps > 0 && !wait_parity(smem_u32(&done_bar), 0u)) {
+        if (lane == 0) atomicOr(p.failure, 1u);
+        aborted = 1;
     }
+    // The producer's loads were all consumed by MMAs that "done" covers; the stages are free.
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
-    if (!aborted && k_end > k_begin) {
-        // Epilogue: warp w reads TMEM lanes (rows) 32 (w % 4) .. + 31 (the lane quarter its
-        // position in the warpgroup allows) and every other 32-column chunk, from 32 (w / 4).
+    if (!aborted && steps > 0) {
         const int quarter = warp & 3, half = warp >> 2;
         const int m = row0 + quarter * 32 + lane;
         const bool valid = m < p.rows_a;
+        unsigned char* stage_t = base + warp * (32 * kTransposeStride);  // this warp's transpose tile
         for (int c0 = 32 * half; c0 < N; c0 += 64) {
             uint32_t r[32];
             const uint32_t taddr = tmem + (uint32_t(quarter * 32) << 16) + uint32_t(c0);
@@ -207,34 +221,34 @@ __global__ void __launch_bounds__(kThreads, 1) gemm(Params p) {
                   "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
                 : "r"(taddr));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (!valid) continue;
             const int width = min(32, N - c0);
             const size_t at = size_t(m) * N + c0;
-            // Each thread owns 32 consecutive columns of its row: 16-byte stores (and loads)
-            // instead of scalar ones, whose warp-wide pattern touched 32 rows per instruction.
             if (width == 32 && (N & 7) == 0) {
                 float v[32];
 #pragma unroll
                 for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
                 if (EPI == kStore) {
+                    if (valid)
 #pragma unroll
-                    for (int q = 0; q < 32; q += 4)
-                        *reinterpret_cast<float4*>(p.C + at + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+                        for (int q = 0; q < 32; q += 4)
+                            *reinterpret_cast<float4*>(p.C + at + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
                 } else if (EPI == kAccumulate) {
+                    if (valid)
 #pragma unroll
-                    for (int q = 0; q < 32; q += 4)
-                        atomicAdd(reinterpret_cast<float4*>(p.C + at + q), make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]));
+                        for (int q = 0; q < 32; q += 4)
+                            atomicAdd(reinterpret_cast<float4*>(p.C + at + q), make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]));
                 } else {
                     if (EPI == kForward) {
 #pragma unroll
                         for (int q = 0; q < 32; q += 4) {
                             const float4 b = *reinterpret_cast<const float4*>(p.bias + c0 + q);
                             v[q] += b.x; v[q + 1] += b.y; v[q + 2] += b.z; v[q + 3] += b.w;
-                            *reinterpret_cast<float4*>(p.C + at + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+                            if (valid)
+                                *reinterpret_cast<float4*>(p.C + at + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
                         }
 #pragma unroll
                         for (int q = 0; q < 32; ++q) v[q] = gelu(v[q]);
-                    } else {
+                    } else if (valid) {
 #pragma unroll
                         for (int q = 0; q < 32; q += 4) {
                             const float4 z = *reinterpret_cast<const float4*>(p.zprev + at + q);
@@ -248,17 +262,36 @@ __global__ void __launch_bounds__(kThreads, 1) gemm(Params p) {
                         const __nv_bfloat162 h2 = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
                         packed[q] = *reinterpret_cast<const uint32_t*>(&h2);
                     }
+                    if (valid)
 #pragma unroll
-                    for (int q = 0; q < 16; q += 4)
-                        *reinterpret_cast<uint4*>(p.H + at + 2 * q) = make_uint4(packed[q], packed[q + 1], packed[q + 2], packed[q + 3]);
+                        for (int q = 0; q < 16; q += 4)
+                            *reinterpret_cast<uint4*>(p.H + at + 2 * q) =
+                                make_uint4(packed[q], packed[q + 1], packed[q + 2], packed[q + 3]);
                     if (p.HT) {
+                        // Transpose through shared memory: lane (row m) writes its 32 values down
+                        // a column of the warp's tile, then lane (column c0 + lane) writes the 32
+                        // rows of its column as 64 contiguous bytes.
+                        __nv_bfloat16* tile = reinterpret_cast<__nv_bfloat16*>(stage_t);
 #pragma unroll
                         for (int q = 0; q < 32; ++q)
-                            p.HT[size_t(c0 + q) * p.rows_ht + m] = __float2bfloat16(v[q]);
+                            tile[q * (kTransposeStride / 2) + lane] = valid ? __float2bfloat16(v[q]) : __float2bfloat16(0.f);
+                        __syncwarp();
+                        const int m0 = row0 + quarter * 32;
+                        const uint4* row = reinterpret_cast<const uint4*>(stage_t + lane * kTransposeStride);
+                        __nv_bfloat16* dst = p.HT + size_t(c0 + lane) * p.rows_ht + m0;
+                        if (m0 + 32 <= p.rows_ht) {
+#pragma unroll
+                            for (int q = 0; q < 4; ++q) reinterpret_cast<uint4*>(dst)[q] = row[q];
+                        } else {
+                            const __nv_bfloat16* src = reinterpret_cast<const __nv_bfloat16*>(row);
+                            for (int q = 0; m0 + q < p.rows_ht; ++q) dst[q] = src[q];
+                        }
+                        __syncwarp();
                     }
                 }
                 continue;
             }
+            if (!valid) continue;
 #pragma unroll
             for (int q = 0; q < 32; ++q) {
                 if (q >= width) break;
