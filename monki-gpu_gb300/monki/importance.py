@@ -21,8 +21,12 @@ from dataclasses import dataclass
 import numpy as np
 
 from .execution import native as _native
+from .guided import Guided
 
 FEATURES = 48
+# Guided transport under the learned weight window: Russian roulette below the cell's weight
+# W = roulette x scale[cell] (and splitting above split x W when split is set).
+LEARNED_GUIDE = Guided(0.0, 1.0, 0.0)
 PARAMETERS = 64 * 256 + 256 + 2 * (256 * 256 + 256) + 256 + 1
 
 

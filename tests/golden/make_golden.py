@@ -26,6 +26,10 @@ What each fixture pins, and where it comes from:
                          hdf5_reader.py): radiance, standard error and settings, the
                          Fortran preparer's optical depths, and the tables that
                          monki.preparation builds for the same run.
+  budget_moments.npz     The oracle's per-entry round moments (sums of tally / photons per
+                         column and of its square over 32 rounds) for the workloads at their
+                         own photon budgets and four config-3 scenes; the GPU parity test
+                         compares against them.
   comparator_verdicts.json
                          The reference's own check_result / compare / select_views
                          (python/monki/validation.py) on the seeded products and cases of
@@ -459,6 +463,78 @@ def archived_runs():
     return out
 
 
+# The workloads at their own photon budgets (32 rounds each), for the FP32 GPU parity test:
+# builder of monki.scenes, its arguments, and the oracle's seed (independent of the GPU's).
+# The layered cloud runs on a reduced 6 x 4 grid (its 20,000 photons per column on the full
+# grid would take the oracle half an hour here); config-3 scenes at a tenth of their budgets.
+BUDGETS = {
+    "clear_sky": ("clear_sky", (2000, 32), {}),
+    "layered_cloud": ("layered_cloud", (20000, 32), {"nx": 6, "ny": 4}),
+    "box_cloud": ("box_cloud", (2000, 32), {}),
+}
+BATCHED_SCALE = 0.005  # config-3 photon budgets scaled so every pick gets about 40 per column
+ORACLE_SEED = 1000003
+
+
+def batched_picks():
+    """Four config-3 scenes (seed, grid override): seed 93's draws on a 128 x 128 grid (the
+    workload's largest), and the first seeds of 0-199 with I only, with I/Q/U, and with a
+    grid under 32 x 32."""
+
+    sys.path.insert(0, str(REPO / "monki-gpu_gb300"))
+    import monki.scenes as scenes
+
+    shapes = {seed: scenes.batched_scene(seed, photons_scale=BATCHED_SCALE).shape for seed in range(200)}
+    nmat1 = next(s for s in shapes if shapes[s][0] == 1 and s != 93)
+    nmat3 = next(s for s in shapes if shapes[s][0] == 3 and s not in (93, nmat1))
+    small = next(s for s in shapes if shapes[s][1] * shapes[s][2] < 32 * 32 and s not in (93, nmat1, nmat3))
+    picks = {"largest": (93, (128, 128)), "nmat1": (nmat1, None), "nmat3": (nmat3, None), "small": (small, None)}
+    out = {}
+    for label, (seed, grid) in picks.items():
+        full = scenes.batched_scene(seed, grid=grid).photons_per_column
+        out[label] = (seed, grid, min(1.0, 40.0 / full))
+    return out
+
+
+def budget_moments():
+    """Per-entry round moments of the oracle at the workloads' own budgets: for every tally
+    entry (Stokes, and layer paths and weights when the scene has them) the sum over the
+    rounds of tally / photons per column and of its square; the per-round domain means of
+    the Stokes components (the convergence history); the scatters; the tables' SHA-256."""
+
+    import hashlib
+
+    sys.path.insert(0, str(REPO / "monki-gpu_gb300"))
+    sys.path.insert(0, str(REPO))
+    import monki.scenes as scenes
+    from oracle import oracle
+
+    specs = dict(BUDGETS)
+    for label, (seed, grid, scale) in batched_picks().items():
+        specs[f"batched_{label}"] = ("batched_scene", (seed,), {"photons_scale": scale, "grid": grid})
+    out = {}
+    for name, (builder, args, kwargs) in specs.items():
+        scene = getattr(scenes, builder)(*args, **kwargs)
+        rounds = 32
+        ppc = scene.photons_per_column
+        nmat, nx, ny, nz, angles = scene.shape
+        per_round = ppc * nx * ny
+        tallies, counters = oracle.run(scene.tables, [per_round * rounds, 0, 1, ORACLE_SEED, 100000, 0, per_round, rounds],
+                                       os.cpu_count() or 1)
+        x = tallies / ppc
+        stokes = np.stack([oracle.split(scene.tables, tallies[r])[0] for r in range(rounds)])
+        out[name] = {
+            "builder": np.array(builder), "args": np.array(json.dumps([list(args), kwargs])),
+            "rounds": np.array(rounds), "photons_per_column": np.array(ppc), "seed": np.array(ORACLE_SEED),
+            "sum": x.sum(0), "squares": (x * x).sum(0),
+            "history": stokes.sum(axis=(2, 3, 4)) / (nx * ny * angles) / ppc,
+            "scatters": np.array(counters["scatters"]),
+            "tables_sha256": np.array(hashlib.sha256(np.ascontiguousarray(scene.tables).tobytes()).hexdigest()),
+        }
+        print(name, scene.shape, ppc, counters["scatters"], flush=True)
+    return out
+
+
 def comparator_verdicts(ref):
     """The reference comparator's verdicts on the cases of comparator_cases.py."""
 
@@ -518,6 +594,10 @@ def main(names=()):
         np.savez_compressed(HERE / f"prepared_{name.replace('-', '_')}.npz", **arrays)
     for name, arrays in archived_runs().items() if want("archived") else ():
         np.savez_compressed(HERE / f"archived_{name}.npz", **arrays)
+    if want("budget_moments"):
+        np.savez_compressed(HERE / "budget_moments.npz",
+                            **{f"{name}.{key}": value for name, arrays in budget_moments().items()
+                               for key, value in arrays.items()})
     _forget_package()
     ref, Dataset = reference_package()
     if want("philox_kat"):
