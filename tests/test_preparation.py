@@ -72,6 +72,11 @@ def test_mie_table_is_read_and_normalized():
 
 @needs_fixtures
 def test_prepared_fixture_matches_the_kept_tables(oracle):
+    """A regression snapshot: the kept tables were made by this package's own preparer, so
+    this test only detects changes. The independent evidence for the preparer is
+    tests/test_archived.py, which finds the Fortran preparer's optical depths, altitudes and
+    layer thicknesses (stored in the reference's archived outputs) equal to this package's."""
+
     from monki import ReferenceCase
     from monki.preparation import prepare_reference_case
 
