@@ -169,6 +169,9 @@ size_t monki_cuda_multi_tally_count(void *handle, uint32_t scene);
 int monki_cuda_multi_run(void *handle, const uint32_t *controls, double *const *out, char *err, size_t errlen);
 /* scatters, free-path cell visits, detector cell visits, tally updates, photons, launches. */
 int monki_cuda_multi_counters(void *handle, uint64_t out[6]);
+/* One scene's totals over the session's runs: scatters, free-path cell visits, detector cell
+ * visits, tally updates, photons, tail launches. Nonzero for an unknown scene. */
+int monki_cuda_multi_scene_counters(void *handle, uint32_t scene, uint64_t out[6]);
 /* Milliseconds of the last run: transport, and transport plus the FP64 flush. */
 int monki_cuda_multi_last_timing(void *handle, float out[2]);
 void monki_cuda_multi_close(void *handle);

@@ -43,11 +43,14 @@ struct SceneEntry {
     Pool<T> P;          // the scene's pool segment, work lists and counts
     T* banks;           // rounds x shards x W.count
     WaveTally W;
+    unsigned long long* counters;  // the scene's scatters, cell visits, detector visits, tally updates
     uint32_t block0;    // first block (of 256 slots) of the segment in the launches
     uint32_t blocks;    // blocks of the segment
 };
 
 constexpr int kMultiBlock = 256;
+constexpr int kSceneCounters = 4;  // device counters per scene: scatters, cell visits, detector visits, tally updates
+constexpr int kSceneTotals = 6;    // host totals per scene: the four counters, photons, tail launches
 
 // The entry of this block's scene, copied into shared memory by the whole block.
 template <typename T>
@@ -95,26 +98,26 @@ __global__ void wf_reset_multi(const SceneEntry<T>* __restrict__ scenes, const u
 template <typename T, int NMAT>
 __global__ void __launch_bounds__(kMultiBlock, 4)
 wf_step_multi(const SceneEntry<T>* __restrict__ scenes, const uint16_t* __restrict__ block_scene, Guide<T> g,
-              uint32_t walk, uint32_t cur, uint32_t* __restrict__ failure, unsigned long long* __restrict__ counters) {
+              uint32_t walk, uint32_t cur, uint32_t* __restrict__ failure) {
     extern __shared__ __align__(16) unsigned char staged[];
     __shared__ __align__(16) SceneEntry<T> E;
     if (idle_block(scenes, block_scene, cur, 0, 4)) return;
     load_entry(E, scenes, block_scene);
     const T* band = stage_band<T>(E.s, staged, failure);
-    step_phase<T, NMAT, false, false>(E.s, band, E.ctl, E.dv, E.P, g, walk, cur, failure, counters, blockIdx.x - E.block0,
+    step_phase<T, NMAT, false, false>(E.s, band, E.ctl, E.dv, E.P, g, walk, cur, failure, E.counters, blockIdx.x - E.block0,
                                       E.blocks);
 }
 
 template <typename T, int NMAT>
 __global__ void __launch_bounds__(kMultiBlock, sizeof(T) == 4 ? 4 : 3)
 wf_peel_multi(const SceneEntry<T>* __restrict__ scenes, const uint16_t* __restrict__ block_scene, uint32_t b,
-              uint32_t* __restrict__ failure, unsigned long long* __restrict__ counters) {
+              uint32_t* __restrict__ failure) {
     extern __shared__ __align__(16) unsigned char staged[];
     __shared__ __align__(16) SceneEntry<T> E;
     if (idle_block(scenes, block_scene, b, 0, 2)) return;
     load_entry(E, scenes, block_scene);
     const T* band = stage_band<T>(E.s, staged, failure);
-    peel_phase<T, T, NMAT, false, false>(E.s, band, E.ctl, E.dv, E.P, E.banks, E.W, b, failure, counters,
+    peel_phase<T, T, NMAT, false, false>(E.s, band, E.ctl, E.dv, E.P, E.banks, E.W, b, failure, E.counters,
                                          blockIdx.x - E.block0, E.blocks);
 }
 
@@ -159,12 +162,12 @@ struct Multi {
     std::vector<Scene> scenes;
     std::vector<Group> groups;
     uint32_t* failure = nullptr;
-    unsigned long long* counters = nullptr;
+    unsigned long long* counters = nullptr;    // per scene: kSceneCounters of the current run
+    std::vector<uint64_t> scene_totals;        // per scene: its counters, photons and tail launches, summed over runs
     uint32_t* tail_next = nullptr;             // one counter per scene for its tail launch
     std::vector<cudaStream_t> tail_streams;    // the scenes' tails run side by side
     cudaEvent_t t0 = nullptr, t1 = nullptr, t2 = nullptr;
     uint64_t totals[6] = {0, 0, 0, 0, 0, 0};
-    uint64_t tails = 0;
     float last_kernel_ms = 0.f, last_run_ms = 0.f;
     std::string name;
 };
@@ -256,6 +259,7 @@ void lay_out(Multi& m, Group& g, const std::vector<Controls>& ctl) {
         P.counts = counts + q * kCountWords;
         E.banks = static_cast<T*>(sc.banks);
         E.W = sc.W;
+        E.counters = m.counters + size_t(id) * kSceneCounters;
         E.block0 = block;
         E.blocks = capacity / 256;
         for (uint32_t b = 0; b < E.blocks; ++b) g.host_block_scene[block + b] = uint16_t(q);
@@ -302,9 +306,9 @@ void batch(Multi& m, Group& g, cudaStream_t stream, cudaGraph_t graph) {
         }
         uint32_t walk = m.cfg.walk;
         void* step_args[] = {const_cast<const SceneEntry<T>**>(&entries), const_cast<const uint16_t**>(&block_scene),
-                             const_cast<Guide<T>*>(&guide), &walk, &cur, &m.failure, &m.counters};
+                             const_cast<Guide<T>*>(&guide), &walk, &cur, &m.failure};
         void* peel_args[] = {const_cast<const SceneEntry<T>**>(&entries), const_cast<const uint16_t**>(&block_scene), &out,
-                             &m.failure, &m.counters};
+                             &m.failure};
         const void* fns[2] = {reinterpret_cast<const void*>(&wf_step_multi<T, NMAT>),
                               reinterpret_cast<const void*>(&wf_peel_multi<T, NMAT>)};
         void** args[2] = {step_args, peel_args};
@@ -407,10 +411,10 @@ void run(Multi& m, const std::vector<Controls>& ctl) {
                     const SceneEntry<T>& E = host[q];
                     cudaStream_t t = m.tail_streams[used++ % m.tail_streams.size()];
                     const unsigned blocks = unsigned(std::max<uint64_t>(1, (live + 255) / 256));
-                    check(launch_tail<T>(E.s, E.ctl, E.dv, E.P, E.banks, E.W, guide, 0u, true, m.failure, m.counters,
+                    check(launch_tail<T>(E.s, E.ctl, E.dv, E.P, E.banks, E.W, guide, 0u, true, m.failure, E.counters,
                                          m.tail_next + g.members[q], t, blocks), "tail launch");
                     launches += 2;
-                    m.tails += 1;
+                    m.scene_totals[size_t(g.members[q]) * kSceneTotals + 5] += 1;
                 }
                 for (size_t k = 0; k < std::min(used, m.tail_streams.size()); ++k)
                     check(cudaStreamSynchronize(m.tail_streams[k]), "tail");
@@ -532,7 +536,9 @@ void* monki_cuda_multi_create(uint32_t device, uint32_t scenes, const double* co
             check(cudaStreamSynchronize(stream), "upload(flush info)");
         }
         check(cudaMalloc(&m->failure, sizeof(uint32_t)), "cudaMalloc(failure)");
-        check(cudaMalloc(&m->counters, 4 * sizeof(unsigned long long)), "cudaMalloc(counters)");
+        check(cudaMalloc(&m->counters, m->scenes.size() * kSceneCounters * sizeof(unsigned long long)),
+              "cudaMalloc(counters)");
+        m->scene_totals.assign(m->scenes.size() * kSceneTotals, 0);
         check(cudaMalloc(&m->tail_next, m->scenes.size() * sizeof(uint32_t)), "cudaMalloc(tail)");
         m->tail_streams.resize(8);
         for (cudaStream_t& t : m->tail_streams) check(cudaStreamCreateWithFlags(&t, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -569,7 +575,8 @@ int monki_cuda_multi_run(void* handle, const uint32_t* controls, double* const* 
         check(cudaSetDevice(m->device), "cudaSetDevice");
         cudaStream_t first = m->groups.front().stream;
         check(cudaMemsetAsync(m->failure, 0, sizeof(uint32_t), first), "memset(failure)");
-        check(cudaMemsetAsync(m->counters, 0, 4 * sizeof(unsigned long long), first), "memset(counters)");
+        const size_t counter_bytes = m->scenes.size() * kSceneCounters * sizeof(unsigned long long);
+        check(cudaMemsetAsync(m->counters, 0, counter_bytes, first), "memset(counters)");
         check(cudaEventRecord(m->t0, first), "event");
         // Every group's stream starts after the clears above.
         for (Group& g : m->groups)
@@ -580,9 +587,9 @@ int monki_cuda_multi_run(void* handle, const uint32_t* controls, double* const* 
         if (m->cfg.fp64) flush<double>(*m, ctl, first); else flush<float>(*m, ctl, first);
         check(cudaEventRecord(m->t2, first), "event");
         uint32_t flag = 0;
-        unsigned long long cnt[4] = {0, 0, 0, 0};
+        std::vector<unsigned long long> cnt(m->scenes.size() * kSceneCounters, 0ull);
         check(cudaMemcpyAsync(&flag, m->failure, sizeof(flag), cudaMemcpyDeviceToHost, first), "copy(failure)");
-        check(cudaMemcpyAsync(cnt, m->counters, sizeof(cnt), cudaMemcpyDeviceToHost, first), "copy(counters)");
+        check(cudaMemcpyAsync(cnt.data(), m->counters, counter_bytes, cudaMemcpyDeviceToHost, first), "copy(counters)");
         check(cudaStreamSynchronize(first), "flush");
         if (flag) {
             char msg[128];
@@ -595,8 +602,15 @@ int monki_cuda_multi_run(void* handle, const uint32_t* controls, double* const* 
         check(cudaStreamSynchronize(first), "copy(tallies)");
         check(cudaEventElapsedTime(&m->last_kernel_ms, m->t0, m->t1), "elapsed");
         check(cudaEventElapsedTime(&m->last_run_ms, m->t0, m->t2), "elapsed");
-        for (int q = 0; q < 4; ++q) m->totals[q] += cnt[q];
-        for (const Controls& c : ctl) m->totals[4] += c.count;
+        for (size_t q = 0; q < m->scenes.size(); ++q) {
+            uint64_t* t = m->scene_totals.data() + q * kSceneTotals;
+            for (int k = 0; k < kSceneCounters; ++k) {
+                t[k] += cnt[q * kSceneCounters + size_t(k)];
+                m->totals[k] += cnt[q * kSceneCounters + size_t(k)];
+            }
+            t[4] += ctl[q].count;
+            m->totals[4] += ctl[q].count;
+        }
         m->totals[5] += m->scenes.size();  // the flushes
         return 0;
     } catch (const std::exception& e) {
@@ -609,6 +623,13 @@ int monki_cuda_multi_counters(void* handle, uint64_t out[6]) {
     if (!handle || !out) return 1;
     Multi* m = static_cast<Multi*>(handle);
     for (int q = 0; q < 6; ++q) out[q] = m->totals[q];
+    return 0;
+}
+
+int monki_cuda_multi_scene_counters(void* handle, uint32_t scene, uint64_t out[6]) {
+    Multi* m = static_cast<Multi*>(handle);
+    if (!m || !out || scene >= m->scenes.size()) return 1;
+    for (int k = 0; k < kSceneTotals; ++k) out[k] = m->scene_totals[size_t(scene) * kSceneTotals + size_t(k)];
     return 0;
 }
 

@@ -34,7 +34,7 @@ def run_scene(scene, *, device: int = 0, seed: int = 23274, rounds: int = 1, opt
 
 def run_persistent(scenes, *, device: int = 0, seed: int = 23274, rounds: int = 1, precision: str = "fp32",
                    pool: int = 1 << 21, walk: int = 24, check_every: int = 8, graphs: bool = True,
-                   max_steps: int = 100_000, library=None):
+                   max_steps: int = 100_000, tail: int = 1 << 16, library=None):
     """Every scene in one multi-scene session: returns (per-scene (batches, provenance),
     summary). Scenes are forward, without layer paths, with I or I/Q/U."""
 
@@ -47,7 +47,8 @@ def run_persistent(scenes, *, device: int = 0, seed: int = 23274, rounds: int = 
     n = len(tables)
     pointers = (_native.F64P * n)(*[t.ctypes.data_as(_native.F64P) for t in tables])
     counts = (ctypes.c_size_t * n)(*[t.size for t in tables])
-    config = f"precision={precision},pool={pool},walk={walk},check_every={check_every},graphs={int(graphs)}"
+    config = (f"precision={precision},pool={pool},walk={walk},check_every={check_every},graphs={int(graphs)},"
+              f"tail={int(tail)}")
     error = ctypes.create_string_buffer(8192)
     handle = native.monki_cuda_multi_create(device, n, pointers, counts, rounds, config.encode(), error, len(error))
     if not handle:
@@ -69,19 +70,25 @@ def run_persistent(scenes, *, device: int = 0, seed: int = 23274, rounds: int = 
         timing = (ctypes.c_float * 2)()
         native.monki_cuda_multi_counters(handle, totals)
         native.monki_cuda_multi_last_timing(handle, timing)
+        per_scene = []
+        for q in range(n):
+            counts = (ctypes.c_uint64 * 6)()
+            native.monki_cuda_multi_scene_counters(handle, q, counts)
+            per_scene.append([int(v) for v in counts])
     finally:
         native.monki_cuda_multi_close(handle)
     results = []
-    for scene, values in zip(scenes, outputs, strict=True):
+    for scene, values, counts in zip(scenes, outputs, per_scene, strict=True):
         nmat, nx, ny, nz, angles = scene.shape
         per = values.reshape(rounds, -1)
         batches = [RawTallies(BatchControls(r + 1, scene.photons_per_column),
                               per[r].reshape((nmat, nx, ny, angles), order="F").copy()) for r in range(rounds)]
-        results.append((batches, {"backend": "cuda-multi-scene", "precision": precision, "seed": seed}))
+        results.append((batches, {"backend": "cuda-multi-scene", "precision": precision, "seed": seed,
+                                  "scatters": counts[0], "photons": counts[4], "tail_launches": counts[5]}))
     summary = {"scenes": n, "wall_s": wall, "device_s": timing[1] / 1e3, "scatters": int(totals[0]),
                "photons": int(totals[4]), "scatters_per_s": totals[0] / wall,
                "device_scatters_per_s": totals[0] / max(timing[1] / 1e3, 1e-9), "kernel_launches": int(totals[5]),
-               "persistent": True, "pool": pool}
+               "tails": sum(c[5] for c in per_scene), "persistent": True, "pool": pool}
     return results, summary
 
 

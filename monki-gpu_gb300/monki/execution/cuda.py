@@ -62,6 +62,7 @@ class CUDA(Backend):
         device_statistics: bool = True,
         orders: bool = False,
         rectangles: bool = True,
+        tail: int = 1 << 16,
         monki_home=None,
         library=None,
     ):
@@ -72,6 +73,7 @@ class CUDA(Backend):
             ("photons_per_dispatch", photons_per_dispatch, 1, 2**31 - 1),
             ("max_steps", max_steps, 1, 10_000_000),
             ("block", block, 32, 256),
+            ("tail", tail, 0, 1 << 26),
         ):
             if type(value) is not int or not minimum <= value <= maximum:
                 raise ValueError(f"{name} must be an integer in [{minimum}, {maximum}]")
@@ -138,6 +140,9 @@ class CUDA(Backend):
         # varying layer in one step (the same path in exact arithmetic as the face-by-face
         # walk); False keeps the face-by-face walk.
         self.rectangles = rectangles
+        # A round group's last photons (at most this many, every photon claimed) run to their
+        # ends in one tail launch; 0 keeps the wavefront launches to the end.
+        self.tail = tail
         self.monki_home = monki_home
         # Per-cell roulette scale (nx, ny, nz) applied at every prepare; set_roulette_scale
         # changes it for the prepared session only.
@@ -214,7 +219,7 @@ class CUDA(Backend):
         error = ctypes.create_string_buffer(8192)
         config = (
             f"precision={self.precision},shards={self.tally_shards},block={self.block},"
-            f"engine={self.engine},pool={self.pool},walk={self.walk}"
+            f"engine={self.engine},pool={self.pool},walk={self.walk},tail={self.tail}"
             + (self.guided.config() if self.guided is not None else "")
             + (",importance=1" if self.importance_tally else "")
             + (",orders=1" if self.orders else "")
@@ -523,6 +528,7 @@ class CUDA(Backend):
             self.walk,
             self.orders,
             self.rectangles,
+            self.tail,
             self.guided,
             self.importance_tally,
         )

@@ -102,6 +102,7 @@ _SIGNATURES = {
         [ctypes.c_void_p, _U32P, ctypes.POINTER(_F64P), ctypes.c_char_p, ctypes.c_size_t],
     ),
     "monki_cuda_multi_counters": (ctypes.c_int, [ctypes.c_void_p, _U64P]),
+    "monki_cuda_multi_scene_counters": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, _U64P]),
     "monki_cuda_multi_last_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]),
     "monki_cuda_multi_close": (None, [ctypes.c_void_p]),
     "monki_cuda_probe_philox": (

@@ -363,12 +363,32 @@ def objective_weights(batches, photons_per_column: int, power: float = 2.0):
 # ------------------------------------------------------------------------------------
 # Training set, training and evaluation.
 # ------------------------------------------------------------------------------------
-def training_rows(scene, *, device: int = 0, rounds: int = 2, photons_per_column: int = 300, seed: int = 7,
-                  limit: int = 40000, rng=None):
-    """(features, target, weight) of the cells of one scene with enough pilot events, at
-    most ``limit`` of them (drawn at random)."""
+def relative_weights(batches, photons_per_column: int, low: float = 0.1, high: float = 10.0):
+    """Per-pixel weights (nx, ny, angles) for a target on the relative error of every pixel
+    and view: the domain-mean intensity over the pixel's own, clipped to [low, high], so a
+    unit of a dark pixel's intensity counts as much as the same fraction of a bright one."""
 
-    tally, _ = pilot(scene, device=device, rounds=rounds, photons_per_column=photons_per_column, seed=seed)
+    intensity = np.mean([b.stokes[0] for b in batches], axis=0) / photons_per_column
+    mean = float(np.mean(np.abs(intensity)))
+    ratio = np.divide(mean, np.abs(intensity), out=np.full_like(intensity, high), where=np.abs(intensity) > 0)
+    return np.clip(ratio, low, high)
+
+
+def training_rows(scene, *, device: int = 0, rounds: int = 2, photons_per_column: int = 300, seed: int = 7,
+                  limit: int = 40000, rng=None, objective: str = "relative"):
+    """(features, target, weight) of the cells of one scene with enough pilot events, at
+    most ``limit`` of them (drawn at random). ``objective`` "relative": contributions are
+    weighted per pixel by ``relative_weights`` of a one-round analog pre-pilot (the target
+    is every pixel's relative error); "total": unweighted (the summed intensity)."""
+
+    if objective not in ("relative", "total"):
+        raise ValueError("objective must be 'relative' or 'total'")
+    weights = None
+    if objective == "relative":
+        _, first = pilot(scene, device=device, rounds=1, photons_per_column=photons_per_column, seed=seed + 1)
+        weights = relative_weights(first, photons_per_column)
+    tally, _ = pilot(scene, device=device, rounds=rounds, photons_per_column=photons_per_column, seed=seed,
+                     pixel_weights=weights)
     target, weight = importance_targets(tally)
     keep = np.flatnonzero(weight > 0)
     if keep.size > limit:
@@ -401,12 +421,13 @@ def training_scenes(count: int = 24):
 
 
 def train_model(training, *, device: int = 0, steps: int = 3000, batch: int = 65536, learning_rate: float = 1e-3,
-                photons_per_column: int = 300, rows_per_scene: int = 20000, seed: int = 1):
+                photons_per_column: int = 300, rows_per_scene: int = 20000, seed: int = 1, objective: str = "relative"):
     """Pilot every training scene, then train a network on the device. Returns
     (model, per-step losses, training rows)."""
 
     rng = np.random.default_rng(seed)
-    parts = [training_rows(scene, device=device, photons_per_column=photons_per_column, limit=rows_per_scene, rng=rng)
+    parts = [training_rows(scene, device=device, photons_per_column=photons_per_column, limit=rows_per_scene, rng=rng,
+                           objective=objective)
              for scene in training]
     x = np.concatenate([p[0] for p in parts])
     t = np.concatenate([p[1] for p in parts])

@@ -496,13 +496,24 @@ def batched_picks():
     return out
 
 
+def table_fingerprint(tables):
+    """Sums and an evenly strided sample (at most 4,096 entries, the header included) of a
+    scene's tables. The scene builders call numpy's exp, log and trigonometry, whose last
+    bits differ between x86 and Arm builds, so a consumer compares these within a relative
+    1e-10 rather than byte for byte."""
+
+    t = np.asarray(tables, dtype=np.float64)
+    stride = max(1, -(-t.size // 4096))
+    return {"tables_size": np.array(t.size), "tables_sums": np.array([t.sum(), np.abs(t).sum(), (t * t).sum()]),
+            "tables_head": t[:16].copy(), "tables_sample": t[::stride].copy()}
+
+
 def budget_moments():
     """Per-entry round moments of the oracle at the workloads' own budgets: for every tally
     entry (Stokes, and layer paths and weights when the scene has them) the sum over the
     rounds of tally / photons per column and of its square; the per-round domain means of
-    the Stokes components (the convergence history); the scatters; the tables' SHA-256."""
-
-    import hashlib
+    the Stokes components (the convergence history); the scatters; a fingerprint of the
+    tables (table_fingerprint)."""
 
     sys.path.insert(0, str(REPO / "monki-gpu_gb300"))
     sys.path.insert(0, str(REPO))
@@ -529,7 +540,7 @@ def budget_moments():
             "sum": x.sum(0), "squares": (x * x).sum(0),
             "history": stokes.sum(axis=(2, 3, 4)) / (nx * ny * angles) / ppc,
             "scatters": np.array(counters["scatters"]),
-            "tables_sha256": np.array(hashlib.sha256(np.ascontiguousarray(scene.tables).tobytes()).hexdigest()),
+            **table_fingerprint(scene.tables),
         }
         print(name, scene.shape, ppc, counters["scatters"], flush=True)
     return out

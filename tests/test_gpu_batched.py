@@ -57,41 +57,67 @@ def test_batched_scenes_equal_scenes_run_alone(device):
         np.testing.assert_allclose(_flat(batches), _flat(alone), rtol=1e-9, atol=1e-15)
 
 
-@pytest.mark.parametrize("graphs", [True, False])
-def test_persistent_scenes_equal_scenes_run_alone(device, graphs):
-    """Seven uneven scenes (grids 8-128 columns a side, I and I/Q/U, 20-60 layers) in one
-    multi-scene session, FP64, two rounds each: every scene's tallies and scatter count
-    equal the scene run alone in its own session (same seed)."""
-
+def _persistent_batch():
     import monki.scenes as scenes
-    from monki.batched import run_persistent, run_scene
 
     batch = [scenes.batched_scene(seed, photons_scale=0.002) for seed in (0, 1, 2, 5, 11, 17)]
     batch.append(scenes.batched_scene(93, photons_scale=0.0005, grid=(128, 128)))
     assert {s.shape[0] for s in batch} == {1, 3}
-    results, summary = run_persistent(batch, rounds=2, precision="fp64", pool=1 << 18, graphs=graphs)
+    return batch
+
+
+@pytest.mark.parametrize("graphs", [True, False])
+def test_persistent_scenes_equal_scenes_run_alone(device, graphs):
+    """Seven uneven scenes (grids 8-128 columns a side, I and I/Q/U, 20-60 layers) in one
+    multi-scene session, FP64, two rounds each, wavefront launches to the end (no tail
+    kernel): every scene's tallies and scatter count equal the scene run alone in its own
+    session (same seed)."""
+
+    from monki.batched import run_persistent, run_scene
+
+    batch = _persistent_batch()
+    results, summary = run_persistent(batch, rounds=2, precision="fp64", pool=1 << 18, graphs=graphs, tail=0)
     assert summary["scenes"] == len(batch) and summary["scatters"] > 0
     scatters = 0
-    for scene, (batches, _) in zip(batch, results, strict=True):
-        alone, provenance = run_scene(scene, rounds=2, options={"precision": "fp64"})
-        scatters += provenance["scatters"]
+    for scene, (batches, provenance) in zip(batch, results, strict=True):
+        alone, alone_provenance = run_scene(scene, rounds=2, options={"precision": "fp64", "tail": 0})
+        assert provenance["scatters"] == alone_provenance["scatters"]
+        scatters += alone_provenance["scatters"]
         np.testing.assert_allclose(_flat(batches), _flat(alone), rtol=1e-9, atol=1e-15)
     assert summary["scatters"] == scatters
 
 
+def test_persistent_tail_launches_match_scenes_run_alone(device):
+    """The same scenes with tail launches (each scene's last photons in its own launch, once
+    the group's photons are all claimed): equal scatter counts and FP64 tallies within the
+    tolerance of the single-scene tail test. The tail kernel inlines the same slot
+    functions as the wavefront kernels, but the compiler may contract their arithmetic
+    differently, and a scene's tail starts at another iteration than when it runs alone."""
+
+    from monki.batched import run_persistent, run_scene
+
+    batch = _persistent_batch()
+    results, summary = run_persistent(batch, rounds=2, precision="fp64", pool=1 << 18, tail=1 << 12)
+    assert summary["tails"] > 0
+    for scene, (batches, provenance) in zip(batch, results, strict=True):
+        alone, alone_provenance = run_scene(scene, rounds=2, options={"precision": "fp64", "tail": 1 << 12})
+        assert provenance["scatters"] == alone_provenance["scatters"]
+        np.testing.assert_allclose(_flat(batches), _flat(alone), rtol=1e-6, atol=1e-12)
+
+
 def test_persistent_fp32_scenes_agree_with_scenes_run_alone(device):
-    """The FP32 product path of the multi-scene session: the same scatters as the scenes run
-    alone (the histories do not depend on the launch layout), tallies equal to FP32
-    summation order."""
+    """The FP32 product path of the multi-scene session (wavefront launches to the end in
+    both): the same scatters as the scenes run alone (the histories do not depend on the
+    launch layout), tallies equal to FP32 summation order."""
 
     import monki.scenes as scenes
     from monki.batched import run_persistent, run_scene
 
     batch = [scenes.batched_scene(seed, photons_scale=0.01) for seed in (3, 4, 6, 7)]
-    results, summary = run_persistent(batch, rounds=1)
+    results, summary = run_persistent(batch, rounds=1, tail=0)
     scatters = 0
     for scene, (batches, _) in zip(batch, results, strict=True):
-        alone, provenance = run_scene(scene)
+        alone, provenance = run_scene(scene, options={"tail": 0})
         scatters += provenance["scatters"]
         np.testing.assert_allclose(_flat(batches), _flat(alone), rtol=2e-4, atol=1e-7 * np.abs(_flat(alone)).max())
     assert summary["scatters"] == scatters

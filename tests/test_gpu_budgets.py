@@ -15,7 +15,6 @@ standard errors) accepts the GPU product of simulate() against the oracle's.
 
 from __future__ import annotations
 
-import hashlib
 import json
 from pathlib import Path
 
@@ -42,8 +41,15 @@ def _scene(m):
     args, kwargs = json.loads(str(m["args"]))
     kwargs = {k: (tuple(v) if isinstance(v, list) else v) for k, v in kwargs.items()}
     scene = getattr(scenes, str(m["builder"]))(*args, **kwargs)
-    digest = hashlib.sha256(np.ascontiguousarray(scene.tables).tobytes()).hexdigest()
-    assert digest == str(m["tables_sha256"]), "the scene builder no longer makes the fixture's tables"
+    # The builder still makes the fixture's tables (up to the last bits of numpy's
+    # transcendental functions, which differ between x86 and Arm).
+    t = np.asarray(scene.tables, dtype=np.float64)
+    assert t.size == int(m["tables_size"]), "the scene builder no longer makes the fixture's tables"
+    np.testing.assert_array_equal(t[:8], m["tables_head"][:8])  # version, grid and list sizes
+    np.testing.assert_allclose(t[:16], m["tables_head"], rtol=1e-10)
+    stride = max(1, -(-t.size // 4096))
+    np.testing.assert_allclose(t[::stride], m["tables_sample"], rtol=1e-10, atol=1e-300)
+    np.testing.assert_allclose([t.sum(), np.abs(t).sum(), (t * t).sum()], m["tables_sums"], rtol=1e-10)
     return scene
 
 
