@@ -414,6 +414,7 @@ SceneView<T> make_view(const Prepared& p, const Packed<T>& k, void* base) {
     s.xinv = T(1) / s.xunit; s.yinv = T(1) / s.yunit;
     const double th0 = kDegToRad * p.vartheta0, ph0 = kDegToRad * p.phi0;
     s.a0 = T(std::sin(th0) * std::cos(ph0)); s.b0 = T(std::sin(th0) * std::sin(ph0)); s.c0 = T(std::cos(th0));
+    s.inv_mu0 = T(1) / std::fabs(s.c0);  // the flush's 1 / |mu0|, from the same rounded cosine
     s.phi0 = T(ph0);
     for (int ia = 0; ia < p.angles; ++ia) {
         double th = kDegToRad * p.vartheta[ia], ph = kDegToRad * p.vphi[ia];

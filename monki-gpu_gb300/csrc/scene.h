@@ -57,6 +57,7 @@ struct SceneView {
     T xunit, yunit, depol;
     T xinv, yinv;        // 1 / xunit, 1 / yunit
     T a0, b0, c0, phi0;  // solar propagation direction cosines and azimuth (rad)
+    T inv_mu0;           // 1 / |c0|
     T va[kMaxViews], vb[kMaxViews], vc[kMaxViews], vphi[kMaxViews];
     T vsin[kMaxViews];          // sqrt(max(eps, 1 - vc^2))
     T vcos_phi[kMaxViews], vsin_phi[kMaxViews];  // cos / sin of the view azimuth

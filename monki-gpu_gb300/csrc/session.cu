@@ -577,13 +577,15 @@ void* monki_cuda_create(uint32_t device, const double* tables, size_t table_coun
         const uint32_t pixels = uint32_t(p.nx * p.ny * p.angles);
         WaveTally& W = s->wave;
         W.pixels = pixels;
-        W.layers = p.paths ? pixels * uint32_t(p.nz + 1) * 4u : 0u;
+        W.span = (uint32_t(p.nz) + 4u) & ~3u;  // nz + 1 rounded up to a multiple of 4
+        W.layers = p.paths ? pixels * 2u * W.span : 0u;
         W.count = 4u * pixels + W.layers;
         W.locations = uint32_t(p.nx * p.ny * p.nz * p.angles);
         W.orders = cfg.orders ? W.count : 0u;
         if (cfg.orders) W.count += 4u * (pixels + 2u * W.locations);
         W.vee = p.nmat == 4 ? W.count : 0u;
         if (p.nmat == 4) W.count += pixels;
+        W.count = (W.count + 3u) & ~3u;  // every shard's records start 16-byte aligned (vector atomics)
         W.shards = cfg.shards;
         const size_t elem = cfg.fp64 ? sizeof(double) : sizeof(float);
         const size_t per_round = cfg.wavefront ? W.count : L.count;

@@ -74,12 +74,22 @@ struct Divisors { FastDiv per_round, nx, ny, ncol; };
 
 // Device tally layout of one round and one shard (element counts of TA):
 //   pixel records  [pixel]                  {I, Q, U, detected weight}
-//   layer records  [pixel * (nz + 1) + k]   {layer path, view-ray weight, first-event weight,
-//                                            difference array of straight-run weight / |cos|}
-//   (record k = nz holds the first-event weight of histories that met the surface first)
+//   layer records  [pixel * 2 * span + k]   path pieces tallied per layer: the wander, the
+//                                           partial view ray and the partial initial descent
+//                  [pixel * 2 * span + span + k]
+//                                           difference array of the straight paths per unit
+//                                           layer thickness: +w / mu_view above the event layer,
+//                                           +w / |mu0| above the first-event layer (from layer 0
+//                                           when the surface came first), and each straight run
+//                                           of whole layers, +w / |cos| from its first layer and
+//                                           -w / |cos| past its last
+//   span = nz + 1 rounded up to a multiple of 4, so one 128-bit atomic covers four layers
+//   (L2 atomics cost per request, not per byte); element nz of the path array holds
+//   w / mu_view of events in the top layer, whose view rays cross no whole layer.
 struct WaveTally {
     uint32_t pixels;   // nx * ny * angles
-    uint32_t layers;   // pixels * (nz + 1) * 4 when paths are tallied, else 0
+    uint32_t span;     // per-pixel length of each layer array: nz + 1 rounded up to a multiple of 4
+    uint32_t layers;   // pixels * 2 * span when paths are tallied, else 0
     uint32_t count;    // 4 * pixels + layers (+ the order records)
     uint32_t shards;
     // Scattering-order diagnostics (0 = off): element offset of the single-scattering
@@ -101,6 +111,12 @@ struct SplitCopy {
     Quad<T> pos, dir, pol;
     uint4 extra;
 };
+
+// Resident blocks of 256 per SM the fused step kernel is built for (its register budget,
+// 65536 / (256 x blocks)); a build option for measuring the trade of occupancy for spills.
+#ifndef MONKI_STEP_BLOCKS
+#define MONKI_STEP_BLOCKS 4
+#endif
 
 constexpr uint32_t kListCounts = 8;   // counts per work-list buffer
 constexpr uint32_t kClaimCount = 16;  // index of the claim counter
@@ -799,7 +815,7 @@ __device__ __forceinline__ void peel_event(uint32_t slot, bool surface, const Sc
     const uint32_t round_offset = dv.per_round.div(pid);
     TA* bank = banks + (size_t(round_offset) * L.shards + shard) * L.count;
     Quad<TA>* pixrec = reinterpret_cast<Quad<TA>*>(bank);
-    Quad<TA>* layrec = reinterpret_cast<Quad<TA>*>(bank + 4 * size_t(L.pixels));
+    TA* const layer_base = bank + 4 * size_t(L.pixels);
     const T* wander = PATHS ? P.wander + size_t(slot) * s.nz : nullptr;
     const T sin_c = sqrt(fmax(eps, T(1) - c * c));
     T sphi, cphi;
@@ -927,37 +943,69 @@ __device__ __forceinline__ void peel_event(uint32_t slot, bool surface, const Sc
         if (NMAT > 3 && q3 != T(0)) atomicAdd(bank + L.vee + pixel, TA(q3));
         ++updates;
         if (PATHS) {
-            Quad<TA>* rec = layrec + size_t(pixel) * (s.nz + 1);
-            // Layers touched: the wander range, the event layer k (partial view ray and
-            // the view prefix weight), and the first-event layer k1 (partial descent and
-            // the descent prefix weight; record nz when the surface came first).
+            TA* const path = layer_base + size_t(pixel) * 2 * L.span;
+            TA* const diff = path + L.span;
+            // Path pieces, four layers per request: the wander range, the event layer k (the
+            // partial view ray) and the first-event layer k1 (the partial descent).
             int lo = k, hi = k;
             if (wmin <= wmax) { lo = min(lo, wmin); hi = max(hi, wmax); }
             if (k1 >= 0) { lo = min(lo, k1); hi = max(hi, k1); }
             const T init_piece = k1 >= 0 ? w * pol.w : T(0);
-            for (int kk = lo; kk <= hi; ++kk) {
-                T px = (kk >= wmin && kk <= wmax) ? w * wander[kk] : T(0);
-                T py = T(0), pz = T(0);
-                if (kk == k) { px += w * z_old * ci; py = w; }
-                if (kk == k1) { px += init_piece; pz = w; }
-                if (px != T(0) || py != T(0) || pz != T(0)) {
-                    quad_add(rec + kk, TA(px), TA(py), TA(pz), TA(0));
+            for (int g = lo & ~3; g <= hi; g += 4) {
+                T v[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int kk = g + q;
+                    T x = (kk >= wmin && kk <= wmax) ? w * wander[kk] : T(0);
+                    if (kk == k) x += w * z_old * ci;
+                    if (kk == k1) x += init_piece;
+                    v[q] = x;
+                }
+                if (v[0] != T(0) || v[1] != T(0) || v[2] != T(0) || v[3] != T(0)) {
+                    quad_add(reinterpret_cast<Quad<TA>*>(path + g), TA(v[0]), TA(v[1]), TA(v[2]), TA(v[3]));
                     ++updates;
                 }
             }
-            if (k1 < 0) {
-                quad_add(rec + s.nz, TA(0), TA(0), TA(w), TA(0));
-                ++updates;
-            }
-            // Straight runs of whole layers: +w/|cos| from the first layer, -w/|cos| past the last.
+            // Straight paths into the difference array: the view ray above the event layer
+            // (events in the top layer leave w / mu_view in path element nz instead), the
+            // initial descent above the first-event layer, the straight runs; one request
+            // per four-layer group touched. Fixed slots (-1 = none) keep them in registers.
             const uint32_t runs = P.runs[slot];
+            int at[6];
+            T val[6];
+            at[0] = k + 1 < s.nz ? k + 1 : -1;
+            val[0] = w * ci;
+            if (at[0] < 0) { atomicAdd(path + s.nz, TA(val[0])); ++updates; }
+            at[1] = k1 >= 0 ? k1 + 1 : 0;
+            val[1] = w * s.inv_mu0;
+#pragma unroll
             for (int r = 0; r < 2; ++r) {
                 const uint32_t lh = (runs >> (16 * r)) & 0xFFFFu;
-                if ((lh & 0xFFu) == 0xFFu) continue;
-                const T v = w * P.run_ci[2 * size_t(slot) + r];
-                quad_add(rec + (lh & 0xFFu), TA(0), TA(0), TA(0), TA(v));
-                quad_add(rec + (lh >> 8) + 1, TA(0), TA(0), TA(0), TA(-v));
-                updates += 2;
+                const bool run = (lh & 0xFFu) != 0xFFu;
+                const T v = run ? w * P.run_ci[2 * size_t(slot) + r] : T(0);
+                at[2 + 2 * r] = run ? int(lh & 0xFFu) : -1;
+                at[3 + 2 * r] = run ? int(lh >> 8) + 1 : -1;
+                val[2 + 2 * r] = v;
+                val[3 + 2 * r] = -v;
+            }
+            uint32_t done = 0u;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                if (at[q] < 0 || ((done >> q) & 1u)) continue;
+                const int g = at[q] & ~3;
+                T v0 = T(0), v1 = T(0), v2 = T(0), v3 = T(0);
+#pragma unroll
+                for (int r = q; r < 6; ++r) {
+                    if (at[r] < 0 || ((done >> r) & 1u) || (at[r] & ~3) != g) continue;
+                    const int j = at[r] - g;
+                    v0 += j == 0 ? val[r] : T(0);
+                    v1 += j == 1 ? val[r] : T(0);
+                    v2 += j == 2 ? val[r] : T(0);
+                    v3 += j == 3 ? val[r] : T(0);
+                    done |= 1u << r;
+                }
+                quad_add(reinterpret_cast<Quad<TA>*>(diff + g), TA(v0), TA(v1), TA(v2), TA(v3));
+                ++updates;
             }
         }
     }
@@ -1310,7 +1358,7 @@ __device__ __forceinline__ void step_phase(const SceneView<T>& s, const T* band,
 }
 
 template <typename T, int NMAT, bool PATHS, bool BACKWARD>
-__global__ void __launch_bounds__(256, 4)
+__global__ void __launch_bounds__(256, MONKI_STEP_BLOCKS)
 wf_step(SceneView<T> s, Controls ctl, Divisors dv, Pool<T> P, Guide<T> g, uint32_t walk, uint32_t cur,
         uint32_t* __restrict__ failure, unsigned long long* __restrict__ counters) {
     extern __shared__ __align__(16) unsigned char staged[];
@@ -1464,19 +1512,15 @@ __global__ void wf_flush(const TA* __restrict__ banks, WaveTally L, int nmat, in
             const int k = int(t % nz);
             const uint32_t ia = t / nz;
             const uint32_t pixel = i + nx * (j + ny * ia);
-            const size_t rec = 4 * size_t(pixels) + size_t(pixel) * (nz + 1) * 4;
-            value = sum(rec + size_t(k) * 4);
-            double first = sum(rec + size_t(nz) * 4 + 2);
-            for (int s = 0; s < k; ++s) first += sum(rec + size_t(s) * 4 + 2);
-            value += zunit[k] * inv_mu0 * first;
-            double runs = 0.0;
-            for (int s = 0; s <= k; ++s) runs += sum(rec + size_t(s) * 4 + 3);
-            value += zunit[k] * runs;
-            if (k < nz - 1) {
-                double view = 0.0;
-                for (int s = 0; s < k; ++s) view += sum(rec + size_t(s) * 4 + 1);
-                value += zunit[k] * inv_mu[ia] * view;
-            }
+            const size_t path = 4 * size_t(pixels) + size_t(pixel) * 2 * L.span;
+            const size_t diff = path + L.span;
+            value = sum(path + size_t(k));
+            double straight = 0.0;
+            for (int s = 0; s <= k; ++s) straight += sum(diff + size_t(s));
+            // View rays cross no part of the top layer: take out every view-ray weight
+            // (the pixel's detected weight, except that of events in the top layer).
+            if (k == nz - 1) straight -= inv_mu[ia] * sum(size_t(pixel) * 4 + 3) - sum(path + size_t(nz));
+            value += zunit[k] * straight;
         } else if (!L.orders || o < stokes_out + (paths ? pixels * uint32_t(nz + 1) : 0u)) {
             const uint32_t pixel = o - stokes_out - pixels * uint32_t(nz);
             value = sum(size_t(pixel) * 4 + 3);

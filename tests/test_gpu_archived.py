@@ -4,18 +4,35 @@ monki.preparation builds for them (the Fortran preparer's optical depths exactly
 
 Per run, every view's I, Q, U (every pixel of the box clouds): the reference's criterion
 |z| < 3 in at least 99 % of entries, and no |z| beyond the Bonferroni bound at family
-error 1e-6; the mean z where the entries are many and weakly correlated (box clouds). The
-layered-cloud run also archived its layer AMFs (without their standard error): those are
-compared with twice our own error (the same budget), layer by layer, below 40 km, and
-within 1 % relative above it (heavy-tailed path tallies; see the test).
+error 1e-6; the mean z where the entries are many and weakly correlated (box clouds).
+
+The layered-cloud run also archived its layer AMFs, without their standard error. Layer
+path tallies are heavy tailed (a photon scattered near the horizontal crosses hundreds of
+kilometres of a thin layer, and every later peel-off of its history carries that path), so
+a run's round-variance error understates its spread and neighbouring views deviate
+together. The AMFs are therefore checked twice:
+  * against the oracle at the same budget (its layer-path round moments in
+    tests/golden/archived_amf_oracle.npz, independent random streams), combined standard
+    error from both runs: |z| < 3 in at least 99 % of the view x layer entries and no |z|
+    beyond the Bonferroni bound. No mean-z criterion: two oracle runs with different seeds
+    differ by a mean z of -0.20 here (one run catches a long path the other misses);
+  * against the archived Fortran values, with twice our error as the combined error, as
+    closely as the oracle itself agrees with them: the fraction of entries with |z| < 3 at
+    most one point below the oracle's (98.2 %; another oracle seed gives 99.2 %), the
+    deviations correlated with the oracle's (the archived run's own spikes are shared),
+    and the four layers above 40 km (optical depth below 0.002) within 1 % relative.
 """
 
 from __future__ import annotations
+
+from pathlib import Path
 
 import numpy as np
 import pytest
 
 import archived_runs as ar
+
+ORACLE_AMF = Path(__file__).resolve().parent / "golden" / "archived_amf_oracle.npz"
 
 pytestmark = pytest.mark.gpu
 
@@ -72,22 +89,34 @@ def test_fp32_transport_agrees_with_the_archived_fortran_run(device, name):
     if name == "2boxclouds":
         assert abs(z.mean()) < 0.1, z.mean()
     if amf is not None:
-        # Layers above 40 km (optical depth below 0.002) have heavy-tailed path tallies: in
-        # the 50,000 km periodic column a photon scattered near the horizontal there crosses
-        # hundreds to thousands of kilometres of one layer (mean free paths of thousands of
-        # km), and every later peel-off of its history carries that path. Neither run's
-        # round-variance error is reliable there (the oracle's 45-50 km AMF drifts up as the
-        # budget grows ten-fold while its error shrinks half as fast as the square root), so
-        # those layers must agree within 1 % relative; the others by the z-criterion.
-        archived = fixture["AMF_layer"][..., 0]
+        archived = fixture["AMF_layer"][..., 0]  # (view, layer, 1, 1)
         optical_depth = fixture["bmsca"][:, 0] + fixture["bmabs"][:, 0] + fixture["baer"][..., 0].sum(axis=(1, 2, 3))
         thin = optical_depth < 2e-3
-        combined = np.sqrt(2.0) * amf_error[:, ~thin]
+        dz = fixture["z_unit"]
+        ours, our_error = amf[:, :, 0, 0], amf_error[:, :, 0, 0]
+        # Against the oracle at the same budget.
+        o = np.load(ORACLE_AMF)
+        n = int(o["rounds"])
+        ratio = o["p"] / o["w"][:, None]
+        spread = np.sqrt(n / (n - 1) * np.maximum(o["pp"] - 2 * ratio * o["pw"] + ratio**2 * o["ww"][:, None], 0.0))
+        oracle_amf = ratio / dz[None, :]
+        oracle_error = spread / o["w"][:, None] / dz[None, :]
+        combined = np.hypot(our_error, oracle_error)
         mask = combined > 0
-        za = (amf[:, ~thin] - archived[:, ~thin])[mask] / combined[mask]
-        assert za.size >= 0.8 * archived[:, ~thin].size
-        layers = np.nonzero(~thin)[0][np.nonzero(mask)[1]]
-        failing = {int(k): int(np.sum(np.abs(za[layers == k]) >= 3)) for k in np.unique(layers[np.abs(za) >= 3])}
-        assert np.mean(np.abs(za) < 3) >= 0.99, (np.sort(np.abs(za))[-5:], "failures by layer", failing)
-        relative = np.abs(amf[:, thin] / archived[:, thin] - 1.0)
+        zo = (ours - oracle_amf)[mask] / combined[mask]
+        assert zo.size >= 0.9 * ours.size
+        assert np.mean(np.abs(zo) < 3) >= 0.99, np.sort(np.abs(zo))[-5:]
+        assert np.abs(zo).max() < ar.bonferroni_bound(zo.size), np.abs(zo).max()
+        # Against the archived Fortran values, as closely as the oracle agrees with them.
+        z_ours = (ours - archived[:, :, 0, 0])[:, ~thin] / (np.sqrt(2.0) * our_error[:, ~thin])
+        z_oracle = (oracle_amf - archived[:, :, 0, 0])[:, ~thin] / (np.sqrt(2.0) * oracle_error[:, ~thin])
+        ok = np.isfinite(z_ours) & np.isfinite(z_oracle)
+        layers = np.nonzero(~thin)[0][np.nonzero(ok)[1]]
+        z_ours, z_oracle = z_ours[ok], z_oracle[ok]
+        assert z_ours.size >= 0.9 * archived[:, ~thin].size
+        ours_pass, oracle_pass = np.mean(np.abs(z_ours) < 3), np.mean(np.abs(z_oracle) < 3)
+        failing = {int(k): int(np.sum(np.abs(z_ours[layers == k]) >= 3)) for k in np.unique(layers[np.abs(z_ours) >= 3])}
+        assert ours_pass >= oracle_pass - 0.01, (ours_pass, oracle_pass, "failures by layer", failing)
+        assert np.corrcoef(z_ours, z_oracle)[0, 1] > 0.2, np.corrcoef(z_ours, z_oracle)[0, 1]
+        relative = np.abs(ours[:, thin] / archived[:, thin, 0, 0] - 1.0)
         assert relative.max() < 0.01, relative.max()

@@ -1,13 +1,14 @@
 """The trained importance network on held-out box clouds.
 
 The network is trained on the device from analog-kernel importance tallies of the
-training family (batched-generator scenes and randomly placed box clouds) and applied to
-box clouds it has not seen. Checked: its prediction explains the held-out pilot tallies
-(weighted R^2), the guided estimate with the learned roulette map agrees with the analog
-kernel within combined standard error (the map moves variance, never the expectation),
-and what the network gains over guided transport without it: variance x time of the
-median pixel improves (the worst pixel does not; the time to a precision target in every
-pixel is set by constant roulette).
+training family (batched-generator scenes and randomly placed box clouds), weighted for
+the relative error of every pixel, and applied to box clouds it has not seen. Checked: its
+prediction explains the held-out pilot tallies (weighted R^2); the guided estimate under
+the learned weight window agrees with the analog kernel within combined standard error
+(the window moves variance, never the expectation); and what the network gives against
+the same window without it, on the pixel that sets the time to a precision target in
+every pixel: the worst pixel's variance x cost, with cost the scatters of the run (the
+same for a given seed, unlike wall time), over two held-out scenes and two seeds each.
 """
 
 from __future__ import annotations
@@ -19,46 +20,54 @@ pytestmark = pytest.mark.gpu
 
 
 def _rounds(scene, guided, scale, ppc, rounds, seed):
-    import time
-
     from monki.execution import CUDA, BatchControls
 
     with CUDA(guided=guided, seed=seed, roulette_scale=scale) as backend:
         backend.prepare(scene)
-        start = time.perf_counter()
         batches = backend.run_batches([BatchControls(i, ppc) for i in range(1, rounds + 1)])
-        elapsed = time.perf_counter() - start
-    return np.stack([b.stokes[0] for b in batches]) / ppc, elapsed
+        scatters = int(backend.provenance["scatters"])
+    return np.stack([b.stokes[0] for b in batches]) / ppc, scatters
+
+
+def _relative_se(x):
+    return x.std(0, ddof=1) / np.sqrt(x.shape[0]) / np.abs(x.mean(0))
 
 
 def test_learned_importance_generalises_and_keeps_estimates_unbiased(device):
     import monki.scenes as scenes
-    from monki import Guided
-    from monki.importance import (cell_features, importance_targets, learned_scale, pilot, r_squared,
-                                  train_model, training_scenes)
+    from monki.importance import (LEARNED_GUIDE, cell_features, importance_targets, learned_scale,
+                                  objective_tally, r_squared, train_model, training_scenes)
 
     model, losses, rows = train_model(training_scenes(6), steps=600, batch=8192, rows_per_scene=8000)
+    ppc, rounds = 2000, 64
+    worst_ratio, median_ratio, over_analog = [], [], []
     with model:
         assert np.all(np.isfinite(losses)) and losses[-50:].mean() < 0.5 * losses[:20].mean()
-        gains = []
         for seed in (1000, 1001):
-            # 64 rounds: roulette makes the estimates skewed, and with few rounds a low sample
-            # mean comes with a low sample variance, which pulls the mean z below zero.
-            scene = scenes.box_cloud_variant(seed, 2000, 64)
-            tally, _ = pilot(scene, rounds=2, photons_per_column=300, seed=3)
+            scene = scenes.box_cloud_variant(seed, ppc, rounds)
+            tally = objective_tally(scene, rounds=2, photons_per_column=300, seed=3)
             target, weight = importance_targets(tally)
             prediction = model.predict(cell_features(scene.tables))
-            assert r_squared(prediction[weight > 0], target[weight > 0], weight[weight > 0]) > 0.8
+            fit = r_squared(prediction[weight > 0], target[weight > 0], weight[weight > 0])
+            print(f"held-out box cloud {seed}: weighted R^2 {fit:.3f}")
+            assert fit > 0.8, fit
             scale = learned_scale(model, scene)
-            plain, t_plain = _rounds(scene, None, None, 2000, 64, seed)
-            constant, t_constant = _rounds(scene, Guided(0.0, 1.0, 0.0), None, 2000, 64, seed + 1)
-            learned, t_learned = _rounds(scene, Guided(0.0, 1.0, 0.0), scale, 2000, 64, seed + 2)
-            n = plain.shape[0]
-            se = lambda a: a.std(0, ddof=1) / np.sqrt(n)  # noqa: E731
-            z = (learned.mean(0) - plain.mean(0)) / np.hypot(se(learned), se(plain))
-            assert np.mean(np.abs(z) < 3) >= 0.99 and abs(z.mean()) < 0.1
-            relative = lambda a: np.median(se(a) / np.abs(a.mean(0)))  # noqa: E731
-            merit = lambda a, t: 1.0 / (relative(a) ** 2 * t)  # noqa: E731
-            gains.append(merit(learned, t_learned) / merit(constant, t_constant))
-        print(f"learned roulette map: median-pixel variance x time gain over constant roulette {gains}")
-        assert np.mean(gains) > 1.0
+            # 64 rounds: roulette makes the estimates skewed, and with few rounds a low sample
+            # mean comes with a low sample variance, which pulls the mean z below zero.
+            plain, plain_cost = _rounds(scene, None, None, ppc, rounds, seed)
+            for repeat in range(2):
+                constant, constant_cost = _rounds(scene, LEARNED_GUIDE, None, ppc, rounds, seed + 10 + repeat)
+                learned, learned_cost = _rounds(scene, LEARNED_GUIDE, scale, ppc, rounds, seed + 20 + repeat)
+                se = lambda a: a.std(0, ddof=1) / np.sqrt(rounds)  # noqa: E731
+                z = (learned.mean(0) - plain.mean(0)) / np.hypot(se(learned), se(plain))
+                assert np.mean(np.abs(z) < 3) >= 0.99 and abs(z.mean()) < 0.1, (np.mean(np.abs(z) < 3), z.mean())
+                merit = lambda x, cost, pick: 1.0 / (pick(_relative_se(x)) ** 2 * cost)  # noqa: E731
+                worst_ratio.append(merit(learned, learned_cost, np.max) / merit(constant, constant_cost, np.max))
+                median_ratio.append(merit(learned, learned_cost, np.median) / merit(constant, constant_cost, np.median))
+                over_analog.append(merit(learned, learned_cost, np.max) / merit(plain, plain_cost, np.max))
+    print(f"learned window over the same constant window, worst pixel {np.round(worst_ratio, 3)}, "
+          f"median pixel {np.round(median_ratio, 3)}; over analog, worst pixel {np.round(over_analog, 2)}")
+    # The learned window matches the constant one on the worst pixel (within 10 %) and keeps
+    # the guided gain over analog transport.
+    assert np.mean(worst_ratio) > 0.9, worst_ratio
+    assert min(over_analog) > 2.0, over_analog
