@@ -443,7 +443,8 @@ def batched_scenes(device, scale):
     one round each. Persistent: every scene in one multi-scene launch sequence (one shared
     photon pool; graph-replayed batches), after one warm-up run. Beside it, the scenes as
     concurrent sessions from four host threads with launch shapes from the autotuner
-    (tuned once per size class)."""
+    (tuned once per size class), and one after another in their own sessions (default
+    launch options), the way a caller without the batched API would run them."""
 
     import monki.scenes as scenes
     from monki.batched import run_batched, run_persistent
@@ -464,7 +465,9 @@ def batched_scenes(device, scale):
     _, sessions = run_batched(batch, device=device, concurrency=4, tune=lambda s: tuned[size_class(s)].options(),
                               persistent=False)
     sessions["tuned"] = {str(k): v.options() for k, v in tuned.items()}
-    return {"photons_scale": scale, "persistent": persistent, "concurrent_sessions": sessions}
+    _, one_at_a_time = run_batched(batch, device=device, concurrency=1, persistent=False)
+    return {"photons_scale": scale, "persistent": persistent, "concurrent_sessions": sessions,
+            "one_at_a_time": one_at_a_time}
 
 
 def main():

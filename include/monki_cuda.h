@@ -85,6 +85,14 @@ void monki_cuda_close(void *session);
  * A failed group leaves the statistics unchanged. */
 int monki_cuda_run_accumulate(void *session, const uint32_t controls[8], double photons_per_column, double *history,
                               char *err, size_t errlen);
+/* A round group run ahead of its stopping checks: like monki_cuda_run_accumulate, but the
+ * group's flushed rounds are held on the device unfolded; monki_cuda_fold_next then folds
+ * them one at a time, in round order, writing that round's nmat history values. Rounds
+ * left unfolded when the caller stops are discarded by the next run. Replaces the
+ * reference driver's round-by-round dispatch after its minimum rounds
+ * (python/monki/simulation.py:86-103) with the same rounds, folds and checks. */
+int monki_cuda_run_held(void *session, const uint32_t controls[8], char *err, size_t errlen);
+int monki_cuda_fold_next(void *session, double photons_per_column, double *history, char *err, size_t errlen);
 
 /* Length of the statistics vector: total, sum, squares (nmat nx ny angles each); with path
  * diagnostics the path sum, mean, M2 and covariance (nx ny nz angles each) and the weight

@@ -9,9 +9,10 @@
 //   W1[256 x 64], b1[256], W2[256 x 256], b2[256], W3[256 x 256], b3[256], w4[256], b4[1]
 //
 // Per layer l with input X (rows x K) and weights W (256 x K):
-//   forward   Z = X W^T + b (tcgen05, epilogue adds b, writes Z, H = GELU(Z), H^T)
+//   forward   Z = X W^T + b (tcgen05, epilogue adds b, writes Z in BF16, H = GELU(Z), H^T)
 //   backward  dW += dZ^T X (tcgen05 split-K over the rows, A = dZ^T, B = X^T)
-//             dX' = (dZ W) * GELU'(Z_prev) (tcgen05, B = W^T, epilogue applies GELU')
+//             dX' = (dZ W) * GELU'(Z_prev) (tcgen05, B = W^T, epilogue applies GELU' and
+//             adds the column sums of dX' to the previous layer's bias gradient)
 // so every operand is K-major and the transposed activations come from the epilogues.
 #include <cuda_runtime.h>
 #include <algorithm>
@@ -114,78 +115,55 @@ __global__ void loss_grad(const float* __restrict__ y, const float* __restrict__
     if ((threadIdx.x & 31) == 0 && part != 0.f) atomicAdd(loss, part);
 }
 
-// Output layer backward: dw4 += dy^T H3, db4 += sum dy, and dZ3 = dy w4^T * GELU'(Z3).
-// Block: 256 threads (one per hidden unit) over a slab of 64 rows.
+// Output layer backward: dw4 += dy^T H3, db4 += sum dy, dZ3 = dy w4^T * GELU'(Z3) in BF16,
+// its transpose (row n of GT: 64 contiguous rows of column n per thread, written as eight
+// 16-byte stores) and db3 += the column sums of dZ3. Block: 256 threads (one per hidden
+// unit) over a slab of 64 rows; rows from `rows` to the slab's end are written as zeros.
 __global__ void head_backward(const float* __restrict__ dy, const bf16* __restrict__ H, const float* __restrict__ w4,
-                              const float* __restrict__ Z, int R, float* __restrict__ grads, bf16* __restrict__ G) {
+                              const bf16* __restrict__ Z, int rows, int R, float* __restrict__ grads,
+                              bf16* __restrict__ G, bf16* __restrict__ GT) {
     const int n = threadIdx.x;
     const int m0 = blockIdx.x * 64;
-    float acc = 0.f, bias = 0.f;
+    float acc = 0.f, bias = 0.f, column = 0.f;
     const float wn = w4[n];
-    for (int m = m0; m < min(m0 + 64, R); ++m) {
-        const float d = dy[m];
-        const size_t at = size_t(m) * kHidden + n;
-        acc += d * __bfloat162float(H[at]);
-        bias += d;
-        G[at] = __float2bfloat16(d * wn * umma::gelu_grad(Z[at]));
-    }
-    atomicAdd(grads + ow4 + n, acc);
-    if (n == 0) atomicAdd(grads + ob4, bias);
-}
-
-// out (cols x R) = in^T for a BF16 rows x cols matrix (row-major), 32 x 32 tiles.
-__global__ void transpose(const bf16* __restrict__ in, int rows, int cols, int R, bf16* __restrict__ out) {
-    __shared__ bf16 tile[32][33];
-    const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
-    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-        const int m = by + r, c = bx + threadIdx.x;
-        tile[r][threadIdx.x] = (m < rows && c < cols) ? in[size_t(m) * cols + c] : __float2bfloat16(0.f);
-    }
-    __syncthreads();
-    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-        const int c = bx + r, m = by + threadIdx.x;
-        if (c < cols && m < R) out[size_t(c) * R + m] = tile[threadIdx.x][r];
-    }
-}
-
-// Bias gradients: out[n] += sum over m < rows of GT[n R + m]. Grid (height, segments): a
-// block sums one segment of row n with 16-byte loads of eight values (R is a multiple of
-// 128, so every row starts 256-byte aligned), the last segment adds the rows past the last
-// whole group of eight, and each block adds its sum with one atomic. One block per row
-// with 2-byte loads was latency bound (116 us per launch at 65,536 rows).
-__global__ void row_sums(const bf16* __restrict__ GT, int rows, int R, float* __restrict__ out) {
-    const int n = blockIdx.x;
-    const bf16* row = GT + size_t(n) * R;
-    const int groups = rows >> 3;
-    const int per = (groups + int(gridDim.y) - 1) / int(gridDim.y);
-    const int g0 = int(blockIdx.y) * per, g1 = min(groups, g0 + per);
-    float acc = 0.f;
-    for (int g = g0 + int(threadIdx.x); g < g1; g += int(blockDim.x)) {
-        const uint4 v = reinterpret_cast<const uint4*>(row)[g];
-        const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&v);
+    uint32_t packed[32];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const float2 f = __bfloat1622float2(h[q]);
-            acc += f.x + f.y;
+    for (int q = 0; q < 32; ++q) {
+        float g2[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int m = m0 + 2 * q + u;
+            g2[u] = 0.f;
+            if (m < rows) {
+                const float d = dy[m];
+                const size_t at = size_t(m) * kHidden + n;
+                acc += d * __bfloat162float(H[at]);
+                bias += d;
+                const bf16 g = __float2bfloat16(d * wn * umma::gelu_grad(__bfloat162float(Z[at])));
+                G[at] = g;
+                g2[u] = __bfloat162float(g);
+                column += g2[u];
+            }
+        }
+        const __nv_bfloat162 pair = __floats2bfloat162_rn(g2[0], g2[1]);
+        packed[q] = *reinterpret_cast<const uint32_t*>(&pair);
+    }
+    bf16* dst = GT + size_t(n) * R + m0;
+    if (m0 + 64 <= R) {
+#pragma unroll
+        for (int q = 0; q < 32; q += 4)
+            reinterpret_cast<uint4*>(dst)[q / 4] = make_uint4(packed[q], packed[q + 1], packed[q + 2], packed[q + 3]);
+    } else {
+#pragma unroll
+        for (int q = 0; q < 32; ++q) {
+            const __nv_bfloat162 pair = *reinterpret_cast<const __nv_bfloat162*>(&packed[q]);
+            if (m0 + 2 * q < R) dst[2 * q] = pair.x;
+            if (m0 + 2 * q + 1 < R) dst[2 * q + 1] = pair.y;
         }
     }
-    if (blockIdx.y == gridDim.y - 1)
-        for (int m = (groups << 3) + int(threadIdx.x); m < rows; m += int(blockDim.x)) acc += __bfloat162float(row[m]);
-    __shared__ float part[32];
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float s = 0.f;
-        for (int q = 0; q < int(blockDim.x >> 5); ++q) s += part[q];
-        atomicAdd(out + n, s);
-    }
-}
-
-// Segments per row for row_sums: about 1,024 groups of eight per block, at most 32.
-inline unsigned row_segments(int rows) {
-    return unsigned(std::min(32, std::max(1, ((rows >> 3) + 1023) / 1024)));
+    atomicAdd(grads + ow4 + n, acc);
+    atomicAdd(grads + ob3 + n, column);
+    if (n == 0) atomicAdd(grads + ob4, bias);
 }
 
 __global__ void adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1, float* __restrict__ m2,
@@ -224,7 +202,8 @@ struct Net {
     bf16 *W1 = nullptr, *W2 = nullptr, *W3 = nullptr, *W2T = nullptr, *W3T = nullptr;
     bf16 *X = nullptr, *XT = nullptr, *H1 = nullptr, *H2 = nullptr, *H3 = nullptr, *H1T = nullptr, *H2T = nullptr;
     bf16 *G3 = nullptr, *G3T = nullptr, *G2 = nullptr, *G2T = nullptr, *G1 = nullptr, *G1T = nullptr;
-    float *Z1 = nullptr, *Z2 = nullptr, *Z3 = nullptr, *y = nullptr, *dy = nullptr, *tb = nullptr, *wb = nullptr;
+    bf16 *Z1 = nullptr, *Z2 = nullptr, *Z3 = nullptr;  // pre-activations
+    float *y = nullptr, *dy = nullptr, *tb = nullptr, *wb = nullptr;
     float* loss = nullptr;
     uint32_t* failure = nullptr;
     uint32_t* idx = nullptr;
@@ -340,13 +319,13 @@ void clear_tail(bf16* T, int rows, int R, int height, cudaStream_t stream) {
 void forward(Net& n, int rows) {
     const int R = n.R;
     Gemm g = params_for(n.X, n.W1, rows, kHidden, kIn, n.failure);
-    g.p.C = n.Z1; g.p.bias = n.params + ob1; g.p.H = n.H1; g.p.HT = n.H1T; g.p.rows_ht = R;
+    g.p.Z = n.Z1; g.p.bias = n.params + ob1; g.p.H = n.H1; g.p.HT = n.H1T; g.p.rows_ht = R;
     gemm<umma::kForward>(g, 1, n.stream);
     g = params_for(n.H1, n.W2, rows, kHidden, kHidden, n.failure);
-    g.p.C = n.Z2; g.p.bias = n.params + ob2; g.p.H = n.H2; g.p.HT = n.H2T; g.p.rows_ht = R;
+    g.p.Z = n.Z2; g.p.bias = n.params + ob2; g.p.H = n.H2; g.p.HT = n.H2T; g.p.rows_ht = R;
     gemm<umma::kForward>(g, 1, n.stream);
     g = params_for(n.H2, n.W3, rows, kHidden, kHidden, n.failure);
-    g.p.C = n.Z3; g.p.bias = n.params + ob3; g.p.H = n.H3; g.p.HT = nullptr; g.p.rows_ht = R;
+    g.p.Z = n.Z3; g.p.bias = n.params + ob3; g.p.H = n.H3; g.p.HT = nullptr; g.p.rows_ht = R;
     gemm<umma::kForward>(g, 1, n.stream);
     clear_tail(n.H1T, rows, R, kHidden, n.stream);
     clear_tail(n.H2T, rows, R, kHidden, n.stream);
@@ -359,10 +338,8 @@ void forward(Net& n, int rows) {
 void backward(Net& n, int rows, float inv_weight, float* loss) {
     const int R = n.R;
     loss_grad<<<256, 256, 0, n.stream>>>(n.y, n.tb, n.wb, rows, inv_weight, n.dy, loss);
-    check(cudaMemsetAsync(n.G3, 0, size_t(R) * kHidden * sizeof(bf16), n.stream), "memset");
-    head_backward<<<(rows + 63) / 64, kHidden, 0, n.stream>>>(n.dy, n.H3, n.params + ow4, n.Z3, rows, n.grads, n.G3);
-    transpose<<<dim3(kHidden / 32, (R + 31) / 32), dim3(32, 8), 0, n.stream>>>(n.G3, R, kHidden, R, n.G3T);
-    row_sums<<<dim3(kHidden, row_segments(rows)), 256, 0, n.stream>>>(n.G3T, rows, R, n.grads + ob3);
+    head_backward<<<(rows + 63) / 64, kHidden, 0, n.stream>>>(n.dy, n.H3, n.params + ow4, n.Z3, rows, R, n.grads,
+                                                              n.G3, n.G3T);
     check(cudaGetLastError(), "head backward launch");
     // Split-K over the rows for the weight gradients: 64-row multiples, slices of 1,024 rows
     // (at batch 65,536 two row tiles x 64 slices = 128 CTAs, each adding one partial).
@@ -371,18 +348,16 @@ void backward(Net& n, int rows, float inv_weight, float* loss) {
     g.lda = R; g.ldb = R; g.p.k_chunk = chunk; g.p.C = n.grads + oW3;
     gemm<umma::kAccumulate>(g, splits, n.stream);
     g = params_for(n.G3, n.W3T, rows, kHidden, kHidden, n.failure);
-    g.p.zprev = n.Z2; g.p.H = n.G2; g.p.HT = n.G2T; g.p.rows_ht = R;
+    g.p.zprev = n.Z2; g.p.H = n.G2; g.p.HT = n.G2T; g.p.rows_ht = R; g.p.bias_grad = n.grads + ob2;
     gemm<umma::kBackward>(g, 1, n.stream);
     clear_tail(n.G2T, rows, R, kHidden, n.stream);
-    row_sums<<<dim3(kHidden, row_segments(rows)), 256, 0, n.stream>>>(n.G2T, rows, R, n.grads + ob2);
     g = params_for(n.G2T, n.H1T, kHidden, kHidden, K, n.failure);
     g.lda = R; g.ldb = R; g.p.k_chunk = chunk; g.p.C = n.grads + oW2;
     gemm<umma::kAccumulate>(g, splits, n.stream);
     g = params_for(n.G2, n.W2T, rows, kHidden, kHidden, n.failure);
-    g.p.zprev = n.Z1; g.p.H = n.G1; g.p.HT = n.G1T; g.p.rows_ht = R;
+    g.p.zprev = n.Z1; g.p.H = n.G1; g.p.HT = n.G1T; g.p.rows_ht = R; g.p.bias_grad = n.grads + ob1;
     gemm<umma::kBackward>(g, 1, n.stream);
     clear_tail(n.G1T, rows, R, kHidden, n.stream);
-    row_sums<<<dim3(kHidden, row_segments(rows)), 256, 0, n.stream>>>(n.G1T, rows, R, n.grads + ob1);
     g = params_for(n.G1T, n.XT, kHidden, kIn, K, n.failure);
     g.lda = R; g.ldb = R; g.p.k_chunk = chunk; g.p.C = n.grads + oW1;
     gemm<umma::kAccumulate>(g, splits, n.stream);
@@ -439,7 +414,7 @@ void* monki_mlp_create(uint32_t device, uint32_t features, uint32_t rows, uint32
         n->X = n->alloc<bf16>(R * kIn); n->XT = n->alloc<bf16>(R * kIn);
         for (bf16** b : {&n->H1, &n->H2, &n->H3, &n->H1T, &n->H2T, &n->G3, &n->G3T, &n->G2, &n->G2T, &n->G1, &n->G1T})
             *b = n->alloc<bf16>(R * H);
-        n->Z1 = n->alloc<float>(R * H); n->Z2 = n->alloc<float>(R * H); n->Z3 = n->alloc<float>(R * H);
+        n->Z1 = n->alloc<bf16>(R * H); n->Z2 = n->alloc<bf16>(R * H); n->Z3 = n->alloc<bf16>(R * H);
         n->y = n->alloc<float>(R); n->dy = n->alloc<float>(R); n->tb = n->alloc<float>(R); n->wb = n->alloc<float>(R);
         n->loss = n->alloc<float>(1);
         n->failure = n->alloc<uint32_t>(1);

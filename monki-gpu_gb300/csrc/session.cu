@@ -57,6 +57,8 @@ struct Session {
     double* stats = nullptr;          // FP64 round statistics (statistics_layout), lazily
     double* history = nullptr;        // round_capacity x nmat spatial sums
     uint64_t stats_rounds = 0;
+    uint32_t held = 0;                // rounds of s.out run by monki_cuda_run_held
+    uint32_t held_next = 0;           // the next of them to fold
     void* pixel_weight = nullptr;     // nx * ny * angles (T), or null
     uint32_t* host_counts = nullptr;  // pinned
     uint64_t iterations = 0;
@@ -496,9 +498,9 @@ StatsLayout statistics_layout(const Session& s) {
     return L;
 }
 
-// Add the rounds of s.out to the device accumulators (FP64, rounds in order) and write the
-// per-round spatial sums of the normalized Stokes tallies to the host.
-void accumulate(Session& s, uint32_t rounds, double photons_per_column, double* history) {
+// Add rounds first .. first + rounds - 1 of s.out to the device accumulators (FP64, rounds in
+// order) and write their per-round spatial sums of the normalized Stokes tallies to the host.
+void accumulate(Session& s, uint32_t first, uint32_t rounds, double photons_per_column, double* history) {
     const StatsLayout L = statistics_layout(s);
     if (!s.stats) {
         check(cudaMalloc(&s.stats, L.count * sizeof(double)), "cudaMalloc(statistics)");
@@ -508,12 +510,13 @@ void accumulate(Session& s, uint32_t rounds, double photons_per_column, double* 
     const uint32_t elements = L.stokes + L.paths + L.weights;
     const int grid = int(std::min<uint32_t>((elements + 255) / 256, 8192));
     // Paths read the weight means of the previous groups, so the weights update second.
-    stats_update<<<grid, 256, 0, s.stream>>>(s.out, uint32_t(s.layout.count), rounds, uint32_t(s.stats_rounds), L,
+    const double* out = s.out + size_t(first) * s.layout.count;
+    stats_update<<<grid, 256, 0, s.stream>>>(out, uint32_t(s.layout.count), rounds, uint32_t(s.stats_rounds), L,
                                             photons_per_column, s.stats, 0);
     if (L.weights)
-        stats_update<<<grid, 256, 0, s.stream>>>(s.out, uint32_t(s.layout.count), rounds, uint32_t(s.stats_rounds), L,
+        stats_update<<<grid, 256, 0, s.stream>>>(out, uint32_t(s.layout.count), rounds, uint32_t(s.stats_rounds), L,
                                                 photons_per_column, s.stats, 1);
-    round_sums<<<dim3(rounds, uint32_t(s.prep.nmat)), 256, 0, s.stream>>>(s.out, uint32_t(s.layout.count),
+    round_sums<<<dim3(rounds, uint32_t(s.prep.nmat)), 256, 0, s.stream>>>(out, uint32_t(s.layout.count),
                                                                           uint32_t(s.prep.nmat), L.stokes,
                                                                           photons_per_column, s.history);
     check(cudaGetLastError(), "statistics launch");
@@ -658,6 +661,8 @@ int monki_cuda_run(void* handle, const uint32_t controls[8], double* out, char* 
     if (!s || !controls || !out) { write_error(err, errlen, "Invalid CUDA session or buffers"); return 1; }
     try {
         const Controls c = group_controls(*s, controls);
+        s->held = 0;
+        s->held_next = 0;
         execute(*s, c);
         check(cudaMemcpyAsync(out, s->out, size_t(s->layout.count) * c.rounds * sizeof(double), cudaMemcpyDeviceToHost,
                               s->stream), "copy(tallies)");
@@ -679,7 +684,41 @@ int monki_cuda_run_accumulate(void* handle, const uint32_t controls[8], double p
         execute(*s, c);
         // A failed group must not touch the accumulators: check before accumulating.
         finish(*s, c);
-        accumulate(*s, c.rounds, photons_per_column, history);
+        accumulate(*s, 0, c.rounds, photons_per_column, history);
+        s->held = 0;
+        s->held_next = 0;
+        return 0;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        return 1;
+    }
+}
+
+int monki_cuda_run_held(void* handle, const uint32_t controls[8], char* err, size_t errlen) {
+    Session* s = static_cast<Session*>(handle);
+    if (!s || !controls) { write_error(err, errlen, "Invalid CUDA session or buffers"); return 1; }
+    try {
+        s->held = 0;
+        s->held_next = 0;
+        const Controls c = group_controls(*s, controls);
+        execute(*s, c);
+        finish(*s, c);
+        s->held = c.rounds;
+        return 0;
+    } catch (const std::exception& e) {
+        write_error(err, errlen, e.what());
+        return 1;
+    }
+}
+
+int monki_cuda_fold_next(void* handle, double photons_per_column, double* history, char* err, size_t errlen) {
+    Session* s = static_cast<Session*>(handle);
+    if (!s || !history) { write_error(err, errlen, "Invalid CUDA session or buffers"); return 1; }
+    try {
+        if (!(photons_per_column > 0.0)) throw std::runtime_error("photons_per_column must be positive");
+        if (s->held_next >= s->held) throw std::runtime_error("no held round left to fold");
+        accumulate(*s, s->held_next, 1, photons_per_column, history);
+        s->held_next += 1;
         return 0;
     } catch (const std::exception& e) {
         write_error(err, errlen, e.what());

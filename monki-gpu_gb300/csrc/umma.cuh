@@ -11,7 +11,8 @@
 //   epilogue  (all eight warps) after "done": TMEM lanes 32 (w % 4) .. + 31, every other
 //             32-column chunk from 32 (w / 4); bias, GELU or GELU', FP32 / BF16 stores, and
 //             transposed BF16 stores staged through shared memory so that each thread
-//             writes 64 contiguous bytes of a transposed row.
+//             writes 64 contiguous bytes of a transposed row (and, in the backward
+//             epilogue, adds that row's 32 values to the column's bias gradient).
 //
 // Tile: 128 rows of C per CTA (the MMA's M), all N <= 256 columns (one MMA covers them),
 // K in steps of 64 (one 128-byte swizzle row of BF16). The K range of a CTA is blockIdx.y's
@@ -47,17 +48,19 @@ constexpr uint32_t kTransposeStride = 80;          // bytes per staged transpose
 
 enum Epilogue : int {
     kStore = 0,      // C (fp32) = acc
-    kForward = 1,    // Z (fp32) = acc + bias; H (bf16) = GELU(Z); H^T (bf16)
-    kBackward = 2,   // G = acc * GELU'(Zprev); G (bf16) and G^T (bf16)
+    kForward = 1,    // Z (bf16) = acc + bias; H (bf16) = GELU(Z); H^T (bf16)
+    kBackward = 2,   // G = acc * GELU'(Zprev); G (bf16), G^T (bf16), column sums of G
     kAccumulate = 3, // C (fp32) += acc (split-K partial, atomics)
 };
 
 struct Params {
     int rows_a, N, K;
     int k_chunk;              // K elements per blockIdx.y slice (multiple of 64)
-    float* C;                 // kStore / kAccumulate / kForward (Z): rows_a x N, stride N
+    float* C;                 // kStore / kAccumulate: rows_a x N, stride N
+    __nv_bfloat16* Z;         // kForward: rows_a x N pre-activations (BF16)
     const float* bias;        // kForward: N
-    const float* zprev;       // kBackward: rows_a x N pre-activations
+    const __nv_bfloat16* zprev;  // kBackward: rows_a x N pre-activations (BF16)
+    float* bias_grad;         // kBackward: N column sums of G are added here (needs HT), or null
     __nv_bfloat16* H;         // kForward / kBackward: rows_a x N
     __nv_bfloat16* HT;        // kForward / kBackward: N x rows_ht (transposed), or null
     int rows_ht;              // row stride of HT (>= rows_a, a multiple of 8)
@@ -239,21 +242,35 @@ gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensor
                             atomicAdd(reinterpret_cast<float4*>(p.C + at + q), make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]));
                 } else {
                     if (EPI == kForward) {
+                        uint32_t zp[16];
 #pragma unroll
                         for (int q = 0; q < 32; q += 4) {
                             const float4 b = *reinterpret_cast<const float4*>(p.bias + c0 + q);
                             v[q] += b.x; v[q + 1] += b.y; v[q + 2] += b.z; v[q + 3] += b.w;
-                            if (valid)
-                                *reinterpret_cast<float4*>(p.C + at + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
                         }
+#pragma unroll
+                        for (int q = 0; q < 16; ++q) {
+                            const __nv_bfloat162 z2 = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+                            zp[q] = *reinterpret_cast<const uint32_t*>(&z2);
+                        }
+                        if (valid)
+#pragma unroll
+                            for (int q = 0; q < 16; q += 4)
+                                *reinterpret_cast<uint4*>(p.Z + at + 2 * q) = make_uint4(zp[q], zp[q + 1], zp[q + 2], zp[q + 3]);
 #pragma unroll
                         for (int q = 0; q < 32; ++q) v[q] = gelu(v[q]);
                     } else if (valid) {
+                        // GELU' of the stored (BF16) pre-activations.
 #pragma unroll
-                        for (int q = 0; q < 32; q += 4) {
-                            const float4 z = *reinterpret_cast<const float4*>(p.zprev + at + q);
-                            v[q] *= gelu_grad(z.x); v[q + 1] *= gelu_grad(z.y);
-                            v[q + 2] *= gelu_grad(z.z); v[q + 3] *= gelu_grad(z.w);
+                        for (int q = 0; q < 32; q += 8) {
+                            const uint4 z8 = *reinterpret_cast<const uint4*>(p.zprev + at + q);
+                            const uint32_t zw[4] = {z8.x, z8.y, z8.z, z8.w};
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) {
+                                const float2 z2 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&zw[u]));
+                                v[q + 2 * u] *= gelu_grad(z2.x);
+                                v[q + 2 * u + 1] *= gelu_grad(z2.y);
+                            }
                         }
                     }
                     uint32_t packed[16];
@@ -286,6 +303,18 @@ gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensor
                             const __nv_bfloat16* src = reinterpret_cast<const __nv_bfloat16*>(row);
                             for (int q = 0; m0 + q < p.rows_ht; ++q) dst[q] = src[q];
                         }
+                        if (EPI == kBackward && p.bias_grad) {
+                            // Column c0 + lane of G over this warp's 32 rows (rows past rows_a
+                            // were staged as zeros).
+                            const __nv_bfloat162* g2 = reinterpret_cast<const __nv_bfloat162*>(row);
+                            float sum = 0.f;
+#pragma unroll
+                            for (int q = 0; q < 16; ++q) {
+                                const float2 f = __bfloat1622float2(g2[q]);
+                                sum += f.x + f.y;
+                            }
+                            atomicAdd(p.bias_grad + c0 + lane, sum);
+                        }
                         __syncwarp();
                     }
                 }
@@ -304,14 +333,15 @@ gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensor
                     atomicAdd(p.C + e, acc);
                 } else if (EPI == kForward) {
                     const float z = acc + p.bias[n];
-                    p.C[e] = z;
+                    p.Z[e] = __float2bfloat16(z);
                     const __nv_bfloat16 h = __float2bfloat16(gelu(z));
                     p.H[e] = h;
                     if (p.HT) p.HT[size_t(n) * p.rows_ht + m] = h;
                 } else {
-                    const __nv_bfloat16 g = __float2bfloat16(acc * gelu_grad(p.zprev[e]));
+                    const __nv_bfloat16 g = __float2bfloat16(acc * gelu_grad(__bfloat162float(p.zprev[e])));
                     p.H[e] = g;
                     if (p.HT) p.HT[size_t(n) * p.rows_ht + m] = g;
+                    if (p.bias_grad) atomicAdd(p.bias_grad + n, __bfloat162float(g));
                 }
             }
         }

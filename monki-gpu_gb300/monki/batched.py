@@ -113,3 +113,29 @@ def run_batched(scenes, *, device: int = 0, seed: int = 23274, rounds: int = 1, 
     photons = sum(p["photons"] for _, p in results)
     return results, {"scenes": len(scenes), "wall_s": wall, "scatters": scatters, "photons": photons,
                      "scatters_per_s": scatters / wall, "concurrency": concurrency, "persistent": False}
+
+
+def main(argv=None) -> int:
+    """``python -m monki.batched``: the batched workload's seeded scenes (``batched_scene``)
+    in one multi-scene session; prints the run's summary."""
+
+    import argparse
+    import json
+
+    from .scenes import batched_scene
+
+    parser = argparse.ArgumentParser(prog="python -m monki.batched")
+    parser.add_argument("--scenes", type=int, default=64)
+    parser.add_argument("--photons-scale", type=float, default=0.05)
+    parser.add_argument("--rounds", type=int, default=1)
+    parser.add_argument("--precision", choices=("fp32", "fp64"), default="fp32")
+    parser.add_argument("--device", type=int, default=0)
+    args = parser.parse_args(argv)
+    batch = [batched_scene(seed, photons_scale=args.photons_scale) for seed in range(args.scenes)]
+    _, summary = run_persistent(batch, device=args.device, rounds=args.rounds, precision=args.precision)
+    print(json.dumps(summary))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

@@ -191,6 +191,15 @@ class AMFStopping:
             }
         )
 
+    def rounds_estimate(self):
+        """Rounds the target needs by the last check (the standard error falls as one over the
+        square root of the rounds), or None before a check or with an infinite error."""
+
+        if not self.history or self.history[-1]["max_relative_se"] is None:
+            return None
+        last = self.history[-1]
+        return last["rounds"] * (last["max_relative_se"] / self.policy.relative_error) ** 2
+
     def load(self, statistics: dict) -> None:
         """Take the moments from device round statistics (``CUDA.statistics``)."""
 

@@ -63,6 +63,7 @@ class CUDA(Backend):
         orders: bool = False,
         rectangles: bool = True,
         tail: int = 1 << 16,
+        lookahead: bool = True,
         monki_home=None,
         library=None,
     ):
@@ -117,6 +118,9 @@ class CUDA(Backend):
         if type(rectangles) is not bool:
             raise ValueError("rectangles must be a bool")
 
+        if type(lookahead) is not bool:
+            raise ValueError("lookahead must be a bool")
+
         self.device = device
         self.save_path = save_path
         self.profile = profile
@@ -143,6 +147,9 @@ class CUDA(Backend):
         # A round group's last photons (at most this many, every photon claimed) run to their
         # ends in one tail launch; 0 keeps the wavefront launches to the end.
         self.tail = tail
+        # simulate() with a stopping rule runs, after the first check, the rounds the last
+        # check says are still needed in one held dispatch, folded and checked one by one.
+        self.lookahead = lookahead
         self.monki_home = monki_home
         # Per-cell roulette scale (nx, ny, nz) applied at every prepare; set_roulette_scale
         # changes it for the prepared session only.
@@ -457,6 +464,66 @@ class CUDA(Backend):
             self.provenance["gpu_seconds"] = self._native.monki_cuda_gpu_seconds(self._handle)
 
         return np.concatenate(history) if history else np.zeros((0, nmat))
+
+    def held_capacity(self, photons_per_column: int) -> int:
+        """How many rounds of this size one held group (``run_held``) can run."""
+
+        _, nx, ny, _, _ = self._shape
+        return max(1, min(self._round_capacity, self.photons_per_dispatch // max(1, photons_per_column * nx * ny)))
+
+    def run_held(self, controls: list) -> None:
+        """Run consecutive rounds (one dispatch) ahead of their stopping checks: their tallies
+        stay on the device, unfolded, until ``fold_next`` folds them one by one in round order;
+        the ones never folded are discarded by the next run. The same rounds, folds and
+        checks as dispatching the rounds one at a time, with the straggler tail of a dispatch
+        paid once per group."""
+
+        self._validate_requests(controls)
+        _, nx, ny, _, _ = self._shape
+        ppc = controls[0].photons_per_column
+        if any(c.photons_per_column != ppc for c in controls) or any(
+            b.round_index != a.round_index + 1 for a, b in zip(controls, controls[1:])
+        ):
+            raise ValueError("a held group is consecutive rounds of one size")
+        if len(controls) > self.held_capacity(ppc):
+            raise ValueError("held group larger than one dispatch")
+        per_round = ppc * nx * ny
+        command = (ctypes.c_uint32 * 8)(
+            per_round * len(controls), 0, controls[0].round_index, self.seed, self.max_steps, int(self.profile),
+            per_round, len(controls),
+        )
+        error = ctypes.create_string_buffer(8192)
+        try:
+            if self._native.monki_cuda_run_held(self._handle, command, error, len(error)):
+                raise RuntimeError(error.value.decode() or "CUDA transport failed")
+        except BaseException:
+            self.close()
+            raise
+        self.provenance["gpu_dispatches"] += 1
+        self._held = [c.photons_per_column for c in controls]
+        self._round = controls[-1].round_index
+        counters = (ctypes.c_uint64 * 6)()
+        self._native.monki_cuda_counters(self._handle, counters)
+        self.provenance["scatters"] = int(counters[0])
+        self.provenance["photons"] = int(counters[4])
+        self.provenance["kernel_launches"] = int(counters[5])
+
+    def fold_next(self) -> np.ndarray:
+        """Fold the next held round into the device statistics; returns its nmat spatial
+        sums of the normalized Stokes tallies."""
+
+        if not getattr(self, "_held", None):
+            raise RuntimeError("no held round left to fold")
+        nmat = self._shape[0]
+        row = np.zeros(nmat, dtype=np.float64)
+        error = ctypes.create_string_buffer(8192)
+        ppc = self._held.pop(0)
+        if self._native.monki_cuda_fold_next(self._handle, float(ppc), row.ctypes.data_as(_native.F64P), error,
+                                             len(error)):
+            raise RuntimeError(error.value.decode() or "folding the held round failed")
+        if not np.all(np.isfinite(row)):
+            raise RuntimeError("Nonfinite CUDA tallies")
+        return row
 
     def statistics(self) -> dict:
         """The device's FP64 round statistics: ``rounds`` and, in RawTallies shapes, the

@@ -55,6 +55,8 @@ _SIGNATURES = {
         ctypes.c_int,
         [ctypes.c_void_p, _U32P, ctypes.c_double, _F64P, ctypes.c_char_p, ctypes.c_size_t],
     ),
+    "monki_cuda_run_held": (ctypes.c_int, [ctypes.c_void_p, _U32P, ctypes.c_char_p, ctypes.c_size_t]),
+    "monki_cuda_fold_next": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, _F64P, ctypes.c_char_p, ctypes.c_size_t]),
     "monki_cuda_statistics_count": (ctypes.c_size_t, [ctypes.c_void_p]),
     "monki_cuda_statistics": (
         ctypes.c_int,

@@ -84,24 +84,71 @@ def _host_rounds(case, backend, stopping):
     return total, rounds_sum, rounds_squared, history, paths, weights
 
 
+def _lookahead(stopping, groups, g, backend, ppc) -> int:
+    """How many checked groups, from ``g`` on, to run in one held dispatch: 90 % of the rounds
+    the last check says the target still needs (at least one group), within one dispatch."""
+
+    estimate = stopping.rounds_estimate()
+    if estimate is None:
+        return 1
+    first = groups[g][0]
+    capacity = backend.held_capacity(ppc)
+    wanted = max(1.0, 0.9 * (estimate - (first - 1)))
+    count, rounds = 0, 0
+    for f, e, _ in groups[g:]:
+        size = e - f + 1
+        if count and (rounds + size > capacity or rounds + size > wanted):
+            break
+        count, rounds = count + 1, rounds + size
+    return count
+
+
 def _device_rounds(case, backend, stopping):
     """Round sums folded on the device in FP64 (``backend.accumulate``): the same rounds,
     schedule and checks; only the per-round tallies stay on the GPU. The history is the
-    running pixel sum of the device's per-round sums (equal to the host's to rounding)."""
+    running pixel sum of the device's per-round sums (equal to the host's to rounding).
+
+    After the first check, backends with held groups (``run_held`` / ``fold_next``) run the
+    rounds the last check says are still needed in one dispatch and fold them one at a time,
+    checking where the schedule checks: the same rounds are folded and the same checks made
+    as when each group is its own dispatch, rounds past the stopping point are computed and
+    discarded, and a dispatch's straggling histories are waited for once per held group
+    instead of once per check."""
 
     ppc = case.photons_per_column
-    groups = stopping.groups(case.rounds) if stopping is not None else [(1, case.rounds, False)]
+    groups = list(stopping.groups(case.rounds)) if stopping is not None else [(1, case.rounds, False)]
+    held = bool(getattr(backend, "lookahead", False)) and hasattr(backend, "run_held")
     rows = []
+    g = 0
 
-    for first, end, checked in groups:
-        rows.append(backend.accumulate([BatchControls(i, ppc) for i in range(first, end + 1)]))
+    while g < len(groups):
+        first, end, checked = groups[g]
+        if held and checked and stopping.history:
+            ahead = _lookahead(stopping, groups, g, backend, ppc)
+            last = groups[g + ahead - 1][1]
+            backend.run_held([BatchControls(i, ppc) for i in range(first, last + 1)])
 
-        if checked:
-            stopping.load(backend.statistics())
-            stopping.check(end)
+            for f, e, c in groups[g : g + ahead]:
+                rows.extend(backend.fold_next()[None, :] for _ in range(f, e + 1))
 
-            if stopping.converged:
-                break
+                if c:
+                    stopping.load(backend.statistics())
+                    stopping.check(e)
+
+                    if stopping.converged:
+                        break
+
+            g += ahead
+        else:
+            rows.append(backend.accumulate([BatchControls(i, ppc) for i in range(first, end + 1)]))
+            g += 1
+
+            if checked:
+                stopping.load(backend.statistics())
+                stopping.check(end)
+
+        if stopping is not None and stopping.converged:
+            break
 
     statistics = backend.statistics()
     total = statistics["total"]

@@ -87,13 +87,14 @@ def gradients(params, x, target, weight, scale=None, bf16_values=True):
     g = {}
     g["w4"] = c["H3"].T @ dy
     g["b4"] = np.array([dy.sum()])
-    G3 = r(np.outer(dy, c["p"]["w4"]) * gelu_grad(c["Z3"]))
+    # The kernels keep the pre-activations in BF16 for the backward pass.
+    G3 = r(np.outer(dy, c["p"]["w4"]) * gelu_grad(r(c["Z3"])))
     g["W3"] = G3.T @ c["H2"]
     g["b3"] = G3.sum(0)
-    G2 = r((G3 @ c["W3"]) * gelu_grad(c["Z2"]))
+    G2 = r((G3 @ c["W3"]) * gelu_grad(r(c["Z2"])))
     g["W2"] = G2.T @ c["H1"]
     g["b2"] = G2.sum(0)
-    G1 = r((G2 @ c["W2"]) * gelu_grad(c["Z1"]))
+    G1 = r((G2 @ c["W2"]) * gelu_grad(r(c["Z1"])))
     g["W1"] = G1.T @ c["X"]
     g["b1"] = G1.sum(0)
     return loss, pack(g)

@@ -31,10 +31,11 @@ What each fixture pins, and where it comes from:
                          own photon budgets and four config-3 scenes; the GPU parity test
                          compares against them.
   archived_amf_oracle.npz
-                         The oracle's layer-path round moments for the archived 1-layer-cloud
-                         run at that run's own budget (20,000 photons per column, 100 rounds,
-                         every view): per view and layer the sums over rounds of the path
-                         tally p, of the weight tally w, and of p^2, w^2 and p w.
+                         The oracle's layer-path round moments for the archived clear-sky and
+                         1-layer-cloud runs at their own budgets (10,000 and 20,000 photons per
+                         column, 100 rounds, every view): per view and layer the sums over
+                         rounds of the path tally p, of the weight tally w, and of p^2, w^2
+                         and p w.
   comparator_verdicts.json
                          The reference's own check_result / compare / select_views
                          (python/monki/validation.py) on the seeded products and cases of
@@ -552,33 +553,39 @@ def budget_moments():
 
 
 def archived_amf_oracle():
-    """Layer-path round moments of the oracle for the archived 1-layer-cloud run, at that
-    run's photons and rounds, views in the archived order (about 8 minutes on 8 cores)."""
+    """Layer-path round moments of the oracle for the archived runs that kept layer AMFs
+    (the clear sky and the 1-layer cloud), at each run's photons and rounds, views in the
+    archived order (about 12 minutes on 8 cores); keys "<run>.<moment>"."""
 
     sys.path.insert(0, str(HERE.parent))
     sys.path.insert(0, str(REPO))
     import archived_runs as ar
     from oracle import oracle
 
-    fixture = ar.load("1layercloud")
-    ppc, rounds = int(fixture["n_photons_per_column"][0]), int(fixture["n_rounds"][0])
-    layers = fixture["z_unit"].size
-    views = fixture["theta"].size
-    out = {key: np.zeros((views, layers)) for key in ("p", "pp", "pw")}
-    out.update({key: np.zeros(views) for key in ("w", "ww")})
-    for lo, hi in ar.view_groups(fixture):
-        tables = ar.with_views(fixture["tables"], fixture["theta"][lo:hi])
-        tallies, _ = oracle.run(tables, [ppc * rounds, 0, 1, ORACLE_SEED, 100000, 0, ppc, rounds], os.cpu_count() or 1)
-        parts = [oracle.split(tables, tallies[r]) for r in range(rounds)]
-        p = np.stack([q[1][0, 0, :layers, :] for q in parts])  # (round, layer, view), 1 x 1 column
-        w = np.stack([q[2][0, 0, :] for q in parts])  # (round, view)
-        out["p"][lo:hi] = p.sum(0).T
-        out["pp"][lo:hi] = (p * p).sum(0).T
-        out["pw"][lo:hi] = (p * w[:, None, :]).sum(0).T
-        out["w"][lo:hi] = w.sum(0)
-        out["ww"][lo:hi] = (w * w).sum(0)
-        print("views", lo, hi, flush=True)
-    return {**out, "photons_per_column": np.array(ppc), "rounds": np.array(rounds), "seed": np.array(ORACLE_SEED)}
+    out = {}
+    for name in ("cloudfree", "1layercloud"):
+        fixture = ar.load(name)
+        ppc, rounds = int(fixture["n_photons_per_column"][0]), int(fixture["n_rounds"][0])
+        layers = fixture["z_unit"].size
+        views = fixture["theta"].size
+        moments = {key: np.zeros((views, layers)) for key in ("p", "pp", "pw")}
+        moments.update({key: np.zeros(views) for key in ("w", "ww")})
+        for lo, hi in ar.view_groups(fixture):
+            tables = ar.with_views(fixture["tables"], fixture["theta"][lo:hi])
+            tallies, _ = oracle.run(tables, [ppc * rounds, 0, 1, ORACLE_SEED, 100000, 0, ppc, rounds],
+                                    os.cpu_count() or 1)
+            parts = [oracle.split(tables, tallies[r]) for r in range(rounds)]
+            p = np.stack([q[1][0, 0, :layers, :] for q in parts])  # (round, layer, view), 1 x 1 column
+            w = np.stack([q[2][0, 0, :] for q in parts])  # (round, view)
+            moments["p"][lo:hi] = p.sum(0).T
+            moments["pp"][lo:hi] = (p * p).sum(0).T
+            moments["pw"][lo:hi] = (p * w[:, None, :]).sum(0).T
+            moments["w"][lo:hi] = w.sum(0)
+            moments["ww"][lo:hi] = (w * w).sum(0)
+            print(name, "views", lo, hi, flush=True)
+        moments.update({"photons_per_column": np.array(ppc), "rounds": np.array(rounds), "seed": np.array(ORACLE_SEED)})
+        out.update({f"{name}.{key}": value for key, value in moments.items()})
+    return out
 
 
 def comparator_verdicts(ref):

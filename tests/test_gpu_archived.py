@@ -6,21 +6,23 @@ Per run, every view's I, Q, U (every pixel of the box clouds): the reference's c
 |z| < 3 in at least 99 % of entries, and no |z| beyond the Bonferroni bound at family
 error 1e-6; the mean z where the entries are many and weakly correlated (box clouds).
 
-The layered-cloud run also archived its layer AMFs, without their standard error. Layer
-path tallies are heavy tailed (a photon scattered near the horizontal crosses hundreds of
-kilometres of a thin layer, and every later peel-off of its history carries that path), so
-a run's round-variance error understates its spread and neighbouring views deviate
-together. The AMFs are therefore checked twice:
+The clear-sky and layered-cloud runs also archived their layer AMFs, without their
+standard error. Layer path tallies are heavy tailed (a photon scattered near the horizontal
+crosses hundreds of kilometres of a thin layer, and every later peel-off of its history
+carries that path), so a run's round-variance error understates its spread and neighbouring
+views deviate together. The AMFs are therefore checked twice:
   * against the oracle at the same budget (its layer-path round moments in
     tests/golden/archived_amf_oracle.npz, independent random streams), combined standard
     error from both runs: |z| < 3 in at least 99 % of the view x layer entries and no |z|
-    beyond the Bonferroni bound. No mean-z criterion: two oracle runs with different seeds
-    differ by a mean z of -0.20 here (one run catches a long path the other misses);
+    beyond the Bonferroni bound. No mean-z criterion: two oracle runs of the layered cloud
+    with different seeds differ by a mean z of -0.20 (one run catches a long path the other
+    misses);
   * against the archived Fortran values, with twice our error as the combined error, as
     closely as the oracle itself agrees with them: the fraction of entries with |z| < 3 at
-    most one point below the oracle's (98.2 %; another oracle seed gives 99.2 %), the
-    deviations correlated with the oracle's (the archived run's own spikes are shared),
-    and the four layers above 40 km (optical depth below 0.002) within 1 % relative.
+    most one point below the oracle's (98.2 % for the layered cloud; another oracle seed
+    gives 99.2 %), the deviations correlated with the oracle's (the archived run's own
+    spikes are shared), and the layers above 40 km (optical depth below 0.002) within 1 %
+    relative.
 """
 
 from __future__ import annotations
@@ -95,7 +97,8 @@ def test_fp32_transport_agrees_with_the_archived_fortran_run(device, name):
         dz = fixture["z_unit"]
         ours, our_error = amf[:, :, 0, 0], amf_error[:, :, 0, 0]
         # Against the oracle at the same budget.
-        o = np.load(ORACLE_AMF)
+        with np.load(ORACLE_AMF) as data:
+            o = {key.split(".", 1)[1]: data[key] for key in data.files if key.startswith(name + ".")}
         n = int(o["rounds"])
         ratio = o["p"] / o["w"][:, None]
         spread = np.sqrt(n / (n - 1) * np.maximum(o["pp"] - 2 * ratio * o["pw"] + ratio**2 * o["ww"][:, None], 0.0))

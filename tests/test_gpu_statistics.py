@@ -2,8 +2,9 @@
 
 The same scene, seed and rounds through ``simulate`` twice: once with the round sums,
 sums of squares and AMF moments folded on the GPU (``CUDA(device_statistics=True)``,
-the default) and once from each round's tallies on the host (the reference driver's
-loop). FP64 transport keeps the per-round tallies equal up to the order of the device's
+the default, which after the first check also runs the rounds the last check says are
+still needed as one held group, folded and checked round by round) and once from each
+round's tallies on the host (the reference driver's loop). FP64 transport keeps the per-round tallies equal up to the order of the device's
 atomic sums, so the products agree to 1e-9 (the AMF standard error, a difference of
 nearly equal moments, to 1e-6) and the stopping decisions match.
 """
