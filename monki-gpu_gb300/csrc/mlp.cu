@@ -55,17 +55,27 @@ void write_error(char* err, size_t n, const std::string& msg) {
 // ----------------------------------------------------------------------------------
 
 // Rows of FP32 features (gathered through idx when given) into the padded BF16 input and
-// its transpose; rows >= n and columns >= F are zero.
-__global__ void pack_input(const float* __restrict__ x, const uint32_t* __restrict__ idx, int n, int F, int R,
-                           bf16* __restrict__ X, bf16* __restrict__ XT) {
-    const int total = R * kIn;
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
-        const int m = e / kIn, c = e % kIn;
+// its transpose; rows >= n and columns >= F are zero. Block: 256 threads over 64 rows; the
+// rows are read and X written row by row, then the tile is transposed in shared memory so
+// the XT rows are written as contiguous 128-byte segments too.
+constexpr int kPackRows = 64, kPackStride = kIn + 1;
+__global__ void __launch_bounds__(256)
+pack_input(const float* __restrict__ x, const uint32_t* __restrict__ idx, int n, int F, int R,
+           bf16* __restrict__ X, bf16* __restrict__ XT) {
+    __shared__ bf16 tile[kPackRows * kPackStride];
+    const int m0 = blockIdx.x * kPackRows;
+    for (int e = threadIdx.x; e < kPackRows * kIn; e += blockDim.x) {
+        const int q = e / kIn, c = e % kIn, m = m0 + q;
         float v = 0.f;
         if (m < n && c < F) v = x[size_t(idx ? idx[m] : uint32_t(m)) * F + c];
         const bf16 b = __float2bfloat16(v);
-        X[size_t(m) * kIn + c] = b;
-        XT[size_t(c) * R + m] = b;
+        tile[q * kPackStride + c] = b;
+        if (m < R) X[size_t(m) * kIn + c] = b;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < kPackRows * kIn; e += blockDim.x) {
+        const int c = e / kPackRows, q = e % kPackRows, m = m0 + q;
+        if (m < R) XT[size_t(c) * R + m] = tile[q * kPackStride + c];
     }
 }
 
@@ -116,54 +126,48 @@ __global__ void loss_grad(const float* __restrict__ y, const float* __restrict__
 }
 
 // Output layer backward: dw4 += dy^T H3, db4 += sum dy, dZ3 = dy w4^T * GELU'(Z3) in BF16,
-// its transpose (row n of GT: 64 contiguous rows of column n per thread, written as eight
-// 16-byte stores) and db3 += the column sums of dZ3. Block: 256 threads (one per hidden
-// unit) over a slab of 64 rows; rows from `rows` to the slab's end are written as zeros.
-__global__ void head_backward(const float* __restrict__ dy, const bf16* __restrict__ H, const float* __restrict__ w4,
-                              const bf16* __restrict__ Z, int rows, int R, float* __restrict__ grads,
-                              bf16* __restrict__ G, bf16* __restrict__ GT) {
+// its transpose and db3 += the column sums of dZ3. Block: 256 threads (one per hidden unit)
+// over a slab of 64 rows; the slab's dZ3 is staged in shared memory (odd row stride, so the
+// column reads are free of bank conflicts) and each warp then writes 32 rows of the
+// transpose as 128-byte segments. Rows from `rows` to the slab's end are written as zeros.
+constexpr int kSlab = 64, kSlabStride = kHidden + 1;
+__global__ void __launch_bounds__(kHidden)
+head_backward(const float* __restrict__ dy, const bf16* __restrict__ H, const float* __restrict__ w4,
+              const bf16* __restrict__ Z, int rows, int R, float* __restrict__ grads, bf16* __restrict__ G,
+              bf16* __restrict__ GT) {
+    __shared__ bf16 tile[kSlab * kSlabStride];
     const int n = threadIdx.x;
-    const int m0 = blockIdx.x * 64;
+    const int m0 = blockIdx.x * kSlab;
     float acc = 0.f, bias = 0.f, column = 0.f;
     const float wn = w4[n];
-    uint32_t packed[32];
-#pragma unroll
-    for (int q = 0; q < 32; ++q) {
-        float g2[2];
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            const int m = m0 + 2 * q + u;
-            g2[u] = 0.f;
-            if (m < rows) {
-                const float d = dy[m];
-                const size_t at = size_t(m) * kHidden + n;
-                acc += d * __bfloat162float(H[at]);
-                bias += d;
-                const bf16 g = __float2bfloat16(d * wn * umma::gelu_grad(__bfloat162float(Z[at])));
-                G[at] = g;
-                g2[u] = __bfloat162float(g);
-                column += g2[u];
-            }
+    for (int q = 0; q < kSlab; ++q) {
+        const int m = m0 + q;
+        bf16 g = __float2bfloat16(0.f);
+        if (m < rows) {
+            const float d = dy[m];
+            const size_t at = size_t(m) * kHidden + n;
+            acc += d * __bfloat162float(H[at]);
+            bias += d;
+            g = __float2bfloat16(d * wn * umma::gelu_grad(__bfloat162float(Z[at])));
+            G[at] = g;
+            column += __bfloat162float(g);
         }
-        const __nv_bfloat162 pair = __floats2bfloat162_rn(g2[0], g2[1]);
-        packed[q] = *reinterpret_cast<const uint32_t*>(&pair);
-    }
-    bf16* dst = GT + size_t(n) * R + m0;
-    if (m0 + 64 <= R) {
-#pragma unroll
-        for (int q = 0; q < 32; q += 4)
-            reinterpret_cast<uint4*>(dst)[q / 4] = make_uint4(packed[q], packed[q + 1], packed[q + 2], packed[q + 3]);
-    } else {
-#pragma unroll
-        for (int q = 0; q < 32; ++q) {
-            const __nv_bfloat162 pair = *reinterpret_cast<const __nv_bfloat162*>(&packed[q]);
-            if (m0 + 2 * q < R) dst[2 * q] = pair.x;
-            if (m0 + 2 * q + 1 < R) dst[2 * q + 1] = pair.y;
-        }
+        tile[q * kSlabStride + n] = g;
     }
     atomicAdd(grads + ow4 + n, acc);
     atomicAdd(grads + ob3 + n, column);
     if (n == 0) atomicAdd(grads + ob4, bias);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m = m0 + 2 * lane;
+    for (int c = warp; c < kHidden; c += kHidden / 32) {
+        __nv_bfloat162 pair;
+        pair.x = tile[(2 * lane) * kSlabStride + c];
+        pair.y = tile[(2 * lane + 1) * kSlabStride + c];
+        bf16* dst = GT + size_t(c) * R + m;
+        if (m + 1 < R) *reinterpret_cast<__nv_bfloat162*>(dst) = pair;
+        else if (m < R) dst[0] = pair.x;
+    }
 }
 
 __global__ void adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1, float* __restrict__ m2,
@@ -483,7 +487,7 @@ int monki_mlp_forward(void* handle, const float* x, uint32_t rows, float* y, cha
                 const int m = int(std::min<uint32_t>(uint32_t(n->R), rows - r0));
                 check(cudaMemcpyAsync(dx, x + size_t(r0) * n->features, size_t(m) * n->features * sizeof(float),
                                       cudaMemcpyHostToDevice, n->stream), "upload");
-                pack_input<<<1024, 256, 0, n->stream>>>(dx, nullptr, m, n->features, n->R, n->X, n->XT);
+                pack_input<<<(n->R + kPackRows - 1) / kPackRows, 256, 0, n->stream>>>(dx, nullptr, m, n->features, n->R, n->X, n->XT);
                 forward(*n, m);
                 check(cudaMemcpyAsync(y + r0, n->y, size_t(m) * sizeof(float), cudaMemcpyDeviceToHost, n->stream), "download");
                 check_failure(*n);
@@ -518,7 +522,7 @@ int monki_mlp_gradients(void* handle, const float* x, const float* target, const
         check(cudaMemcpyAsync(dx, x, size_t(rows) * n->features * sizeof(float), cudaMemcpyHostToDevice, n->stream), "upload");
         check(cudaMemcpyAsync(dt, target, rows * sizeof(float), cudaMemcpyHostToDevice, n->stream), "upload");
         check(cudaMemcpyAsync(dw, weight, rows * sizeof(float), cudaMemcpyHostToDevice, n->stream), "upload");
-        pack_input<<<1024, 256, 0, n->stream>>>(dx, nullptr, int(rows), n->features, n->R, n->X, n->XT);
+        pack_input<<<(n->R + kPackRows - 1) / kPackRows, 256, 0, n->stream>>>(dx, nullptr, int(rows), n->features, n->R, n->X, n->XT);
         gather_targets<<<256, 256, 0, n->stream>>>(dt, dw, nullptr, int(rows), n->R, n->tb, n->wb);
         check(cudaMemsetAsync(n->grads, 0, kParams * sizeof(float), n->stream), "memset");
         check(cudaMemsetAsync(n->loss, 0, sizeof(float), n->stream), "memset");
@@ -577,7 +581,7 @@ int monki_mlp_train(void* handle, uint32_t steps, uint32_t batch, float lr, floa
             for (uint32_t s = 0; s < steps; ++s) {
                 const uint32_t t = ++n->step;
                 sample_indices<<<(batch + 255) / 256, 256, 0, n->stream>>>(t, n->seed, int(batch), n->data_n, n->idx);
-                pack_input<<<1024, 256, 0, n->stream>>>(n->data_x, n->idx, int(batch), n->features, n->R, n->X, n->XT);
+                pack_input<<<(n->R + kPackRows - 1) / kPackRows, 256, 0, n->stream>>>(n->data_x, n->idx, int(batch), n->features, n->R, n->X, n->XT);
                 gather_targets<<<256, 256, 0, n->stream>>>(n->data_t, n->data_w, n->idx, int(batch), n->R, n->tb, n->wb);
                 check(cudaMemsetAsync(n->grads, 0, kParams * sizeof(float), n->stream), "memset");
                 forward(*n, int(batch));
