@@ -62,9 +62,10 @@ TARGET = 0.01  # SE/|I| in every pixel and view
 TARGET_PPC = 1000
 TARGET_SEEDS = (23274, 23275, 23276)
 TARGET_CAP = 1024  # round cap of a time-to-target run
-# epsilon, roulette weight, cap, split: Russian roulette below weight 0.35, splitting above 0.7
-# (the best constant weight window of a sweep of roulette 0.25-1 and split 1.5-3 on this scene).
-GUIDED = (0.0, 0.35, 0.0, 2.0)
+# epsilon, roulette weight, cap, split: Russian roulette below weight 0.25, splitting above 0.5
+# (the fastest constant weight window to the target of a sweep of roulette 0.2-1 and split
+# 1.5-3 on this scene).
+GUIDED = (0.0, 0.25, 0.0, 2.0)
 E2E_ROUNDS = 32  # rounds of the end-to-end run at the workload's own round size
 STATE_BYTES = 64  # one event's photon state records read by the peel kernel
 CELL_BYTES = 16  # one cell record (beta + cumulative species fractions)

@@ -26,10 +26,10 @@ from .guided import Guided
 FEATURES = 48
 # Guided transport under the learned weight window: Russian roulette below the cell's weight
 # W = roulette x scale[cell], splitting above split x W; the window is the best constant one
-# (roulette 0.35, split 2) moved per cell by the network, (importance / median) ** -0.25
+# (roulette 0.25, split 2) moved per cell by the network, (importance / median) ** -0.25
 # clipped to [0.7, 1.4]. Stronger moves (exponent 0.5, [0.5, 2]) gained 11-29 % on the
 # median pixel's variance x cost of held-out box clouds and lost 10-25 % on the worst pixel.
-LEARNED_GUIDE = Guided(0.0, 0.35, 0.0, 2.0)
+LEARNED_GUIDE = Guided(0.0, 0.25, 0.0, 2.0)
 LEARNED_WINDOW = {"exponent": 0.25, "low": 0.7, "high": 1.4}
 PARAMETERS = 64 * 256 + 256 + 2 * (256 * 256 + 256) + 256 + 1
 
