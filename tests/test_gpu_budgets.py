@@ -119,3 +119,31 @@ def test_fp32_product_at_the_workload_budget_agrees_with_the_oracle(device, tmp_
     gpu = simulate(scene, CUDA(seed=0), tmp_path / "gpu.nc")
     verdict = compare(_oracle_product(gpu, m, scene), gpu)
     assert verdict.passed, verdict.details
+
+
+def test_multi_scene_session_agrees_with_the_oracle_at_the_workload_budgets(device):
+    """The four config-3 scenes of the fixtures in one multi-scene session (one launch
+    sequence over a shared photon pool, FP32, seed 0), 32 rounds each at their own budgets:
+    every tally entry by the same z-criteria against the oracle's round moments."""
+
+    from monki.batched import run_persistent
+
+    names = [name for name in NAMES if name.startswith("batched_")]
+    moments = [_moments(name) for name in names]
+    batch = [_scene(m) for m in moments]
+    rounds = int(moments[0]["rounds"])
+    assert all(int(m["rounds"]) == rounds for m in moments)
+    results, summary = run_persistent(batch, seed=0, rounds=rounds)
+    assert summary["scenes"] == len(batch)
+    for name, m, (batches, _) in zip(names, moments, results, strict=True):
+        ppc = int(m["photons_per_column"])
+        x = np.stack([_flat(b) for b in batches]) / ppc
+        n = x.shape[0]
+        mean_o = m["sum"] / n
+        var_o = np.maximum(m["squares"] - m["sum"] ** 2 / n, 0.0) / (n - 1) / n
+        se = np.sqrt(x.var(0, ddof=1) / n + var_o)
+        mask = se > 0
+        z = (x.mean(0) - mean_o)[mask] / se[mask]
+        assert z.size > 1000, name
+        assert np.mean(np.abs(z) < 3) >= 0.99, (name, np.sort(np.abs(z))[-10:])
+        assert abs(z.mean()) < 0.1, (name, z.mean())

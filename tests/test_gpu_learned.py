@@ -8,7 +8,9 @@ the learned weight window agrees with the analog kernel within combined standard
 (the window moves variance, never the expectation); and what the network gives against
 the same window without it, on the pixel that sets the time to a precision target in
 every pixel: the worst pixel's variance x cost, with cost the scatters of the run (the
-same for a given seed, unlike wall time), over two held-out scenes and two seeds each.
+same for a given seed, unlike wall time), over two held-out scenes and two seeds each —
+on the best constant window (roulette 0.25, where the network's mild move matches it) and
+on a roulette-0.35 window (where its move gains).
 """
 
 from __future__ import annotations
@@ -35,12 +37,18 @@ def _relative_se(x):
 
 def test_learned_importance_generalises_and_keeps_estimates_unbiased(device):
     import monki.scenes as scenes
+    from monki import Guided
     from monki.importance import (LEARNED_GUIDE, cell_features, importance_targets, learned_scale,
                                   objective_tally, r_squared, train_model, training_scenes)
 
     model, losses, rows = train_model(training_scenes(6), steps=600, batch=8192, rows_per_scene=8000)
     ppc, rounds = 2000, 64
-    worst_ratio, median_ratio, over_analog = [], [], []
+    # The learned window on the best constant window, and the network's move on a
+    # roulette-0.35 window against that window alone.
+    settings = {"best": (LEARNED_GUIDE, {}), "r35": (Guided(0.0, 0.35, 0.0, 2.0), {"low": 0.7, "high": 1.4})}
+    worst = {key: [] for key in settings}
+    median = {key: [] for key in settings}
+    over_analog = []
     with model:
         assert np.all(np.isfinite(losses)) and losses[-50:].mean() < 0.5 * losses[:20].mean()
         for seed in (1000, 1001):
@@ -51,23 +59,28 @@ def test_learned_importance_generalises_and_keeps_estimates_unbiased(device):
             fit = r_squared(prediction[weight > 0], target[weight > 0], weight[weight > 0])
             print(f"held-out box cloud {seed}: weighted R^2 {fit:.3f}")
             assert fit > 0.8, fit
-            scale = learned_scale(model, scene)
             # 64 rounds: roulette makes the estimates skewed, and with few rounds a low sample
             # mean comes with a low sample variance, which pulls the mean z below zero.
             plain, plain_cost = _rounds(scene, None, None, ppc, rounds, seed)
-            for repeat in range(2):
-                constant, constant_cost = _rounds(scene, LEARNED_GUIDE, None, ppc, rounds, seed + 10 + repeat)
-                learned, learned_cost = _rounds(scene, LEARNED_GUIDE, scale, ppc, rounds, seed + 20 + repeat)
-                se = lambda a: a.std(0, ddof=1) / np.sqrt(rounds)  # noqa: E731
-                z = (learned.mean(0) - plain.mean(0)) / np.hypot(se(learned), se(plain))
-                assert np.mean(np.abs(z) < 3) >= 0.99 and abs(z.mean()) < 0.1, (np.mean(np.abs(z) < 3), z.mean())
-                merit = lambda x, cost, pick: 1.0 / (pick(_relative_se(x)) ** 2 * cost)  # noqa: E731
-                worst_ratio.append(merit(learned, learned_cost, np.max) / merit(constant, constant_cost, np.max))
-                median_ratio.append(merit(learned, learned_cost, np.median) / merit(constant, constant_cost, np.median))
-                over_analog.append(merit(learned, learned_cost, np.max) / merit(plain, plain_cost, np.max))
-    print(f"learned window over the same constant window, worst pixel {np.round(worst_ratio, 3)}, "
-          f"median pixel {np.round(median_ratio, 3)}; over analog, worst pixel {np.round(over_analog, 2)}")
-    # The learned window matches the constant one on the worst pixel (within 10 %) and keeps
-    # the guided gain over analog transport.
-    assert np.mean(worst_ratio) > 0.9, worst_ratio
+            for key, (guide, window) in settings.items():
+                scale = learned_scale(model, scene, **window)
+                for repeat in range(2):
+                    constant, constant_cost = _rounds(scene, guide, None, ppc, rounds, seed + 10 + repeat)
+                    learned, learned_cost = _rounds(scene, guide, scale, ppc, rounds, seed + 20 + repeat)
+                    se = lambda a: a.std(0, ddof=1) / np.sqrt(rounds)  # noqa: E731
+                    z = (learned.mean(0) - plain.mean(0)) / np.hypot(se(learned), se(plain))
+                    assert np.mean(np.abs(z) < 3) >= 0.99 and abs(z.mean()) < 0.1, (np.mean(np.abs(z) < 3), z.mean())
+                    merit = lambda x, cost, pick: 1.0 / (pick(_relative_se(x)) ** 2 * cost)  # noqa: E731
+                    worst[key].append(merit(learned, learned_cost, np.max) / merit(constant, constant_cost, np.max))
+                    median[key].append(merit(learned, learned_cost, np.median) / merit(constant, constant_cost, np.median))
+                    if key == "best":
+                        over_analog.append(merit(learned, learned_cost, np.max) / merit(plain, plain_cost, np.max))
+    for key in settings:
+        print(f"learned window over the same window without the network ({key}): worst pixel "
+              f"{np.round(worst[key], 3)}, median pixel {np.round(median[key], 3)}")
+    print(f"learned window over analog, worst pixel {np.round(over_analog, 2)}")
+    # On the best constant window the network's mild move matches it on the worst pixel; on the
+    # roulette-0.35 window its move gains there; both keep the guided gain over analog.
+    assert np.mean(worst["best"]) > 0.93, worst["best"]
+    assert np.mean(worst["r35"]) > 1.0, worst["r35"]
     assert min(over_analog) > 2.0, over_analog
