@@ -21,6 +21,20 @@ from ..guided import Guided
 from ..input import ReferenceCase
 from ..scenes import TransportScene
 from . import native as _native
+
+_DIGESTS: dict = {}
+
+
+def _library_digest(path) -> str:
+    """SHA-256 of the native library file, computed once per file version in a process (the
+    receipts carry it; hashing the library on every prepare cost a few milliseconds)."""
+
+    stat = os.stat(path)
+    key = (os.fspath(path), stat.st_size, stat.st_mtime_ns)
+    if key not in _DIGESTS:
+        with open(path, "rb") as f:
+            _DIGESTS[key] = hashlib.sha256(f.read()).hexdigest()
+    return _DIGESTS[key]
 from .backend import Backend
 from .tallies import BatchControls, RawTallies
 
@@ -279,7 +293,7 @@ class CUDA(Backend):
             "pool": self.pool,
             "walk": self.walk,
             "guided": None if self.guided is None else self.guided.describe(),
-            "library_sha256": hashlib.sha256(open(self.library, "rb").read()).hexdigest(),
+            "library_sha256": _library_digest(self.library),
             "tables_sha256": hashlib.sha256(tables.tobytes()).hexdigest(),
             "machine": platform.machine(),
             "python_version": platform.python_version(),

@@ -85,15 +85,17 @@ def _host_rounds(case, backend, stopping):
 
 
 def _lookahead(stopping, groups, g, backend, ppc) -> int:
-    """How many checked groups, from ``g`` on, to run in one held dispatch: 90 % of the rounds
-    the last check says the target still needs (at least one group), within one dispatch."""
+    """How many checked groups, from ``g`` on, to run in one held dispatch: the rounds the last
+    check says the target still needs, at least three, within one dispatch. A round past the
+    stopping point costs its transport; one dispatch too few costs a wait for the slowest
+    histories of a dispatch, worth about three rounds on the box cloud."""
 
     estimate = stopping.rounds_estimate()
     if estimate is None:
         return 1
     first = groups[g][0]
     capacity = backend.held_capacity(ppc)
-    wanted = max(1.0, 0.9 * (estimate - (first - 1)))
+    wanted = max(3.0, estimate - (first - 1))
     count, rounds = 0, 0
     for f, e, _ in groups[g:]:
         size = e - f + 1
