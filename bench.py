@@ -605,7 +605,7 @@ def main():
     fused = not scene.save_path  # the session's default: fused step unless the scene has layer paths
     names = ("step", "peel") if fused else ("transit", "peel", "scatter")
     stage_share = {name: stage_ms[q] / stage_total for q, name in enumerate(names)}
-    pool = 1 << 20
+    pool = 1 << 22  # the session's default pool (every slot scanned by a transit launch)
     algorithmic = {
         "step": STEP_EVENT_BYTES * p_scatters + CELL_BYTES * p_visits_fp,
         "transit": SLOT_SCAN_BYTES * pool * int(stage_launches[0]) + TRANSIT_EVENT_BYTES * p_scatters + CELL_BYTES * p_visits_fp,

@@ -68,7 +68,7 @@ class CUDA(Backend):
         precision: str = "fp32",
         block: int = 256,
         engine: str = "wavefront",
-        pool: int = 1 << 20,
+        pool: int = 1 << 22,
         walk: int = 24,
         guided: Guided | None = None,
         importance: bool = False,

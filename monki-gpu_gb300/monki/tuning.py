@@ -18,6 +18,7 @@ import numpy as np
 from .execution import native as _native
 
 CANDIDATES = (
+    {"pool": 1 << 22, "block": 256, "walk": 24},
     {"pool": 1 << 20, "block": 256, "walk": 24},
     {"pool": 1 << 20, "block": 128, "walk": 24},
     {"pool": 1 << 19, "block": 256, "walk": 8},
