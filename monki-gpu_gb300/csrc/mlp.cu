@@ -9,7 +9,8 @@
 //   W1[256 x 64], b1[256], W2[256 x 256], b2[256], W3[256 x 256], b3[256], w4[256], b4[1]
 //
 // Per layer l with input X (rows x K) and weights W (256 x K):
-//   forward   Z = X W^T + b (tcgen05, epilogue adds b, writes Z in BF16, H = GELU(Z), H^T)
+//   forward   Z = X W^T + b (tcgen05, epilogue adds b, writes Z in BF16, H = GELU(Z), H^T;
+//             the last layer's epilogue also forms the output y = H3 w4 + b4)
 //   backward  dW += dZ^T X (tcgen05 split-K over the rows, A = dZ^T, B = X^T)
 //             dX' = (dZ W) * GELU'(Z_prev) (tcgen05, B = W^T, epilogue applies GELU' and
 //             adds the column sums of dX' to the previous layer's bias gradient)
@@ -95,20 +96,6 @@ __global__ void sample_indices(uint32_t step, uint32_t seed, int batch, uint32_t
         const uint32_t r = lane == 0 ? w.x : lane == 1 ? w.y : lane == 2 ? w.z : w.w;
         idx[i] = uint32_t((uint64_t(r) * n) >> 32);
     }
-}
-
-// y = H3 w4 + b4, one warp per row.
-__global__ void head_forward(const bf16* __restrict__ H, const float* __restrict__ w4, const float* __restrict__ b4,
-                             int rows, float* __restrict__ y) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (warp >= rows) return;
-    const bf16* h = H + size_t(warp) * kHidden + lane * 8;
-    float acc = 0.f;
-#pragma unroll
-    for (int q = 0; q < 8; ++q) acc += __bfloat162float(h[q]) * w4[lane * 8 + q];
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-    if (lane == 0) y[warp] = acc + b4[0];
 }
 
 // dy = 2 w (y - t) / sum(w); loss accumulates sum w (y - t)^2 / sum(w).
@@ -330,11 +317,11 @@ void forward(Net& n, int rows) {
     gemm<umma::kForward>(g, 1, n.stream);
     g = params_for(n.H2, n.W3, rows, kHidden, kHidden, n.failure);
     g.p.Z = n.Z3; g.p.bias = n.params + ob3; g.p.H = n.H3; g.p.HT = nullptr; g.p.rows_ht = R;
+    // The output layer rides on this epilogue: y = H3 w4 + b4.
+    g.p.head_w = n.params + ow4; g.p.head_b = n.params + ob4; g.p.head_y = n.y;
     gemm<umma::kForward>(g, 1, n.stream);
     clear_tail(n.H1T, rows, R, kHidden, n.stream);
     clear_tail(n.H2T, rows, R, kHidden, n.stream);
-    head_forward<<<(rows * 32 + 255) / 256, 256, 0, n.stream>>>(n.H3, n.params + ow4, n.params + ob4, rows, n.y);
-    check(cudaGetLastError(), "head launch");
 }
 
 // Loss and gradients of the first `rows` rows against tb / wb (gradients accumulate into

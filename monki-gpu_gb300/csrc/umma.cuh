@@ -64,6 +64,11 @@ struct Params {
     __nv_bfloat16* H;         // kForward / kBackward: rows_a x N
     __nv_bfloat16* HT;        // kForward / kBackward: N x rows_ht (transposed), or null
     int rows_ht;              // row stride of HT (>= rows_a, a multiple of 8)
+    // kForward, optional: a linear output layer on the BF16 activations, y = H head_w +
+    // head_b[0] per row (head_w: N values), written to head_y (rows_a values).
+    const float* head_w;
+    const float* head_b;
+    float* head_y;
     uint32_t* failure;        // bit 1: an mbarrier wait gave up
 };
 
@@ -207,10 +212,14 @@ gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensor
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
+    // The output layer's partial sums of each row (two halves of the columns), after the
+    // transpose tiles.
+    float* head_part = reinterpret_cast<float*>(base + 32 * 1024);
     if (!aborted && steps > 0) {
         const int quarter = warp & 3, half = warp >> 2;
         const int m = row0 + quarter * 32 + lane;
         const bool valid = m < p.rows_a;
+        float head = 0.f;
         unsigned char* stage_t = base + warp * (32 * kTransposeStride);  // this warp's transpose tile
         for (int c0 = 32 * half; c0 < N; c0 += 64) {
             uint32_t r[32];
@@ -284,6 +293,15 @@ gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensor
                         for (int q = 0; q < 16; q += 4)
                             *reinterpret_cast<uint4*>(p.H + at + 2 * q) =
                                 make_uint4(packed[q], packed[q + 1], packed[q + 2], packed[q + 3]);
+                    if (EPI == kForward && p.head_w) {
+#pragma unroll
+                        for (int q = 0; q < 16; q += 2) {
+                            const float4 w = *reinterpret_cast<const float4*>(p.head_w + c0 + 2 * q);
+                            const float2 h0 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&packed[q]));
+                            const float2 h1 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&packed[q + 1]));
+                            head += h0.x * w.x + h0.y * w.y + h1.x * w.z + h1.y * w.w;
+                        }
+                    }
                     if (p.HT) {
                         // Transpose through shared memory: lane (row m) writes its 32 values down
                         // a column of the warp's tile, then lane (column c0 + lane) writes the 32
@@ -337,6 +355,7 @@ gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensor
                     const __nv_bfloat16 h = __float2bfloat16(gelu(z));
                     p.H[e] = h;
                     if (p.HT) p.HT[size_t(n) * p.rows_ht + m] = h;
+                    if (p.head_w) head += __bfloat162float(h) * p.head_w[n];
                 } else {
                     const __nv_bfloat16 g = __float2bfloat16(acc * gelu_grad(__bfloat162float(p.zprev[e])));
                     p.H[e] = g;
@@ -345,9 +364,14 @@ gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensor
                 }
             }
         }
+        if (EPI == kForward && p.head_w) head_part[half * 128 + quarter * 32 + lane] = head;
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
+    if (EPI == kForward && p.head_w && !aborted && steps > 0 && warp < 4) {
+        const int r = warp * 32 + lane, m = row0 + r;
+        if (m < p.rows_a) p.head_y[m] = head_part[r] + head_part[128 + r] + p.head_b[0];
+    }
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(columns) : "memory");
 }
