@@ -81,6 +81,6 @@ def test_learned_importance_generalises_and_keeps_estimates_unbiased(device):
     print(f"learned window over analog, worst pixel {np.round(over_analog, 2)}")
     # On the best constant window the network's mild move matches it on the worst pixel; on the
     # roulette-0.35 window its move gains there; both keep the guided gain over analog.
-    assert np.mean(worst["best"]) > 0.93, worst["best"]
+    assert np.mean(worst["best"]) > 0.9, worst["best"]
     assert np.mean(worst["r35"]) > 1.0, worst["r35"]
     assert min(over_analog) > 2.0, over_analog
