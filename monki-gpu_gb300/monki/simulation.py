@@ -86,15 +86,18 @@ def _host_rounds(case, backend, stopping):
 
 def _lookahead(stopping, groups, g, backend, ppc) -> int:
     """How many checked groups, from ``g`` on, to run in one held dispatch: the rounds the last
-    check says the target still needs, at least three, within one dispatch. A round past the
-    stopping point costs its transport; one dispatch too few costs a wait for the slowest
-    histories of a dispatch, worth about three rounds on the box cloud."""
+    check says the target still needs, at least three, within one dispatch (0 when group ``g``
+    alone exceeds a dispatch). A round past the stopping point costs its transport; one
+    dispatch too few costs a wait for the slowest histories of a dispatch, worth about three
+    rounds on the box cloud."""
 
     estimate = stopping.rounds_estimate()
-    if estimate is None:
-        return 1
     first = groups[g][0]
     capacity = backend.held_capacity(ppc)
+    if groups[g][1] - first + 1 > capacity:
+        return 0  # a group larger than one dispatch goes through accumulate
+    if estimate is None:
+        return 1
     wanted = max(3.0, estimate - (first - 1))
     count, rounds = 0, 0
     for f, e, _ in groups[g:]:
@@ -125,8 +128,8 @@ def _device_rounds(case, backend, stopping):
 
     while g < len(groups):
         first, end, checked = groups[g]
-        if held and checked and stopping.history:
-            ahead = _lookahead(stopping, groups, g, backend, ppc)
+        ahead = _lookahead(stopping, groups, g, backend, ppc) if held and checked and stopping.history else 0
+        if ahead:
             last = groups[g + ahead - 1][1]
             backend.run_held([BatchControls(i, ppc) for i in range(first, last + 1)])
 

@@ -105,3 +105,22 @@ def test_rounds_estimate_follows_the_square_root_law():
     assert stopping.rounds_estimate() is None
     stopping.history.append({"rounds": 32, "max_relative_se": 0.02, "below_target": False, "streak": 0})
     assert stopping.rounds_estimate() == pytest.approx(128.0)
+
+
+def test_groups_larger_than_a_dispatch_go_through_accumulate(tmp_path):
+    from monki import RadianceConvergence, simulate
+
+    golden = dict(np.load(GOLDEN / "driver_statistics.npz"))
+    rounds = golden["stokes"].shape[0]
+    ppc = int(golden["photons_per_column"])
+    case = type("Case", (), {"photons_per_column": ppc, "rounds": rounds, "backward": False})
+    # Checks every 12 rounds with room for 8 rounds per held dispatch: every group runs
+    # through accumulate, and the products equal the round-by-round driver's.
+    rule = RadianceConvergence(1e-9, minimum_rounds=32, check_every=12, consecutive_checks=1)
+    results = {}
+    for lookahead in (False, True):
+        backend = _device_backend(golden, lookahead)
+        results[lookahead] = simulate(case(), backend, tmp_path / f"{lookahead}.nc", convergence=rule)
+        assert not backend._held
+    for name in ("radiance", "std_radiance"):
+        np.testing.assert_array_equal(results[True].values[name], results[False].values[name])
