@@ -127,19 +127,32 @@ head_backward(const float* __restrict__ dy, const bf16* __restrict__ H, const fl
     const int m0 = blockIdx.x * kSlab;
     float acc = 0.f, bias = 0.f, column = 0.f;
     const float wn = w4[n];
-    for (int q = 0; q < kSlab; ++q) {
-        const int m = m0 + q;
-        bf16 g = __float2bfloat16(0.f);
-        if (m < rows) {
-            const float d = dy[m];
+    // Eight rows in flight per thread: their loads are issued before any is used (rows past
+    // `rows` are inside the R-row buffers, read and then masked).
+    for (int q0 = 0; q0 < kSlab; q0 += 8) {
+        float d[8];
+        bf16 h[8], z[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int m = m0 + q0 + u;
             const size_t at = size_t(m) * kHidden + n;
-            acc += d * __bfloat162float(H[at]);
-            bias += d;
-            g = __float2bfloat16(d * wn * umma::gelu_grad(__bfloat162float(Z[at])));
-            G[at] = g;
-            column += __bfloat162float(g);
+            d[u] = m < rows ? dy[m] : 0.f;
+            h[u] = H[at];
+            z[u] = Z[at];
         }
-        tile[q * kSlabStride + n] = g;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int m = m0 + q0 + u;
+            bf16 g = __float2bfloat16(0.f);
+            if (m < rows) {
+                acc += d[u] * __bfloat162float(h[u]);
+                bias += d[u];
+                g = __float2bfloat16(d[u] * wn * umma::gelu_grad(__bfloat162float(z[u])));
+                G[size_t(m) * kHidden + n] = g;
+                column += __bfloat162float(g);
+            }
+            tile[(q0 + u) * kSlabStride + n] = g;
+        }
     }
     atomicAdd(grads + ow4 + n, acc);
     atomicAdd(grads + ob3 + n, column);
