@@ -90,9 +90,12 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def recorded_traffic(workload, kernel):
+def recorded_traffic(workload, kernel, per_launch=None):
     """Per-launch DRAM bytes (read + write) of one wavefront kernel from the committed ncu
-    summary of the workload, or None."""
+    summary of the workload, or None. The captures ran a smaller pool than the bench's
+    launches; when the summary gives the algorithmic bytes of the captured launch, its
+    traffic is scaled to this launch by the algorithmic bytes (the units processed): the
+    traffic grows with the events a launch handles."""
 
     name = {"box": "box_cloud", "layered": "layered_cloud"}[workload]
     path = ROOT / "profiles" / f"transport_kernel_{name}.md"
@@ -104,7 +107,13 @@ def recorded_traffic(workload, kernel):
     match = re.search(rf"traffic_{kernel}_bytes_per_launch:\s*([0-9.eE+]+)", text)
     if match is None and kernel == "peel":
         match = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", text)
-    return float(match.group(1)) if match else None
+    if match is None:
+        return None
+    traffic = float(match.group(1))
+    captured = re.search(rf"algorithmic_{kernel}_bytes_per_captured_launch:\s*([0-9.eE+]+)", text)
+    if captured is not None and per_launch:
+        traffic *= per_launch / float(captured.group(1))
+    return traffic
 
 
 class Clocks:
@@ -623,7 +632,7 @@ def main():
             "launches": launches_q,
             "achieved_gbs": per_launch / seconds / 1e9,
             "frac": per_launch / seconds / 1e9 / peak,
-            "traffic": recorded_traffic(args.workload, name),
+            "traffic": recorded_traffic(args.workload, name, per_launch),
             "share": stage_share[name],
         }
     dominant = max(names, key=lambda name: stage_share[name])
