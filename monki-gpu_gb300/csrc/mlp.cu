@@ -240,7 +240,8 @@ void configure(int device) {
     check(cudaFuncSetAttribute(umma::gemm<umma::kStore>, cudaFuncAttributeMaxDynamicSharedMemorySize, umma::kSmemBytes), "attr");
     check(cudaFuncSetAttribute(umma::gemm<umma::kForward>, cudaFuncAttributeMaxDynamicSharedMemorySize, umma::kSmemBytes), "attr");
     check(cudaFuncSetAttribute(umma::gemm<umma::kBackward>, cudaFuncAttributeMaxDynamicSharedMemorySize, umma::kSmemBytes), "attr");
-    check(cudaFuncSetAttribute(umma::gemm<umma::kAccumulate>, cudaFuncAttributeMaxDynamicSharedMemorySize, umma::kSmemBytes), "attr");
+    check(cudaFuncSetAttribute(umma::gemm<umma::kAccumulate>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               umma::smem_bytes_of<umma::kAccumulate>()), "attr");
     g_attr_done[device] = true;
 }
 
@@ -299,7 +300,7 @@ void gemm(const Gemm& g, int splits, cudaStream_t stream) {
     const CUtensorMap map_a = tile_map(g.A, p.rows_a, p.K, g.lda, umma::kBlockM);
     const CUtensorMap map_b = tile_map(g.B, p.N, p.K, g.ldb, p.N);
     dim3 grid((p.rows_a + umma::kBlockM - 1) / umma::kBlockM, splits);
-    umma::gemm<EPI><<<grid, umma::kThreads, umma::kSmemBytes, stream>>>(map_a, map_b, p);
+    umma::gemm<EPI><<<grid, umma::kThreads, umma::smem_bytes_of<EPI>(), stream>>>(map_a, map_b, p);
     check(cudaGetLastError(), "gemm launch");
 }
 

@@ -4,7 +4,8 @@
 // Roles inside a CTA of eight warps:
 //   producer  (warp 0, one thread) loads the K-steps' A and B tiles with the Tensor Memory
 //             Accelerator (cp.async.bulk.tensor, 128-byte swizzle) into a ring of shared-
-//             memory stages; each load completes on the stage's "full" mbarrier;
+//             memory stages (two; four for the split-K weight gradients, one CTA per SM);
+//             each load completes on the stage's "full" mbarrier;
 //   MMA       (warp 1, one thread) waits for a stage, issues four tcgen05.mma of K = 16 and
 //             commits them to the stage's "empty" mbarrier, which frees it for the next
 //             load; the last commit also arrives on the "done" mbarrier;
@@ -36,7 +37,7 @@ namespace umma {
 constexpr int kBlockM = 128;
 constexpr int kBlockK = 64;
 constexpr int kThreads = 256;                    // eight warps
-constexpr int kStages = 2;
+constexpr int kStages = 2;                       // shared-memory stages of the output-tile GEMMs
 constexpr uint32_t kSmemA = kBlockM * kBlockK * 2;   // 16 KB
 constexpr uint32_t kSmemB = 256 * kBlockK * 2;       // 32 KB (N <= 256)
 constexpr uint32_t kStage = kSmemA + kSmemB;         // 48 KB, 1024-byte multiple
@@ -52,6 +53,14 @@ enum Epilogue : int {
     kBackward = 2,   // G = acc * GELU'(Zprev); G (bf16), G^T (bf16), column sums of G
     kAccumulate = 3, // C (fp32) += acc (split-K partial, atomics)
 };
+
+// The split-K weight-gradient GEMM runs one CTA per SM (its grid is about one wave) over 16
+// K steps, so it keeps four stages in flight instead of two.
+constexpr int kAccumulateStages = 4;
+template <int EPI>
+constexpr int stages_of() { return EPI == kAccumulate ? kAccumulateStages : kStages; }
+template <int EPI>
+constexpr uint32_t smem_bytes_of() { return EPI == kAccumulate ? uint32_t(kAccumulateStages) * (kSmemA + kSmemB) + 4096u : kSmemBytes; }
 
 struct Params {
     int rows_a, N, K;
@@ -124,7 +133,8 @@ template <int EPI>
 __global__ void __launch_bounds__(kThreads, 1)
 gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, Params p) {
     extern __shared__ __align__(1024) unsigned char raw[];
-    __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages], done_bar;
+    constexpr int kRing = stages_of<EPI>();
+    __shared__ __align__(8) uint64_t full_bar[kRing], empty_bar[kRing], done_bar;
     __shared__ uint32_t tmem_base;
     __shared__ int aborted;
     unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(raw) + 1023) & ~uintptr_t(1023));
@@ -145,7 +155,7 @@ gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensor
     }
     if (threadIdx.x == 32) {
         aborted = 0;
-        for (int s = 0; s < kStages; ++s) {
+        for (int s = 0; s < kRing; ++s) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full_bar[s])) : "memory");
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty_bar[s])) : "memory");
         }
@@ -162,7 +172,7 @@ gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensor
         asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_a)) : "memory");
         asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_b)) : "memory");
         for (int step = 0; step < steps; ++step) {
-            const int s = step % kStages, round = step / kStages;
+            const int s = step % kRing, round = step / kRing;
             if (round > 0 && !wait_parity(smem_u32(&empty_bar[s]), uint32_t(round - 1) & 1u)) {
                 atomicOr(p.failure, 1u);
                 aborted = 1;
@@ -179,7 +189,7 @@ gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensor
         // MMA issuer.
         const uint32_t idesc = instr_desc(kBlockM, N);
         for (int step = 0; step < steps; ++step) {
-            const int s = step % kStages, round = step / kStages;
+            const int s = step % kRing, round = step / kRing;
             if (!wait_parity(smem_u32(&full_bar[s]), uint32_t(round) & 1u)) {
                 atomicOr(p.failure, 1u);
                 aborted = 1;
