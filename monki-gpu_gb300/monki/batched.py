@@ -33,7 +33,7 @@ def run_scene(scene, *, device: int = 0, seed: int = 23274, rounds: int = 1, opt
 
 
 def run_persistent(scenes, *, device: int = 0, seed: int = 23274, rounds: int = 1, precision: str = "fp32",
-                   pool: int = 1 << 22, walk: int = 24, check_every: int = 8, graphs: bool = True,
+                   pool: int = 1 << 22, walk: int = 2, check_every: int = 8, graphs: bool = True,
                    max_steps: int = 100_000, tail: int = 1 << 16, library=None):
     """Every scene in one multi-scene session: returns (per-scene (batches, provenance),
     summary). Scenes are forward, without layer paths, with I or I/Q/U."""

@@ -69,7 +69,7 @@ class CUDA(Backend):
         block: int = 256,
         engine: str = "wavefront",
         pool: int = 1 << 22,
-        walk: int = 24,
+        walk: int = 3,
         guided: Guided | None = None,
         importance: bool = False,
         roulette_scale=None,

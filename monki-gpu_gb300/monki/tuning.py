@@ -18,12 +18,14 @@ import numpy as np
 from .execution import native as _native
 
 CANDIDATES = (
+    {"pool": 1 << 22, "block": 256, "walk": 3},
+    {"pool": 1 << 22, "block": 256, "walk": 2},
+    {"pool": 1 << 20, "block": 256, "walk": 3},
+    {"pool": 1 << 20, "block": 128, "walk": 3},
+    {"pool": 1 << 19, "block": 256, "walk": 2},
+    {"pool": 1 << 21, "block": 256, "walk": 3},
+    {"pool": 1 << 18, "block": 128, "walk": 2},
     {"pool": 1 << 22, "block": 256, "walk": 24},
-    {"pool": 1 << 20, "block": 256, "walk": 24},
-    {"pool": 1 << 20, "block": 128, "walk": 24},
-    {"pool": 1 << 19, "block": 256, "walk": 8},
-    {"pool": 1 << 21, "block": 256, "walk": 24},
-    {"pool": 1 << 18, "block": 128, "walk": 8},
 )
 
 
