@@ -137,6 +137,7 @@ gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensor
     __shared__ __align__(8) uint64_t full_bar[kRing], empty_bar[kRing], done_bar;
     __shared__ uint32_t tmem_base;
     __shared__ int aborted;
+    __shared__ int issued, consumed;  // K steps whose loads were issued / whose MMAs were committed
     unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(raw) + 1023) & ~uintptr_t(1023));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int row0 = blockIdx.x * kBlockM;
@@ -155,6 +156,8 @@ gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensor
     }
     if (threadIdx.x == 32) {
         aborted = 0;
+        issued = 0;
+        consumed = 0;
         for (int s = 0; s < kRing; ++s) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full_bar[s])) : "memory");
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty_bar[s])) : "memory");
@@ -184,6 +187,7 @@ gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensor
             const int k0 = k_begin + step * kBlockK;
             tma_load(tile_a, &map_a, k0, row0, full);
             tma_load(tile_b, &map_b, k0, 0, full);
+            issued = step + 1;
         }
     } else if (threadIdx.x == 32 && steps > 0) {
         // MMA issuer.
@@ -208,6 +212,7 @@ gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensor
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                          ::"r"(smem_u32(&empty_bar[s])) : "memory");
+            consumed = step + 1;
         }
         // Every MMA issued so far completes before "done" arrives.
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
@@ -221,6 +226,12 @@ gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensor
     // The producer's loads were all consumed by MMAs that "done" covers; the stages are free.
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (aborted && threadIdx.x == 0) {
+        // A wait gave up: the loads issued but never consumed may still be in flight. Wait for
+        // them (each wait bounded) before the block ends and its shared memory is reused.
+        for (int step = consumed; step < issued; ++step)
+            wait_parity(smem_u32(&full_bar[step % kRing]), uint32_t(step / kRing) & 1u);
+    }
 
     // The output layer's partial sums of each row (two halves of the columns), after the
     // transpose tiles.

@@ -236,6 +236,13 @@ __device__ __forceinline__ const T* stage_band(const SceneView<T>& s, unsigned c
     }
     if (!done) {
         if (threadIdx.x == 0) atomicOr(failure, kStageTimeout);
+        // The copy may still be in flight: give it a second bounded wait before the block goes
+        // on without the staged band (a later landing only touches the unused staging area).
+        for (uint32_t attempt = 0; attempt < (1u << 22) && !done; ++attempt) {
+            asm volatile(
+                "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.b32 %0, 1, 0, p;\n}"
+                : "=r"(done) : "r"(bar) : "memory");
+        }
         return nullptr;
     }
     return reinterpret_cast<const T*>(smem);
