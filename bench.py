@@ -75,8 +75,8 @@ TRANSIT_EVENT_BYTES = 109  # per event: state read (52 B) and written (52 B), qu
 SCATTER_EVENT_BYTES = 116  # per event: queue entry (4 B), state read (64 B) and written (48 B)
 # Fused step (scenes without layer paths): per event its list entry (4 B), its state read once
 # (64 B) and written once after the walk (52 B), its new queue entry and kind (5 B) — the
-# algorithmic minimum; the kernel also stores the state after the scattering and reads it
-# back for the walk, which the measured DRAM traffic shows.
+# algorithmic minimum; the measured DRAM traffic adds what misses L2 (a record block read by
+# the peel-off is read again by the next step) and walks paused by the step budget.
 STEP_EVENT_BYTES = 125
 
 

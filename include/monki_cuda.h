@@ -42,7 +42,8 @@ void *monki_cuda_create(uint32_t device, const double *tables, size_t table_coun
                         uint32_t round_capacity, const char *config, char *err, size_t errlen);
 
 /* Replaces monki_metal_run (kernels/metal/bridge.m:88-133). Runs one round group and
- * copies its FP64 tallies to out (rounds x tally_count). Nonzero on failure. */
+ * copies its FP64 tallies to out (rounds x tally_count). Nonzero on failure. controls:
+ * {count, first, first_round, seed, max_steps (1..10,000,000), profile, per_round, rounds}. */
 int monki_cuda_run(void *session, const uint32_t controls[8], double *out, char *err,
                    size_t errlen);
 

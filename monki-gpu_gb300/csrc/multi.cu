@@ -172,9 +172,15 @@ struct Multi {
     std::string name;
 };
 
+// Pool layout: per slot its record block, then the work-list entries (10 words per slot),
+// then the counts of every member scene. The scenes have no layer paths, so each walk's
+// step count rides in its record block (Pool::steps null). Every offset comes from here.
+size_t lists_offset(size_t slots, size_t record) { return align_up(slots * record, 256); }
+size_t counts_offset(size_t slots, size_t record) {
+    return lists_offset(slots, record) + align_up(10 * slots * 4, 256);
+}
 size_t pool_bytes(size_t slots, size_t members, size_t record) {
-    return align_up(slots * record, 256) + align_up(slots * 4, 256) + align_up(10 * slots * 4, 256) +
-           align_up(members * kCountWords * 4, 256);
+    return counts_offset(slots, record) + align_up(members * kCountWords * 4, 256);
 }
 
 template <typename T>
@@ -224,10 +230,8 @@ void lay_out(Multi& m, Group& g, const std::vector<Controls>& ctl) {
     const size_t record = kRecordBytes<T>;
     char* base = static_cast<char*>(g.pool);
     unsigned char* records = reinterpret_cast<unsigned char*>(base);
-    uint32_t* steps = reinterpret_cast<uint32_t*>(base + align_up(slots * record, 256));
-    uint32_t* lists = reinterpret_cast<uint32_t*>(base + align_up(slots * record, 256) + align_up(slots * 4, 256));
-    uint32_t* counts = reinterpret_cast<uint32_t*>(base + align_up(slots * record, 256) + align_up(slots * 4, 256) +
-                                                   align_up(10 * slots * 4, 256));
+    uint32_t* lists = reinterpret_cast<uint32_t*>(base + lists_offset(slots, record));
+    uint32_t* counts = reinterpret_cast<uint32_t*>(base + counts_offset(slots, record));
     SceneEntry<T>* entries = static_cast<SceneEntry<T>*>(g.host_entries);
     uint32_t slot0 = 0, block = 0;
     g.band_bytes = 0;
@@ -250,7 +254,7 @@ void lay_out(Multi& m, Group& g, const std::vector<Controls>& ctl) {
         Pool<T>& P = E.P;
         P.capacity = capacity;
         P.records = records + size_t(slot0) * record;
-        P.steps = steps + slot0;
+        P.steps = nullptr;
         for (int b = 0; b < 2; ++b) {
             for (int k = 0; k < 3; ++k) P.queue[b][k] = lists + size_t(5 * b + k) * slots + slot0;
             P.paused[b] = lists + size_t(5 * b + 3) * slots + slot0;
@@ -282,12 +286,8 @@ void batch(Multi& m, Group& g, cudaStream_t stream, cudaGraph_t graph) {
     const SceneEntry<T>* entries = static_cast<const SceneEntry<T>*>(g.entries);
     const uint16_t* block_scene = g.block_scene;
     const Guide<T> guide{T(0), T(0), T(INFINITY), nullptr, T(0)};
-    uint32_t* counts = nullptr;
-    {
-        const size_t slots = m.cfg.pool;
-        counts = reinterpret_cast<uint32_t*>(static_cast<char*>(g.pool) + align_up(slots * kRecordBytes<T>, 256) +
-                                             align_up(slots * 4, 256) + align_up(10 * slots * 4, 256));
-    }
+    uint32_t* const counts =
+        reinterpret_cast<uint32_t*>(static_cast<char*>(g.pool) + counts_offset(m.cfg.pool, kRecordBytes<T>));
     const size_t members = g.members.size();
     for (uint32_t it = 0; it < m.cfg.check_every; ++it) {
         uint32_t cur = it & 1u, out = cur ^ 1u;  // kernel arguments: copied when the node or launch is made
@@ -567,7 +567,7 @@ int monki_cuda_multi_run(void* handle, const uint32_t* controls, double* const* 
         for (size_t q = 0; q < m->scenes.size(); ++q) {
             const uint32_t* w = controls + 8 * q;
             Controls c{w[0], w[1], w[2], w[3], w[4], w[5], w[6], w[7]};
-            if (!c.per_round || !c.rounds || c.rounds > m->round_capacity || !c.max_steps ||
+            if (!c.per_round || !c.rounds || c.rounds > m->round_capacity || !c.max_steps || c.max_steps > kMaxHistorySteps ||
                 uint64_t(c.first) + c.count > uint64_t(c.per_round) * c.rounds || !out[q])
                 throw std::runtime_error("Invalid CUDA round group for scene " + std::to_string(q));
             ctl[q] = c;

@@ -116,6 +116,10 @@ struct Controls {
     uint32_t count, first, first_round, seed, max_steps, profile, per_round, rounds;
 };
 
+// The largest history step limit (max_steps) a session accepts; a count up to it is exact
+// in FP32, where walks without layer paths keep it.
+constexpr uint32_t kMaxHistorySteps = 10000000u;
+
 // Device tally layout of one round and one shard (TA = float or double):
 //   stokes[m + nmat * (i + nx * (j + ny * ia))]
 //   paths [k + nz * (i + nx * (j + ny * ia))]      k contiguous for vector reductions

@@ -101,7 +101,7 @@ Pool<T> allocate_pool(Session& s) {
     const size_t nz = size_t(s.prep.nz);
     const size_t block = n * kRecordBytes<T>;
     const size_t ring = s.cfg.importance ? n * kRing : 0;
-    const size_t parts[] = {block, n * sizeof(uint32_t),
+    const size_t parts[] = {block, s.prep.paths ? n * sizeof(uint32_t) : 0,
                             n * nz * sizeof(T), n * sizeof(uint32_t), 2 * n * sizeof(T),
                             10 * n * sizeof(uint32_t), kCountWords * sizeof(uint32_t),
                             ring * sizeof(uint32_t), ring * sizeof(T), s.cfg.importance ? n * sizeof(uint32_t) : 0,
@@ -120,7 +120,8 @@ Pool<T> allocate_pool(Session& s) {
     Pool<T> P{};
     P.capacity = uint32_t(n);
     P.records = reinterpret_cast<unsigned char*>(take(block));
-    P.steps = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
+    // Scenes without layer paths keep each walk's step count in its record block.
+    if (s.prep.paths) P.steps = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
     P.wander = reinterpret_cast<T*>(take(n * nz * sizeof(T)));
     P.runs = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
     P.run_ci = reinterpret_cast<T*>(take(2 * n * sizeof(T)));
@@ -411,7 +412,7 @@ void destroy(Session* s) {
 
 Controls group_controls(const Session& s, const uint32_t controls[8]) {
     Controls c{controls[0], controls[1], controls[2], controls[3], controls[4], controls[5], controls[6], controls[7]};
-    if (!c.per_round || !c.rounds || c.rounds > s.round_capacity || !c.max_steps ||
+    if (!c.per_round || !c.rounds || c.rounds > s.round_capacity || !c.max_steps || c.max_steps > kMaxHistorySteps ||
         uint64_t(c.first) + c.count > uint64_t(c.per_round) * c.rounds)
         throw std::runtime_error("Invalid CUDA round group");
     return c;

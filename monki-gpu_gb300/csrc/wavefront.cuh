@@ -144,7 +144,11 @@ struct Pool {
     // next draw, pack_cell(i, j, pending event kind), packed layers}. The four records of a
     // slot are read and written together, so its accesses fill whole 32-byte sectors.
     unsigned char* records;
-    uint32_t* steps; // walk steps so far (history step limit)
+    // Walk steps so far (the history step limit), one word per slot in scenes with layer
+    // paths; null in scenes without them, where the count rides in the polarization record's
+    // fourth element (init_part, unused there) as an exact FP value (at most 10^7 + 1 steps),
+    // so a walk reads and writes its slot's 64-byte block and nothing else.
+    uint32_t* steps;
     T* wander;       // capacity * nz path lengths after the first event
     uint32_t* runs;  // two straight runs of whole layers: lo0 | hi0 << 8 | lo1 << 16 | hi1 << 24
     T* run_ci;       // capacity * 2: 1 / |cos| of each run
@@ -557,7 +561,7 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
     } else {
         meta = P.meta(slot); pos_in = P.pos(slot); dir_in = P.dir(slot); pol_in = P.pol(slot);
     }
-    const uint32_t steps_in = P.steps[slot];
+    const uint32_t steps_in = P.steps ? P.steps[slot] : uint32_t(pol_in.w);
     uint32_t pid = meta.x;
     DrawStream rng;
     int i = 0, j = 0, k = 0, k1 = -2, wmin = 255, wmax = 0;
@@ -742,11 +746,12 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
     }
     // The whole block, direction included (a scattering or a claim changed it; storing it
     // always also keeps every sector of the block fully written).
+    if (!P.steps) pol.w = T(steps);
     P.pos(slot) = pos;
     P.dir(slot) = dir;
     P.pol(slot) = pol;
     P.meta(slot) = make_uint4(pid, rng.draw, pack_cell(i, j, pending), pack_layers(k, k1, path.wmin, path.wmax));
-    P.steps[slot] = steps;
+    if (P.steps) P.steps[slot] = steps;
     if (P.order) P.order[slot] = order;
     if (PATHS) {
         P.runs[slot] = path.runs;
@@ -1279,7 +1284,7 @@ __device__ __forceinline__ bool scatter_event(uint32_t slot, bool surface, const
         if (n >= 2) {
             pos.w = pos.w / T(n);
             const uint32_t lineage = P.lineage[slot];
-            const uint32_t steps = P.steps[slot];
+            const uint32_t steps = P.steps ? P.steps[slot] : uint32_t(pol.w);
             const uint32_t order = P.order ? P.order[slot] : 0u;
             const Quad<T> dir_out{a, b, c, phi_out};
             const Quad<T> pol_out{q, u, v, pol.w};
