@@ -192,6 +192,28 @@ def test_truncated_histories_fail_and_release_session(device):
     assert backend._handle is None and backend.metadata is None
 
 
+@pytest.mark.parametrize("layered", [False, True])
+def test_step_counts_persist_across_paused_walks(device, layered):
+    """A one-step walk budget pauses every walk after each cell step, so a history's step
+    count must survive many launches (in the record block without layer paths, in its own
+    array with them): a cap of 8 steps rejects the round, a cap of 100,000 does not."""
+
+    import monki.scenes as scenes
+    from monki.execution import BatchControls
+
+    scene = scenes.layered_cloud(20, 1) if layered else scenes.box_cloud(20, 1)
+    ppc = scene.photons_per_column
+    backend = _session(scene, walk=1, max_steps=8, tail=0)
+    with pytest.raises(RuntimeError, match="round rejected"):
+        backend.run_batch(BatchControls(1, ppc))
+    assert backend._handle is None
+
+    backend = _session(scene, walk=1, max_steps=100_000, tail=0)
+    batch = backend.run_batch(BatchControls(1, ppc))
+    assert np.isfinite(batch.stokes).all() and batch.stokes[0].sum() > 0
+    backend.close()
+
+
 def test_invalid_device_does_not_fall_back(device):
     import monki.scenes as scenes
     from monki.execution import CUDA
