@@ -103,13 +103,16 @@ struct WaveTally {
     uint32_t vee;
 };
 
-// A photon copy made by splitting, waiting in its slot: the records of the pool (with V in
-// place of the free path, which the copy draws anew) and {steps, lineage, order, 0}.
+// A photon copy made by splitting, waiting in its slot: the records of the pool, one
+// 64-byte block in FP32 — {photon id, the copy's stream lineage (its draws start at 0),
+// cell | kind, packed layers}, position, direction, and {Q, U, V in place of the free path
+// (which the copy draws anew), the fourth polarization element (the initial partial path
+// with layer paths, else the step count)}. The step count with layer paths and the
+// scattering order with order tallies go beside it in Pool::copy_extra.
 template <typename T>
 struct SplitCopy {
     uint4 meta;
     Quad<T> pos, dir, pol;
-    uint4 extra;
 };
 
 // Resident blocks of 256 per SM the fused step kernel is built for (its register budget,
@@ -180,6 +183,7 @@ struct Pool {
     // slot s at copies[s * kSplitStack + c]) and their count.
     uint32_t* lineage;
     SplitCopy<T>* copies;
+    uint2* copy_extra;  // {steps, order} of each copy with layer paths or order tallies, else null
     uint32_t* waiting;
 
     __device__ __forceinline__ Quad<T>& pos(uint32_t s) const {
@@ -599,14 +603,21 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
             // A copy left by splitting continues in this slot, with its own stream and a
             // new free path drawn from it.
             const uint32_t n = P.waiting[slot] - 1u;
-            const SplitCopy<T> cp = P.copies[size_t(slot) * kSplitStack + n];
+            const size_t c = size_t(slot) * kSplitStack + n;
+            const SplitCopy<T> cp = P.copies[c];
             P.waiting[slot] = n;
             pid = cp.meta.x;
+            lineage = cp.meta.y;
             i = cell_i(cp.meta.z); j = cell_j(cp.meta.z);
             unpack_layers(cp.meta.w, k, k1, wmin, wmax);
             path.wmin = wmin; path.wmax = wmax;
             pos = cp.pos; dir = cp.dir; pol = cp.pol;
-            steps = cp.extra.x; lineage = cp.extra.y; order = cp.extra.z;
+            if (P.copy_extra) {
+                const uint2 e = P.copy_extra[c];
+                steps = e.x; order = e.y;
+            } else {
+                steps = uint32_t(cp.pol.w); order = 0u;
+            }
             vee = cp.pol.z;
             const uint32_t ro = dv.per_round.div(pid);
             rng.init(pid - ro * ctl.per_round, ctl.first_round + ro, ctl.seed, 0u, lineage);
@@ -1289,12 +1300,13 @@ __device__ __forceinline__ bool scatter_event(uint32_t slot, bool surface, const
             const Quad<T> dir_out{a, b, c, phi_out};
             const Quad<T> pol_out{q, u, v, pol.w};
             for (int copy = 1; copy < n; ++copy) {
-                SplitCopy<T>& cp = P.copies[size_t(slot) * kSplitStack + held + uint32_t(copy) - 1u];
-                cp.meta = make_uint4(pid, 0u, meta.z, meta.w);
+                const size_t c = size_t(slot) * kSplitStack + held + uint32_t(copy) - 1u;
+                SplitCopy<T>& cp = P.copies[c];
+                cp.meta = make_uint4(pid, split_lineage(lineage, rng.draw, uint32_t(copy)), meta.z, meta.w);
                 cp.pos = pos;
                 cp.dir = dir_out;
                 cp.pol = pol_out;
-                cp.extra = make_uint4(steps, split_lineage(lineage, rng.draw, uint32_t(copy)), order, 0u);
+                if (P.copy_extra) P.copy_extra[c] = make_uint2(steps, order);
             }
             P.waiting[slot] = held + uint32_t(n) - 1u;
         }
