@@ -111,7 +111,7 @@ Pool<T> allocate_pool(Session& s) {
                             (s.prep.backward && s.cfg.orders) ? n * sizeof(uint32_t) : 0,
                             s.cfg.split > 0.0 ? n * sizeof(uint32_t) : 0,
                             s.cfg.split > 0.0 ? n * kSplitStack * sizeof(SplitCopy<T>) : 0,
-                            (s.cfg.split > 0.0 && (s.prep.paths || s.cfg.orders)) ? n * kSplitStack * sizeof(uint2) : 0,
+                            (s.cfg.split > 0.0 && s.cfg.orders) ? n * kSplitStack * sizeof(uint32_t) : 0,
                             s.cfg.split > 0.0 ? n * sizeof(uint32_t) : 0};
     size_t bytes = 0;
     for (size_t part : parts) bytes += align_up(part, 256);
@@ -146,7 +146,7 @@ Pool<T> allocate_pool(Session& s) {
     if (s.cfg.split > 0.0) {
         P.lineage = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
         P.copies = reinterpret_cast<SplitCopy<T>*>(take(n * kSplitStack * sizeof(SplitCopy<T>)));
-        if (s.prep.paths || s.cfg.orders) P.copy_extra = reinterpret_cast<uint2*>(take(n * kSplitStack * sizeof(uint2)));
+        if (s.cfg.orders) P.copy_order = reinterpret_cast<uint32_t*>(take(n * kSplitStack * sizeof(uint32_t)));
         P.waiting = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
     }
     return P;

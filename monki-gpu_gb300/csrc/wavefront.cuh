@@ -106,9 +106,9 @@ struct WaveTally {
 // A photon copy made by splitting, waiting in its slot: the records of the pool, one
 // 64-byte block in FP32 — {photon id, the copy's stream lineage (its draws start at 0),
 // cell | kind, packed layers}, position, direction, and {Q, U, V in place of the free path
-// (which the copy draws anew), the fourth polarization element (the initial partial path
-// with layer paths, else the step count)}. The step count with layer paths and the
-// scattering order with order tallies go beside it in Pool::copy_extra.
+// (which the copy draws anew), the step count} (splitting runs only in scenes without layer
+// paths, whose slots keep the step count there too). With order tallies the history's
+// scattering order goes beside it in Pool::copy_order.
 template <typename T>
 struct SplitCopy {
     uint4 meta;
@@ -183,7 +183,7 @@ struct Pool {
     // slot s at copies[s * kSplitStack + c]) and their count.
     uint32_t* lineage;
     SplitCopy<T>* copies;
-    uint2* copy_extra;  // {steps, order} of each copy with layer paths or order tallies, else null
+    uint32_t* copy_order;  // scattering order of each waiting copy with order tallies, else null
     uint32_t* waiting;
 
     __device__ __forceinline__ Quad<T>& pos(uint32_t s) const {
@@ -612,12 +612,8 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
             unpack_layers(cp.meta.w, k, k1, wmin, wmax);
             path.wmin = wmin; path.wmax = wmax;
             pos = cp.pos; dir = cp.dir; pol = cp.pol;
-            if (P.copy_extra) {
-                const uint2 e = P.copy_extra[c];
-                steps = e.x; order = e.y;
-            } else {
-                steps = uint32_t(cp.pol.w); order = 0u;
-            }
+            steps = uint32_t(cp.pol.w);
+            order = P.copy_order ? P.copy_order[c] : 0u;
             vee = cp.pol.z;
             const uint32_t ro = dv.per_round.div(pid);
             rng.init(pid - ro * ctl.per_round, ctl.first_round + ro, ctl.seed, 0u, lineage);
@@ -1295,7 +1291,6 @@ __device__ __forceinline__ bool scatter_event(uint32_t slot, bool surface, const
         if (n >= 2) {
             pos.w = pos.w / T(n);
             const uint32_t lineage = P.lineage[slot];
-            const uint32_t steps = P.steps ? P.steps[slot] : uint32_t(pol.w);
             const uint32_t order = P.order ? P.order[slot] : 0u;
             const Quad<T> dir_out{a, b, c, phi_out};
             const Quad<T> pol_out{q, u, v, pol.w};
@@ -1306,7 +1301,7 @@ __device__ __forceinline__ bool scatter_event(uint32_t slot, bool surface, const
                 cp.pos = pos;
                 cp.dir = dir_out;
                 cp.pol = pol_out;
-                if (P.copy_extra) P.copy_extra[c] = make_uint2(steps, order);
+                if (P.copy_order) P.copy_order[c] = order;
             }
             P.waiting[slot] = held + uint32_t(n) - 1u;
         }

@@ -108,6 +108,29 @@ def test_fp64_splitting_reproduces_oracle(oracle, device, pool):
     assert close.mean() == 1.0, f"{(~close).sum()} of {close.size} tallies differ"
 
 
+def test_fp64_splitting_with_order_tallies_reproduces_oracle(oracle, device):
+    """Splitting with scattering-order tallies, where each waiting copy keeps its history's
+    order beside its record block: FP64 Stokes and order tallies are the oracle's, with
+    equal scatter counts."""
+    from monki import Guided
+
+    scene = _box(8, 2)
+    scale = _splitting_map(scene)
+    guide = Guided(0.0, 0.5, 0.0, 2.0)
+    batches, provenance, _ = _run(scene, 2, 31, "fp64", scale=scale, guided=guide, pool=1024, orders=True)
+    expected, counters = oracle.run(scene.tables, _controls(scene, 2, 31), 8, guide=guide.oracle(), scale=scale,
+                                    orders=True)
+    assert provenance["scatters"] == counters["scatters"]
+    for batch, row in zip(batches, expected, strict=True):
+        stokes = batch.stokes.ravel(order="F")
+        close = np.isclose(stokes, row[: stokes.size], rtol=1e-6, atol=1e-12)
+        assert close.mean() == 1.0, ("stokes", (~close).sum())
+        single, located, located_single = oracle.split_orders(scene.tables, row)
+        for name, ref in (("single", single), ("locations", located), ("single_locations", located_single)):
+            close = np.isclose(batch.orders[name], ref, rtol=1e-6, atol=1e-12)
+            assert close.mean() == 1.0, (name, (~close).sum())
+
+
 def test_fp32_splitting_agrees_with_analog_oracle(oracle, device):
     import monki.scenes as scenes
     from monki import Guided
