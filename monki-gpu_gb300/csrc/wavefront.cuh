@@ -603,8 +603,8 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
             // A copy left by splitting continues in this slot, with its own stream and a
             // new free path drawn from it.
             const uint32_t n = P.waiting[slot] - 1u;
-            const size_t c = size_t(slot) * kSplitStack + n;
-            const SplitCopy<T> cp = P.copies[c];
+            const size_t entry = size_t(slot) * kSplitStack + n;
+            const SplitCopy<T> cp = P.copies[entry];
             P.waiting[slot] = n;
             pid = cp.meta.x;
             lineage = cp.meta.y;
@@ -613,7 +613,7 @@ __device__ __forceinline__ int transit_slot(uint32_t slot, const SceneView<T>& s
             path.wmin = wmin; path.wmax = wmax;
             pos = cp.pos; dir = cp.dir; pol = cp.pol;
             steps = uint32_t(cp.pol.w);
-            order = P.copy_order ? P.copy_order[c] : 0u;
+            order = P.copy_order ? P.copy_order[entry] : 0u;
             vee = cp.pol.z;
             const uint32_t ro = dv.per_round.div(pid);
             rng.init(pid - ro * ctl.per_round, ctl.first_round + ro, ctl.seed, 0u, lineage);
@@ -1295,13 +1295,13 @@ __device__ __forceinline__ bool scatter_event(uint32_t slot, bool surface, const
             const Quad<T> dir_out{a, b, c, phi_out};
             const Quad<T> pol_out{q, u, v, pol.w};
             for (int copy = 1; copy < n; ++copy) {
-                const size_t c = size_t(slot) * kSplitStack + held + uint32_t(copy) - 1u;
-                SplitCopy<T>& cp = P.copies[c];
+                const size_t entry = size_t(slot) * kSplitStack + held + uint32_t(copy) - 1u;
+                SplitCopy<T>& cp = P.copies[entry];
                 cp.meta = make_uint4(pid, split_lineage(lineage, rng.draw, uint32_t(copy)), meta.z, meta.w);
                 cp.pos = pos;
                 cp.dir = dir_out;
                 cp.pol = pol_out;
-                if (P.copy_order) P.copy_order[c] = order;
+                if (P.copy_order) P.copy_order[entry] = order;
             }
             P.waiting[slot] = held + uint32_t(n) - 1u;
         }
