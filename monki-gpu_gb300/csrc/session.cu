@@ -224,6 +224,11 @@ struct Recorder {
     template <typename Tuple, size_t... I>
     void launch(const void* fn, unsigned grid, unsigned block, size_t smem, Tuple& values, std::index_sequence<I...>) {
         void* params[] = {static_cast<void*>(&std::get<I>(values))...};
+        // A staged band may take all of kBandMaxBytes beside the kernel's own static shared
+        // memory, past the 48 KB a launch gets without opting in.
+        if (smem)
+            check(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kBandMaxBytes)),
+                  "shared memory attribute");
         if (!graph) {
             check(cudaLaunchKernel(fn, dim3(grid), dim3(block), params, smem, stream), "wavefront launch");
             return;
