@@ -175,6 +175,20 @@ void launch_transport(Session& s, const Controls& c, int grid) {
 // independent of what other host threads do meanwhile: a capture is invalidated by any
 // device-wide synchronization (cudaFree, cudaDeviceSynchronize, a synchronous copy) that
 // another session's thread makes while it is open.
+// Opt a kernel into kBandMaxBytes of dynamic shared memory, once per kernel and device.
+void allow_band(const void* fn) {
+    static std::mutex lock;
+    static std::vector<std::pair<const void*, int>> done;
+    int device = 0;
+    check(cudaGetDevice(&device), "cudaGetDevice");
+    std::lock_guard<std::mutex> guard(lock);
+    const std::pair<const void*, int> key{fn, device};
+    if (std::find(done.begin(), done.end(), key) != done.end()) return;
+    check(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kBandMaxBytes)),
+          "shared memory attribute");
+    done.push_back(key);
+}
+
 struct Recorder {
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;     // null: launch on the stream
@@ -225,10 +239,8 @@ struct Recorder {
     void launch(const void* fn, unsigned grid, unsigned block, size_t smem, Tuple& values, std::index_sequence<I...>) {
         void* params[] = {static_cast<void*>(&std::get<I>(values))...};
         // A staged band may take all of kBandMaxBytes beside the kernel's own static shared
-        // memory, past the 48 KB a launch gets without opting in.
-        if (smem)
-            check(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kBandMaxBytes)),
-                  "shared memory attribute");
+        // memory, past the 48 KB a launch gets without opting in (set once per kernel).
+        if (smem) allow_band(fn);
         if (!graph) {
             check(cudaLaunchKernel(fn, dim3(grid), dim3(block), params, smem, stream), "wavefront launch");
             return;
